@@ -1,0 +1,160 @@
+/*
+ * pbrt_gb300.h -- C ABI of the GB300 ray-batch intersection library
+ * (libpbrtgb300.so).
+ *
+ * This is the boundary the pbrt-v2 fork's batch accelerators call instead of
+ * their OpenCL host code.  Each entry point names the reference interface it
+ * replaces (paths relative to the fork's src/).  Plain pointers and sizes
+ * only; every function returns a pbg status (0 = success) and never aborts;
+ * pbg_last_error() gives the text of the last failure on the calling thread.
+ *
+ * Data layout
+ *   triangles  float[9*ntri], v0.xyz v1.xyz v2.xyz per triangle in world
+ *              space, the packing of accelerators/naive.cpp:59-101
+ *              ("vertices[9*n]"); optional uv float[6*ntri] (u,v per vertex,
+ *              shapes/trianglemesh.h:81-95; NULL = pbrt's defaults).
+ *   host rays  pbg_rays: eight float arrays (o.xyz, d.xyz, mint, maxt; the
+ *              fields of Ray, core/geometry.h:314-336) and an optional
+ *              validity mask (the `hit` array of the batch calls; 0 = skip).
+ *   device rays two arrays of 16-byte records: o4[i] = (ox, oy, oz, mint),
+ *              d4[i] = (dx, dy, dz, maxt), 16-byte aligned.
+ *   hits       prim (int32, index into the triangle array, -1 = miss), t, b1,
+ *              b2; prim/t/b1/b2 equal pbrt's Triangle::Intersect
+ *              (shapes/trianglemesh.cpp:119-156) looped over the triangles
+ *              in index order: the least t, and on an exact tie in t the
+ *              highest index.
+ *   occlusion  uint8 0/1 per ray (the batch API's '0'/'1' chars are
+ *              produced by the adapter).
+ *
+ * Threading: calls on one scene must be serialised by the caller (the
+ * reference serialises its device with Semaphore(1), naive.cpp:109); distinct
+ * scenes may be used from distinct threads.
+ */
+#ifndef PBRT_GB300_H
+#define PBRT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define PBG_OK 0
+#define PBG_ERR_INVALID_ARGUMENT 1
+#define PBG_ERR_CUDA 2
+#define PBG_ERR_OUT_OF_MEMORY 3
+#define PBG_ERR_DEVICE_TIMEOUT 4 /* a bounded device-side wait gave up */
+#define PBG_ERR_NO_DEVICE 5
+#define PBG_ERR_UNSUPPORTED 6
+#define PBG_ERR_INTERNAL 7
+
+/* Accelerator kinds: the scene-file names of api.cpp:586-591. */
+#define PBG_ACCEL_NAIVE 0        /* Accelerator "naive"        */
+#define PBG_ACCEL_RAYHIERARCHY 1 /* Accelerator "rayhierarchy" */
+#define PBG_ACCEL_RAYBVH 2       /* Accelerator "ray-bvh"      */
+
+typedef struct pbg_scene pbg_scene;
+
+/* Construction parameters.  Names follow the scene-file parameters of
+ * rayhierarchy.cpp:1331-1339 and rayBVH.cpp:1328-1335; 0 selects the
+ * library's tuned default. */
+typedef struct pbg_params {
+    int32_t chunk_x;      /* "chunkXSize": rays per leaf along x (rayhierarchy) */
+    int32_t chunk_y;      /* "chunkYSize" */
+    int32_t height;       /* "height": ray-hierarchy levels */
+    int32_t bvh_height;   /* "BVHheight": levels of the BVH cut for ray-bvh */
+    int32_t max_bvh_prim; /* "maxBVHPrim": triangles per BVH leaf */
+    int32_t device;       /* CUDA device ordinal */
+    int32_t reserved[10];
+} pbg_params;
+
+typedef struct pbg_rays {
+    const float *ox, *oy, *oz;
+    const float *dx, *dy, *dz;
+    const float *mint, *maxt;
+    const uint8_t* valid; /* may be NULL: every ray valid */
+} pbg_rays;
+
+typedef struct pbg_hits {
+    int32_t* prim;
+    float* t;
+    float* b1;
+    float* b2;
+} pbg_hits;
+
+typedef struct pbg_counters {
+    uint64_t rays_nearest;   /* rays traced by intersect calls */
+    uint64_t rays_occluded;  /* rays traced by occluded calls */
+    uint64_t calls;
+    uint64_t bvh_nodes;      /* nodes of the scene's BVH (ray-bvh) */
+    uint64_t reserved[12];
+} pbg_counters;
+
+/* Library version, e.g. "pbrt-gb300 1.0 (sm_103a)". */
+const char* pbg_version(void);
+const char* pbg_status_string(int status);
+/* Text of the last failure on the calling thread ("" if none). */
+const char* pbg_last_error(void);
+/* Number of CUDA devices visible (0 when none); never fails. */
+int pbg_device_count(void);
+
+/* Builds the device-resident scene for one accelerator.  Replaces the
+ * constructors NaiveAccel::NaiveAccel (accelerators/naive.cpp:18-110),
+ * RayHieararchy::RayHieararchy (accelerators/rayhierarchy.cpp:35-227) and
+ * RayBVH::RayBVH (accelerators/rayBVH.cpp:31-165), and the BVH they upload
+ * (rayBVH.cpp:204-276).  params may be NULL.  ntri may be 0. */
+int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t accel,
+                     const pbg_params* params, pbg_scene** out);
+/* Replaces the accelerators' destructors (naive.cpp:112-121). */
+void pbg_scene_destroy(pbg_scene* scene);
+
+/* Batch size cap.  Replaces NaiveAccel::MaxRaysPerCall (naive.cpp:127-142),
+ * RayHieararchy::MaxRaysPerCall (rayhierarchy.cpp:267-310) and
+ * RayBVH::MaxRaysPerCall (rayBVH.cpp:279-324), which return 409600. */
+int pbg_max_rays_per_call(const pbg_scene* scene, int64_t* out);
+
+/* Nearest hit of n rays, host buffers in and out (copies included).
+ * Replaces the batch Intersect of naive.cpp:204-338,
+ * rayhierarchy.cpp:602-813 / :816-1140 and rayBVH.cpp:615-836 / :839-1138
+ * (the traversal part; the Intersection records are filled by the caller
+ * from prim/t/b1/b2 and pbg_hit_geometry).  Rays with valid[i] == 0 get
+ * prim = -1. */
+int pbg_intersect(pbg_scene* scene, const pbg_rays* rays, int64_t n, pbg_hits* out);
+
+/* Shadow any-hit of n rays, host buffers.  Replaces the batch IntersectP of
+ * naive.cpp:357-437, rayhierarchy.cpp:1170-1326 and rayBVH.cpp:1170-1323.
+ * occ[i] = 1 when a triangle is hit with t in [mint, maxt]; 0 for a ray with
+ * valid[i] == 0. */
+int pbg_occluded(pbg_scene* scene, const pbg_rays* rays, int64_t n, uint8_t* occ);
+
+/* Device-resident forms: every pointer is device memory, work is enqueued
+ * on `stream` (a cudaStream_t; NULL = the scene's own stream) and the call
+ * returns without synchronising.  valid may be NULL. */
+int pbg_intersect_device(pbg_scene* scene, const float* o4, const float* d4,
+                         const uint8_t* valid, int64_t n, int32_t* prim, float* t, float* b1,
+                         float* b2, void* stream);
+int pbg_occluded_device(pbg_scene* scene, const float* o4, const float* d4,
+                        const uint8_t* valid, int64_t n, uint8_t* occ, void* stream);
+
+/* Differential geometry of each hit, the part of Triangle::Intersect that
+ * builds the DifferentialGeometry (shapes/trianglemesh.cpp:158-190,
+ * core/diffgeom.cpp:32-47) and the fork's computeDpTuTv kernel
+ * (bin/cl/computeDpTuTv.cl:8-91).  out14 is [n][14] float: p.xyz,
+ * dpdu.xyz, dpdv.xyz, nn.xyz, u, v; rows of misses are zero.  Host buffers. */
+int pbg_hit_geometry(pbg_scene* scene, const pbg_rays* rays, const pbg_hits* hits, int64_t n,
+                     float* out14);
+int pbg_hit_geometry_device(pbg_scene* scene, const float* o4, const float* d4,
+                            const int32_t* prim, const float* t, const float* b1,
+                            const float* b2, int64_t n, float* out14, void* stream);
+
+/* Counters (replaces the GPU_TIMES / STAT_* printouts,
+ * core/GPUparallel.h:532-538). */
+int pbg_stats(const pbg_scene* scene, pbg_counters* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBRT_GB300_H */

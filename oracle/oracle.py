@@ -1,0 +1,211 @@
+"""ctypes access to the CPU oracle (oracle/_build/liboracle.so) and, where it
+was built, to the reference's own CPU classes (oracle/_ref/libpbrtref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.  The product never imports it.
+
+Arrays follow the ray-batch conventions of the package: triangles [T, 9]
+float32, rays [8, N] float32 (ox oy oz dx dy dz mint maxt), hits as
+(prim int32 with -1 for a miss, t, b1, b2) and occlusion as uint8 0/1.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libpbrtref.so")
+
+_lib = None
+_ref = None
+
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int32)
+_up = C.POINTER(C.c_uint8)
+
+
+def build() -> None:
+    """Compile the restatement (and, when the reference tree is present, the
+    reference harness)."""
+    subprocess.check_call(["make", "-s", "-C", HERE])
+
+
+def build_ref() -> bool:
+    """Build oracle/_ref/libpbrtref.so from the reference sources; returns
+    False when the reference tree is not on this machine."""
+    ref = os.environ.get("PBRT_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src", "shapes")):
+        return False
+    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={ref}"])
+    return True
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_tri_intersect.restype = C.c_int
+        L.orc_tri_intersect.argtypes = [_fp, _fp, _fp, C.c_float, C.c_float, _fp, _fp, _fp]
+        L.orc_nearest_brute.argtypes = [_fp, C.c_int64, _fp, C.c_int64, _up, _ip, _fp, _fp, _fp, C.c_int]
+        L.orc_anyhit_brute.argtypes = [_fp, C.c_int64, _fp, C.c_int64, _up, _up, C.c_int]
+        L.orc_hits_geometry.argtypes = [_fp, _fp, _fp, C.c_int64, _ip, _fp, _fp, _fp, _fp]
+        L.orc_bvh_build.restype = C.c_void_p
+        L.orc_bvh_build.argtypes = [_fp, C.c_int64, C.c_int]
+        L.orc_bvh_free.argtypes = [C.c_void_p]
+        L.orc_bvh_node_count.restype = C.c_int64
+        L.orc_bvh_node_count.argtypes = [C.c_void_p]
+        L.orc_bvh_nearest.argtypes = [C.c_void_p, _fp, C.c_int64, _up, _ip, _fp, _fp, _fp, C.c_int]
+        L.orc_bvh_anyhit.argtypes = [C.c_void_p, _fp, C.c_int64, _up, _up, C.c_int]
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        R = C.CDLL(REF_PATH)
+        R.ref_scene_create.restype = C.c_void_p
+        R.ref_scene_create.argtypes = [_fp, C.c_int64, C.c_int, _fp, C.c_int]
+        R.ref_scene_destroy.argtypes = [C.c_void_p]
+        R.ref_nearest.argtypes = [C.c_void_p, _fp, C.c_int64, C.c_int, _ip, _fp, _fp, _fp, _fp]
+        R.ref_anyhit.argtypes = [C.c_void_p, _fp, C.c_int64, C.c_int, _up]
+        _ref = R
+    return _ref
+
+
+def _f(a):
+    return a.ctypes.data_as(_fp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _u(a):
+    return None if a is None else a.ctypes.data_as(_up)
+
+
+def _prep(tris, rays, valid=None):
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    rays = np.ascontiguousarray(rays, np.float32)
+    assert rays.ndim == 2 and rays.shape[0] == 8
+    if valid is not None:
+        valid = np.ascontiguousarray(valid, np.uint8)
+    return tris, rays, valid
+
+
+def nearest(tris, rays, valid=None, threads: int | None = None):
+    """Brute force over triangles in index order: pbrt's Triangle::Intersect
+    with the aggregate's maxt update.  Returns (prim, t, b1, b2)."""
+    tris, rays, valid = _prep(tris, rays, valid)
+    n = rays.shape[1]
+    prim = np.empty(n, np.int32)
+    t, b1, b2 = (np.empty(n, np.float32) for _ in range(3))
+    lib().orc_nearest_brute(_f(tris), tris.shape[0], _f(rays), n, _u(valid), _i(prim), _f(t),
+                            _f(b1), _f(b2), threads or os.cpu_count() or 1)
+    return prim, t, b1, b2
+
+
+def anyhit(tris, rays, valid=None, threads: int | None = None):
+    tris, rays, valid = _prep(tris, rays, valid)
+    n = rays.shape[1]
+    occ = np.empty(n, np.uint8)
+    lib().orc_anyhit_brute(_f(tris), tris.shape[0], _f(rays), n, _u(valid), _u(occ),
+                           threads or os.cpu_count() or 1)
+    return occ
+
+
+def hits_geometry(tris, uvs, rays, prim, t, b1, b2):
+    """DifferentialGeometry of each hit: [n, 14] = p, dpdu, dpdv, nn, u, v."""
+    tris, rays, _ = _prep(tris, rays)
+    n = rays.shape[1]
+    out = np.empty((n, 14), np.float32)
+    uvp = None if uvs is None else _f(np.ascontiguousarray(uvs, np.float32))
+    lib().orc_hits_geometry(_f(tris), uvp, _f(rays), n, _i(np.ascontiguousarray(prim, np.int32)),
+                            _f(np.ascontiguousarray(t, np.float32)),
+                            _f(np.ascontiguousarray(b1, np.float32)),
+                            _f(np.ascontiguousarray(b2, np.float32)), _f(out))
+    return out
+
+
+def tri_intersect(tri9, o, d, mint, maxt):
+    tri9 = np.ascontiguousarray(tri9, np.float32)
+    o = np.ascontiguousarray(o, np.float32)
+    d = np.ascontiguousarray(d, np.float32)
+    t, b1, b2 = C.c_float(), C.c_float(), C.c_float()
+    hit = lib().orc_tri_intersect(_f(tri9), _f(o), _f(d), mint, maxt, C.byref(t), C.byref(b1),
+                                  C.byref(b2))
+    return bool(hit), t.value, b1.value, b2.value
+
+
+class BVH:
+    """The timed CPU baseline: SAH BVH in the manner of pbrt's BVHAccel with
+    a conservative box test, so answers equal the brute-force loop."""
+
+    def __init__(self, tris, maxprims: int = 4):
+        self.tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        self.h = lib().orc_bvh_build(_f(self.tris), self.tris.shape[0], maxprims)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_bvh_free(self.h)
+            self.h = None
+
+    def nearest(self, rays, valid=None, threads: int | None = None):
+        _, rays, valid = _prep(self.tris, rays, valid)
+        n = rays.shape[1]
+        prim = np.empty(n, np.int32)
+        t, b1, b2 = (np.empty(n, np.float32) for _ in range(3))
+        lib().orc_bvh_nearest(self.h, _f(rays), n, _u(valid), _i(prim), _f(t), _f(b1), _f(b2),
+                              threads or os.cpu_count() or 1)
+        return prim, t, b1, b2
+
+    def anyhit(self, rays, valid=None, threads: int | None = None):
+        _, rays, valid = _prep(self.tris, rays, valid)
+        n = rays.shape[1]
+        occ = np.empty(n, np.uint8)
+        lib().orc_bvh_anyhit(self.h, _f(rays), n, _u(valid), _u(occ),
+                             threads or os.cpu_count() or 1)
+        return occ
+
+
+class RefScene:
+    """The reference's own TriangleMesh + GeometricPrimitive (+ BVHAccel)."""
+
+    def __init__(self, tris, uv_mode: int = 1, uvs=None, bvh_maxprims: int = 4):
+        self.tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        self.uvs = None if uvs is None else np.ascontiguousarray(uvs, np.float32)
+        self.h = ref().ref_scene_create(_f(self.tris), self.tris.shape[0], uv_mode,
+                                        None if self.uvs is None else _f(self.uvs), bvh_maxprims)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref().ref_scene_destroy(self.h)
+            self.h = None
+
+    def nearest(self, rays, use_bvh: bool = False, geometry: bool = False):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[1]
+        prim = np.empty(n, np.int32)
+        t, u, v = (np.empty(n, np.float32) for _ in range(3))
+        geo = np.empty((n, 14), np.float32) if geometry else None
+        ref().ref_nearest(self.h, _f(rays), n, int(use_bvh), _i(prim), _f(t), _f(u), _f(v),
+                          None if geo is None else _f(geo))
+        return (prim, t, u, v, geo) if geometry else (prim, t, u, v)
+
+    def anyhit(self, rays, use_bvh: bool = False):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[1]
+        occ = np.empty(n, np.uint8)
+        ref().ref_anyhit(self.h, _f(rays), n, int(use_bvh), _u(occ))
+        return occ

@@ -1,0 +1,161 @@
+// ref_harness.cpp -- C entry points into the reference's own CPU classes.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled against the unmodified pbrt-v2 fork
+// sources (shapes/trianglemesh.cpp, accelerators/bvh.cpp and the core files
+// they need) by oracle/ref/Makefile into oracle/_ref/libpbrtref.so.  It is used
+// to pin the C restatement in oracle/pbrt_oracle.c and to generate the golden
+// fixtures under tests/golden/; nothing on the GPU side loads it.
+//
+// Every answer comes from pbrt's own code:
+//   - Triangle::Intersect / IntersectP   shapes/trianglemesh.cpp:119-245
+//   - GeometricPrimitive::Intersect      core/primitive.cpp:88-100 (maxt update)
+//   - BVHAccel::Intersect / IntersectP   accelerators/bvh.cpp:464-566
+//   - DifferentialGeometry               core/diffgeom.cpp:32-47
+// The triangle index of a hit is recovered from Intersection::primitiveId
+// (core/intersection.h:52), which counts GeometricPrimitive construction order.
+// Barycentrics are recovered exactly by giving every triangle the vertex
+// uvs (0,0), (1,0), (0,1): pbrt's interpolation b0*u0 + b1*u1 + b2*u2 then
+// returns u = b1 and v = b2 bit for bit.
+#include "stdafx.h"
+#include "pbrt.h"
+#include "primitive.h"
+#include "intersection.h"
+#include "shapes/trianglemesh.h"
+#include "accelerators/bvh.h"
+#include "transform.h"
+#include "texture.h"
+#include "material.h"
+
+#include <stdint.h>
+#include <vector>
+
+// Globals that pbrt's api.cpp and parser would define; the harness links
+// neither (core/pbrt.h:126, core/error.cpp:62-67).
+Options PbrtOptions;
+string current_file;
+int line_num = 0;
+
+struct RefScene {
+    Transform* identity;
+    Reference<TriangleMesh> mesh;
+    vector<Reference<Primitive> > prims;
+    BVHAccel* bvh;
+    uint32_t firstId;
+    int64_t ntri;
+};
+
+extern "C" {
+
+// uv_mode: 0 = no uvs (pbrt's defaults), 1 = barycentric probe uvs,
+// 2 = caller uvs (uv6 = 6 floats per triangle).
+void* ref_scene_create(const float* tris9, int64_t ntri, int uv_mode, const float* uv6,
+                       int bvh_maxprims) {
+    RefScene* s = new RefScene();
+    s->identity = new Transform();
+    s->ntri = ntri;
+    int nv = (int)(3 * ntri);
+    std::vector<int> vi(nv);
+    std::vector<Point> P(nv);
+    std::vector<float> uv;
+    for (int i = 0; i < nv; ++i) {
+        vi[i] = i;
+        P[i] = Point(tris9[3 * i], tris9[3 * i + 1], tris9[3 * i + 2]);
+    }
+    if (uv_mode == 1) {
+        uv.resize(2 * nv);
+        for (int64_t k = 0; k < ntri; ++k) {
+            float* u = &uv[6 * k];
+            u[0] = 0.f; u[1] = 0.f; u[2] = 1.f; u[3] = 0.f; u[4] = 0.f; u[5] = 1.f;
+        }
+    } else if (uv_mode == 2) {
+        uv.assign(uv6, uv6 + 6 * ntri);
+    }
+    s->mesh = new TriangleMesh(s->identity, s->identity, false, (int)ntri, nv,
+                               vi.empty() ? NULL : &vi[0], P.empty() ? NULL : &P[0], NULL, NULL,
+                               uv.empty() ? NULL : &uv[0], Reference<Texture<float> >(NULL));
+    vector<Reference<Shape> > tris;
+    s->mesh->Refine(tris);
+    s->firstId = 0;
+    for (size_t i = 0; i < tris.size(); ++i) {
+        GeometricPrimitive* gp =
+            new GeometricPrimitive(tris[i], Reference<Material>(NULL), NULL);
+        if (i == 0) s->firstId = gp->primitiveId;
+        s->prims.push_back(gp);
+    }
+    s->bvh = bvh_maxprims > 0 ? new BVHAccel(s->prims, (uint32_t)bvh_maxprims, "sah") : NULL;
+    return s;
+}
+
+void ref_scene_destroy(void* p) {
+    RefScene* s = (RefScene*)p;
+    if (!s) return;
+    delete s->bvh;
+    s->prims.clear();
+    s->mesh = NULL;
+    delete s->identity;
+    delete s;
+}
+
+static Ray make_ray(const float* rays, int64_t n, int64_t i) {
+    Point o(rays[0 * n + i], rays[1 * n + i], rays[2 * n + i]);
+    Vector d(rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]);
+    return Ray(o, d, rays[6 * n + i], rays[7 * n + i]);
+}
+
+// Nearest hit for every ray.  use_bvh = 0: the primitives in index order
+// with pbrt's maxt update (the semantics of a sequential aggregate);
+// use_bvh = 1: pbrt's BVHAccel.  geo (optional, [n][14]) receives
+// p, dpdu, dpdv, nn, u, v of the hit's DifferentialGeometry.
+void ref_nearest(void* p, const float* rays, int64_t n, int use_bvh, int32_t* prim, float* t,
+                 float* u, float* v, float* geo) {
+    RefScene* s = (RefScene*)p;
+    for (int64_t i = 0; i < n; ++i) {
+        Ray r = make_ray(rays, n, i);
+        Intersection isect;
+        bool hit = false;
+        if (use_bvh) {
+            hit = s->bvh->Intersect(r, &isect);
+        } else {
+            for (size_t k = 0; k < s->prims.size(); ++k)
+                if (s->prims[k]->Intersect(r, &isect)) hit = true;
+        }
+        if (hit) {
+            prim[i] = (int32_t)(isect.primitiveId - s->firstId);
+            t[i] = r.maxt;
+            u[i] = isect.dg.u;
+            v[i] = isect.dg.v;
+            if (geo) {
+                float* g = geo + 14 * i;
+                const DifferentialGeometry& dg = isect.dg;
+                g[0] = dg.p.x; g[1] = dg.p.y; g[2] = dg.p.z;
+                g[3] = dg.dpdu.x; g[4] = dg.dpdu.y; g[5] = dg.dpdu.z;
+                g[6] = dg.dpdv.x; g[7] = dg.dpdv.y; g[8] = dg.dpdv.z;
+                g[9] = dg.nn.x; g[10] = dg.nn.y; g[11] = dg.nn.z;
+                g[12] = dg.u; g[13] = dg.v;
+            }
+        } else {
+            prim[i] = -1;
+            t[i] = 0.f; u[i] = 0.f; v[i] = 0.f;
+            if (geo)
+                for (int k = 0; k < 14; ++k) geo[14 * i + k] = 0.f;
+        }
+    }
+}
+
+// Shadow any-hit for every ray: 1 if some triangle is hit in [mint, maxt].
+void ref_anyhit(void* p, const float* rays, int64_t n, int use_bvh, uint8_t* occ) {
+    RefScene* s = (RefScene*)p;
+    for (int64_t i = 0; i < n; ++i) {
+        Ray r = make_ray(rays, n, i);
+        bool hit = false;
+        if (use_bvh) {
+            hit = s->bvh->IntersectP(r);
+        } else {
+            for (size_t k = 0; k < s->prims.size() && !hit; ++k)
+                hit = s->prims[k]->IntersectP(r);
+        }
+        occ[i] = hit ? 1 : 0;
+    }
+}
+
+}  // extern "C"

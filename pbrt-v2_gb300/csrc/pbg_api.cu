@@ -1,0 +1,560 @@
+// pbg_api.cu -- the C ABI (include/pbrt_gb300.h): scene lifetime, batch
+// calls with host or device buffers, hit geometry and counters.
+//
+// Host-side duties of the reference accelerators that live here:
+//   - packing triangles once at construction (accelerators/naive.cpp:59-101,
+//     rayhierarchy.cpp:158-205) -> TriRec records built on the device;
+//   - AoS -> SoA ray packing per batch (naive.cpp:224-262,
+//     rayhierarchy.cpp:833-853) -> one H2D copy of the caller's SoA rows and
+//     a pack kernel into 16-byte records;
+//   - reading back tHit/index and computeDpTuTv results
+//     (rayhierarchy.cpp:1048-1091) -> D2H copies of prim/t/b1/b2 and of the
+//     hit geometry.
+// Errors become status codes; nothing aborts (the reference calls Severe(),
+// core/error.cpp:130).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "pbg_internal.h"
+#include "pbg_tma.cuh"
+
+namespace pbg {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_status(cudaError_t e, const char* what) {
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    set_last_error(buf);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();  // clear the sticky-free allocation error
+        return PBG_ERR_OUT_OF_MEMORY;
+    }
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return PBG_ERR_NO_DEVICE;
+    return PBG_ERR_CUDA;
+}
+
+int ensure(DeviceBuffer& b, size_t bytes) {
+    if (bytes <= b.bytes && b.ptr) return PBG_OK;
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&b.ptr, want);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        return cuda_status(e, "cudaMalloc");
+    }
+    b.bytes = want;
+    return PBG_OK;
+}
+
+void release(DeviceBuffer& b) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+// ---------------------------------------------------------------- kernels
+
+// TriRec from original vertices; e1, e2 rounded as pbrt rounds p2 - p1 and
+// p3 - p1 (shapes/trianglemesh.cpp:127-128).  order (may be NULL) lists the
+// original index of each record; pos receives the inverse map.
+__global__ void build_tris_kernel(const float* __restrict__ tri9, const int32_t* __restrict__ order,
+                                  int64_t ntri, TriRec* __restrict__ out, int32_t* __restrict__ pos) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntri) return;
+    const int32_t src = order ? order[i] : (int32_t)i;
+    const float* v = tri9 + 9 * (int64_t)src;
+    const float p1x = v[0], p1y = v[1], p1z = v[2];
+    const float e1x = __fsub_rn(v[3], p1x), e1y = __fsub_rn(v[4], p1y), e1z = __fsub_rn(v[5], p1z);
+    const float e2x = __fsub_rn(v[6], p1x), e2y = __fsub_rn(v[7], p1y), e2z = __fsub_rn(v[8], p1z);
+    TriRec r;
+    r.a = make_float4(p1x, p1y, p1z, fabsf(e1x) + fabsf(e1y) + fabsf(e1z));
+    r.b = make_float4(e1x, e1y, e1z, fabsf(e2x) + fabsf(e2y) + fabsf(e2z));
+    r.c = make_float4(e2x, e2y, e2z, __int_as_float(src));
+    out[i] = r;
+    if (pos) pos[src] = (int32_t)i;
+}
+
+// Caller SoA rows (8 x n floats, one staging block) -> 16-byte records.
+__global__ void pack_rays_kernel(const float* __restrict__ stage, int64_t n, float4* __restrict__ o,
+                                 float4* __restrict__ d) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    o[i] = make_float4(stage[i], stage[n + i], stage[2 * n + i], stage[6 * n + i]);
+    d[i] = make_float4(stage[3 * n + i], stage[4 * n + i], stage[5 * n + i], stage[7 * n + i]);
+}
+
+__device__ __forceinline__ void xcross3(float ax, float ay, float az, float bx, float by, float bz,
+                                        float* x, float* y, float* z) {
+    *x = xcross(ay, bz, az, by);
+    *y = xcross(az, bx, ax, bz);
+    *z = xcross(ax, by, ay, bx);
+}
+
+// DifferentialGeometry of a hit (shapes/trianglemesh.cpp:158-190,
+// core/diffgeom.cpp:32-47, core/geometry.h:512-522), pbrt's rounding.
+__global__ void hit_geometry_kernel(const float* __restrict__ tri9, const float* __restrict__ uv6,
+                                    const float4* __restrict__ ro, const float4* __restrict__ rd,
+                                    const int32_t* __restrict__ prim, const float* __restrict__ tt,
+                                    const float* __restrict__ b1v, const float* __restrict__ b2v,
+                                    int64_t n, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float* g = out + 14 * i;
+    const int32_t p = prim[i];
+    if (p < 0) {
+        for (int k = 0; k < 14; ++k) g[k] = 0.f;
+        return;
+    }
+    const float* v = tri9 + 9 * (int64_t)p;
+    float u[3][2];
+    if (uv6) {
+        const float* q = uv6 + 6 * (int64_t)p;
+        u[0][0] = q[0]; u[0][1] = q[1]; u[1][0] = q[2]; u[1][1] = q[3]; u[2][0] = q[4]; u[2][1] = q[5];
+    } else {
+        u[0][0] = 0.f; u[0][1] = 0.f; u[1][0] = 1.f; u[1][1] = 0.f; u[2][0] = 1.f; u[2][1] = 1.f;
+    }
+    const float du1 = __fsub_rn(u[0][0], u[2][0]), du2 = __fsub_rn(u[1][0], u[2][0]);
+    const float dv1 = __fsub_rn(u[0][1], u[2][1]), dv2 = __fsub_rn(u[1][1], u[2][1]);
+    float dp1[3], dp2[3], dpdu[3], dpdv[3];
+    for (int k = 0; k < 3; ++k) {
+        dp1[k] = __fsub_rn(v[k], v[6 + k]);
+        dp2[k] = __fsub_rn(v[3 + k], v[6 + k]);
+    }
+    const float det = __fsub_rn(__fmul_rn(du1, dv2), __fmul_rn(dv1, du2));
+    if (det == 0.f) {
+        float e1[3], e2[3];
+        for (int k = 0; k < 3; ++k) {
+            e1[k] = __fsub_rn(v[3 + k], v[k]);
+            e2[k] = __fsub_rn(v[6 + k], v[k]);
+        }
+        float nx, ny, nz;
+        xcross3(e2[0], e2[1], e2[2], e1[0], e1[1], e1[2], &nx, &ny, &nz);
+        const float inv = __frcp_rn(__fsqrt_rn(xdot(nx, ny, nz, nx, ny, nz)));
+        const float v1x = __fmul_rn(nx, inv), v1y = __fmul_rn(ny, inv), v1z = __fmul_rn(nz, inv);
+        if (fabsf(v1x) > fabsf(v1y)) {
+            const float il = __frcp_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(v1x, v1x), __fmul_rn(v1z, v1z))));
+            dpdu[0] = __fmul_rn(-v1z, il); dpdu[1] = 0.f; dpdu[2] = __fmul_rn(v1x, il);
+        } else {
+            const float il = __frcp_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(v1y, v1y), __fmul_rn(v1z, v1z))));
+            dpdu[0] = 0.f; dpdu[1] = __fmul_rn(v1z, il); dpdu[2] = __fmul_rn(-v1y, il);
+        }
+        xcross3(v1x, v1y, v1z, dpdu[0], dpdu[1], dpdu[2], &dpdv[0], &dpdv[1], &dpdv[2]);
+    } else {
+        const float invdet = __frcp_rn(det);
+        for (int k = 0; k < 3; ++k) {
+            dpdu[k] = __fmul_rn(__fsub_rn(__fmul_rn(dv2, dp1[k]), __fmul_rn(dv1, dp2[k])), invdet);
+            dpdv[k] = __fmul_rn(__fadd_rn(__fmul_rn(-du2, dp1[k]), __fmul_rn(du1, dp2[k])), invdet);
+        }
+    }
+    const float b1 = b1v[i], b2 = b2v[i], t = tt[i];
+    const float b0 = __fsub_rn(__fsub_rn(1.f, b1), b2);
+    const float tu = __fadd_rn(__fadd_rn(__fmul_rn(b0, u[0][0]), __fmul_rn(b1, u[1][0])), __fmul_rn(b2, u[2][0]));
+    const float tv = __fadd_rn(__fadd_rn(__fmul_rn(b0, u[0][1]), __fmul_rn(b1, u[1][1])), __fmul_rn(b2, u[2][1]));
+    const float4 o = ro[i], d = rd[i];
+    g[0] = __fadd_rn(o.x, __fmul_rn(d.x, t));
+    g[1] = __fadd_rn(o.y, __fmul_rn(d.y, t));
+    g[2] = __fadd_rn(o.z, __fmul_rn(d.z, t));
+    float nx, ny, nz;
+    xcross3(dpdu[0], dpdu[1], dpdu[2], dpdv[0], dpdv[1], dpdv[2], &nx, &ny, &nz);
+    const float inv = __frcp_rn(__fsqrt_rn(xdot(nx, ny, nz, nx, ny, nz)));
+    g[3] = dpdu[0]; g[4] = dpdu[1]; g[5] = dpdu[2];
+    g[6] = dpdv[0]; g[7] = dpdv[1]; g[8] = dpdv[2];
+    g[9] = __fmul_rn(nx, inv); g[10] = __fmul_rn(ny, inv); g[11] = __fmul_rn(nz, inv);
+    g[12] = tu;
+    g[13] = tv;
+}
+
+int launch_pack_rays(pbg_scene* s, const float* stage, int64_t n, float4* o, float4* d,
+                     cudaStream_t st) {
+    (void)s;
+    if (n <= 0) return PBG_OK;
+    pack_rays_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(stage, n, o, d);
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
+int hit_geometry(pbg_scene* s, const float4* o, const float4* d, const int32_t* prim,
+                 const float* t, const float* b1, const float* b2, int64_t n, float* out14,
+                 cudaStream_t st) {
+    if (n <= 0) return PBG_OK;
+    hit_geometry_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(
+        (const float*)s->tri9.ptr, (const float*)s->uv6.ptr, o, d, prim, t, b1, b2, n, out14);
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
+int check_device_status(pbg_scene* s, cudaStream_t st) {
+    int h[4] = {0, 0, 0, 0};
+    PBG_CUDA(cudaMemcpyAsync(h, s->err.ptr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PBG_CUDA(cudaStreamSynchronize(st));
+    if (h[kStatusTimeout] != 0 || h[kStatusOverflow] != 0) {
+        PBG_CUDA(cudaMemsetAsync(s->err.ptr, 0, sizeof(h), st));
+        char buf[160];
+        snprintf(buf, sizeof(buf), "device status: %d bounded waits expired, %d stack overflows",
+                 h[kStatusTimeout], h[kStatusOverflow]);
+        set_last_error(buf);
+        return h[kStatusTimeout] ? PBG_ERR_DEVICE_TIMEOUT : PBG_ERR_INTERNAL;
+    }
+    return PBG_OK;
+}
+
+int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order) {
+    const int64_t ntri = s->ntri;
+    int rc = ensure(s->tri9, (size_t)(ntri > 0 ? ntri : 1) * 9 * sizeof(float));
+    if (rc) return rc;
+    rc = ensure(s->tris, (size_t)(ntri > 0 ? ntri : 1) * sizeof(TriRec));
+    if (rc) return rc;
+    if (ntri == 0) return PBG_OK;
+    PBG_CUDA(cudaMemcpyAsync(s->tri9.ptr, tri9_host, (size_t)ntri * 9 * sizeof(float),
+                             cudaMemcpyHostToDevice, s->stream));
+    DeviceBuffer dorder;
+    if (order) {
+        rc = ensure(dorder, (size_t)ntri * sizeof(int32_t));
+        if (rc) return rc;
+        PBG_CUDA(cudaMemcpyAsync(dorder.ptr, order, (size_t)ntri * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, s->stream));
+    }
+    build_tris_kernel<<<(unsigned)((ntri + 255) / 256), 256, 0, s->stream>>>(
+        (const float*)s->tri9.ptr, (const int32_t*)dorder.ptr, ntri, (TriRec*)s->tris.ptr, nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    release(dorder);
+    if (e != cudaSuccess) return cuda_status(e, "build_tris_kernel");
+    return PBG_OK;
+}
+
+// ------------------------------------------------------------- dispatch
+
+static int run_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,
+                       int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
+    switch (s->accel) {
+        case PBG_ACCEL_NAIVE: return naive_nearest(s, o, d, valid, n, prim, t, b1, b2, st);
+        case PBG_ACCEL_RAYBVH: return bvh_nearest(s, o, d, valid, n, prim, t, b1, b2, st);
+        case PBG_ACCEL_RAYHIERARCHY: return rh_nearest(s, o, d, valid, n, prim, t, b1, b2, st);
+    }
+    set_last_error("unknown accelerator kind");
+    return PBG_ERR_INVALID_ARGUMENT;
+}
+
+static int run_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,
+                        int64_t n, uint8_t* occ, cudaStream_t st) {
+    switch (s->accel) {
+        case PBG_ACCEL_NAIVE: return naive_occluded(s, o, d, valid, n, occ, st);
+        case PBG_ACCEL_RAYBVH: return bvh_occluded(s, o, d, valid, n, occ, st);
+        case PBG_ACCEL_RAYHIERARCHY: return rh_occluded(s, o, d, valid, n, occ, st);
+    }
+    set_last_error("unknown accelerator kind");
+    return PBG_ERR_INVALID_ARGUMENT;
+}
+
+// Copies the caller's host rays into the scene's work buffers.
+static int stage_rays(pbg_scene* s, const pbg_rays* r, int64_t n, float4** o, float4** d,
+                      uint8_t** valid) {
+    Work& w = s->work;
+    int rc;
+    if ((rc = ensure(w.stage, (size_t)n * 8 * sizeof(float)))) return rc;
+    if ((rc = ensure(w.ray_o, (size_t)n * sizeof(float4)))) return rc;
+    if ((rc = ensure(w.ray_d, (size_t)n * sizeof(float4)))) return rc;
+    float* stage = (float*)w.stage.ptr;
+    const float* rows[8] = {r->ox, r->oy, r->oz, r->dx, r->dy, r->dz, r->mint, r->maxt};
+    bool contiguous = true;
+    for (int k = 1; k < 8; ++k)
+        if (rows[k] != rows[0] + k * n) contiguous = false;
+    if (contiguous) {
+        PBG_CUDA(cudaMemcpyAsync(stage, rows[0], (size_t)n * 8 * sizeof(float),
+                                 cudaMemcpyHostToDevice, s->stream));
+    } else {
+        for (int k = 0; k < 8; ++k)
+            PBG_CUDA(cudaMemcpyAsync(stage + (size_t)k * n, rows[k], (size_t)n * sizeof(float),
+                                     cudaMemcpyHostToDevice, s->stream));
+    }
+    *valid = nullptr;
+    if (r->valid) {
+        if ((rc = ensure(w.valid, (size_t)n))) return rc;
+        PBG_CUDA(cudaMemcpyAsync(w.valid.ptr, r->valid, (size_t)n, cudaMemcpyHostToDevice,
+                                 s->stream));
+        *valid = (uint8_t*)w.valid.ptr;
+    }
+    *o = (float4*)w.ray_o.ptr;
+    *d = (float4*)w.ray_d.ptr;
+    return launch_pack_rays(s, stage, n, *o, *d, s->stream);
+}
+
+static bool rays_ok(const pbg_rays* r) {
+    return r && r->ox && r->oy && r->oz && r->dx && r->dy && r->dz && r->mint && r->maxt;
+}
+
+}  // namespace pbg
+
+using namespace pbg;
+
+extern "C" {
+
+const char* pbg_version(void) { return "pbrt-gb300 1.0 (sm_103a)"; }
+
+const char* pbg_status_string(int status) {
+    switch (status) {
+        case PBG_OK: return "ok";
+        case PBG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PBG_ERR_CUDA: return "CUDA error";
+        case PBG_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case PBG_ERR_DEVICE_TIMEOUT: return "bounded device wait expired";
+        case PBG_ERR_NO_DEVICE: return "no CUDA device";
+        case PBG_ERR_UNSUPPORTED: return "unsupported";
+        case PBG_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+const char* pbg_last_error(void) { return g_last_error.c_str(); }
+
+int pbg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t accel,
+                     const pbg_params* params, pbg_scene** out) {
+    if (!out) {
+        set_last_error("pbg_scene_create: out is NULL");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    if (ntri < 0 || (ntri > 0 && !tri9) || ntri > (int64_t)INT32_MAX / 2) {
+        set_last_error("pbg_scene_create: bad triangle array");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (accel != PBG_ACCEL_NAIVE && accel != PBG_ACCEL_RAYHIERARCHY && accel != PBG_ACCEL_RAYBVH) {
+        set_last_error("pbg_scene_create: unknown accelerator kind");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (pbg_device_count() == 0) {
+        set_last_error("pbg_scene_create: no CUDA device");
+        return PBG_ERR_NO_DEVICE;
+    }
+    pbg_scene* s = new (std::nothrow) pbg_scene();
+    if (!s) return PBG_ERR_OUT_OF_MEMORY;
+    if (params) s->params = *params;
+    s->device = s->params.device;
+    s->accel = accel;
+    s->ntri = ntri;
+    int rc = PBG_OK;
+    auto fail = [&](int code) {
+        pbg_scene_destroy(s);
+        return code;
+    };
+    {
+        cudaError_t e = cudaSetDevice(s->device);
+        if (e != cudaSuccess) return fail(cuda_status(e, "cudaSetDevice"));
+        e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return fail(cuda_status(e, "cudaStreamCreate"));
+    }
+    if ((rc = ensure(s->err, 4 * sizeof(int)))) return fail(rc);
+    if (cudaMemset(s->err.ptr, 0, 4 * sizeof(int)) != cudaSuccess)
+        return fail(cuda_status(cudaGetLastError(), "cudaMemset"));
+    for (int64_t i = 0; i < ntri; ++i)
+        for (int k = 0; k < 9; ++k) {
+            float v = tri9[9 * i + k];
+            if (i == 0 && k < 3) s->scene_lo[k] = s->scene_hi[k] = v;
+            int a = k % 3;
+            s->scene_lo[a] = v < s->scene_lo[a] ? v : s->scene_lo[a];
+            s->scene_hi[a] = v > s->scene_hi[a] ? v : s->scene_hi[a];
+        }
+    HostBvh hb;
+    const int32_t* order = nullptr;
+    if (accel == PBG_ACCEL_RAYBVH) {
+        build_bvh(tri9, ntri, s->params.max_bvh_prim > 0 ? s->params.max_bvh_prim : 4, &hb);
+        order = hb.order.empty() ? nullptr : hb.order.data();
+        if ((rc = ensure(s->bvh, hb.nodes.size() * sizeof(BvhNode)))) return fail(rc);
+        cudaError_t e = cudaMemcpy(s->bvh.ptr, hb.nodes.data(), hb.nodes.size() * sizeof(BvhNode),
+                                   cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(cuda_status(e, "cudaMemcpy(bvh)"));
+        s->bvh_nodes = (int64_t)hb.nodes.size();
+        s->bvh_depth = hb.max_depth;
+        s->unculled = hb.unculled;
+        s->counters.bvh_nodes = (uint64_t)hb.nodes.size();
+    }
+    if ((rc = upload_triangles(s, tri9, order))) return fail(rc);
+    if (uv6 && ntri > 0) {
+        if ((rc = ensure(s->uv6, (size_t)ntri * 6 * sizeof(float)))) return fail(rc);
+        cudaError_t e = cudaMemcpy(s->uv6.ptr, uv6, (size_t)ntri * 6 * sizeof(float),
+                                   cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(cuda_status(e, "cudaMemcpy(uv)"));
+    }
+    *out = s;
+    return PBG_OK;
+}
+
+void pbg_scene_destroy(pbg_scene* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    release(s->tris);
+    release(s->tri9);
+    release(s->uv6);
+    release(s->bvh);
+    release(s->err);
+    Work& w = s->work;
+    DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.valid, &w.prim, &w.t, &w.b1, &w.b2,
+                           &w.occ, &w.keys, &w.stage, &w.perm, &w.perm_tmp, &w.mkeys,
+                           &w.mkeys_tmp, &w.hist, &w.nodes, &w.counters, &w.geo};
+    for (DeviceBuffer* b : all) release(*b);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int pbg_max_rays_per_call(const pbg_scene* s, int64_t* out) {
+    if (!s || !out) return PBG_ERR_INVALID_ARGUMENT;
+    // The reference's cap (naive.cpp:141) keeps its task tiling; the device
+    // path itself has no per-call limit below 2^31 rays.
+    *out = 409600;
+    return PBG_OK;
+}
+
+int pbg_intersect_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid,
+                         int64_t n, int32_t* prim, float* t, float* b1, float* b2, void* stream) {
+    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2))) {
+        set_last_error("pbg_intersect_device: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (n > (int64_t)INT32_MAX) return PBG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    int rc = run_nearest(s, (const float4*)o4, (const float4*)d4, valid, n, prim, t, b1, b2, st);
+    if (rc == PBG_OK) {
+        s->counters.rays_nearest += (uint64_t)n;
+        s->counters.calls++;
+    }
+    return rc;
+}
+
+int pbg_occluded_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid,
+                        int64_t n, uint8_t* occ, void* stream) {
+    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !occ))) {
+        set_last_error("pbg_occluded_device: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (n > (int64_t)INT32_MAX) return PBG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    int rc = run_occluded(s, (const float4*)o4, (const float4*)d4, valid, n, occ, st);
+    if (rc == PBG_OK) {
+        s->counters.rays_occluded += (uint64_t)n;
+        s->counters.calls++;
+    }
+    return rc;
+}
+
+int pbg_intersect(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_hits* out) {
+    if (!s || n < 0 || (n > 0 && (!rays_ok(r) || !out || !out->prim || !out->t || !out->b1 ||
+                                  !out->b2))) {
+        set_last_error("pbg_intersect: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return PBG_OK;
+    cudaSetDevice(s->device);
+    float4 *o, *d;
+    uint8_t* valid;
+    int rc = stage_rays(s, r, n, &o, &d, &valid);
+    if (rc) return rc;
+    Work& w = s->work;
+    if ((rc = ensure(w.prim, (size_t)n * 4)) || (rc = ensure(w.t, (size_t)n * 4)) ||
+        (rc = ensure(w.b1, (size_t)n * 4)) || (rc = ensure(w.b2, (size_t)n * 4)))
+        return rc;
+    rc = run_nearest(s, o, d, valid, n, (int32_t*)w.prim.ptr, (float*)w.t.ptr, (float*)w.b1.ptr,
+                     (float*)w.b2.ptr, s->stream);
+    if (rc) return rc;
+    PBG_CUDA(cudaMemcpyAsync(out->prim, w.prim.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    PBG_CUDA(cudaMemcpyAsync(out->t, w.t.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    PBG_CUDA(cudaMemcpyAsync(out->b1, w.b1.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    PBG_CUDA(cudaMemcpyAsync(out->b2, w.b2.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    rc = check_device_status(s, s->stream);
+    if (rc) return rc;
+    s->counters.rays_nearest += (uint64_t)n;
+    s->counters.calls++;
+    return PBG_OK;
+}
+
+int pbg_occluded(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t* occ) {
+    if (!s || n < 0 || (n > 0 && (!rays_ok(r) || !occ))) {
+        set_last_error("pbg_occluded: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return PBG_OK;
+    cudaSetDevice(s->device);
+    float4 *o, *d;
+    uint8_t* valid;
+    int rc = stage_rays(s, r, n, &o, &d, &valid);
+    if (rc) return rc;
+    Work& w = s->work;
+    if ((rc = ensure(w.occ, (size_t)n))) return rc;
+    rc = run_occluded(s, o, d, valid, n, (uint8_t*)w.occ.ptr, s->stream);
+    if (rc) return rc;
+    PBG_CUDA(cudaMemcpyAsync(occ, w.occ.ptr, (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    rc = check_device_status(s, s->stream);
+    if (rc) return rc;
+    s->counters.rays_occluded += (uint64_t)n;
+    s->counters.calls++;
+    return PBG_OK;
+}
+
+int pbg_hit_geometry_device(pbg_scene* s, const float* o4, const float* d4, const int32_t* prim,
+                            const float* t, const float* b1, const float* b2, int64_t n,
+                            float* out14, void* stream) {
+    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2 || !out14)))
+        return PBG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    return hit_geometry(s, (const float4*)o4, (const float4*)d4, prim, t, b1, b2, n, out14, st);
+}
+
+int pbg_hit_geometry(pbg_scene* s, const pbg_rays* r, const pbg_hits* h, int64_t n,
+                     float* out14) {
+    if (!s || n < 0 || (n > 0 && (!rays_ok(r) || !h || !h->prim || !h->t || !h->b1 || !h->b2 ||
+                                  !out14))) {
+        set_last_error("pbg_hit_geometry: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return PBG_OK;
+    cudaSetDevice(s->device);
+    float4 *o, *d;
+    uint8_t* valid;
+    int rc = stage_rays(s, r, n, &o, &d, &valid);
+    if (rc) return rc;
+    Work& w = s->work;
+    if ((rc = ensure(w.prim, (size_t)n * 4)) || (rc = ensure(w.t, (size_t)n * 4)) ||
+        (rc = ensure(w.b1, (size_t)n * 4)) || (rc = ensure(w.b2, (size_t)n * 4)) ||
+        (rc = ensure(w.geo, (size_t)n * 14 * 4)))
+        return rc;
+    PBG_CUDA(cudaMemcpyAsync(w.prim.ptr, h->prim, (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+    PBG_CUDA(cudaMemcpyAsync(w.t.ptr, h->t, (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+    PBG_CUDA(cudaMemcpyAsync(w.b1.ptr, h->b1, (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+    PBG_CUDA(cudaMemcpyAsync(w.b2.ptr, h->b2, (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+    rc = hit_geometry(s, o, d, (const int32_t*)w.prim.ptr, (const float*)w.t.ptr,
+                      (const float*)w.b1.ptr, (const float*)w.b2.ptr, n, (float*)w.geo.ptr,
+                      s->stream);
+    if (rc) return rc;
+    PBG_CUDA(cudaMemcpyAsync(out14, w.geo.ptr, (size_t)n * 14 * 4, cudaMemcpyDeviceToHost, s->stream));
+    PBG_CUDA(cudaStreamSynchronize(s->stream));
+    return PBG_OK;
+}
+
+int pbg_stats(const pbg_scene* s, pbg_counters* out) {
+    if (!s || !out) return PBG_ERR_INVALID_ARGUMENT;
+    *out = s->counters;
+    return PBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,105 @@
+// pbg_internal.h -- host-side state shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pbrt_gb300.h"
+#include "pbg_exact.cuh"
+
+namespace pbg {
+
+// Two-wide BVH node (64 bytes): both children's boxes, so one node fetch
+// decides both children.  A child index >= 0 is an inner node; a negative
+// index ~start is a leaf holding triangles [start, start + count).
+struct __align__(16) BvhNode {
+    float4 n0;  // c0.lo.x c0.hi.x c0.lo.y c0.hi.y
+    float4 n1;  // c1.lo.x c1.hi.x c1.lo.y c1.hi.y
+    float4 n2;  // c0.lo.z c0.hi.z c1.lo.z c1.hi.z
+    int4 n3;    // child0, child1, count0, count1
+};
+
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// Error-reporting helpers: every entry point returns a pbg status and keeps
+// the text of the last failure in a thread-local string.
+void set_last_error(const std::string& msg);
+int cuda_status(cudaError_t e, const char* what);
+
+#define PBG_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_status(e_, #call); \
+    } while (0)
+
+int ensure(DeviceBuffer& b, size_t bytes);
+void release(DeviceBuffer& b);
+
+// Host-built SAH BVH over the triangles (bvh_build.cpp).  order[i] = the
+// original index of the i-th triangle in leaf order.
+struct HostBvh {
+    std::vector<BvhNode> nodes;
+    std::vector<int32_t> order;
+    int max_depth = 0;
+    int32_t unculled = 0;  // order[0, unculled): degenerate, outside the tree
+};
+bool triangle_degenerate(const float* v9);
+void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out);
+
+// Per-batch device scratch owned by a scene.
+struct Work {
+    DeviceBuffer ray_o, ray_d, valid, prim, t, b1, b2, occ, keys, stage, perm, perm_tmp, mkeys,
+        mkeys_tmp, hist, nodes, counters, geo;
+    int64_t cap = 0;
+};
+
+}  // namespace pbg
+
+struct pbg_scene {
+    int device = 0;
+    int32_t accel = 0;
+    pbg_params params{};
+    int64_t ntri = 0;
+    cudaStream_t stream = nullptr;
+    pbg::DeviceBuffer tris;    // TriRec[ntri], in traversal order (c.w = original index)
+    pbg::DeviceBuffer tri9;    // original vertices, float[9*ntri]
+    pbg::DeviceBuffer uv6;     // optional per-triangle uvs, float[6*ntri]
+    pbg::DeviceBuffer bvh;     // BvhNode[] (ray-bvh)
+    int64_t bvh_nodes = 0;
+    int bvh_depth = 0;
+    int32_t unculled = 0;      // records [0, unculled) are tested by every ray
+    float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
+    pbg::DeviceBuffer err;     // int[4] device status words
+    pbg::Work work;
+    pbg_counters counters{};
+};
+
+namespace pbg {
+
+// Kernel launchers (one translation unit each).
+int launch_pack_rays(pbg_scene* s, const float* stage, int64_t n, float4* o, float4* d,
+                     cudaStream_t st);
+int naive_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                  int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
+int naive_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                   uint8_t* occ, cudaStream_t st);
+int bvh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
+int bvh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                 uint8_t* occ, cudaStream_t st);
+int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+               int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
+int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                uint8_t* occ, cudaStream_t st);
+int hit_geometry(pbg_scene* s, const float4* o, const float4* d, const int32_t* prim,
+                 const float* t, const float* b1, const float* b2, int64_t n, float* out14,
+                 cudaStream_t st);
+int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order);
+int check_device_status(pbg_scene* s, cudaStream_t st);
+
+}  // namespace pbg
