@@ -1,0 +1,438 @@
+"""Benchmark of the ray-batch intersection path (one JSON line on rank 0).
+
+Workload (default): the ray-hierarchy direct-lighting frame -- 1024x1024,
+4 spp jittered camera rays (4,194,304) into the 181,250-triangle terrain +
+40 icospheres scene, nearest hit through Accelerator "rayhierarchy", then
+4 shadow batches (one per area-light sample, as DirectLightingIntegrator's
+batch path issues them, core/integrator.cpp:358-455) of any-hit rays from
+every hit point to seeded points on the 1x1 area light.  One step = that
+frame's five batch calls (1 nearest + 4 any-hit), hierarchy rebuilt per call.
+
+value     rays completed per second with rays and shadow rays resident in HBM
+          (device-pointer entry points), CUDA-event time per step, L2 flushed
+          between steps (outside the timed region).
+e2e       the same frame through the host-buffer C ABI calls (pbg_intersect /
+          pbg_occluded) with pinned host arrays: H2D of rays, D2H of results.
+roofline  the dominant kernel (the traversal kernels), algorithmic bytes over
+          their event-timed duration, against the measured HBM peak.
+cpu_baseline  the oracle's SAH-BVH port of pbrt's CPU path on the host cores,
+          on a bounded sample of the same rays.
+
+--impl reference runs the reference's CPU path (the oracle port: the
+reference's own build needs its source tree, which the GPU host lacks) on
+all host cores and prints the same line with "impl": "reference".
+--gpus N under torchrun: one replica of the frame per GPU ("replicas only":
+rays are independent, nothing is exchanged).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import pbg_import  # noqa: E402
+
+pbg_import.load()
+
+METRIC = "Mrays/s nearest+any-hit at exact hit-ID match: plain vs learned-ordered, 1 GB300"
+L2_BYTES = 129 * 1024 * 1024
+CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(scale: float = 1.0):
+    from pbrt_gb300 import scenes as S
+    sc = S.terrain_icospheres(seed=2)
+    res = int(1024 * scale)
+    rays = S.pinhole_rays(res, res, CAMERA["eye"], CAMERA["target"], CAMERA["fov"], spp=4,
+                          jitter_seed=7)
+    return sc, rays
+
+
+def shadow_batches(rays, prim, t, light_quad, nsamples=4, seed=13):
+    """Shadow segments from each hit point to seeded points on the quad light,
+    one batch per light sample (core/integrator.cpp:358-455); rays that
+    missed are invalid in every batch.  mint = rayEpsilon = 1e-3 t
+    (shapes/trianglemesh.cpp:190), maxt = dist (1 - 1e-3) (core/light.h:79-84)."""
+    g = np.random.default_rng(seed)
+    n = rays.shape[1]
+    hit = prim >= 0
+    p = rays[0:3] + rays[3:6] * np.where(hit, t, 0)[None]
+    q0, q1, q3 = light_quad[0].astype(np.float64), light_quad[1].astype(np.float64), light_quad[3].astype(np.float64)
+    out = []
+    for _ in range(nsamples):
+        u, v = g.random(n), g.random(n)
+        lp = q0[:, None] + (q1 - q0)[:, None] * u[None] + (q3 - q0)[:, None] * v[None]
+        d = lp - p
+        dist = np.sqrt((d ** 2).sum(0))
+        dist = np.where(dist > 0, dist, 1.0)
+        r = np.empty((8, n), np.float32)
+        r[0:3] = p
+        r[3:6] = d / dist[None]
+        r[6] = np.where(hit, 1e-3 * t, 0.0)
+        r[7] = dist * (1 - 1e-3)
+        out.append(r)
+    return out, hit.astype(np.uint8)
+
+
+def to_dev(rays):
+    import torch
+    o = torch.from_numpy(np.ascontiguousarray(np.stack([rays[0], rays[1], rays[2], rays[6]], 1)))
+    d = torch.from_numpy(np.ascontiguousarray(np.stack([rays[3], rays[4], rays[5], rays[7]], 1)))
+    return o.cuda(), d.cuda()
+
+
+def run_gpu(args, rank, world, dev):
+    import torch
+    from pbrt_gb300 import accel as A
+    torch.cuda.set_device(dev)
+    sc, rays = make_workload()
+    tris = sc["tris"]
+    n = rays.shape[1]
+    acc = A.MakeAccelerator(args.accel, tris, {"device": dev})
+    stream = torch.cuda.Stream()
+    o4, d4 = to_dev(rays)
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    tt, b1, b2 = (torch.empty(n, device="cuda") for _ in range(3))
+    with torch.cuda.stream(stream):
+        acc.intersect_device(o4, d4, prim, tt, b1, b2, stream=stream)
+    stream.synchronize()
+    hp, ht = prim.cpu().numpy(), tt.cpu().numpy()
+    shadows, hitmask = shadow_batches(rays, hp, ht, sc["area_light_quad"])
+    sdev = [to_dev(s) for s in shadows]
+    valid = torch.from_numpy(hitmask).cuda()
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    nhit = int(hitmask.sum())
+    rays_per_step = n + len(shadows) * nhit
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        acc.intersect_device(o4, d4, prim, tt, b1, b2, stream=stream)
+        for so, sd in sdev:
+            acc.occluded_device(so, sd, occ, valid=valid, stream=stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+    acc.stats()
+    launches0 = acc.stats()["kernel_launches"]
+    acc.profile(True)
+    times = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)  # evict L2 between steps, outside the timed region
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step()
+                e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    st = acc.stats()
+    acc.profile(False)
+    launches = st["kernel_launches"] - launches0
+    step_ms = sum(times) / len(times)
+    if world > 1:
+        t = torch.tensor([step_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+
+    # dominant kernel: the traversal stage (event-timed inside the library)
+    trav_ms = st["stage_ms"]["traverse"]
+    trav_launches = st["timed_launches"]["traverse"]
+    valid_shadow = nhit
+    # algorithmic bytes per traversal launch (averaged over the step's five):
+    # rays read once (32 B), scene records read once (48 B + 16 B sphere),
+    # results written once (8 B key nearest, 1 bit any-hit)
+    step_bytes = (n * 32 + n * 8 + len(shadows) * (valid_shadow * 32 + valid_shadow / 8)
+                  + (1 + len(shadows)) * len(tris) * 64)
+    per_launch_bytes = step_bytes / (1 + len(shadows))
+    avg_launch_ms = trav_ms / max(trav_launches, 1)
+    hbm, peak_kind = peaks()
+    achieved = per_launch_bytes / (avg_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tj = os.path.join(ROOT, "profiles", f"traffic_{args.accel}.json")
+    if os.path.exists(tj):
+        traffic = json.load(open(tj)).get("bytes_per_launch")
+
+    # parity sample: hit IDs of a ray sample against the oracle port (CPU)
+    parity = None
+    if rank == 0 and not args.no_parity:
+        from oracle import oracle as O
+        sel = np.arange(0, n, max(1, n // 8192))
+        got = prim.cpu().numpy()[sel]
+        B = O.BVH(tris)
+        want = B.nearest(rays[:, sel])[0]
+        occ_got = occ.cpu().numpy()[sel]
+        occ_want = B.anyhit(shadows[-1][:, sel], valid=hitmask[sel])
+        parity = {"sample_rays": int(2 * len(sel)),
+                  "hit_id_mismatches": int((got != want).sum()),
+                  "occlusion_mismatches": int((occ_got != occ_want).sum())}
+
+    e2e = run_e2e(args, acc, rays, shadows, hitmask, rays_per_step) if rank == 0 else None
+    cpu = cpu_baseline(tris, rays, shadows, hitmask) if (rank == 0 and world == 1 and not args.no_cpu) else None
+    if rank == 0:
+        clocks = clk.summary()
+        value = rays_per_step * world / (step_ms * 1e-3) / 1e6
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded terrain + icospheres, seeded jitter and light samples)",
+            "config": {"workload": "rayhierarchy direct lighting 1024x1024x4spp, 181,250 triangles, "
+                                   "1 nearest + 4 shadow batches per frame",
+                       "accelerator": args.accel, "rays_per_step": rays_per_step,
+                       "primary_rays": n, "shadow_rays": len(shadows) * nhit,
+                       "triangles": int(len(tris)), "parallelism": f"replicas x{world}",
+                       "l2": "flushed between steps (256 MB write), outside the timed region"},
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
+                         "unit": "GB/s", "frac": round(achieved / hbm, 5),
+                         "traffic": traffic, "kernel": "traversal (rh_traverse / bvh / naive)",
+                         "algorithmic_bytes_per_launch": int(per_launch_bytes),
+                         "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind},
+            "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in st["stage_ms"].items()},
+            "gpu_launches": int(launches),
+            "cpu_baseline": cpu,
+            "parity": parity,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(args, acc, rays, shadows, hitmask, rays_per_step):
+    """Host-buffer frame through the C ABI: pinned arrays in and out."""
+    import torch
+    n = rays.shape[1]
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    hr = pinned((8, n), torch.float32)
+    hr[...] = rays
+    hs = []
+    for s in shadows:
+        a = pinned((8, n), torch.float32)
+        a[...] = s
+        hs.append(a)
+    hv = pinned((n,), torch.uint8)
+    hv[...] = hitmask
+    out_p = pinned((n,), torch.int32)
+    out_t, out_b1, out_b2 = (pinned((n,), torch.float32) for _ in range(3))
+    out_o = pinned((n,), torch.uint8)
+    import ctypes as C
+    from pbrt_gb300 import _lib as L
+    lib = L.lib()
+
+    def rays_struct(a, valid):
+        return acc._rays_struct(a, valid)
+
+    def frame():
+        h = L.Hits(out_p.ctypes.data_as(C.POINTER(C.c_int32)), out_t.ctypes.data_as(C.POINTER(C.c_float)),
+                   out_b1.ctypes.data_as(C.POINTER(C.c_float)), out_b2.ctypes.data_as(C.POINTER(C.c_float)))
+        rs = rays_struct(hr, None)
+        L.check(lib.pbg_intersect(acc.handle, C.byref(rs), n, C.byref(h)), "pbg_intersect")
+        for a in hs:
+            rs2 = rays_struct(a, hv)
+            L.check(lib.pbg_occluded(acc.handle, C.byref(rs2), n, out_o.ctypes.data), "pbg_occluded")
+
+    for _ in range(max(1, args.warmup)):
+        frame()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    k = max(1, args.steps)
+    for _ in range(k):
+        frame()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / k
+    h2d = n * 32 + len(shadows) * (n * 32 + n)
+    d2h = n * 16 + len(shadows) * n
+    return {"value": round(rays_per_step / (ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
+            "ms_per_step": round(ms, 3), "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "api": "pbg_intersect + 4 x pbg_occluded (host buffers)"}
+
+
+def cpu_sample(rays, shadows, hitmask, frac):
+    n = rays.shape[1]
+    sel = np.arange(0, n, max(1, int(round(1 / frac))))
+    return sel
+
+
+def cpu_baseline(tris, rays, shadows, hitmask, target_s: float = 12.0, threads=None):
+    """Oracle port of pbrt's CPU BVH path, all host cores, bounded sample."""
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    B = O.BVH(tris)
+    n = rays.shape[1]
+    # calibrate on a small slice, then size the sample to ~target_s seconds
+    sel = np.arange(0, n, 512)
+    t0 = time.perf_counter()
+    B.nearest(rays[:, sel], threads=threads)
+    for s in shadows:
+        B.anyhit(s[:, sel], valid=hitmask[sel], threads=threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    stride = max(1, int(512 * dt / target_s))
+    sel = np.arange(0, n, stride)
+    t0 = time.perf_counter()
+    B.nearest(rays[:, sel], threads=threads)
+    nr = len(sel)
+    for s in shadows:
+        B.anyhit(s[:, sel], valid=hitmask[sel], threads=threads)
+        nr += int(hitmask[sel].sum())
+    dt = time.perf_counter() - t0
+    return {"value": round(nr / dt / 1e6, 3), "unit": "Mrays/s", "cores": int(threads),
+            "kind": "port", "seconds": round(dt, 2),
+            "sample": f"every {stride}th camera ray of the frame ({len(sel)} rays) and its 4 shadow rays; "
+                      "SAH BVH + pbrt's triangle test (oracle/pbrt_oracle.c)"}
+
+
+def run_reference(args):
+    """The reference's CPU path for this frame on the host cores."""
+    sc, rays = make_workload()
+    tris = sc["tris"]
+    # hit points for the shadow batches come from the CPU path itself
+    from oracle import oracle as O
+    B = O.BVH(tris)
+    n = rays.shape[1]
+    threads = os.cpu_count() or 1
+    stride = 64
+    sel = np.arange(0, n, stride)
+    sub = np.ascontiguousarray(rays[:, sel])
+    times = []
+    nrays = 0
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        prim, t, _, _ = B.nearest(sub, threads=threads)
+        shadows, hit = shadow_batches(sub, prim, t, sc["area_light_quad"])
+        nr = sub.shape[1]
+        for s in shadows:
+            B.anyhit(s, valid=hit, threads=threads)
+            nr += int(hit.sum())
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            nrays = nr
+    sec = sum(times) / len(times)
+    value = nrays / sec / 1e6
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded terrain + icospheres)", "impl": "reference",
+            "config": {"workload": "rayhierarchy direct lighting 1024x1024x4spp, 181,250 triangles, "
+                                   "1 nearest + 4 shadow batches per frame",
+                       "sample": f"every {stride}th camera ray per step"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads,
+                             "kind": "port",
+                             "sample": f"every {stride}th camera ray ({len(sel)}) + 4 shadow rays each"},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--accel", default="rayhierarchy", choices=["naive", "rayhierarchy", "ray-bvh"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    run_gpu(args, rank, world, local)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -85,11 +85,17 @@ typedef struct pbg_hits {
 } pbg_hits;
 
 typedef struct pbg_counters {
-    uint64_t rays_nearest;   /* rays traced by intersect calls */
-    uint64_t rays_occluded;  /* rays traced by occluded calls */
+    uint64_t rays_nearest;    /* rays traced by intersect calls */
+    uint64_t rays_occluded;   /* rays traced by occluded calls */
     uint64_t calls;
-    uint64_t bvh_nodes;      /* nodes of the scene's BVH (ray-bvh) */
-    uint64_t reserved[12];
+    uint64_t bvh_nodes;       /* nodes of the scene's BVH (ray-bvh) */
+    uint64_t kernel_launches; /* kernels this scene has launched */
+    uint64_t timed_launches[4]; /* launches timed per stage (profiling on) */
+    uint64_t reserved[7];
+    /* Device time per stage in ms while profiling is on (CUDA events around
+     * each launch on its stream): [0] ray sort, [1] hierarchy build,
+     * [2] traversal (the intersection kernels), [3] finalize / other. */
+    double stage_ms[4];
 } pbg_counters;
 
 /* Library version, e.g. "pbrt-gb300 1.0 (sm_103a)". */
@@ -149,9 +155,13 @@ int pbg_hit_geometry_device(pbg_scene* scene, const float* o4, const float* d4,
                             const int32_t* prim, const float* t, const float* b1,
                             const float* b2, int64_t n, float* out14, void* stream);
 
-/* Counters (replaces the GPU_TIMES / STAT_* printouts,
- * core/GPUparallel.h:532-538). */
-int pbg_stats(const pbg_scene* scene, pbg_counters* out);
+/* Counters and per-stage device times (replaces the GPU_TIMES / STAT_*
+ * printouts, core/GPUparallel.h:532-538 and rayhierarchy.cpp:229-239).
+ * Reading them synchronises the scene's pending timing events. */
+int pbg_stats(pbg_scene* scene, pbg_counters* out);
+/* Turns per-stage event timing on (1) or off (0) and clears the stage
+ * times.  Off by default: timing adds two event records per launch. */
+int pbg_profile(pbg_scene* scene, int on);
 
 #ifdef __cplusplus
 }

@@ -52,7 +52,12 @@ class Hits(C.Structure):
 
 class Counters(C.Structure):
     _fields_ = [("rays_nearest", C.c_uint64), ("rays_occluded", C.c_uint64),
-                ("calls", C.c_uint64), ("bvh_nodes", C.c_uint64), ("reserved", C.c_uint64 * 12)]
+                ("calls", C.c_uint64), ("bvh_nodes", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("timed_launches", C.c_uint64 * 4), ("reserved", C.c_uint64 * 7),
+                ("stage_ms", C.c_double * 4)]
+
+
+STAGES = ("sort", "build", "traverse", "other")
 
 
 _lib = None
@@ -93,6 +98,7 @@ def lib():
     L.pbg_hit_geometry.argtypes = [vp, C.POINTER(Rays), C.POINTER(Hits), C.c_int64, vp]
     L.pbg_hit_geometry_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64, vp, vp]
     L.pbg_stats.argtypes = [vp, C.POINTER(Counters)]
+    L.pbg_profile.argtypes = [vp, C.c_int]
     _lib = L
     return L
 

@@ -146,7 +146,14 @@ class Aggregate:
         c = L.Counters()
         L.check(L.lib().pbg_stats(self.handle, C.byref(c)), "pbg_stats")
         return {"rays_nearest": c.rays_nearest, "rays_occluded": c.rays_occluded,
-                "calls": c.calls, "bvh_nodes": c.bvh_nodes}
+                "calls": c.calls, "bvh_nodes": c.bvh_nodes, "kernel_launches": c.kernel_launches,
+                "timed_launches": dict(zip(L.STAGES, list(c.timed_launches))),
+                "stage_ms": dict(zip(L.STAGES, list(c.stage_ms)))}
+
+    def profile(self, on: bool = True) -> None:
+        """Per-stage CUDA-event timing (the GPU_TIMES printouts of the
+        reference, core/GPUparallel.h:532-538)."""
+        L.check(L.lib().pbg_profile(self.handle, int(on)), "pbg_profile")
 
 
 class NaiveAccel(Aggregate):

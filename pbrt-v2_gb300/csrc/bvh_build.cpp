@@ -267,3 +267,44 @@ void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out) {
 }
 
 }  // namespace pbg
+
+namespace pbg {
+
+// Triangles by the Morton code of their centroids (10 bits per axis over the
+// scene box): neighbouring records are neighbours in space, so the threads
+// of a warp walk similar parts of a ray hierarchy.
+void morton_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order) {
+    order->resize((size_t)ntri);
+    if (ntri == 0) return;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    std::vector<float> c((size_t)ntri * 3);
+    for (int64_t i = 0; i < ntri; ++i)
+        for (int a = 0; a < 3; ++a) {
+            const float* v = tri9 + 9 * i;
+            float x = (v[a] + v[3 + a] + v[6 + a]) * (1.f / 3.f);
+            if (!std::isfinite(x)) x = 0.f;
+            c[3 * i + a] = x;
+            lo[a] = std::min(lo[a], x);
+            hi[a] = std::max(hi[a], x);
+        }
+    auto spread10 = [](uint64_t v) {
+        uint64_t r = 0;
+        for (int b = 0; b < 10; ++b) r |= ((v >> b) & 1ull) << (3 * b);
+        return r;
+    };
+    std::vector<std::pair<uint64_t, int32_t>> keys((size_t)ntri);
+    for (int64_t i = 0; i < ntri; ++i) {
+        uint64_t k = 0;
+        for (int a = 0; a < 3; ++a) {
+            float ext = hi[a] - lo[a];
+            float q = ext > 0.f ? (c[3 * i + a] - lo[a]) / ext * 1023.f : 0.f;
+            uint64_t qi = (uint64_t)std::min(std::max(q, 0.f), 1023.f);
+            k |= spread10(qi) << (2 - a);
+        }
+        keys[(size_t)i] = {k, (int32_t)i};
+    }
+    std::sort(keys.begin(), keys.end());
+    for (int64_t i = 0; i < ntri; ++i) (*order)[(size_t)i] = keys[(size_t)i].second;
+}
+
+}  // namespace pbg

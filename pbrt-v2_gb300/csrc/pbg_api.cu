@@ -12,6 +12,7 @@
 //     hit geometry.
 // Errors become status codes; nothing aborts (the reference calls Severe(),
 // core/error.cpp:130).
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -176,7 +177,9 @@ int launch_pack_rays(pbg_scene* s, const float* stage, int64_t n, float4* o, flo
                      cudaStream_t st) {
     (void)s;
     if (n <= 0) return PBG_OK;
+    prof_begin(s, st);
     pack_rays_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(stage, n, o, d);
+    prof_end(s, st, kStageOther, 1);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
 }
@@ -185,10 +188,58 @@ int hit_geometry(pbg_scene* s, const float4* o, const float4* d, const int32_t* 
                  const float* t, const float* b1, const float* b2, int64_t n, float* out14,
                  cudaStream_t st) {
     if (n <= 0) return PBG_OK;
+    prof_begin(s, st);
     hit_geometry_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(
         (const float*)s->tri9.ptr, (const float*)s->uv6.ptr, o, d, prim, t, b1, b2, n, out14);
+    prof_end(s, st, kStageOther, 1);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
+}
+
+static cudaEvent_t prof_event(pbg_scene* s) {
+    cudaEvent_t e = nullptr;
+    if (!s->prof.pool.empty()) {
+        e = s->prof.pool.back();
+        s->prof.pool.pop_back();
+        return e;
+    }
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+static thread_local cudaEvent_t g_open_event = nullptr;
+
+void prof_begin(pbg_scene* s, cudaStream_t st) {
+    if (!s->prof.on) return;
+    g_open_event = prof_event(s);
+    if (g_open_event) cudaEventRecord(g_open_event, st);
+}
+
+void prof_end(pbg_scene* s, cudaStream_t st, int stage, int launches) {
+    s->counters.kernel_launches += (uint64_t)launches;
+    if (!s->prof.on || !g_open_event) return;
+    cudaEvent_t b = prof_event(s);
+    if (!b) return;
+    cudaEventRecord(b, st);
+    s->prof.pending.push_back({g_open_event, b, stage});
+    s->counters.timed_launches[stage] += (uint64_t)launches;
+    g_open_event = nullptr;
+}
+
+static void prof_collect(pbg_scene* s) {
+    for (auto& r : s->prof.pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess)
+            s->counters.stage_ms[r.stage] += ms;
+        else
+            cudaGetLastError();
+        s->prof.pool.push_back(r.a);
+        s->prof.pool.push_back(r.b);
+    }
+    s->prof.pending.clear();
 }
 
 int check_device_status(pbg_scene* s, cudaStream_t st) {
@@ -206,14 +257,47 @@ int check_device_status(pbg_scene* s, cudaStream_t st) {
     return PBG_OK;
 }
 
+// Bounding sphere of each record for the ray-hierarchy node test: box
+// centre, farthest vertex, padded by 2^-20 relative and 2^-16 of the
+// centre's magnitude; degenerate triangles get an infinite radius (no node
+// may cull them).
+static void triangle_spheres(const float* tri9, const int32_t* order, int64_t ntri,
+                             std::vector<float4>* out) {
+    out->resize((size_t)ntri);
+    for (int64_t i = 0; i < ntri; ++i) {
+        const float* v = tri9 + 9 * (int64_t)(order ? order[i] : i);
+        float c[3];
+        for (int a = 0; a < 3; ++a) {
+            float lo = fminf(v[a], fminf(v[3 + a], v[6 + a]));
+            float hi = fmaxf(v[a], fmaxf(v[3 + a], v[6 + a]));
+            c[a] = 0.5f * (lo + hi);
+        }
+        double r = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            double dx = (double)v[3 * k] - c[0], dy = (double)v[3 * k + 1] - c[1],
+                   dz = (double)v[3 * k + 2] - c[2];
+            r = fmax(r, sqrt(dx * dx + dy * dy + dz * dz));
+        }
+        float rr = (float)(r * (1.0 + 0x1p-20) +
+                           (fabs(c[0]) + fabs(c[1]) + fabs(c[2])) * 0x1p-16 + 1e-30);
+        if (triangle_degenerate(v) || !std::isfinite(rr)) rr = INFINITY;
+        (*out)[(size_t)i] = make_float4(c[0], c[1], c[2], rr);
+    }
+}
+
 int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order) {
     const int64_t ntri = s->ntri;
-    int rc = ensure(s->tri9, (size_t)(ntri > 0 ? ntri : 1) * 9 * sizeof(float));
-    if (rc) return rc;
-    rc = ensure(s->tris, (size_t)(ntri > 0 ? ntri : 1) * sizeof(TriRec));
-    if (rc) return rc;
+    const size_t nt = (size_t)(ntri > 0 ? ntri : 1);
+    int rc;
+    if ((rc = ensure(s->tri9, nt * 9 * sizeof(float))) || (rc = ensure(s->tris, nt * sizeof(TriRec))) ||
+        (rc = ensure(s->tri_pos, nt * sizeof(int32_t))) || (rc = ensure(s->spheres, nt * sizeof(float4))))
+        return rc;
     if (ntri == 0) return PBG_OK;
     PBG_CUDA(cudaMemcpyAsync(s->tri9.ptr, tri9_host, (size_t)ntri * 9 * sizeof(float),
+                             cudaMemcpyHostToDevice, s->stream));
+    std::vector<float4> sph;
+    triangle_spheres(tri9_host, order, ntri, &sph);
+    PBG_CUDA(cudaMemcpyAsync(s->spheres.ptr, sph.data(), (size_t)ntri * sizeof(float4),
                              cudaMemcpyHostToDevice, s->stream));
     DeviceBuffer dorder;
     if (order) {
@@ -223,7 +307,8 @@ int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order)
                                  cudaMemcpyHostToDevice, s->stream));
     }
     build_tris_kernel<<<(unsigned)((ntri + 255) / 256), 256, 0, s->stream>>>(
-        (const float*)s->tri9.ptr, (const int32_t*)dorder.ptr, ntri, (TriRec*)s->tris.ptr, nullptr);
+        (const float*)s->tri9.ptr, (const int32_t*)dorder.ptr, ntri, (TriRec*)s->tris.ptr,
+        (int32_t*)s->tri_pos.ptr);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     release(dorder);
@@ -373,7 +458,12 @@ int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t 
             s->scene_hi[a] = v > s->scene_hi[a] ? v : s->scene_hi[a];
         }
     HostBvh hb;
+    std::vector<int32_t> morder;
     const int32_t* order = nullptr;
+    if (accel == PBG_ACCEL_RAYHIERARCHY) {
+        morton_triangle_order(tri9, ntri, &morder);
+        order = morder.empty() ? nullptr : morder.data();
+    }
     if (accel == PBG_ACCEL_RAYBVH) {
         build_bvh(tri9, ntri, s->params.max_bvh_prim > 0 ? s->params.max_bvh_prim : 4, &hb);
         order = hb.order.empty() ? nullptr : hb.order.data();
@@ -401,15 +491,21 @@ void pbg_scene_destroy(pbg_scene* s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    prof_collect(s);
+    for (cudaEvent_t e : s->prof.pool) cudaEventDestroy(e);
+    s->prof.pool.clear();
     release(s->tris);
     release(s->tri9);
     release(s->uv6);
     release(s->bvh);
+    release(s->spheres);
+    release(s->tri_pos);
     release(s->err);
     Work& w = s->work;
-    DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.valid, &w.prim, &w.t, &w.b1, &w.b2,
-                           &w.occ, &w.keys, &w.stage, &w.perm, &w.perm_tmp, &w.mkeys,
-                           &w.mkeys_tmp, &w.hist, &w.nodes, &w.counters, &w.geo};
+    DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.ray_o2, &w.ray_d2, &w.valid, &w.prim,
+                           &w.t, &w.b1, &w.b2, &w.occ, &w.keys, &w.stage, &w.perm,
+                           &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
+                           &w.leafmask, &w.counters, &w.geo};
     for (DeviceBuffer* b : all) release(*b);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -551,9 +647,23 @@ int pbg_hit_geometry(pbg_scene* s, const pbg_rays* r, const pbg_hits* h, int64_t
     return PBG_OK;
 }
 
-int pbg_stats(const pbg_scene* s, pbg_counters* out) {
+int pbg_stats(pbg_scene* s, pbg_counters* out) {
     if (!s || !out) return PBG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->device);
+    prof_collect(s);
     *out = s->counters;
+    return PBG_OK;
+}
+
+int pbg_profile(pbg_scene* s, int on) {
+    if (!s) return PBG_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->device);
+    prof_collect(s);
+    s->prof.on = on != 0;
+    for (int k = 0; k < 4; ++k) {
+        s->counters.stage_ms[k] = 0.0;
+        s->counters.timed_launches[k] = 0;
+    }
     return PBG_OK;
 }
 

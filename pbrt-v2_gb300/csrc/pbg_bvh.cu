@@ -185,9 +185,11 @@ int bvh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
     const int32_t* perm = nullptr;
     int rc = ray_order(s, o, d, n, &perm, st);
     if (rc) return rc;
+    prof_begin(s, st);
     bvh_kernel<false><<<(unsigned)((n + kBvhThreads - 1) / kBvhThreads), kBvhThreads, 0, st>>>(
         (const BvhNode*)s->bvh.ptr, (const TriRec*)s->tris.ptr, s->unculled, o, d, valid, perm, n, prim, t, b1,
         b2, nullptr, (int*)s->err.ptr);
+    prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
 }
@@ -198,9 +200,11 @@ int bvh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* 
     const int32_t* perm = nullptr;
     int rc = ray_order(s, o, d, n, &perm, st);
     if (rc) return rc;
+    prof_begin(s, st);
     bvh_kernel<true><<<(unsigned)((n + kBvhThreads - 1) / kBvhThreads), kBvhThreads, 0, st>>>(
         (const BvhNode*)s->bvh.ptr, (const TriRec*)s->tris.ptr, s->unculled, o, d, valid, perm, n, nullptr,
         nullptr, nullptr, nullptr, occ, (int*)s->err.ptr);
+    prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
 }

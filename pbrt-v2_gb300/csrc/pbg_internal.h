@@ -21,6 +21,17 @@ struct __align__(16) BvhNode {
     int4 n3;    // child0, child1, count0, count1
 };
 
+// Event pairs around launches, summed per stage when counters are read.
+struct Profiler {
+    bool on = false;
+    struct Rec {
+        cudaEvent_t a, b;
+        int stage;
+    };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+};
+
 struct DeviceBuffer {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -53,8 +64,8 @@ void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out);
 
 // Per-batch device scratch owned by a scene.
 struct Work {
-    DeviceBuffer ray_o, ray_d, valid, prim, t, b1, b2, occ, keys, stage, perm, perm_tmp, mkeys,
-        mkeys_tmp, hist, nodes, counters, geo;
+    DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
+        perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo;
     int64_t cap = 0;
 };
 
@@ -70,6 +81,8 @@ struct pbg_scene {
     pbg::DeviceBuffer tri9;    // original vertices, float[9*ntri]
     pbg::DeviceBuffer uv6;     // optional per-triangle uvs, float[6*ntri]
     pbg::DeviceBuffer bvh;     // BvhNode[] (ray-bvh)
+    pbg::DeviceBuffer spheres; // float4 bounding sphere per record (rayhierarchy)
+    pbg::DeviceBuffer tri_pos; // original index -> record position
     int64_t bvh_nodes = 0;
     int bvh_depth = 0;
     int32_t unculled = 0;      // records [0, unculled) are tested by every ray
@@ -77,6 +90,7 @@ struct pbg_scene {
     pbg::DeviceBuffer err;     // int[4] device status words
     pbg::Work work;
     pbg_counters counters{};
+    pbg::Profiler prof;
 };
 
 namespace pbg {
@@ -100,6 +114,13 @@ int hit_geometry(pbg_scene* s, const float4* o, const float4* d, const int32_t* 
                  const float* t, const float* b1, const float* b2, int64_t n, float* out14,
                  cudaStream_t st);
 int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order);
+void morton_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order);
 int check_device_status(pbg_scene* s, cudaStream_t st);
+
+// Stage timing around one launch (no-ops unless profiling is on); stages:
+// 0 ray sort, 1 hierarchy build, 2 traversal, 3 finalize / other.
+enum { kStageSort = 0, kStageBuild = 1, kStageTraverse = 2, kStageOther = 3 };
+void prof_begin(pbg_scene* s, cudaStream_t st);
+void prof_end(pbg_scene* s, cudaStream_t st, int stage, int launches);
 
 }  // namespace pbg

@@ -162,8 +162,10 @@ int finalize_keys(pbg_scene* s, const int32_t* pos, const float4* o, const float
                   float* b2, cudaStream_t st) {
     if (n <= 0) return PBG_OK;
     const int threads = 256;
+    prof_begin(s, st);
     finalize_keys_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, st>>>(
         (const TriRec*)s->tris.ptr, pos, o, d, keys, n, prim, t, b1, b2);
+    prof_end(s, st, kStageOther, 1);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
 }
@@ -200,9 +202,11 @@ int naive_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t*
         keys = (unsigned long long*)s->work.keys.ptr;
         PBG_CUDA(cudaMemsetAsync(keys, 0, (size_t)n * sizeof(unsigned long long), st));
     }
+    prof_begin(s, st);
     naive_kernel<false><<<grid, kNaiveThreads, 0, st>>>((const TriRec*)s->tris.ptr, s->ntri, per, o,
                                                         d, valid, n, prim, t, b1, b2, keys, nullptr,
                                                         (int*)s->err.ptr);
+    prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
     if (splits > 1) return finalize_keys(s, nullptr, o, d, keys, n, prim, t, b1, b2, st);
     return PBG_OK;
@@ -216,9 +220,11 @@ int naive_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t
     naive_launch_shape(s, n, &per, &splits);
     dim3 grid((unsigned)((n + kNaiveThreads - 1) / kNaiveThreads), splits);
     if (splits > 1) PBG_CUDA(cudaMemsetAsync(occ, 0, (size_t)n, st));
+    prof_begin(s, st);
     naive_kernel<true><<<grid, kNaiveThreads, 0, st>>>((const TriRec*)s->tris.ptr, s->ntri, per, o,
                                                        d, valid, n, nullptr, nullptr, nullptr,
                                                        nullptr, nullptr, occ, (int*)s->err.ptr);
+    prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
 }

@@ -1,0 +1,428 @@
+// pbg_rayhier.cu -- Accelerator "rayhierarchy": a hierarchy over the rays of
+// each batch, rebuilt per call, traversed by the triangles.
+//
+// Reference: RayHieararchy (accelerators/rayhierarchy.cpp:375-1326) builds a
+// quadtree over the batch's 2-D ray image -- leaves of chunkX x chunkY rays
+// bounded by a 6-D box (origin AABB + direction AABB, bin/cl/rayhconstruct6DB.cl),
+// parents by 2x2 merges (levelConstruct6DB.cl) -- and launches one thread per
+// triangle that walks the tree with a global-memory stack
+// (intersection6DB.cl:6-120), racing on tHit and repairing the races with
+// extra passes (yetAnotherIntersection6DB.cl).
+//
+// Here:
+//   build     rays sorted by 6-D Morton code (pbg_rayorder.cu) and gathered;
+//             a leaf is 32 consecutive rays (one warp builds it with shuffle
+//             reductions); parents merge 4 children.  A node is bounded by an
+//             origin sphere (centre, radius), a direction cone (unit axis,
+//             cos/sin of the half-angle) and the farthest reach of its rays
+//             (max maxt*|d|).
+//   traverse  one thread per triangle (triangles sorted by the Morton code of
+//             their centroids, so a warp's triangles are neighbours), private
+//             stack, node test = "can any ray of the node come within R of the
+//             triangle's bounding sphere", leaf test = the exact test per ray.
+//             Nearest hits merge through a 64-bit atomicMax on (t, index)
+//             keys -- race-free by construction, no repair pass; a thread
+//             reads a ray's current key first and filters with that t.
+//             Any-hit keeps one occlusion bit per ray (a 32-bit mask per
+//             leaf) and skips leaves whose rays are all occluded.
+#include "pbg_internal.h"
+
+namespace pbg {
+
+int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+             const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st);
+
+constexpr int kLeafRays = 32;
+constexpr int kFan = 4;
+constexpr int kMaxLevels = 16;
+constexpr int kRhThreads = 128;
+constexpr int kRhStack = 48;
+
+struct __align__(16) RayNode {
+    float4 a;  // origin sphere: centre.xyz, radius
+    float4 b;  // cone axis.xyz, cos(half-angle)
+    float4 c;  // sin(half-angle), reach = max maxt*|d|, count (int bits), unused
+};
+
+struct Levels {
+    int64_t off[kMaxLevels];
+    int64_t cnt[kMaxLevels];
+    int nlev;
+};
+
+__device__ __forceinline__ float round_up_rel(float x) { return fmaf(fabsf(x), 0x1p-20f, x) + 0x1p-126f; }
+
+// ---------------------------------------------------------------- build
+
+__global__ void gather_rays_kernel(const float4* __restrict__ ro, const float4* __restrict__ rd,
+                                   const int32_t* __restrict__ perm, int64_t n,
+                                   float4* __restrict__ so, float4* __restrict__ sd) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t r = perm[i];
+    so[i] = ro[r];
+    sd[i] = rd[r];
+}
+
+// One warp per leaf of 32 sorted rays.
+__global__ void leaf_build_kernel(const float4* __restrict__ so, const float4* __restrict__ sd,
+                                  const uint32_t* __restrict__ skeys, int64_t n, int64_t nleaf,
+                                  RayNode* __restrict__ leaves) {
+    const int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (leaf >= nleaf) return;
+    const int64_t i = leaf * kLeafRays + lane;
+    const bool ok = i < n && skeys[i] != 0xffffffffu;
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+    if (ok) {
+        o = so[i];
+        d = sd[i];
+    }
+    const unsigned full = 0xffffffffu;
+    const int count = __popc(__ballot_sync(full, ok));
+    float lo[3] = {ok ? o.x : INFINITY, ok ? o.y : INFINITY, ok ? o.z : INFINITY};
+    float hi[3] = {ok ? o.x : -INFINITY, ok ? o.y : -INFINITY, ok ? o.z : -INFINITY};
+    const float len = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+    const float il = len > 0.f ? 1.f / len : 0.f;
+    float nx = d.x * il, ny = d.y * il, nz = d.z * il;
+    float sx = ok ? nx : 0.f, sy = ok ? ny : 0.f, sz = ok ? nz : 0.f;
+    float reach = ok ? d.w * len * (1.f + 0x1p-20f) : 0.f;
+    if (ok && !(reach == reach)) reach = INFINITY;  // 0 * inf
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(full, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(full, hi[a], off));
+        }
+        sx += __shfl_xor_sync(full, sx, off);
+        sy += __shfl_xor_sync(full, sy, off);
+        sz += __shfl_xor_sync(full, sz, off);
+        reach = fmaxf(reach, __shfl_xor_sync(full, reach, off));
+    }
+    const float cx = 0.5f * (lo[0] + hi[0]), cy = 0.5f * (lo[1] + hi[1]), cz = 0.5f * (lo[2] + hi[2]);
+    float dist = ok ? sqrtf((o.x - cx) * (o.x - cx) + (o.y - cy) * (o.y - cy) + (o.z - cz) * (o.z - cz)) : 0.f;
+    const float sl = sqrtf(sx * sx + sy * sy + sz * sz);
+    float ax = 0.f, ay = 0.f, az = 1.f;
+    bool axis_ok = sl > 1e-3f * (float)(count > 0 ? count : 1);
+    if (axis_ok) {
+        ax = sx / sl;
+        ay = sy / sl;
+        az = sz / sl;
+    }
+    float cosv = ok ? (axis_ok ? ax * nx + ay * ny + az * nz : -1.f) : 2.f;
+    if (ok && !(len > 0.f && isfinite(len))) cosv = -1.f;
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        dist = fmaxf(dist, __shfl_xor_sync(full, dist, off));
+        cosv = fminf(cosv, __shfl_xor_sync(full, cosv, off));
+    }
+    if (lane == 0) {
+        RayNode nd;
+        if (count == 0) {
+            nd.a = make_float4(0.f, 0.f, 0.f, 0.f);
+            nd.b = make_float4(0.f, 0.f, 1.f, 1.f);
+            nd.c = make_float4(0.f, 0.f, __int_as_float(0), 0.f);
+        } else {
+            // Margins: 2^-20 relative on the radius, 2^-18 on the cone cosine.
+            const float ro_ = round_up_rel(dist);
+            float c = fmaxf(cosv - 0x1p-18f, -1.f);
+            if (c > 1.f) c = 1.f;
+            const float s = fminf(sqrtf(fmaxf(0.f, 1.f - c * c)) + 0x1p-18f, 1.f);
+            nd.a = make_float4(cx, cy, cz, ro_);
+            nd.b = make_float4(ax, ay, az, c);
+            nd.c = make_float4(s, reach, __int_as_float(count), 0.f);
+        }
+        leaves[leaf] = nd;
+    }
+}
+
+// Parent j merges children kFan*j .. kFan*j+kFan-1.
+__global__ void level_build_kernel(const RayNode* __restrict__ child, int64_t nchild,
+                                   RayNode* __restrict__ parent, int64_t nparent) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nparent) return;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float sx = 0.f, sy = 0.f, sz = 0.f, reach = 0.f;
+    int count = 0;
+    RayNode ch[kFan];
+    int nk = 0;
+    for (int k = 0; k < kFan; ++k) {
+        const int64_t c = kFan * j + k;
+        if (c >= nchild) break;
+        ch[nk] = child[c];
+        const int cc = __float_as_int(ch[nk].c.z);
+        if (cc == 0) continue;
+        const float4 a = ch[nk].a;
+        lo[0] = fminf(lo[0], a.x - a.w); hi[0] = fmaxf(hi[0], a.x + a.w);
+        lo[1] = fminf(lo[1], a.y - a.w); hi[1] = fmaxf(hi[1], a.y + a.w);
+        lo[2] = fminf(lo[2], a.z - a.w); hi[2] = fmaxf(hi[2], a.z + a.w);
+        sx += ch[nk].b.x * cc;
+        sy += ch[nk].b.y * cc;
+        sz += ch[nk].b.z * cc;
+        reach = fmaxf(reach, ch[nk].c.y);
+        count += cc;
+        ++nk;
+    }
+    RayNode nd;
+    if (count == 0) {
+        nd.a = make_float4(0.f, 0.f, 0.f, 0.f);
+        nd.b = make_float4(0.f, 0.f, 1.f, 1.f);
+        nd.c = make_float4(0.f, 0.f, __int_as_float(0), 0.f);
+        parent[j] = nd;
+        return;
+    }
+    const float cx = 0.5f * (lo[0] + hi[0]), cy = 0.5f * (lo[1] + hi[1]), cz = 0.5f * (lo[2] + hi[2]);
+    const float sl = sqrtf(sx * sx + sy * sy + sz * sz);
+    const bool axis_ok = sl > 1e-3f * count;
+    float ax = 0.f, ay = 0.f, az = 1.f;
+    if (axis_ok) {
+        ax = sx / sl;
+        ay = sy / sl;
+        az = sz / sl;
+    }
+    float r = 0.f, cmin = 1.f;
+    for (int k = 0; k < nk; ++k) {
+        const float4 a = ch[k].a;
+        const float dx = a.x - cx, dy = a.y - cy, dz = a.z - cz;
+        r = fmaxf(r, sqrtf(dx * dx + dy * dy + dz * dz) + a.w);
+        // cos(angle(axis, child axis) + child half-angle)
+        const float ca = axis_ok ? fminf(1.f, fmaxf(-1.f, ax * ch[k].b.x + ay * ch[k].b.y + az * ch[k].b.z)) : -1.f;
+        const float sa = sqrtf(fmaxf(0.f, 1.f - ca * ca));
+        const float cb = ch[k].b.w, sb = ch[k].c.x;
+        // alpha + beta >= pi  <=>  cos(alpha) <= -cos(beta) (alpha, beta in [0, pi])
+        const float csum = (ca <= -cb) ? -1.f : ca * cb - sa * sb;
+        cmin = fminf(cmin, csum);
+    }
+    const float c = fmaxf(cmin - 0x1p-18f, -1.f);
+    const float s = fminf(sqrtf(fmaxf(0.f, 1.f - c * c)) + 0x1p-18f, 1.f);
+    nd.a = make_float4(cx, cy, cz, round_up_rel(r));
+    nd.b = make_float4(ax, ay, az, c);
+    nd.c = make_float4(s, reach, __int_as_float(count), 0.f);
+    parent[j] = nd;
+}
+
+// --------------------------------------------------------------- traverse
+
+// Can a ray of node `nd` pass within reach of the sphere (c, r)?  r already
+// holds the triangle's padding.  Conservative in float: every comparison
+// carries a relative margin.
+__device__ __forceinline__ bool node_hits_sphere(const RayNode& nd, float4 sph) {
+    const float vx = sph.x - nd.a.x, vy = sph.y - nd.a.y, vz = sph.z - nd.a.z;
+    const float dist2 = vx * vx + vy * vy + vz * vz;
+    const float dist = sqrtf(dist2);
+    // slop of pbrt's float test grows with the distance from the ray origin
+    const float R = sph.w + nd.a.w + dist * 0x1p-12f;
+    if (!(dist > R)) return true;  // overlapping (or NaN): keep
+    if (dist - R > nd.c.y * (1.f + 0x1p-18f)) return false;  // beyond every ray's maxt
+    const float sb = R / dist;
+    const float cb = sqrtf(fmaxf(0.f, 1.f - sb * sb));
+    const float cth = nd.b.w, sth = nd.c.x;
+    if (cth <= -cb) return true;  // cone half-angle + sphere angle >= pi
+    const float cphi = (vx * nd.b.x + vy * nd.b.y + vz * nd.b.z) / dist;
+    return cphi >= cth * cb - sth * sb - 0x1p-16f;
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(kRhThreads)
+    rh_traverse_kernel(const TriRec* __restrict__ tris, const float4* __restrict__ spheres,
+                       int64_t ntri, const RayNode* __restrict__ nodes, Levels lv,
+                       const float4* __restrict__ so, const float4* __restrict__ sd,
+                       unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
+                       int* status) {
+    const int64_t ti = (int64_t)blockIdx.x * kRhThreads + threadIdx.x;
+    if (ti >= ntri) return;
+    const TriRec tr = tris[ti];
+    const float4 sph = spheres[ti];
+    const int32_t id = __float_as_int(tr.c.w);
+    uint32_t stack[kRhStack];
+    int sp = 0;
+    const int top = lv.nlev - 1;
+    for (int64_t k = lv.cnt[top] - 1; k >= 0 && sp < kRhStack; --k)
+        stack[sp++] = ((uint32_t)top << 27) | (uint32_t)k;
+    bool overflow = lv.cnt[top] > kRhStack;
+    while (sp > 0) {
+        const uint32_t e = stack[--sp];
+        const int lvl = (int)(e >> 27);
+        const int64_t idx = (int64_t)(e & 0x7ffffffu);
+        const RayNode nd = nodes[lv.off[lvl] + idx];
+        const int count = __float_as_int(nd.c.z);
+        if (count == 0) continue;
+        if (!node_hits_sphere(nd, sph)) continue;
+        if (lvl > 0) {
+            const int64_t first = idx * kFan;
+            const int64_t last = min(first + kFan, lv.cnt[lvl - 1]);
+            if (sp + (last - first) > kRhStack) {
+                overflow = true;
+                continue;
+            }
+            for (int64_t c = last - 1; c >= first; --c)
+                stack[sp++] = ((uint32_t)(lvl - 1) << 27) | (uint32_t)c;
+            continue;
+        }
+        // leaf: the exact test against each of its rays
+        uint32_t done = 0;
+        if (ANY) {
+            done = leafmask[idx];
+            if (__popc(done) >= count) continue;
+        }
+        const int64_t base = idx * kLeafRays;
+        for (int k = 0; k < count; ++k) {
+            if (ANY && ((done >> k) & 1u)) continue;
+            const int64_t r = base + k;
+            const float4 o = so[r], d = sd[r];
+            const float nd1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+            float maxt = d.w;
+            if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
+            if (!ANY) {
+                const unsigned long long cur = keys[r];
+                if (cur != 0ull) {
+                    maxt = fminf(maxt, key_t(cur));
+                    if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
+                }
+            }
+            float tt, u1, u2;
+            if (!pbg_exact_rec(tr, o, d, maxt, &tt, &u1, &u2)) continue;
+            if (ANY) {
+                atomicOr(&leafmask[idx], 1u << k);
+            } else {
+                atomicMax(&keys[r], hit_key(tt, id));
+            }
+        }
+    }
+    if (overflow) atomicAdd(&status[1], 1);
+}
+
+// Sorted-order results back to the caller's order.
+__global__ void rh_finalize_nearest(const TriRec* __restrict__ tris, const int32_t* __restrict__ pos,
+                                    const float4* __restrict__ so, const float4* __restrict__ sd,
+                                    const int32_t* __restrict__ perm,
+                                    const unsigned long long* __restrict__ keys, int64_t n,
+                                    int32_t* prim, float* t, float* b1, float* b2) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t ray = perm[i];
+    const unsigned long long k = keys[i];
+    int32_t p = -1;
+    float tt = 0.f, u1 = 0.f, u2 = 0.f;
+    if (k != 0ull) {
+        p = key_prim(k);
+        const float4 o = so[i], d = sd[i];
+        if (!pbg_exact_rec(tris[pos[p]], o, d, d.w, &tt, &u1, &u2)) {
+            p = -1;
+            tt = u1 = u2 = 0.f;
+        }
+    }
+    prim[ray] = p;
+    t[ray] = tt;
+    b1[ray] = u1;
+    b2[ray] = u2;
+}
+
+__global__ void rh_finalize_occluded(const int32_t* __restrict__ perm,
+                                     const uint32_t* __restrict__ leafmask, int64_t n,
+                                     uint8_t* occ) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    occ[perm[i]] = (leafmask[i / kLeafRays] >> (i % kLeafRays)) & 1u;
+}
+
+// ------------------------------------------------------------------ host
+
+static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                    const int32_t** perm, float4** so, float4** sd, Levels* lv, cudaStream_t st) {
+    Work& w = s->work;
+    const uint32_t* skeys = nullptr;
+    int rc = ray_sort(s, o, d, valid, n, perm, &skeys, st);
+    if (rc) return rc;
+    // sorted copies of the rays
+    if ((rc = ensure(w.ray_o2, (size_t)n * sizeof(float4))) ||
+        (rc = ensure(w.ray_d2, (size_t)n * sizeof(float4))))
+        return rc;
+    *so = (float4*)w.ray_o2.ptr;
+    *sd = (float4*)w.ray_d2.ptr;
+    prof_begin(s, st);
+    gather_rays_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(o, d, *perm, n, *so, *sd);
+    prof_end(s, st, kStageBuild, 1);
+    // levels: leaves of 32 rays, parents of 4 children, up to one root
+    int64_t cnt = (n + kLeafRays - 1) / kLeafRays, total = 0;
+    lv->nlev = 0;
+    for (;;) {
+        lv->off[lv->nlev] = total;
+        lv->cnt[lv->nlev] = cnt;
+        total += cnt;
+        lv->nlev++;
+        if (cnt <= 1 || lv->nlev == kMaxLevels) break;
+        cnt = (cnt + kFan - 1) / kFan;
+    }
+    if ((rc = ensure(w.nodes, (size_t)total * sizeof(RayNode)))) return rc;
+    RayNode* nodes = (RayNode*)w.nodes.ptr;
+    const int64_t nleaf = lv->cnt[0];
+    prof_begin(s, st);
+    leaf_build_kernel<<<(unsigned)((nleaf * 32 + 255) / 256), 256, 0, st>>>(*so, *sd, skeys, n, nleaf,
+                                                                            nodes);
+    prof_end(s, st, kStageBuild, 1);
+    for (int l = 1; l < lv->nlev; ++l) {
+        prof_begin(s, st);
+        level_build_kernel<<<(unsigned)((lv->cnt[l] + 127) / 128), 128, 0, st>>>(
+            nodes + lv->off[l - 1], lv->cnt[l - 1], nodes + lv->off[l], lv->cnt[l]);
+        prof_end(s, st, kStageBuild, 1);
+    }
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
+int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+               int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
+    if (n <= 0) return PBG_OK;
+    const int32_t* perm;
+    float4 *so, *sd;
+    Levels lv;
+    int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, st);
+    if (rc) return rc;
+    Work& w = s->work;
+    if ((rc = ensure(w.keys, (size_t)n * 8))) return rc;
+    unsigned long long* keys = (unsigned long long*)w.keys.ptr;
+    PBG_CUDA(cudaMemsetAsync(keys, 0, (size_t)n * 8, st));
+    if (s->ntri > 0) {
+        prof_begin(s, st);
+        rh_traverse_kernel<false><<<(unsigned)((s->ntri + kRhThreads - 1) / kRhThreads), kRhThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
+            (const RayNode*)w.nodes.ptr, lv, so, sd, keys, nullptr, (int*)s->err.ptr);
+        prof_end(s, st, kStageTraverse, 1);
+    }
+    prof_begin(s, st);
+    rh_finalize_nearest<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        (const TriRec*)s->tris.ptr, (const int32_t*)s->tri_pos.ptr, so, sd, perm, keys, n, prim, t, b1, b2);
+    prof_end(s, st, kStageOther, 1);
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
+int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                uint8_t* occ, cudaStream_t st) {
+    if (n <= 0) return PBG_OK;
+    const int32_t* perm;
+    float4 *so, *sd;
+    Levels lv;
+    int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, st);
+    if (rc) return rc;
+    Work& w = s->work;
+    const int64_t nleaf = lv.cnt[0];
+    if ((rc = ensure(w.leafmask, (size_t)nleaf * 4))) return rc;
+    uint32_t* mask = (uint32_t*)w.leafmask.ptr;
+    PBG_CUDA(cudaMemsetAsync(mask, 0, (size_t)nleaf * 4, st));
+    if (s->ntri > 0) {
+        prof_begin(s, st);
+        rh_traverse_kernel<true><<<(unsigned)((s->ntri + kRhThreads - 1) / kRhThreads), kRhThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
+            (const RayNode*)w.nodes.ptr, lv, so, sd, nullptr, mask, (int*)s->err.ptr);
+        prof_end(s, st, kStageTraverse, 1);
+    }
+    prof_begin(s, st);
+    rh_finalize_occluded<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(perm, mask, n, occ);
+    prof_end(s, st, kStageOther, 1);
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
+}  // namespace pbg

@@ -1,26 +1,292 @@
-// pbg_rayorder.cu -- placeholder ordering (identity) until the ray-hierarchy
-// sort lands.
+// pbg_rayorder.cu -- per-batch ray ordering: 6-D Morton keys and a
+// hand-written LSD radix sort (warp-cooperative ranking).
+//
+// The reference arranges each batch as a 2-D ray image and groups rays by
+// chunkX x chunkY image tiles (bin/cl/rayhconstruct6DB.cl:10-47,
+// accelerators/rayhierarchy.cpp:375-463); that groups rays well only while
+// they are camera rays in scanline order.  Here every batch -- camera,
+// shadow or bounce rays -- is sorted by a 30-bit Morton code interleaving
+// five bits each of origin x/y/z (quantised over the batch's origin box) and
+// normalised direction x/y/z, so that consecutive rays share origin and
+// direction whatever produced them.  Invalid rays get the key 0xffffffff and
+// sort to the end.
+//
+// Sort: four passes of 8 bits.  Each pass is (1) a per-tile digit histogram,
+// (2) one exclusive scan over [digit][tile] counts, (3) a stable scatter in
+// which each warp ranks its 32 keys per digit with __match_any_sync and the
+// tile's warps are combined through shared-memory prefix sums.
 #include "pbg_internal.h"
 
 namespace pbg {
 
-int ray_order(pbg_scene* s, const float4* o, const float4* d, int64_t n, const int32_t** perm,
-              cudaStream_t st) {
-    (void)s; (void)o; (void)d; (void)n; (void)st;
-    *perm = nullptr;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;                         // keys per thread
+constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys per tile
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kRadix = 256;
+
+__device__ __forceinline__ uint32_t spread5(uint32_t v) {
+    // 5 bits -> positions 0, 6, 12, 18, 24
+    uint32_t r = 0;
+#pragma unroll
+    for (int b = 0; b < 5; ++b) r |= ((v >> b) & 1u) << (6 * b);
+    return r;
+}
+
+__device__ __forceinline__ uint32_t quant5(float x, float lo, float inv_ext) {
+    float q = (x - lo) * inv_ext * 32.f;
+    q = fminf(fmaxf(q, 0.f), 31.f);
+    return (uint32_t)q;
+}
+
+// Block-level min/max of valid ray origins (atomic on ordered ints).
+__device__ __forceinline__ int ord_f(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float unord_f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__global__ void origin_bounds_kernel(const float4* __restrict__ ro, const uint8_t* __restrict__ valid,
+                                     int64_t n, int* __restrict__ bounds /* lo xyz, hi xyz */) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (valid && !valid[i]) continue;
+        const float4 o = ro[i];
+        if (!(isfinite(o.x) && isfinite(o.y) && isfinite(o.z))) continue;
+        lo[0] = fminf(lo[0], o.x); lo[1] = fminf(lo[1], o.y); lo[2] = fminf(lo[2], o.z);
+        hi[0] = fmaxf(hi[0], o.x); hi[1] = fmaxf(hi[1], o.y); hi[2] = fmaxf(hi[2], o.z);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        for (int off = 16; off; off >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&bounds[a], ord_f(lo[a]));
+            atomicMax(&bounds[3 + a], ord_f(hi[a]));
+        }
+    }
+}
+
+__global__ void morton_kernel(const float4* __restrict__ ro, const float4* __restrict__ rd,
+                              const uint8_t* __restrict__ valid, int64_t n,
+                              const int* __restrict__ bounds, uint32_t* __restrict__ keys,
+                              int32_t* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vals[i] = (int32_t)i;
+    if (valid && !valid[i]) {
+        keys[i] = 0xffffffffu;
+        return;
+    }
+    const float4 o = ro[i], d = rd[i];
+    float lo[3], inv[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = unord_f(bounds[a]);
+        float ext = unord_f(bounds[3 + a]) - lo[a];
+        inv[a] = ext > 0.f ? 1.f / ext : 0.f;
+    }
+    const float len = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+    const float il = len > 0.f ? 1.f / len : 0.f;
+    uint32_t qo0 = quant5(o.x, lo[0], inv[0]), qo1 = quant5(o.y, lo[1], inv[1]),
+             qo2 = quant5(o.z, lo[2], inv[2]);
+    uint32_t qd0 = quant5(d.x * il, -1.f, 0.5f), qd1 = quant5(d.y * il, -1.f, 0.5f),
+             qd2 = quant5(d.z * il, -1.f, 0.5f);
+    // Direction bits above origin bits at each level: coherent directions first.
+    keys[i] = (spread5(qd0) << 5) | (spread5(qd1) << 4) | (spread5(qd2) << 3) |
+              (spread5(qo0) << 2) | (spread5(qo1) << 1) | spread5(qo2);
+}
+
+// Pass 1: digit histogram of each tile, stored digit-major: hist[d * tiles + tile].
+__global__ void __launch_bounds__(kSortThreads)
+    radix_hist_kernel(const uint32_t* __restrict__ keys, int64_t n, int shift, int tiles,
+                      uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[kRadix];
+    for (int k = threadIdx.x; k < kRadix; k += kSortThreads) h[k] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kSortTile;
+    for (int k = 0; k < kSortItems; ++k) {
+        const int64_t i = base + (int64_t)k * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xff], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kRadix; k += kSortThreads)
+        hist[(int64_t)k * tiles + blockIdx.x] = h[k];
+}
+
+// Pass 2: exclusive scan of m counts in one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) scan_kernel(uint32_t* __restrict__ a, int64_t m) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t base = 0; base < m; base += 1024) {
+        const int64_t i = base + threadIdx.x;
+        uint32_t v = i < m ? a[i] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sums[lane];
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += y;
+            }
+            warp_sums[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t excl = carry + (warp ? warp_sums[warp - 1] : 0u) + x - v;
+        if (i < m) a[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+}
+
+// Pass 3: stable scatter.  Element order inside a tile is (warp, item, lane),
+// which is the original order, so ranks computed in that order keep the sort
+// stable.
+__global__ void __launch_bounds__(kSortThreads)
+    radix_scatter_kernel(const uint32_t* __restrict__ keys, const int32_t* __restrict__ vals,
+                         int64_t n, int shift, int tiles, const uint32_t* __restrict__ offs,
+                         uint32_t* __restrict__ keys_out, int32_t* __restrict__ vals_out) {
+    __shared__ uint32_t wcount[kSortWarps][kRadix];  // per-warp digit counts, then prefixes
+    __shared__ uint32_t toff[kRadix];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k < kSortWarps * kRadix; k += kSortThreads)
+        (&wcount[0][0])[k] = 0;
+    for (int k = threadIdx.x; k < kRadix; k += kSortThreads)
+        toff[k] = offs[(int64_t)k * tiles + blockIdx.x];
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kSortTile + (int64_t)warp * 32 * kSortItems;
+    uint32_t key[kSortItems];
+    int32_t val[kSortItems];
+    uint32_t rank[kSortItems];
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const int64_t i = base + (int64_t)k * 32 + lane;
+        const bool ok = i < n;
+        key[k] = ok ? keys[i] : 0xffffffffu;
+        val[k] = ok ? vals[i] : 0;
+        const uint32_t dg = (key[k] >> shift) & 0xff;
+        const uint32_t inb = __ballot_sync(0xffffffffu, ok);
+        uint32_t peers = __match_any_sync(0xffffffffu, ok ? dg : 0x100u + 0u) & inb;
+        if (!ok) peers = 0;
+        const uint32_t before = wcount[warp][dg];
+        __syncwarp();
+        rank[k] = before + __popc(peers & lt);
+        const int leader = peers ? __ffs(peers) - 1 : -1;
+        if (ok && lane == leader) wcount[warp][dg] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // Exclusive prefix over warps for every digit.
+    for (int dg = threadIdx.x; dg < kRadix; dg += kSortThreads) {
+        uint32_t run = 0;
+        for (int w = 0; w < kSortWarps; ++w) {
+            uint32_t c = wcount[w][dg];
+            wcount[w][dg] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const int64_t i = base + (int64_t)k * 32 + lane;
+        if (i >= n) continue;
+        const uint32_t dg = (key[k] >> shift) & 0xff;
+        const uint32_t pos = toff[dg] + wcount[warp][dg] + rank[k];
+        keys_out[pos] = key[k];
+        vals_out[pos] = val[k];
+    }
+}
+
+// Sorts (keys, vals) of length n in place through the tmp buffers; returns
+// pointers to the sorted arrays (which alternate between the two buffers).
+int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp,
+                     uint32_t* hist, int64_t n, int bits, uint32_t** keys_out, int32_t** vals_out,
+                     cudaStream_t st) {
+    const int tiles = (int)((n + kSortTile - 1) / kSortTile);
+    uint32_t *ka = keys, *kb = keys_tmp;
+    int32_t *va = vals, *vb = vals_tmp;
+    for (int shift = 0; shift < bits; shift += 8) {
+        prof_begin(s, st);
+        radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ka, n, shift, tiles, hist);
+        prof_end(s, st, kStageSort, 1);
+        prof_begin(s, st);
+        scan_kernel<<<1, 1024, 0, st>>>(hist, (int64_t)tiles * kRadix);
+        prof_end(s, st, kStageSort, 1);
+        prof_begin(s, st);
+        radix_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(ka, va, n, shift, tiles, hist, kb, vb);
+        prof_end(s, st, kStageSort, 1);
+        PBG_CUDA(cudaGetLastError());
+        uint32_t* tk = ka; ka = kb; kb = tk;
+        int32_t* tv = va; va = vb; vb = tv;
+    }
+    *keys_out = ka;
+    *vals_out = va;
     return PBG_OK;
 }
 
-int rh_nearest(pbg_scene*, const float4*, const float4*, const uint8_t*, int64_t, int32_t*,
-               float*, float*, float*, cudaStream_t) {
-    set_last_error("rayhierarchy traversal not built yet");
-    return PBG_ERR_UNSUPPORTED;
+// Computes the Morton order of a batch.  *perm (device, n entries) lists ray
+// indices in sorted order; valid rays come first.
+int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+             const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st) {
+    Work& w = s->work;
+    const int tiles = (int)((n + kSortTile - 1) / kSortTile);
+    int rc;
+    if ((rc = ensure(w.mkeys, (size_t)n * 4)) || (rc = ensure(w.mkeys_tmp, (size_t)n * 4)) ||
+        (rc = ensure(w.perm, (size_t)n * 4)) || (rc = ensure(w.perm_tmp, (size_t)n * 4)) ||
+        (rc = ensure(w.hist, ((size_t)tiles * kRadix + 8) * 4)))
+        return rc;
+    int* bounds = (int*)((uint32_t*)w.hist.ptr + (size_t)tiles * kRadix);
+    const int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000,
+                         (int)0x80000000};
+    PBG_CUDA(cudaMemcpyAsync(bounds, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 4 * sms) blocks = 4 * sms;
+    prof_begin(s, st);
+    origin_bounds_kernel<<<(unsigned)blocks, 256, 0, st>>>(o, valid, n, bounds);
+    prof_end(s, st, kStageSort, 1);
+    prof_begin(s, st);
+    morton_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        o, d, valid, n, bounds, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
+    prof_end(s, st, kStageSort, 1);
+    PBG_CUDA(cudaGetLastError());
+    uint32_t* ko;
+    int32_t* vo;
+    // The bounds words sit after the histogram; a 2048-key tile has < 2^16
+    // counts per digit and 32 key bits need four passes.
+    rc = radix_sort_pairs(s, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr, (uint32_t*)w.mkeys_tmp.ptr,
+                          (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.hist.ptr, n, 32, &ko, &vo, st);
+    if (rc) return rc;
+    *perm = vo;
+    if (sorted_keys) *sorted_keys = ko;
+    return PBG_OK;
 }
 
-int rh_occluded(pbg_scene*, const float4*, const float4*, const uint8_t*, int64_t, uint8_t*,
-                cudaStream_t) {
-    set_last_error("rayhierarchy traversal not built yet");
-    return PBG_ERR_UNSUPPORTED;
+int ray_order(pbg_scene* s, const float4* o, const float4* d, int64_t n, const int32_t** perm,
+              cudaStream_t st) {
+    if (n < 4096) {  // too small to gain from ordering
+        *perm = nullptr;
+        return PBG_OK;
+    }
+    return ray_sort(s, o, d, nullptr, n, perm, nullptr, st);
 }
 
 }  // namespace pbg
