@@ -67,7 +67,9 @@ typedef struct pbg_params {
     int32_t bvh_height;   /* "BVHheight": levels of the BVH cut for ray-bvh */
     int32_t max_bvh_prim; /* "maxBVHPrim": triangles per BVH leaf */
     int32_t device;       /* CUDA device ordinal */
-    int32_t reserved[10];
+    int32_t ray_sort;     /* ray-bvh: 1 = walk each batch in 6-D Morton order
+                           * (helps incoherent bounce rays), 0 = caller order */
+    int32_t reserved[9];
 } pbg_params;
 
 typedef struct pbg_rays {
@@ -91,7 +93,11 @@ typedef struct pbg_counters {
     uint64_t bvh_nodes;       /* nodes of the scene's BVH (ray-bvh) */
     uint64_t kernel_launches; /* kernels this scene has launched */
     uint64_t timed_launches[4]; /* launches timed per stage (profiling on) */
-    uint64_t reserved[7];
+    /* Work counted by the traversal kernels at profiling level 2: [0] node
+     * (or box) tests, [1] leaves visited, [2] ray/triangle filter tests,
+     * [3] exact tests, [4] exact tests that hit.  Zero otherwise. */
+    uint64_t work[5];
+    uint64_t reserved[2];
     /* Device time per stage in ms while profiling is on (CUDA events around
      * each launch on its stream): [0] ray sort, [1] hierarchy build,
      * [2] traversal (the intersection kernels), [3] finalize / other. */
@@ -160,7 +166,9 @@ int pbg_hit_geometry_device(pbg_scene* scene, const float* o4, const float* d4,
  * Reading them synchronises the scene's pending timing events. */
 int pbg_stats(pbg_scene* scene, pbg_counters* out);
 /* Turns per-stage event timing on (1) or off (0) and clears the stage
- * times.  Off by default: timing adds two event records per launch. */
+ * times and work counters.  Off by default: timing adds two event records
+ * per launch.  Level 2 also counts traversal work (counters.work) with a
+ * counting variant of the traversal kernels. */
 int pbg_profile(pbg_scene* scene, int on);
 
 #ifdef __cplusplus

@@ -35,7 +35,7 @@ class PbgError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("chunk_x", C.c_int32), ("chunk_y", C.c_int32), ("height", C.c_int32),
                 ("bvh_height", C.c_int32), ("max_bvh_prim", C.c_int32), ("device", C.c_int32),
-                ("reserved", C.c_int32 * 10)]
+                ("ray_sort", C.c_int32), ("reserved", C.c_int32 * 9)]
 
 
 _fp = C.POINTER(C.c_float)
@@ -53,7 +53,8 @@ class Hits(C.Structure):
 class Counters(C.Structure):
     _fields_ = [("rays_nearest", C.c_uint64), ("rays_occluded", C.c_uint64),
                 ("calls", C.c_uint64), ("bvh_nodes", C.c_uint64), ("kernel_launches", C.c_uint64),
-                ("timed_launches", C.c_uint64 * 4), ("reserved", C.c_uint64 * 7),
+                ("timed_launches", C.c_uint64 * 4), ("work", C.c_uint64 * 5),
+                ("reserved", C.c_uint64 * 2),
                 ("stage_ms", C.c_double * 4)]
 
 

@@ -148,11 +148,14 @@ class Aggregate:
         return {"rays_nearest": c.rays_nearest, "rays_occluded": c.rays_occluded,
                 "calls": c.calls, "bvh_nodes": c.bvh_nodes, "kernel_launches": c.kernel_launches,
                 "timed_launches": dict(zip(L.STAGES, list(c.timed_launches))),
+                "work": dict(zip(("node_tests", "leaves", "filter_tests", "exact_tests",
+                                  "exact_hits"), list(c.work))),
                 "stage_ms": dict(zip(L.STAGES, list(c.stage_ms)))}
 
-    def profile(self, on: bool = True) -> None:
+    def profile(self, on: bool | int = True) -> None:
         """Per-stage CUDA-event timing (the GPU_TIMES printouts of the
-        reference, core/GPUparallel.h:532-538)."""
+        reference, core/GPUparallel.h:532-538); level 2 also counts
+        traversal work (node tests, ray/triangle tests)."""
         L.check(L.lib().pbg_profile(self.handle, int(on)), "pbg_profile")
 
 
@@ -177,6 +180,7 @@ def _params_from(ps: dict | None) -> L.Params:
     p.bvh_height = int(ps.get("BVHheight", 0))
     p.max_bvh_prim = int(ps.get("maxBVHPrim", 0))
     p.device = int(ps.get("device", 0))
+    p.ray_sort = int(ps.get("raySort", 0))
     return p
 
 

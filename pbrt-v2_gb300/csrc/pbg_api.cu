@@ -240,6 +240,13 @@ static void prof_collect(pbg_scene* s) {
         s->prof.pool.push_back(r.b);
     }
     s->prof.pending.clear();
+    if (s->prof.level >= 2 && s->workc.ptr) {
+        unsigned long long h[8];
+        if (cudaMemcpy(h, s->workc.ptr, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess)
+            for (int k = 0; k < 5; ++k) s->counters.work[k] = h[k];
+        else
+            cudaGetLastError();
+    }
 }
 
 int check_device_status(pbg_scene* s, cudaStream_t st) {
@@ -501,6 +508,7 @@ void pbg_scene_destroy(pbg_scene* s) {
     release(s->spheres);
     release(s->tri_pos);
     release(s->err);
+    release(s->workc);
     Work& w = s->work;
     DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.ray_o2, &w.ray_d2, &w.valid, &w.prim,
                            &w.t, &w.b1, &w.b2, &w.occ, &w.keys, &w.stage, &w.perm,
@@ -660,9 +668,16 @@ int pbg_profile(pbg_scene* s, int on) {
     cudaSetDevice(s->device);
     prof_collect(s);
     s->prof.on = on != 0;
+    s->prof.level = on;
     for (int k = 0; k < 4; ++k) {
         s->counters.stage_ms[k] = 0.0;
         s->counters.timed_launches[k] = 0;
+    }
+    for (int k = 0; k < 5; ++k) s->counters.work[k] = 0;
+    if (on >= 2) {
+        int rc = ensure(s->workc, 8 * sizeof(unsigned long long));
+        if (rc) return rc;
+        PBG_CUDA(cudaMemset(s->workc.ptr, 0, 8 * sizeof(unsigned long long)));
     }
     return PBG_OK;
 }

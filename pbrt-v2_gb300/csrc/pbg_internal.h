@@ -24,6 +24,7 @@ struct __align__(16) BvhNode {
 // Event pairs around launches, summed per stage when counters are read.
 struct Profiler {
     bool on = false;
+    int level = 0;  // 2: count traversal work
     struct Rec {
         cudaEvent_t a, b;
         int stage;
@@ -88,6 +89,7 @@ struct pbg_scene {
     int32_t unculled = 0;      // records [0, unculled) are tested by every ray
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     pbg::DeviceBuffer err;     // int[4] device status words
+    pbg::DeviceBuffer workc;   // uint64[8] traversal work counters (profiling level 2)
     pbg::Work work;
     pbg_counters counters{};
     pbg::Profiler prof;

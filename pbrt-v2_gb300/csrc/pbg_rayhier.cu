@@ -26,6 +26,7 @@
 //             Any-hit keeps one occlusion bit per ray (a 32-bit mask per
 //             leaf) and skips leaves whose rays are all occluded.
 #include "pbg_internal.h"
+#include "pbg_count.cuh"
 
 namespace pbg {
 
@@ -222,13 +223,14 @@ __device__ __forceinline__ bool node_hits_sphere(const RayNode& nd, float4 sph) 
     return cphi >= cth * cb - sth * sb - 0x1p-16f;
 }
 
-template <bool ANY>
+template <bool ANY, bool STATS>
 __global__ void __launch_bounds__(kRhThreads)
     rh_traverse_kernel(const TriRec* __restrict__ tris, const float4* __restrict__ spheres,
                        int64_t ntri, const RayNode* __restrict__ nodes, Levels lv,
                        const float4* __restrict__ so, const float4* __restrict__ sd,
                        unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
-                       int* status) {
+                       int* status, unsigned long long* wc) {
+    WorkCount cnt_;
     const int64_t ti = (int64_t)blockIdx.x * kRhThreads + threadIdx.x;
     if (ti >= ntri) return;
     const TriRec tr = tris[ti];
@@ -247,6 +249,7 @@ __global__ void __launch_bounds__(kRhThreads)
         const RayNode nd = nodes[lv.off[lvl] + idx];
         const int count = __float_as_int(nd.c.z);
         if (count == 0) continue;
+        if (STATS) cnt_.node++;
         if (!node_hits_sphere(nd, sph)) continue;
         if (lvl > 0) {
             const int64_t first = idx * kFan;
@@ -260,6 +263,7 @@ __global__ void __launch_bounds__(kRhThreads)
             continue;
         }
         // leaf: the exact test against each of its rays
+        if (STATS) cnt_.leaf++;
         uint32_t done = 0;
         if (ANY) {
             done = leafmask[idx];
@@ -272,6 +276,7 @@ __global__ void __launch_bounds__(kRhThreads)
             const float4 o = so[r], d = sd[r];
             const float nd1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
             float maxt = d.w;
+            if (STATS) cnt_.filt++;
             if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
             if (!ANY) {
                 const unsigned long long cur = keys[r];
@@ -281,7 +286,9 @@ __global__ void __launch_bounds__(kRhThreads)
                 }
             }
             float tt, u1, u2;
+            if (STATS) cnt_.exact++;
             if (!pbg_exact_rec(tr, o, d, maxt, &tt, &u1, &u2)) continue;
+            if (STATS) cnt_.hit++;
             if (ANY) {
                 atomicOr(&leafmask[idx], 1u << k);
             } else {
@@ -290,6 +297,7 @@ __global__ void __launch_bounds__(kRhThreads)
         }
     }
     if (overflow) atomicAdd(&status[1], 1);
+    if (STATS) cnt_.flush(wc);
 }
 
 // Sorted-order results back to the caller's order.
@@ -327,6 +335,21 @@ __global__ void rh_finalize_occluded(const int32_t* __restrict__ perm,
 }
 
 // ------------------------------------------------------------------ host
+
+template <bool ANY>
+static void launch_rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const float4* sd,
+                               unsigned long long* keys, uint32_t* mask, cudaStream_t st) {
+    const unsigned grid = (unsigned)((s->ntri + kRhThreads - 1) / kRhThreads);
+    if (s->prof.level >= 2)
+        rh_traverse_kernel<ANY, true><<<grid, kRhThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
+            (const RayNode*)s->work.nodes.ptr, lv, so, sd, keys, mask, (int*)s->err.ptr,
+            (unsigned long long*)s->workc.ptr);
+    else
+        rh_traverse_kernel<ANY, false><<<grid, kRhThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
+            (const RayNode*)s->work.nodes.ptr, lv, so, sd, keys, mask, (int*)s->err.ptr, nullptr);
+}
 
 static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                     const int32_t** perm, float4** so, float4** sd, Levels* lv, cudaStream_t st) {
@@ -385,9 +408,7 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
     PBG_CUDA(cudaMemsetAsync(keys, 0, (size_t)n * 8, st));
     if (s->ntri > 0) {
         prof_begin(s, st);
-        rh_traverse_kernel<false><<<(unsigned)((s->ntri + kRhThreads - 1) / kRhThreads), kRhThreads, 0, st>>>(
-            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
-            (const RayNode*)w.nodes.ptr, lv, so, sd, keys, nullptr, (int*)s->err.ptr);
+        launch_rh_traverse<false>(s, lv, so, sd, keys, nullptr, st);
         prof_end(s, st, kStageTraverse, 1);
     }
     prof_begin(s, st);
@@ -413,9 +434,7 @@ int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
     PBG_CUDA(cudaMemsetAsync(mask, 0, (size_t)nleaf * 4, st));
     if (s->ntri > 0) {
         prof_begin(s, st);
-        rh_traverse_kernel<true><<<(unsigned)((s->ntri + kRhThreads - 1) / kRhThreads), kRhThreads, 0, st>>>(
-            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
-            (const RayNode*)w.nodes.ptr, lv, so, sd, nullptr, mask, (int*)s->err.ptr);
+        launch_rh_traverse<true>(s, lv, so, sd, nullptr, mask, st);
         prof_end(s, st, kStageTraverse, 1);
     }
     prof_begin(s, st);
