@@ -160,6 +160,8 @@ def run_gpu(args, rank, world, dev):
     tris = sc["tris"]
     n = rays.shape[1]
     acc = A.MakeAccelerator(args.accel, tris, {"device": dev})
+    # the breadth-first renderer's ray image: one tile of 1024 x 1024 pixels x 4 spp
+    acc.Preprocess(None, 4, 1, 1, xres=1024, yres=1024)
     stream = torch.cuda.Stream()
     o4, d4 = to_dev(rays)
     prim = torch.empty(n, dtype=torch.int32, device="cuda")

@@ -127,6 +127,14 @@ void pbg_scene_destroy(pbg_scene* scene);
  * RayBVH::MaxRaysPerCall (rayBVH.cpp:279-324), which return 409600. */
 int pbg_max_rays_per_call(const pbg_scene* scene, int64_t* out);
 
+/* Declares that following batches of exactly width*height rays form a ray
+ * image (ray i at x = i mod width, y = i div width), as the breadth-first
+ * renderer lays them out: width = tile xRes * spp, height = tile yRes.
+ * Replaces RayHieararchy::Preprocess / RayBVH::Preprocess
+ * (rayhierarchy.cpp:250-265, core/primitive.h:296-297).  The ray hierarchy
+ * then groups rays by 2-D image tiles; 0, 0 clears the layout. */
+int pbg_preprocess(pbg_scene* scene, int64_t width, int64_t height);
+
 /* Nearest hit of n rays, host buffers in and out (copies included).
  * Replaces the batch Intersect of naive.cpp:204-338,
  * rayhierarchy.cpp:602-813 / :816-1140 and rayBVH.cpp:615-836 / :839-1138

@@ -100,6 +100,7 @@ def lib():
     L.pbg_hit_geometry_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64, vp, vp]
     L.pbg_stats.argtypes = [vp, C.POINTER(Counters)]
     L.pbg_profile.argtypes = [vp, C.c_int]
+    L.pbg_preprocess.argtypes = [vp, C.c_int64, C.c_int64]
     _lib = L
     return L
 

@@ -73,9 +73,14 @@ class Aggregate:
     def Preprocess(self, camera=None, samplesPerPixel: int = 1, nx: int = 1, ny: int = 1,
                    xres: int | None = None, yres: int | None = None):
         """Ray-image size of one task tile: W = xRes/nx*spp, H = yRes/ny
-        (rayhierarchy.cpp:250-265)."""
+        (rayhierarchy.cpp:250-265).  Batches of exactly W*H rays are then
+        grouped by 2-D image tiles in the ray hierarchy."""
+        if camera is not None and xres is None:
+            xres, yres = camera.xres, camera.yres
         if xres is not None and yres is not None:
             self.tile = (xres // nx * samplesPerPixel, yres // ny)
+            L.check(L.lib().pbg_preprocess(self.handle, self.tile[0], self.tile[1]),
+                    "pbg_preprocess")
 
     @staticmethod
     def _rays_struct(rays: np.ndarray, valid: np.ndarray | None) -> L.Rays:

@@ -663,6 +663,17 @@ int pbg_stats(pbg_scene* s, pbg_counters* out) {
     return PBG_OK;
 }
 
+int pbg_preprocess(pbg_scene* s, int64_t width, int64_t height) {
+    if (!s || width < 0 || height < 0 || (width > 0) != (height > 0) || width > (1 << 15) ||
+        height > (1 << 15)) {
+        set_last_error("pbg_preprocess: bad ray-image size (at most 32768 x 32768)");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    s->image_w = width;
+    s->image_h = height;
+    return PBG_OK;
+}
+
 int pbg_profile(pbg_scene* s, int on) {
     if (!s) return PBG_ERR_INVALID_ARGUMENT;
     cudaSetDevice(s->device);

@@ -66,7 +66,8 @@ void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out);
 // Per-batch device scratch owned by a scene.
 struct Work {
     DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
-        perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo;
+        perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo, queue_a, queue_b,
+        qcount;
     int64_t cap = 0;
 };
 
@@ -87,6 +88,8 @@ struct pbg_scene {
     int64_t bvh_nodes = 0;
     int bvh_depth = 0;
     int32_t unculled = 0;      // records [0, unculled) are tested by every ray
+    int rh_groups = 1;         // triangle groups per rayhierarchy traversal (grows on overflow)
+    int64_t image_w = 0, image_h = 0;  // ray-image layout from pbg_preprocess (0 = none)
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     pbg::DeviceBuffer err;     // int[4] device status words
     pbg::DeviceBuffer workc;   // uint64[8] traversal work counters (profiling level 2)

@@ -25,8 +25,11 @@
 //             reads a ray's current key first and filters with that t.
 //             Any-hit keeps one occlusion bit per ray (a 32-bit mask per
 //             leaf) and skips leaves whose rays are all occluded.
+#include <algorithm>
+
 #include "pbg_internal.h"
 #include "pbg_count.cuh"
+#include "pbg_tma.cuh"
 
 namespace pbg {
 
@@ -223,81 +226,137 @@ __device__ __forceinline__ bool node_hits_sphere(const RayNode& nd, float4 sph) 
     return cphi >= cth * cb - sth * sb - 0x1p-16f;
 }
 
-template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(kRhThreads)
-    rh_traverse_kernel(const TriRec* __restrict__ tris, const float4* __restrict__ spheres,
-                       int64_t ntri, const RayNode* __restrict__ nodes, Levels lv,
-                       const float4* __restrict__ so, const float4* __restrict__ sd,
-                       unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
-                       int* status, unsigned long long* wc) {
-    WorkCount cnt_;
-    const int64_t ti = (int64_t)blockIdx.x * kRhThreads + threadIdx.x;
-    if (ti >= ntri) return;
-    const TriRec tr = tris[ti];
-    const float4 sph = spheres[ti];
-    const int32_t id = __float_as_int(tr.c.w);
-    uint32_t stack[kRhStack];
-    int sp = 0;
-    const int top = lv.nlev - 1;
-    for (int64_t k = lv.cnt[top] - 1; k >= 0 && sp < kRhStack; --k)
-        stack[sp++] = ((uint32_t)top << 27) | (uint32_t)k;
-    bool overflow = lv.cnt[top] > kRhStack;
-    while (sp > 0) {
-        const uint32_t e = stack[--sp];
-        const int lvl = (int)(e >> 27);
-        const int64_t idx = (int64_t)(e & 0x7ffffffu);
-        const RayNode nd = nodes[lv.off[lvl] + idx];
-        const int count = __float_as_int(nd.c.z);
-        if (count == 0) continue;
-        if (STATS) cnt_.node++;
-        if (!node_hits_sphere(nd, sph)) continue;
-        if (lvl > 0) {
-            const int64_t first = idx * kFan;
-            const int64_t last = min(first + kFan, lv.cnt[lvl - 1]);
-            if (sp + (last - first) > kRhStack) {
-                overflow = true;
-                continue;
-            }
-            for (int64_t c = last - 1; c >= first; --c)
-                stack[sp++] = ((uint32_t)(lvl - 1) << 27) | (uint32_t)c;
-            continue;
-        }
-        // leaf: the exact test against each of its rays
-        if (STATS) cnt_.leaf++;
-        uint32_t done = 0;
-        if (ANY) {
-            done = leafmask[idx];
-            if (__popc(done) >= count) continue;
-        }
-        const int64_t base = idx * kLeafRays;
-        for (int k = 0; k < count; ++k) {
-            if (ANY && ((done >> k) & 1u)) continue;
-            const int64_t r = base + k;
-            const float4 o = so[r], d = sd[r];
-            const float nd1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
-            float maxt = d.w;
-            if (STATS) cnt_.filt++;
-            if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
-            if (!ANY) {
-                const unsigned long long cur = keys[r];
-                if (cur != 0ull) {
-                    maxt = fminf(maxt, key_t(cur));
-                    if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
-                }
-            }
-            float tt, u1, u2;
-            if (STATS) cnt_.exact++;
-            if (!pbg_exact_rec(tr, o, d, maxt, &tt, &u1, &u2)) continue;
-            if (STATS) cnt_.hit++;
-            if (ANY) {
-                atomicOr(&leafmask[idx], 1u << k);
-            } else {
-                atomicMax(&keys[r], hit_key(tt, id));
-            }
-        }
+// A (triangle record, node) pair that passed its node test.
+struct Pair {
+    int32_t tri;
+    int32_t node;
+};
+
+// Appends up to kFan items per thread with one atomic per warp; items past
+// the capacity are dropped and flagged (the host then reruns with smaller
+// triangle groups).  Every lane of the warp must call it.
+__device__ __forceinline__ void warp_append(const Pair* items, int k, Pair* q, uint32_t* count,
+                                            uint32_t cap, int* status) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int incl = k;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(full, incl, off);
+        if (lane >= off) incl += y;
     }
-    if (overflow) atomicAdd(&status[1], 1);
-    if (STATS) cnt_.flush(wc);
+    const int total = __shfl_sync(full, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(count, (uint32_t)total);
+    base = __shfl_sync(full, base, 31);
+    const uint32_t start = base + (uint32_t)(incl - k);
+    for (int j = 0; j < k; ++j) {
+        const uint32_t pos = start + (uint32_t)j;
+        if (pos < cap) q[pos] = items[j];
+    }
+    if (lane == 31 && total > 0 && base + (uint32_t)total > cap) atomicAdd(&status[kStatusOverflow], 1);
+}
+
+// Level-synchronous descent.  Pairs of level `lvl` (already tested) produce
+// the pairs of their children that pass; the root level is seeded from the
+// triangles [t0, t1).
+template <bool STATS>
+__global__ void __launch_bounds__(256)
+    rh_seed_kernel(const float4* __restrict__ spheres, int32_t t0, int32_t t1,
+                   const RayNode* __restrict__ root, Pair* __restrict__ out, uint32_t* count,
+                   uint32_t cap, int* status, unsigned long long* wc) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const RayNode nd = *root;
+    const int rc = __float_as_int(nd.c.z);
+    WorkCount c_;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + t0; base < t1; base += stride) {
+        const int64_t t = base + (threadIdx.x);
+        Pair item[1];
+        int k = 0;
+        if (t < t1 && rc > 0) {
+            if (STATS) c_.node++;
+            if (node_hits_sphere(nd, spheres[t])) item[k++] = Pair{(int32_t)t, 0};
+        }
+        warp_append(item, k, out, count, cap, status);
+    }
+    if (STATS) c_.flush(wc);
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(256)
+    rh_expand_kernel(const float4* __restrict__ spheres, const RayNode* __restrict__ child_nodes,
+                     int64_t nchild, const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
+                     Pair* __restrict__ out, uint32_t* out_count, uint32_t cap, int* status,
+                     unsigned long long* wc) {
+    const uint32_t nin = min(*in_count, cap);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    WorkCount c_;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nin; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        Pair item[kFan];
+        int k = 0;
+        if (i < nin) {
+            const Pair p = in[i];
+            const float4 sph = spheres[p.tri];
+            const int64_t first = (int64_t)p.node * kFan;
+            const int64_t last = min(first + kFan, nchild);
+            for (int64_t c = first; c < last; ++c) {
+                const RayNode nd = child_nodes[c];
+                if (__float_as_int(nd.c.z) == 0) continue;
+                if (STATS) c_.node++;
+                if (node_hits_sphere(nd, sph)) item[k++] = Pair{p.tri, (int32_t)c};
+            }
+        }
+        warp_append(item, k, out, out_count, cap, status);
+    }
+    if (STATS) c_.flush(wc);
+}
+
+// One warp per (triangle, leaf) pair: lane k tests ray k of the leaf, so the
+// 32 rays load as two coalesced 512-byte rows and the triangle record is a
+// broadcast.
+template <bool ANY, bool STATS>
+__global__ void __launch_bounds__(256)
+    rh_leaf_kernel(const TriRec* __restrict__ tris, const RayNode* __restrict__ leaves,
+                   const Pair* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t cap,
+                   const float4* __restrict__ so, const float4* __restrict__ sd,
+                   unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
+                   unsigned long long* wc) {
+    const uint32_t nin = min(*in_count, cap);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    WorkCount c_;
+    for (int64_t p = warp; p < nin; p += nwarps) {
+        const Pair pr = in[p];
+        const int count = __float_as_int(leaves[pr.node].c.z);
+        if (STATS && lane == 0) c_.leaf++;
+        if (lane >= count) continue;
+        const int64_t r = (int64_t)pr.node * kLeafRays + lane;
+        if (ANY && ((leafmask[pr.node] >> lane) & 1u)) continue;
+        const TriRec tr = tris[pr.tri];
+        const float4 o = so[r], d = sd[r];
+        const float nd1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+        float maxt = d.w;
+        if (STATS) c_.filt++;
+        if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
+        if (!ANY) {
+            const unsigned long long cur = keys[r];
+            if (cur != 0ull) {
+                maxt = fminf(maxt, key_t(cur));
+                if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
+            }
+        }
+        float tt, u1, u2;
+        if (STATS) c_.exact++;
+        if (!pbg_exact_rec(tr, o, d, maxt, &tt, &u1, &u2)) continue;
+        if (STATS) c_.hit++;
+        if (ANY)
+            atomicOr(&leafmask[pr.node], 1u << lane);
+        else
+            atomicMax(&keys[r], hit_key(tt, __float_as_int(tr.c.w)));
+    }
+    if (STATS) c_.flush(wc);
 }
 
 // Sorted-order results back to the caller's order.
@@ -336,28 +395,12 @@ __global__ void rh_finalize_occluded(const int32_t* __restrict__ perm,
 
 // ------------------------------------------------------------------ host
 
-template <bool ANY>
-static void launch_rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const float4* sd,
-                               unsigned long long* keys, uint32_t* mask, cudaStream_t st) {
-    const unsigned grid = (unsigned)((s->ntri + kRhThreads - 1) / kRhThreads);
-    if (s->prof.level >= 2)
-        rh_traverse_kernel<ANY, true><<<grid, kRhThreads, 0, st>>>(
-            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
-            (const RayNode*)s->work.nodes.ptr, lv, so, sd, keys, mask, (int*)s->err.ptr,
-            (unsigned long long*)s->workc.ptr);
-    else
-        rh_traverse_kernel<ANY, false><<<grid, kRhThreads, 0, st>>>(
-            (const TriRec*)s->tris.ptr, (const float4*)s->spheres.ptr, s->ntri,
-            (const RayNode*)s->work.nodes.ptr, lv, so, sd, keys, mask, (int*)s->err.ptr, nullptr);
-}
-
 static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                     const int32_t** perm, float4** so, float4** sd, Levels* lv, cudaStream_t st) {
     Work& w = s->work;
     const uint32_t* skeys = nullptr;
     int rc = ray_sort(s, o, d, valid, n, perm, &skeys, st);
     if (rc) return rc;
-    // sorted copies of the rays
     if ((rc = ensure(w.ray_o2, (size_t)n * sizeof(float4))) ||
         (rc = ensure(w.ray_d2, (size_t)n * sizeof(float4))))
         return rc;
@@ -394,6 +437,82 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     return PBG_OK;
 }
 
+// Pairs per queue buffer: 2^25 (256 MB); a batch that overflows it reruns
+// with the triangles split into more groups.
+constexpr uint32_t kQueueCap = 1u << 25;
+
+template <bool ANY>
+static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const float4* sd,
+                       unsigned long long* keys, uint32_t* mask, cudaStream_t st) {
+    Work& w = s->work;
+    int rc;
+    if ((rc = ensure(w.queue_a, (size_t)kQueueCap * sizeof(Pair))) ||
+        (rc = ensure(w.queue_b, (size_t)kQueueCap * sizeof(Pair))) ||
+        (rc = ensure(w.qcount, 64 * sizeof(uint32_t))))
+        return rc;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    const unsigned grid = (unsigned)(sms * 8);
+    const bool stats = s->prof.level >= 2;
+    unsigned long long* wc = (unsigned long long*)s->workc.ptr;
+    int* status = (int*)s->err.ptr;
+    const RayNode* nodes = (const RayNode*)w.nodes.ptr;
+    uint32_t* counts = (uint32_t*)w.qcount.ptr;
+    int groups = s->rh_groups > 0 ? s->rh_groups : 1;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        PBG_CUDA(cudaMemsetAsync(status + kStatusOverflow, 0, sizeof(int), st));
+        const int64_t per = (s->ntri + groups - 1) / groups;
+        for (int g = 0; g < groups; ++g) {
+            const int32_t t0 = (int32_t)(g * per), t1 = (int32_t)std::min<int64_t>(s->ntri, (g + 1) * per);
+            if (t0 >= t1) break;
+            PBG_CUDA(cudaMemsetAsync(counts, 0, 64 * sizeof(uint32_t), st));
+            Pair* qa = (Pair*)w.queue_a.ptr;
+            Pair* qb = (Pair*)w.queue_b.ptr;
+            const int top = lv.nlev - 1;
+            prof_begin(s, st);
+            if (stats)
+                rh_seed_kernel<true><<<grid, 256, 0, st>>>((const float4*)s->spheres.ptr, t0, t1,
+                                                           nodes + lv.off[top], qa, &counts[top],
+                                                           kQueueCap, status, wc);
+            else
+                rh_seed_kernel<false><<<grid, 256, 0, st>>>((const float4*)s->spheres.ptr, t0, t1,
+                                                            nodes + lv.off[top], qa, &counts[top],
+                                                            kQueueCap, status, nullptr);
+            for (int l = top; l > 0; --l) {
+                if (stats)
+                    rh_expand_kernel<true><<<grid, 256, 0, st>>>(
+                        (const float4*)s->spheres.ptr, nodes + lv.off[l - 1], lv.cnt[l - 1], qa,
+                        &counts[l], qb, &counts[l - 1], kQueueCap, status, wc);
+                else
+                    rh_expand_kernel<false><<<grid, 256, 0, st>>>(
+                        (const float4*)s->spheres.ptr, nodes + lv.off[l - 1], lv.cnt[l - 1], qa,
+                        &counts[l], qb, &counts[l - 1], kQueueCap, status, nullptr);
+                Pair* tq = qa;
+                qa = qb;
+                qb = tq;
+            }
+            if (stats)
+                rh_leaf_kernel<ANY, true><<<grid * 2, 256, 0, st>>>(
+                    (const TriRec*)s->tris.ptr, nodes, qa, &counts[0], kQueueCap, so, sd, keys, mask, wc);
+            else
+                rh_leaf_kernel<ANY, false><<<grid * 2, 256, 0, st>>>(
+                    (const TriRec*)s->tris.ptr, nodes, qa, &counts[0], kQueueCap, so, sd, keys, mask,
+                    nullptr);
+            prof_end(s, st, kStageTraverse, lv.nlev + 1);
+            PBG_CUDA(cudaGetLastError());
+        }
+        // One status read per call: a dropped pair would lose hits.
+        int ovf = 0;
+        PBG_CUDA(cudaMemcpyAsync(&ovf, status + kStatusOverflow, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PBG_CUDA(cudaStreamSynchronize(st));
+        if (ovf == 0) return PBG_OK;
+        groups *= 4;  // rerun: atomicMax / atomicOr merges make a rerun idempotent
+        s->rh_groups = groups;
+    }
+    set_last_error("rayhierarchy: pair queues overflowed at every triangle grouping");
+    return PBG_ERR_INTERNAL;
+}
+
 int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
     if (n <= 0) return PBG_OK;
@@ -406,11 +525,7 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
     if ((rc = ensure(w.keys, (size_t)n * 8))) return rc;
     unsigned long long* keys = (unsigned long long*)w.keys.ptr;
     PBG_CUDA(cudaMemsetAsync(keys, 0, (size_t)n * 8, st));
-    if (s->ntri > 0) {
-        prof_begin(s, st);
-        launch_rh_traverse<false>(s, lv, so, sd, keys, nullptr, st);
-        prof_end(s, st, kStageTraverse, 1);
-    }
+    if (s->ntri > 0 && (rc = rh_traverse<false>(s, lv, so, sd, keys, nullptr, st))) return rc;
     prof_begin(s, st);
     rh_finalize_nearest<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
         (const TriRec*)s->tris.ptr, (const int32_t*)s->tri_pos.ptr, so, sd, perm, keys, n, prim, t, b1, b2);
@@ -432,11 +547,7 @@ int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
     if ((rc = ensure(w.leafmask, (size_t)nleaf * 4))) return rc;
     uint32_t* mask = (uint32_t*)w.leafmask.ptr;
     PBG_CUDA(cudaMemsetAsync(mask, 0, (size_t)nleaf * 4, st));
-    if (s->ntri > 0) {
-        prof_begin(s, st);
-        launch_rh_traverse<true>(s, lv, so, sd, nullptr, mask, st);
-        prof_end(s, st, kStageTraverse, 1);
-    }
+    if (s->ntri > 0 && (rc = rh_traverse<true>(s, lv, so, sd, nullptr, mask, st))) return rc;
     prof_begin(s, st);
     rh_finalize_occluded<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(perm, mask, n, occ);
     prof_end(s, st, kStageOther, 1);

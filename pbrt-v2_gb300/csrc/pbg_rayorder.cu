@@ -102,6 +102,34 @@ __global__ void morton_kernel(const float4* __restrict__ ro, const float4* __res
               (spread5(qo0) << 2) | (spread5(qo1) << 1) | spread5(qo2);
 }
 
+// Ray-image order: when the caller declared its batches as a W x H ray image
+// (Preprocess, accelerators/rayhierarchy.cpp:250-265; ray i at x = i mod W,
+// y = i div W), the key is the 2-D Morton code of (x, y), so a leaf of 32
+// rays is an 8 x 4 tile of the image -- the reference's chunkX x chunkY
+// leaves, but compact at every level above too.
+__device__ __forceinline__ uint32_t spread16(uint32_t v) {
+    v &= 0xffffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+__global__ void image_key_kernel(const uint8_t* __restrict__ valid, int64_t n, int64_t width,
+                                 uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vals[i] = (int32_t)i;
+    if (valid && !valid[i]) {
+        keys[i] = 0xffffffffu;
+        return;
+    }
+    const uint32_t x = (uint32_t)(i % width), y = (uint32_t)(i / width);
+    // 15 bits per axis keeps valid keys below 0xffffffff
+    keys[i] = (spread16(y & 0x7fffu) << 1) | spread16(x & 0x7fffu);
+}
+
 // Pass 1: digit histogram of each tile, stored digit-major: hist[d * tiles + tile].
 __global__ void __launch_bounds__(kSortThreads)
     radix_hist_kernel(const uint32_t* __restrict__ keys, int64_t n, int shift, int tiles,
@@ -119,7 +147,85 @@ __global__ void __launch_bounds__(kSortThreads)
         hist[(int64_t)k * tiles + blockIdx.x] = h[k];
 }
 
-// Pass 2: exclusive scan of m counts in one CTA of 1024 threads.
+// Pass 2: exclusive scan of the m = tiles*256 counts in three phases:
+// per-chunk sums, one CTA over the chunk sums, per-chunk scans with offsets.
+constexpr int kScanChunk = 4096;  // counts per chunk, 4 per thread
+
+__device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t* warp_sums,
+                                                         uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t excl = (warp ? warp_sums[warp - 1] : 0u) + x - v;
+    if (total) *total = warp_sums[31];
+    return excl;
+}
+
+__global__ void __launch_bounds__(1024) scan_chunk_sums(const uint32_t* __restrict__ a, int64_t m,
+                                                        uint32_t* __restrict__ sums) {
+    __shared__ uint32_t ws[32];
+    const int64_t base = (int64_t)blockIdx.x * kScanChunk + threadIdx.x * 4;
+    uint32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (base + k < m) v += a[base + k];
+    uint32_t total;
+    block_excl_scan_1024(v, ws, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) scan_top(uint32_t* __restrict__ sums, int nchunks) {
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nchunks; base += 1024) {
+        const int i = base + threadIdx.x;
+        const uint32_t v = i < nchunks ? sums[i] : 0u;
+        uint32_t total;
+        const uint32_t e = block_excl_scan_1024(v, ws, &total);
+        if (i < nchunks) sums[i] = carry + e;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) scan_chunks(uint32_t* __restrict__ a, int64_t m,
+                                                    const uint32_t* __restrict__ sums) {
+    __shared__ uint32_t ws[32];
+    const int64_t base = (int64_t)blockIdx.x * kScanChunk + threadIdx.x * 4;
+    uint32_t v[4], s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = base + k < m ? a[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t run = sums[blockIdx.x] + block_excl_scan_1024(s, ws, nullptr);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < m) a[base + k] = run;
+        run += v[k];
+    }
+}
+
+// Single-CTA scan, kept for small inputs.
 __global__ void __launch_bounds__(1024) scan_kernel(uint32_t* __restrict__ a, int64_t m) {
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t carry;
@@ -226,9 +332,14 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
         prof_begin(s, st);
         radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ka, n, shift, tiles, hist);
         prof_end(s, st, kStageSort, 1);
+        const int64_t m = (int64_t)tiles * kRadix;
+        const int nchunks = (int)((m + kScanChunk - 1) / kScanChunk);
+        uint32_t* sums = hist + m + 8;  // after the histogram and the bounds words
         prof_begin(s, st);
-        scan_kernel<<<1, 1024, 0, st>>>(hist, (int64_t)tiles * kRadix);
-        prof_end(s, st, kStageSort, 1);
+        scan_chunk_sums<<<nchunks, 1024, 0, st>>>(hist, m, sums);
+        scan_top<<<1, 1024, 0, st>>>(sums, nchunks);
+        scan_chunks<<<nchunks, 1024, 0, st>>>(hist, m, sums);
+        prof_end(s, st, kStageSort, 3);
         prof_begin(s, st);
         radix_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(ka, va, n, shift, tiles, hist, kb, vb);
         prof_end(s, st, kStageSort, 1);
@@ -250,7 +361,8 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     int rc;
     if ((rc = ensure(w.mkeys, (size_t)n * 4)) || (rc = ensure(w.mkeys_tmp, (size_t)n * 4)) ||
         (rc = ensure(w.perm, (size_t)n * 4)) || (rc = ensure(w.perm_tmp, (size_t)n * 4)) ||
-        (rc = ensure(w.hist, ((size_t)tiles * kRadix + 8) * 4)))
+        (rc = ensure(w.hist, ((size_t)tiles * kRadix + 8 +
+                              ((size_t)tiles * kRadix + kScanChunk - 1) / kScanChunk + 8) * 4)))
         return rc;
     int* bounds = (int*)((uint32_t*)w.hist.ptr + (size_t)tiles * kRadix);
     const int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000,
@@ -260,13 +372,20 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     int64_t blocks = (n + 255) / 256;
     if (blocks > 4 * sms) blocks = 4 * sms;
-    prof_begin(s, st);
-    origin_bounds_kernel<<<(unsigned)blocks, 256, 0, st>>>(o, valid, n, bounds);
-    prof_end(s, st, kStageSort, 1);
-    prof_begin(s, st);
-    morton_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        o, d, valid, n, bounds, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
-    prof_end(s, st, kStageSort, 1);
+    if (s->image_w > 0 && n == s->image_w * s->image_h) {
+        prof_begin(s, st);
+        image_key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            valid, n, s->image_w, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
+        prof_end(s, st, kStageSort, 1);
+    } else {
+        prof_begin(s, st);
+        origin_bounds_kernel<<<(unsigned)blocks, 256, 0, st>>>(o, valid, n, bounds);
+        prof_end(s, st, kStageSort, 1);
+        prof_begin(s, st);
+        morton_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            o, d, valid, n, bounds, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
+        prof_end(s, st, kStageSort, 1);
+    }
     PBG_CUDA(cudaGetLastError());
     uint32_t* ko;
     int32_t* vo;

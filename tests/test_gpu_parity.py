@@ -129,3 +129,22 @@ def test_accelerators_agree_at_scale(gpu_lib):
     for kind in ("ray-bvh", "rayhierarchy"):
         got = make(kind, tris).Intersect(sub.copy())
         assert_hits_equal(got, ref, kind)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_ray_image_layout(gpu_lib, oracle, kind):
+    """Preprocess declares the breadth-first ray image (256 x 256, 1 spp);
+    the ray hierarchy then groups rays by 2-D image tiles.  Shadow batches
+    keep the layout with a validity mask."""
+    cfg = S.config_small_naive()
+    tris, rays = cfg["tris"], cfg["rays"]
+    acc = make(kind, tris)
+    acc.Preprocess(None, 1, 1, 1, xres=256, yres=256)
+    want = oracle.nearest(tris, rays)
+    got = acc.Intersect(rays.copy())
+    assert_hits_equal(got, want, kind)
+    hit = want[0] >= 0
+    p = rays[0:3] + rays[3:6] * np.where(hit, want[1], 0)[None]
+    sh = S.shadow_rays_to_point(p.T.astype(np.float32), cfg["light"])
+    occ = acc.IntersectP(sh, hit=hit)
+    np.testing.assert_array_equal(occ == ord("1"), oracle.anyhit(tris, sh, valid=hit.astype(np.uint8)) == 1)
