@@ -169,6 +169,59 @@ int pbg_hit_geometry_device(pbg_scene* scene, const float* o4, const float* d4,
                             const int32_t* prim, const float* t, const float* b1,
                             const float* b2, int64_t n, float* out14, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Breadth-first renderer on the device (renderers/breadth-first.cpp:18-228
+ * with the batch Li of integrators/directlighting.cpp:112-145 and
+ * integrators/path.cpp:43-157): camera rays of the whole image in one
+ * batch, Lambertian shading, light sampling, shadow and bounce batches
+ * through the scene's accelerator, film accumulation -- all on the GPU.
+ * ------------------------------------------------------------------- */
+
+/* Camera as pbrt's ProjectiveCamera holds it: RasterToCamera and the
+ * (non-animated) CameraToWorld, row-major m[i][j] (core/camera.cpp:68-88,
+ * cameras/perspective.cpp GenerateRayDifferential). */
+typedef struct pbg_camera {
+    float raster_to_camera[16];
+    float camera_to_world[16];
+    int32_t xres, yres;
+} pbg_camera;
+
+#define PBG_LIGHT_POINT 0 /* lights/point.cpp PointLight            */
+#define PBG_LIGHT_QUAD 1  /* lights/diffuse.cpp on a parallelogram  */
+typedef struct pbg_light {
+    int32_t type;
+    int32_t nsamples;  /* "nsamples" of the area light (directlighting) */
+    float pos[3];      /* point light position */
+    float intensity[3];/* point light I, RGB */
+    float quad[12];    /* area light corners p0, p1, p2, p3 (p2 = p1 + p3 - p0) */
+    float radiance[3]; /* area light L, RGB; emits on the side of (p1-p0)x(p3-p0) */
+} pbg_light;
+
+#define PBG_INTEGRATOR_DIRECT 0 /* SurfaceIntegrator "directlighting" */
+#define PBG_INTEGRATOR_PATH 1   /* SurfaceIntegrator "path"           */
+typedef struct pbg_render_params {
+    int32_t integrator;
+    int32_t spp_x, spp_y;   /* stratified sampler grid per pixel */
+    int32_t jitter;         /* 0: sample centres (pbrt "jitter" false) */
+    int32_t max_depth;      /* "maxdepth" (path: default 5) */
+    int32_t reserved0;
+    uint64_t seed;          /* counter-based sample stream seed */
+    float albedo[3];        /* MatteMaterial Kd of every triangle */
+    int32_t reserved[8];
+} pbg_render_params;
+
+typedef struct pbg_render_stats {
+    uint64_t camera_rays, nearest_rays, shadow_rays, bounces;
+    double ms_total;
+} pbg_render_stats;
+
+/* Renders the image; rgb receives [yres][xres][3] floats (host memory),
+ * ImageFilm's XYZ accumulation and box filter (film/image.cpp).  stats may
+ * be NULL. */
+int pbg_render(pbg_scene* scene, const pbg_camera* camera, const pbg_light* lights,
+               int32_t nlights, const pbg_render_params* params, float* rgb,
+               pbg_render_stats* stats);
+
 /* Counters and per-stage device times (replaces the GPU_TIMES / STAT_*
  * printouts, core/GPUparallel.h:532-538 and rayhierarchy.cpp:229-239).
  * Reading them synchronises the scene's pending timing events. */

@@ -179,6 +179,91 @@ class BVH:
         return occ
 
 
+class _Cam(C.Structure):
+    _fields_ = [("r2c", C.c_float * 16), ("c2w", C.c_float * 16), ("xres", C.c_int), ("yres", C.c_int)]
+
+
+class _Light(C.Structure):
+    _fields_ = [("type", C.c_int), ("nsamples", C.c_int), ("pos", C.c_float * 3),
+                ("I", C.c_float * 3), ("quad", C.c_float * 12), ("L", C.c_float * 3)]
+
+
+class _Params(C.Structure):
+    _fields_ = [("integrator", C.c_int), ("spp_x", C.c_int), ("spp_y", C.c_int), ("jitter", C.c_int),
+                ("max_depth", C.c_int), ("seed", C.c_uint64), ("albedo", C.c_float * 3)]
+
+
+def render(tris, r2c, c2w, xres, yres, lights, integrator="directlighting", spp=(1, 1),
+           jitter=False, max_depth=5, seed=1, albedo=(0.7, 0.7, 0.7), threads=None):
+    """The CPU restatement of the renderer (oracle/render_oracle.c).  lights:
+    dicts {"type": "point", "pos", "I"} or {"type": "quad", "quad", "L",
+    "nsamples"}.  Returns rgb [yres, xres, 3]."""
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    cam = _Cam()
+    cam.r2c[:] = [float(x) for x in np.asarray(r2c, np.float32).reshape(16)]
+    cam.c2w[:] = [float(x) for x in np.asarray(c2w, np.float32).reshape(16)]
+    cam.xres, cam.yres = int(xres), int(yres)
+    arr = (_Light * max(1, len(lights)))()
+    for k, lt in enumerate(lights):
+        if lt["type"] == "point":
+            arr[k].type, arr[k].nsamples = 0, 1
+            arr[k].pos[:] = [float(x) for x in lt["pos"]]
+            arr[k].I[:] = [float(x) for x in lt["I"]]
+        else:
+            arr[k].type, arr[k].nsamples = 1, int(lt.get("nsamples", 4))
+            arr[k].quad[:] = [float(x) for x in np.asarray(lt["quad"], np.float32).reshape(12)]
+            arr[k].L[:] = [float(x) for x in lt["L"]]
+    p = _Params()
+    p.integrator = {"directlighting": 0, "path": 1}[integrator]
+    p.spp_x, p.spp_y = spp
+    p.jitter = int(bool(jitter))
+    p.max_depth = max_depth
+    p.seed = seed
+    p.albedo[:] = [float(a) for a in albedo]
+    L = lib()
+    L.orc_render.argtypes = [_fp, C.c_int64, C.POINTER(_Cam), C.POINTER(_Light), C.c_int,
+                             C.POINTER(_Params), _fp, C.c_int]
+    img = np.empty((yres, xres, 3), np.float32)
+    L.orc_render(_f(tris), tris.shape[0], C.byref(cam), arr, len(lights), C.byref(p), _f(img),
+                 threads or os.cpu_count() or 1)
+    return img
+
+
+def ref_camera(xres, yres, eye, look, up, fov, xy):
+    """The reference's PerspectiveCamera: (r2c [4,4], c2w [4,4], rays [n, 6])
+    for raster samples xy [n, 2]."""
+    R = ref()
+    R.ref_camera.argtypes = [C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, _fp, _fp, _fp, C.c_int64, _fp]
+    e = np.asarray(eye, np.float32)
+    lk = np.asarray(look, np.float32)
+    u = np.asarray(up, np.float32)
+    xy = np.ascontiguousarray(xy, np.float32)
+    r2c = np.empty(16, np.float32)
+    c2w = np.empty(16, np.float32)
+    rays = np.empty((len(xy), 6), np.float32)
+    R.ref_camera(xres, yres, _f(e), _f(lk), _f(u), fov, _f(r2c), _f(c2w), _f(xy), len(xy), _f(rays))
+    return r2c.reshape(4, 4), c2w.reshape(4, 4), rays
+
+
+def ref_render(scene_text: str, workdir: str):
+    """Renders a scene file with the reference's own CPU renderer
+    (oracle/_ref/pbrt_ref); returns the PFM image [yres, xres, 3]."""
+    exe = os.path.join(HERE, "_ref", "pbrt_ref")
+    path = os.path.join(workdir, "scene.pbrt")
+    with open(path, "w") as f:
+        f.write(scene_text)
+    subprocess.check_call([exe, path], cwd=workdir, stdout=subprocess.DEVNULL,
+                          stderr=subprocess.DEVNULL)
+    return read_pfm(os.path.join(workdir, "out.pfm"))
+
+
+def read_pfm(path):
+    data = open(path, "rb").read()
+    parts = data.split(b"\n", 3)
+    w, h = (int(x) for x in parts[1].split())
+    return np.frombuffer(parts[3], np.float32, count=w * h * 3).reshape(h, w, 3).copy()
+
+
 class RefScene:
     """The reference's own TriangleMesh + GeometricPrimitive (+ BVHAccel)."""
 

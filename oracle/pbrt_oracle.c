@@ -603,6 +603,18 @@ static void bvh_trace_one(bvh_t* b, const float o[3], const float d[3], float mi
     if (best >= 0) { *tout = bt; *b1o = bb1; *b2o = bb2; }
 }
 
+/* One ray through the BVH baseline; returns the hit index or -1. */
+int32_t orc_bvh_trace(void* bvh, const float o[3], const float d[3], float mint, float maxt,
+                      int anyhit, float* t, float* b1, float* b2) {
+    int32_t prim = -1;
+    float tt = 0.f, u1 = 0.f, u2 = 0.f;
+    bvh_trace_one((bvh_t*)bvh, o, d, mint, maxt, anyhit, &prim, &tt, &u1, &u2);
+    if (t) *t = tt;
+    if (b1) *b1 = u1;
+    if (b2) *b2 = u2;
+    return prim;
+}
+
 static void* bvh_nearest_worker(void* arg) {
     bvh_job_t* j = (bvh_job_t*)arg;
     for (int64_t i = j->begin; i < j->end; ++i) {

@@ -159,3 +159,70 @@ void ref_anyhit(void* p, const float* rays, int64_t n, int use_bvh, uint8_t* occ
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ camera
+#include "cameras/perspective.h"
+#include "film.h"
+#include "camera.h"
+#include "sampler.h"
+
+namespace {
+// A film that only carries the resolution the camera reads.
+struct SizeFilm : public Film {
+    SizeFilm(int x, int y) : Film(x, y) {}
+    void AddSample(const CameraSample&, const Spectrum&) {}
+    void Splat(const CameraSample&, const Spectrum&) {}
+    void GetSampleExtent(int* a, int* b, int* c, int* d) const { *a = 0; *b = xResolution; *c = 0; *d = yResolution; }
+    void GetPixelExtent(int* a, int* b, int* c, int* d) const { *a = 0; *b = xResolution; *c = 0; *d = yResolution; }
+    void WriteImage(float) {}
+};
+// Exposes ProjectiveCamera's protected RasterToCamera.
+struct ExposedCamera : public PerspectiveCamera {
+    ExposedCamera(const AnimatedTransform& c2w, const float sw[4], float fov, Film* f)
+        : PerspectiveCamera(c2w, sw, 0.f, 1.f, 0.f, 1e30f, fov, f) {}
+    const Transform& r2c() const { return RasterToCamera; }
+};
+}  // namespace
+
+extern "C" {
+
+// pbrt's PerspectiveCamera for LookAt(eye, look, up) + Camera "perspective"
+// "fov", the way the scene-file API builds it (core/api.cpp pbrtLookAt,
+// MakeCamera; cameras/perspective.cpp CreatePerspectiveCamera with the
+// default screen window).  Writes RasterToCamera and CameraToWorld
+// (row-major) and the GenerateRayDifferential ray (o, d) of each raster
+// sample (xy[2*i], xy[2*i+1]) into rays6[6*i].
+void ref_camera(int xres, int yres, const float* eye, const float* look, const float* up, float fov,
+                float* r2c16, float* c2w16, const float* xy, int64_t n, float* rays6) {
+    Transform w2c = LookAt(Point(eye[0], eye[1], eye[2]), Point(look[0], look[1], look[2]),
+                           Vector(up[0], up[1], up[2]));
+    Transform c2w = Inverse(w2c);
+    AnimatedTransform at(&c2w, 0.f, &c2w, 1.f);
+    float frame = float(xres) / float(yres);
+    float sw[4];
+    if (frame > 1.f) { sw[0] = -frame; sw[1] = frame; sw[2] = -1.f; sw[3] = 1.f; }
+    else { sw[0] = -1.f; sw[1] = 1.f; sw[2] = -1.f / frame; sw[3] = 1.f / frame; }
+    // Camera's destructor deletes its film (core/camera.cpp), so it is heap-allocated.
+    ExposedCamera cam(at, sw, fov, new SizeFilm(xres, yres));
+    const Matrix4x4& a = cam.r2c().GetMatrix();
+    const Matrix4x4& b = c2w.GetMatrix();
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            r2c16[4 * i + j] = a.m[i][j];
+            c2w16[4 * i + j] = b.m[i][j];
+        }
+    for (int64_t i = 0; i < n; ++i) {
+        CameraSample s;
+        s.imageX = xy[2 * i];
+        s.imageY = xy[2 * i + 1];
+        s.lensU = s.lensV = 0.5f;
+        s.time = 0.f;
+        RayDifferential r;
+        cam.GenerateRayDifferential(s, &r);
+        float* o = rays6 + 6 * i;
+        o[0] = r.o.x; o[1] = r.o.y; o[2] = r.o.z;
+        o[3] = r.d.x; o[4] = r.d.y; o[5] = r.d.z;
+    }
+}
+
+}  // extern "C"

@@ -67,7 +67,7 @@ void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out);
 struct Work {
     DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
         perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo, queue_a, queue_b,
-        qcount;
+        qcount, scan_sums;
     int64_t cap = 0;
 };
 

@@ -399,6 +399,21 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     return PBG_OK;
 }
 
+// In-place exclusive scan of m counts (the renderer's queue compaction).
+int scan_counts(pbg_scene* s, uint32_t* a, int64_t m, cudaStream_t st) {
+    if (m <= 0) return PBG_OK;
+    const int nchunks = (int)((m + kScanChunk - 1) / kScanChunk);
+    int rc = ensure(s->work.scan_sums, (size_t)(nchunks + 8) * 4);
+    if (rc) return rc;
+    uint32_t* sums = (uint32_t*)s->work.scan_sums.ptr;
+    scan_chunk_sums<<<nchunks, 1024, 0, st>>>(a, m, sums);
+    scan_top<<<1, 1024, 0, st>>>(sums, nchunks);
+    scan_chunks<<<nchunks, 1024, 0, st>>>(a, m, sums);
+    s->counters.kernel_launches += 3;
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
 int ray_order(pbg_scene* s, const float4* o, const float4* d, int64_t n, const int32_t** perm,
               cudaStream_t st) {
     if (n < 4096) {  // too small to gain from ordering

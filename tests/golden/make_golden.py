@@ -150,6 +150,50 @@ def ref_answers(tris, rays, uv_mode_geo=0, uvs=None, with_geo=True):
     return out
 
 
+SMALL_CAMERA = dict(eye=(0.0, 1.0, -4.0), look=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fov=45.0)
+SMALL_LIGHT = dict(pos=(2.0, 4.0, -2.0), I=(16.0, 16.0, 16.0))
+
+
+def small_scene_text(tris, out_name="out.pfm"):
+    """The small naive workload as a pbrt scene file: 256x256, 1 spp at pixel
+    centres, point light, matte 0.7, directlighting, the CPU "bvh"."""
+    n = len(tris)
+    P = " ".join(repr(float(x)) for x in tris.reshape(-1))
+    idx = " ".join(str(i) for i in range(3 * n))
+    c, l = SMALL_CAMERA, SMALL_LIGHT
+    return f'''LookAt {c["eye"][0]} {c["eye"][1]} {c["eye"][2]}  {c["look"][0]} {c["look"][1]} {c["look"][2]}  {c["up"][0]} {c["up"][1]} {c["up"][2]}
+Camera "perspective" "float fov" [{c["fov"]}]
+Sampler "stratified" "integer xsamples" [1] "integer ysamples" [1] "bool jitter" ["false"]
+PixelFilter "box"
+Film "image" "integer xresolution" [256] "integer yresolution" [256] "string filename" ["{out_name}"]
+Renderer "sampler"
+SurfaceIntegrator "directlighting"
+Accelerator "bvh"
+WorldBegin
+LightSource "point" "point from" [{l["pos"][0]} {l["pos"][1]} {l["pos"][2]}] "rgb I" [{l["I"][0]} {l["I"][1]} {l["I"][2]}]
+Material "matte" "rgb Kd" [0.7 0.7 0.7]
+Shape "trianglemesh" "integer indices" [{idx}] "point P" [{P}]
+WorldEnd
+'''
+
+
+def case_render_small():
+    import tempfile
+    cfg = S.config_small_naive()
+    tris = cfg["tris"]
+    xs, ys = np.meshgrid(np.arange(256), np.arange(256))
+    xy = np.stack([xs.reshape(-1) + 0.5, ys.reshape(-1) + 0.5], 1).astype(np.float32)
+    c = SMALL_CAMERA
+    r2c, c2w, rays6 = O.ref_camera(256, 256, c["eye"], c["look"], c["up"], c["fov"], xy)
+    with tempfile.TemporaryDirectory() as td:
+        img = O.ref_render(small_scene_text(tris), td)
+    sel = np.arange(0, len(xy), 7)
+    return dict(r2c=r2c, c2w=c2w, image=img, camera_xy=xy[sel], camera_rays=rays6[sel],
+                light_pos=np.array(SMALL_LIGHT["pos"], np.float32),
+                light_I=np.array(SMALL_LIGHT["I"], np.float32),
+                albedo=np.array([0.7, 0.7, 0.7], np.float32))
+
+
 def main():
     if not O.ref_available():
         if not O.build_ref():
@@ -192,6 +236,9 @@ def main():
     above[6] = np.nextafter(t0, np.float32(np.inf))
     rays = np.concatenate([eq_max, eq_min, below, above], 1)
     np.savez_compressed(os.path.join(HERE, "limits.npz"), **ref_answers(tris, rays))
+
+    # the reference's own render of the small naive workload
+    np.savez_compressed(os.path.join(HERE, "render_small.npz"), **case_render_small())
 
     # empty scene
     tris = np.zeros((0, 9), F32)
