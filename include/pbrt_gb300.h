@@ -158,6 +158,7 @@ int pbg_intersect_device(pbg_scene* scene, const float* o4, const float* d4,
 int pbg_occluded_device(pbg_scene* scene, const float* o4, const float* d4,
                         const uint8_t* valid, int64_t n, uint8_t* occ, void* stream);
 
+
 /* Differential geometry of each hit, the part of Triangle::Intersect that
  * builds the DifferentialGeometry (shapes/trianglemesh.cpp:158-190,
  * core/diffgeom.cpp:32-47) and the fork's computeDpTuTv kernel
