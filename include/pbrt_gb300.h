@@ -158,6 +158,22 @@ int pbg_intersect_device(pbg_scene* scene, const float* o4, const float* d4,
 int pbg_occluded_device(pbg_scene* scene, const float* o4, const float* d4,
                         const uint8_t* valid, int64_t n, uint8_t* occ, void* stream);
 
+/* Nearest hit without any device allocation, for callers that cannot call
+ * cudaMalloc (code running inside another framework's memory pool or
+ * allocator hooks, or a host that has already committed the device's memory
+ * to its own arenas).  No counterpart in the reference: its accelerators
+ * always allocate OpenCL buffers per call.  Everything is device memory the
+ * caller owns: tri9 (9 floats per triangle, as pbg_scene_create takes
+ * them), o4/d4 rays, prim/t/b1/b2 outputs; no scene object is needed.
+ * Results equal pbg_intersect_device on a naive scene.  Scratch is one
+ * fixed 8 MB __device__ array inside the library, so at most 1048576 rays
+ * per call (more is rejected with PBG_ERR_INVALID_ARGUMENT); every call
+ * shares that array, so calls that overlap on the GPU race and must be
+ * serialised; the first call on a device looks the array up and should come
+ * before any stream capture.  stream = NULL is the legacy default stream. */
+int pbg_intersect_naive_noalloc(const float* tri9, int64_t ntri, const float* o4,
+                                const float* d4, int64_t n, int32_t* prim, float* t, float* b1,
+                                float* b2, void* stream);
 
 /* Differential geometry of each hit, the part of Triangle::Intersect that
  * builds the DifferentialGeometry (shapes/trianglemesh.cpp:158-190,
