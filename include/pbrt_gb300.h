@@ -239,6 +239,60 @@ int pbg_render(pbg_scene* scene, const pbg_camera* camera, const pbg_light* ligh
                int32_t nlights, const pbg_render_params* params, float* rgb,
                pbg_render_stats* stats);
 
+/* ---------------------------------------------------------------------
+ * Learned traversal ordering (Accelerator "ray-bvh" only).  No counterpart
+ * in the reference.  An MLP (105 ray features -> 64 -> 64 -> 256 logits,
+ * BF16 weights, FP32 accumulation, tcgen05 kernels) predicts which of the
+ * 256 top clusters of the BVH holds a ray's first hit; the traversal visits
+ * that cluster first and then runs the full exact walk, so hits and
+ * occlusion are identical with the ordering on or off.  Training is online,
+ * on first-hit records the accelerator collects from its own nearest-hit
+ * batches.
+ * ------------------------------------------------------------------- */
+typedef struct pbg_learn_params {
+    int32_t batch;            /* records per SGD step (multiple of 128; 0 = 8192) */
+    int32_t steps_per_train;  /* SGD steps per pbg_learn_train call (0 = 8) */
+    float lr;                 /* learning rate (0 = 0.05) */
+    float momentum;           /* (0 = 0.9) */
+    int32_t records;          /* training records kept, ring buffer (0 = 262144) */
+    int32_t reserved0;
+    uint64_t seed;            /* weight initialisation */
+    int32_t reserved[8];
+} pbg_learn_params;
+
+typedef struct pbg_learn_stats {
+    uint64_t trained_steps, records;
+    float last_loss, last_accuracy; /* of the last SGD step (top-1 cluster) */
+    double infer_ms, train_ms;      /* device time spent so far */
+} pbg_learn_stats;
+
+/* on = 1 builds the clusters and the network (params may be NULL);
+ * on = 0 switches the ordering off (the plain kernels run). */
+int pbg_learn_enable(pbg_scene* scene, int32_t on, const pbg_learn_params* params);
+/* Runs SGD steps on the collected records (steps <= 0: steps_per_train). */
+int pbg_learn_train(pbg_scene* scene, int32_t steps);
+int pbg_learn_get_stats(pbg_scene* scene, pbg_learn_stats* out);
+/* Parameters as FP32 host arrays in the order W1 [64 x 112], b1 [64],
+ * W2 [64 x 64], b2 [64], W3 [256 x 64], b3 [256] (27,648 + 384 floats):
+ * read (get = 1) or write (get = 0). */
+int pbg_learn_params_io(pbg_scene* scene, float* params, int32_t get);
+/* One forward + backward pass on host records x [B x 112] (float, rounded
+ * to BF16 as the network sees them) and labels [B] (B % 128 == 0): writes
+ * the FP32 gradients in the layout of pbg_learn_params_io, and the loss.
+ * Leaves the parameters unchanged; for checking the tensor-core backward
+ * pass against a CPU reference. */
+int pbg_learn_gradients(pbg_scene* scene, const float* x, const int32_t* labels, int32_t B,
+                        float* grads, float* loss);
+
+/* Tensor-core GEMM used by the learned traversal ordering, exposed for
+ * checking: C[M x N] (+)= A[M x K] * B[N x K]^T with A, B row-major BF16
+ * (raw 16-bit patterns) and C row-major FP32, all device memory; tcgen05
+ * MMAs with FP32 accumulation in tensor memory.  M % 128 == 0,
+ * 16 <= N <= 256 with N % 16 == 0, K % 16 == 0.  Synchronises the stream.
+ * No counterpart in the reference (it has no learned component). */
+int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t M, int32_t N,
+                     int32_t K, int32_t accumulate, void* stream);
+
 /* Counters and per-stage device times (replaces the GPU_TIMES / STAT_*
  * printouts, core/GPUparallel.h:532-538 and rayhierarchy.cpp:229-239).
  * Reading them synchronises the scene's pending timing events. */

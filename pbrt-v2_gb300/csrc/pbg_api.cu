@@ -20,6 +20,7 @@
 #include <string>
 
 #include "pbg_internal.h"
+#include "pbg_learn.h"
 #include "pbg_tma.cuh"
 
 namespace pbg {
@@ -482,6 +483,8 @@ int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t 
         s->bvh_depth = hb.max_depth;
         s->unculled = hb.unculled;
         s->counters.bvh_nodes = (uint64_t)hb.nodes.size();
+        s->host_nodes = hb.nodes;
+        s->host_order = hb.order;
     }
     if ((rc = upload_triangles(s, tri9, order))) return fail(rc);
     if (uv6 && ntri > 0) {
@@ -509,6 +512,10 @@ void pbg_scene_destroy(pbg_scene* s) {
     release(s->tri_pos);
     release(s->err);
     release(s->workc);
+    if (s->learn) {
+        learn_free(s->learn);
+        s->learn = nullptr;
+    }
     Work& w = s->work;
     DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.ray_o2, &w.ray_d2, &w.valid, &w.prim,
                            &w.t, &w.b1, &w.b2, &w.occ, &w.keys, &w.stage, &w.perm,

@@ -18,6 +18,7 @@
 // by 1 + 2*gamma(3), which is conservative for the (already padded) box.
 #include "pbg_internal.h"
 #include "pbg_count.cuh"
+#include "pbg_learn.h"
 #include "pbg_tma.cuh"
 
 namespace pbg {
@@ -74,14 +75,20 @@ __device__ __forceinline__ bool test_run(const TriRec* __restrict__ tris, int32_
     return false;
 }
 
-template <bool ANY, bool STATS>
+// ORDERED: pred[ray] names the cluster (a child reference cref[2k], with its
+// leaf count cref[2k+1]) the learned model expects the first hit in; the
+// walk visits that subtree first, then the whole tree from the root with the
+// cluster skipped -- every node and leaf is still visited under the same
+// t_max rule, so the result is the plain walk's.
+template <bool ANY, bool STATS, bool ORDERED>
 __global__ void __launch_bounds__(kBvhThreads)
     bvh_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris, int32_t unculled,
                const float4* __restrict__ ro, const float4* __restrict__ rd,
                const uint8_t* __restrict__ valid, const int32_t* __restrict__ perm, int64_t n,
                int32_t* __restrict__ prim_out, float* __restrict__ t_out,
                float* __restrict__ b1_out, float* __restrict__ b2_out, uint8_t* __restrict__ occ,
-               int* status, unsigned long long* wcount) {
+               int* status, unsigned long long* wcount, const uint16_t* __restrict__ pred,
+               const int32_t* __restrict__ cref) {
     const int64_t slot = (int64_t)blockIdx.x * kBvhThreads + threadIdx.x;
     if (slot >= n) return;
     const int64_t ray = perm ? (int64_t)perm[slot] : slot;
@@ -111,6 +118,23 @@ __global__ void __launch_bounds__(kBvhThreads)
     int sp = 0;
     int32_t node = 0;
     bool overflow = false;
+    int32_t skip = INT32_MIN;  // the predicted cluster, once walked
+    if (ORDERED && !done) {
+        const int c = pred[ray];
+        const int32_t ref = cref[2 * c], cnt = cref[2 * c + 1];
+        skip = ref;
+        if (ref == INT32_MIN) {
+            // an unused cluster slot: plain walk
+        } else if (ref < 0) {
+            if (STATS) wc.leaf++;
+            done = test_run<ANY, STATS>(tris, ~ref, cnt, o, d, nd, best_t, best, bb1, bb2, wc);
+        } else {
+            stack[sp] = 0;  // resume at the root afterwards
+            stack_t[sp] = -INFINITY;
+            ++sp;
+            node = ref;
+        }
+    }
     while (!done) {
         const BvhNode nd_ = nodes[node];
         if (STATS) wc.node += 2;
@@ -120,6 +144,10 @@ __global__ void __launch_bounds__(kBvhThreads)
         bool h1 = slab(ri, nd_.n1.x, nd_.n1.y, nd_.n1.z, nd_.n1.w, nd_.n2.z, nd_.n2.w, o.w, best_t,
                        &tn1);
         const int32_t c0 = nd_.n3.x, c1 = nd_.n3.y;
+        if (ORDERED) {  // the predicted cluster has been walked already
+            h0 = h0 && c0 != skip;
+            h1 = h1 && c1 != skip;
+        }
         // Leaf children are tested at once, nearer one first.
         const bool swap = h0 && h1 && tn1 < tn0;
         for (int q = 0; q < 2 && !done; ++q) {
@@ -186,18 +214,38 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
         int rc = ray_order(s, o, d, n, &perm, st);
         if (rc) return rc;
     }
+    const uint16_t* pred = nullptr;
+    const int32_t* cref = nullptr;
+    int rc = learn_predict(s, o, d, n, &pred, &cref, st);
+    if (rc) return rc;
     const unsigned grid = (unsigned)((n + kBvhThreads - 1) / kBvhThreads);
+    const BvhNode* nodes = (const BvhNode*)s->bvh.ptr;
+    const TriRec* tris = (const TriRec*)s->tris.ptr;
+    int* status = (int*)s->err.ptr;
+    unsigned long long* wc = (unsigned long long*)s->workc.ptr;
     prof_begin(s, st);
-    if (s->prof.level >= 2)
-        bvh_kernel<ANY, true><<<grid, kBvhThreads, 0, st>>>(
-            (const BvhNode*)s->bvh.ptr, (const TriRec*)s->tris.ptr, s->unculled, o, d, valid, perm,
-            n, prim, t, b1, b2, occ, (int*)s->err.ptr, (unsigned long long*)s->workc.ptr);
-    else
-        bvh_kernel<ANY, false><<<grid, kBvhThreads, 0, st>>>(
-            (const BvhNode*)s->bvh.ptr, (const TriRec*)s->tris.ptr, s->unculled, o, d, valid, perm,
-            n, prim, t, b1, b2, occ, (int*)s->err.ptr, nullptr);
+    if (pred) {
+        if (s->prof.level >= 2)
+            bvh_kernel<ANY, true, true><<<grid, kBvhThreads, 0, st>>>(
+                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, wc, pred, cref);
+        else
+            bvh_kernel<ANY, false, true><<<grid, kBvhThreads, 0, st>>>(
+                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, nullptr, pred,
+                cref);
+    } else {
+        if (s->prof.level >= 2)
+            bvh_kernel<ANY, true, false><<<grid, kBvhThreads, 0, st>>>(
+                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, wc, nullptr,
+                nullptr);
+        else
+            bvh_kernel<ANY, false, false><<<grid, kBvhThreads, 0, st>>>(
+                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, nullptr,
+                nullptr, nullptr);
+    }
     prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
+    // first-hit records for the learned ordering
+    if (!ANY && s->learn && s->learn->enabled) return learn_collect(s, o, d, prim, n, st);
     return PBG_OK;
 }
 

@@ -11,6 +11,8 @@
 
 namespace pbg {
 
+struct Learner;
+
 // Two-wide BVH node (64 bytes): both children's boxes, so one node fetch
 // decides both children.  A child index >= 0 is an inner node; a negative
 // index ~start is a leaf holding triangles [start, start + count).
@@ -89,6 +91,9 @@ struct pbg_scene {
     int bvh_depth = 0;
     int32_t unculled = 0;      // records [0, unculled) are tested by every ray
     int rh_groups = 1;         // triangle groups per rayhierarchy traversal (grows on overflow)
+    std::vector<pbg::BvhNode> host_nodes;  // ray-bvh tree, kept for the learned clusters
+    std::vector<int32_t> host_order;
+    struct pbg::Learner* learn = nullptr;
     int64_t image_w = 0, image_h = 0;  // ray-image layout from pbg_preprocess (0 = none)
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     pbg::DeviceBuffer err;     // int[4] device status words

@@ -1,0 +1,135 @@
+// pbg_mlp.cu -- tensor-core (tcgen05) kernels of the learned traversal
+// ordering: a generic BF16 GEMM with FP32 accumulation in TMEM (the training
+// passes are built from it) and, in pbg_learn.cu, the fused inference MLP.
+#include "pbg_internal.h"
+#include "pbg_tc.cuh"
+
+namespace pbg {
+
+constexpr int kTcRows = 128;   // M of one MMA (cta_group::1)
+constexpr int kTcKChunk = 128; // K staged per round
+
+// C[M x N] (+)= A[M x K] * B[N x K]^T.  A, B: row-major bf16 (K contiguous,
+// i.e. K-major); C: row-major fp32.  M % 128 == 0, N % 16 == 0 and
+// 16 <= N <= 256, K % 16 == 0.  One CTA of 4 warps per 128-row tile.
+__global__ void __launch_bounds__(128)
+    tc_gemm_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ B, float* __restrict__ C,
+                   int M, int N, int K, int accumulate_c, int* status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sa = smem;                                 // 128 x 128 bf16 = 32 KB
+    uint8_t* sb = smem + kTcRows * kTcKChunk * 2;       // 256 x 128 bf16 = 64 KB
+    uint64_t* bar = (uint64_t*)(sb + 256 * kTcKChunk * 2);
+    uint32_t* tslot = (uint32_t*)(bar + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kTcRows;
+    uint32_t ncols = 32;
+    while ((int)ncols < N) ncols <<= 1;
+    if (warp == 0) tmem_alloc(tslot, ncols);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tslot;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int k0 = 0; k0 < K && ok; k0 += kTcKChunk) {
+        const int kc = min(kTcKChunk, K - k0);
+        const int kb = kc >> 3;  // 16-byte groups per row
+        for (int idx = threadIdx.x; idx < kTcRows * kb; idx += blockDim.x) {
+            const int r = idx / kb, g = idx % kb;
+            const uint4 v = *(const uint4*)(A + (size_t)(m0 + r) * K + k0 + g * 8);
+            *(uint4*)(sa + core_offset(r, g * 8, kc)) = v;
+        }
+        for (int idx = threadIdx.x; idx < N * kb; idx += blockDim.x) {
+            const int r = idx / kb, g = idx % kb;
+            const uint4 v = *(const uint4*)(B + (size_t)r * K + k0 + g * 8);
+            *(uint4*)(sb + core_offset(r, g * 8, kc)) = v;
+        }
+        fence_proxy_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (threadIdx.x == 0) {
+            const uint32_t sbo = (uint32_t)kb * 128u;
+            for (int ks = 0; ks < (kc >> 4); ++ks) {
+                const uint64_t ad = smem_desc(sa + ks * 256, 128u, sbo);
+                const uint64_t bd = smem_desc(sb + ks * 256, 128u, sbo);
+                tc_mma(tbase, ad, bd, idesc_bf16(kTcRows, N), (k0 > 0 || ks > 0) ? 1u : 0u);
+            }
+            tc_commit(bar);
+        }
+        ok = mbar_wait_bounded(bar, phase, status);
+        phase ^= 1u;
+        tc_fence_after();
+    }
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            float* out = C + (size_t)row * N + c0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) out[j] = accumulate_c ? out[j] + v[j] : v[j];
+        }
+    } else if (threadIdx.x == 0) {
+        // give in-flight MMAs one more bounded window before TMEM is released
+        mbar_wait_bounded(bar, phase ^ 1u, status);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_free(tbase, ncols);
+}
+
+size_t tc_gemm_smem_bytes() { return (size_t)kTcRows * kTcKChunk * 2 + 256 * kTcKChunk * 2 + 64; }
+
+int tc_gemm(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K, int accumulate,
+            int* status, cudaStream_t st) {
+    if (M <= 0 || M % kTcRows || N < 16 || N > 256 || N % 16 || K <= 0 || K % 16) {
+        set_last_error("tc_gemm: M % 128, 16 <= N <= 256 with N % 16, K % 16 required");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    static bool attr = false;
+    if (!attr) {
+        PBG_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)tc_gemm_smem_bytes()));
+        attr = true;
+    }
+    tc_gemm_kernel<<<M / kTcRows, 128, tc_gemm_smem_bytes(), st>>>(A, B, C, M, N, K, accumulate, status);
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
+}  // namespace pbg
+
+using namespace pbg;
+
+// Status words for library-level launches that have no scene.
+static int* g_status = nullptr;
+
+extern "C" int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t M, int32_t N,
+                                int32_t K, int32_t accumulate, void* stream) {
+    if (!A || !B || !C) {
+        pbg::set_last_error("pbg_tc_gemm_bf16: null pointer");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (!g_status) {
+        cudaError_t e = cudaMalloc(&g_status, 4 * sizeof(int));
+        if (e != cudaSuccess) return pbg::cuda_status(e, "cudaMalloc(status)");
+        cudaMemset(g_status, 0, 4 * sizeof(int));
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = pbg::tc_gemm(A, B, C, M, N, K, accumulate, g_status, st);
+    if (rc) return rc;
+    int h[4] = {0, 0, 0, 0};
+    PBG_CUDA(cudaMemcpyAsync(h, g_status, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PBG_CUDA(cudaStreamSynchronize(st));
+    if (h[pbg::kStatusTimeout]) {
+        cudaMemset(g_status, 0, 4 * sizeof(int));
+        pbg::set_last_error("pbg_tc_gemm_bf16: bounded mbarrier wait expired");
+        return PBG_ERR_DEVICE_TIMEOUT;
+    }
+    return PBG_OK;
+}

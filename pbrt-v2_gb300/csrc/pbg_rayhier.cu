@@ -39,8 +39,6 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
 constexpr int kLeafRays = 32;
 constexpr int kFan = 4;
 constexpr int kMaxLevels = 16;
-constexpr int kRhThreads = 128;
-constexpr int kRhStack = 48;
 
 struct __align__(16) RayNode {
     float4 a;  // origin sphere: centre.xyz, radius

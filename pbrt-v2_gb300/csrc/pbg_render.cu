@@ -33,6 +33,7 @@
 
 #include "pbg_dg.cuh"
 #include "pbg_internal.h"
+#include "pbg_learn.h"
 
 namespace pbg {
 
@@ -606,6 +607,8 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
         nq = nn;
         stt.bounces = (uint64_t)bounce + 1;
     }
+    // online training of the learned ordering on this frame's records
+    if (s->learn && s->learn->enabled && (r = learn_train(s, 0, st))) return r;
     film_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(npix, rc.spp, (const float*)B.L.ptr,
                                                                  (float*)B.rgb.ptr);
     PBG_CUDA(cudaGetLastError());
