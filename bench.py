@@ -305,23 +305,51 @@ def run_gpu_path(args, rank, world, dev):
     cam = R.camera_struct(r2c, c2w, res, res)
     light = R.quad_light(PATH_LIGHT, (12.0, 12.0, 12.0), 1)
     prm = R.render_params("path", spp=(2, 4), jitter=True, max_depth=5, seed=17)
-    for _ in range(args.warmup):
-        R.render(acc, cam, [light], prm)
-    torch.cuda.synchronize()
-    launches0 = acc.stats()["kernel_launches"]
-    acc.profile(True)
-    frames, walls = [], []
-    if world > 1:
-        torch.distributed.barrier()
-    with ClockSampler(dev) as clk:
-        for k in range(args.steps):
-            prm.seed = 1000 + k
-            w0 = time.perf_counter()
-            img, st = R.render(acc, cam, [light], prm)
-            walls.append(time.perf_counter() - w0)
-            frames.append(st)
-    stt = acc.stats()
-    acc.profile(False)
+
+    def measure(label):
+        for k in range(args.warmup):
+            prm.seed = 500 + k
+            R.render(acc, cam, [light], prm)
+        torch.cuda.synchronize()
+        l0 = acc.stats()["kernel_launches"]
+        acc.profile(True)
+        frames, walls = [], []
+        if world > 1:
+            torch.distributed.barrier()
+        with ClockSampler(dev) as clk:
+            for k in range(args.steps):
+                prm.seed = 1000 + k  # the same frames in every mode
+                w0 = time.perf_counter()
+                img, st = R.render(acc, cam, [light], prm)
+                walls.append(time.perf_counter() - w0)
+                frames.append(st)
+        stt = acc.stats()
+        acc.profile(False)
+        return frames, walls, stt, clk.summary(), stt["kernel_launches"] - l0, img
+
+    learned_line = None
+    frames, walls, stt, clocks, launches, img_plain = measure("plain")
+    if args.learned:
+        plain_rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
+        plain_ms = sum(f["ms_total"] for f in frames) / len(frames)
+        acc.learn_enable(True, seed=5)
+        lf, lw, lstt, lclocks, llaunch, img_learned = measure("learned")
+        ls = acc.learn_stats()
+        l_rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in lf) / len(lf)
+        l_ms = sum(f["ms_total"] for f in lf) / len(lf)
+        learned_line = {
+            "plain_mrays_s": round(plain_rays / (plain_ms * 1e-3) / 1e6, 2),
+            "learned_mrays_s": round(l_rays / (l_ms * 1e-3) / 1e6, 2),
+            "learned_over_plain": round((l_rays / l_ms) / (plain_rays / plain_ms), 3),
+            "learned_traversal_ms_per_step": round(lstt["stage_ms"]["traverse"] / args.steps, 3),
+            "plain_traversal_ms_per_step": round(stt["stage_ms"]["traverse"] / args.steps, 3),
+            "images_identical": bool(np.array_equal(img_plain, img_learned)),
+            "mlp": {"trained_steps": ls["trained_steps"], "records": ls["records"],
+                    "last_loss": round(ls["last_loss"], 4), "top1_accuracy": round(ls["last_accuracy"], 4),
+                    "train_ms_total": round(ls["train_ms"], 2)},
+        }
+        if args.learned == 1:  # report the learned-ordered form as the value
+            frames, walls, stt, clocks, launches = lf, lw, lstt, lclocks, llaunch
     rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
     frame_ms = sum(f["ms_total"] for f in frames) / len(frames)
     trav_ms = stt["stage_ms"]["traverse"] / args.steps
@@ -356,8 +384,10 @@ def run_gpu_path(args, rank, world, dev):
                      "algorithmic_bytes_per_launch": int(per_launch_bytes),
                      "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind},
         "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stt["stage_ms"].items()},
-        "gpu_launches": int(stt["kernel_launches"] - launches0),
-        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "ordering": "learned" if args.learned == 1 else "plain",
+        "learned_vs_plain": learned_line,
+        "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 
@@ -502,6 +532,9 @@ def main():
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--workload", default="frame", choices=["frame", "path"])
     ap.add_argument("--ray-sort", type=int, default=0)
+    ap.add_argument("--learned", type=int, default=0,
+                    help="path workload: 0 plain ordering, 1 learned ordering as the value, "
+                         "2 plain as the value with the learned comparison attached")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

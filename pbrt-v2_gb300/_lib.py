@@ -61,6 +61,17 @@ class Counters(C.Structure):
 STAGES = ("sort", "build", "traverse", "other")
 
 
+class LearnParams(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("steps_per_train", C.c_int32), ("lr", C.c_float),
+                ("momentum", C.c_float), ("records", C.c_int32), ("reserved0", C.c_int32),
+                ("seed", C.c_uint64), ("reserved", C.c_int32 * 8)]
+
+
+class LearnStats(C.Structure):
+    _fields_ = [("trained_steps", C.c_uint64), ("records", C.c_uint64), ("last_loss", C.c_float),
+                ("last_accuracy", C.c_float), ("infer_ms", C.c_double), ("train_ms", C.c_double)]
+
+
 _lib = None
 
 

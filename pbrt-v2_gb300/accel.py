@@ -157,6 +157,33 @@ class Aggregate:
                                   "exact_hits"), list(c.work))),
                 "stage_ms": dict(zip(L.STAGES, list(c.stage_ms)))}
 
+    # -- learned traversal ordering (ray-bvh) ------------------------------
+
+    def learn_enable(self, on: bool = True, batch: int = 0, steps_per_train: int = 0, lr: float = 0.0,
+                     momentum: float = 0.0, records: int = 0, seed: int = 0) -> None:
+        """Builds the BVH clusters and the MLP (pbg_learn_enable); the
+        accelerator then collects first-hit records from its nearest-hit
+        batches, and ordered walks start once the network has trained."""
+        lib = L.lib()
+        lib.pbg_learn_enable.argtypes = [C.c_void_p, C.c_int32, C.POINTER(L.LearnParams)]
+        p = L.LearnParams()
+        p.batch, p.steps_per_train, p.lr, p.momentum = batch, steps_per_train, lr, momentum
+        p.records, p.seed = records, seed
+        L.check(lib.pbg_learn_enable(self.handle, int(on), C.byref(p)), "pbg_learn_enable")
+
+    def learn_train(self, steps: int = 0) -> None:
+        lib = L.lib()
+        lib.pbg_learn_train.argtypes = [C.c_void_p, C.c_int32]
+        L.check(lib.pbg_learn_train(self.handle, steps), "pbg_learn_train")
+
+    def learn_stats(self) -> dict:
+        lib = L.lib()
+        lib.pbg_learn_get_stats.argtypes = [C.c_void_p, C.POINTER(L.LearnStats)]
+        s = L.LearnStats()
+        L.check(lib.pbg_learn_get_stats(self.handle, C.byref(s)), "pbg_learn_get_stats")
+        return {"trained_steps": s.trained_steps, "records": s.records, "last_loss": s.last_loss,
+                "last_accuracy": s.last_accuracy, "infer_ms": s.infer_ms, "train_ms": s.train_ms}
+
     def profile(self, on: bool | int = True) -> None:
         """Per-stage CUDA-event timing (the GPU_TIMES printouts of the
         reference, core/GPUparallel.h:532-538); level 2 also counts
