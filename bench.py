@@ -392,6 +392,213 @@ def run_gpu_path(args, rank, world, dev):
     print(json.dumps(line), flush=True)
 
 
+def _o4d4(rays):
+    o4 = np.ascontiguousarray(np.stack([rays[0], rays[1], rays[2], rays[6]], 1).astype(np.float32))
+    d4 = np.ascontiguousarray(np.stack([rays[3], rays[4], rays[5], rays[7]], 1).astype(np.float32))
+    return o4, d4
+
+
+def run_gpu_batch(args, rank, world, dev):
+    """64 independent terrain + icosphere scenes (log-normal triangle counts,
+    median 20k) with 4k..1M mixed rays each (primary and path rays nearest
+    hit, shadow segments any hit), all answered by one persistent launch per
+    step (pbg_sceneset_trace, CUDA graph replay, autotuned shape)."""
+    import torch
+    from pbrt_gb300 import accel as A
+    from pbrt_gb300 import scenes as S
+    from pbrt_gb300.batch import SceneSet
+    torch.cuda.set_device(dev)
+    scs = S.many_scenes(seed=5)
+    tris_total = sum(len(s["tris"]) for s in scs)
+    t0 = time.perf_counter()
+    sset = SceneSet([s["tris"] for s in scs], device=dev)
+    build_s = time.perf_counter() - t0
+    near_off = np.concatenate([[0], np.cumsum([s["near"].shape[1] for s in scs])]).astype(np.int64)
+    occ_off = np.concatenate([[0], np.cumsum([s["shadow"].shape[1] for s in scs])]).astype(np.int64)
+    on, dn = _o4d4(np.concatenate([s["near"] for s in scs], 1))
+    os_, ds = _o4d4(np.concatenate([s["shadow"] for s in scs], 1))
+    nn, ns = int(near_off[-1]), int(occ_off[-1])
+    rays_per_step = nn + ns
+
+    def pinned(a):
+        h = torch.empty(a.shape, dtype=torch.from_numpy(a[:0]).dtype, pin_memory=True)
+        h.numpy()[...] = a
+        return h
+
+    h_on, h_dn, h_os, h_ds = (pinned(a) for a in (on, dn, os_, ds))
+    o4n, d4n, o4s, d4s = (h.to("cuda") for h in (h_on, h_dn, h_os, h_ds))
+    prim = torch.empty(nn, dtype=torch.int32, device="cuda")
+    tt, b1, b2 = (torch.empty(nn, device="cuda") for _ in range(3))
+    occ = torch.empty(ns, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    dev_args = dict(o4n=o4n, d4n=d4n, near_offsets=near_off, prim=prim, t=tt, b1=b1, b2=b2, o4s=o4s,
+                    d4s=d4s, occ_offsets=occ_off, occ=occ)
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        tuned = sset.autotune(**dev_args, stream=stream)
+    tune_s = time.perf_counter() - t0
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            sset.trace(**dev_args, stream=stream)
+    stream.synchronize()
+    times = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                sset.trace(**dev_args, stream=stream)
+                e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    step_ms = sum(times) / len(times)
+    if world > 1:
+        t = torch.tensor([step_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    # per-scene completion: three synchronising calls with the stamps read back
+    lat = []
+    for _ in range(3):
+        st, per = sset.trace(**dev_args, stats=True, stream=stream)
+        lat.append(st)
+    p50 = statistics.median(x["scene_ms_p50"] for x in lat)
+    p99 = statistics.median(x["scene_ms_p99"] for x in lat)
+    if rank != 0:
+        return
+    got_prim, got_t, got_occ = prim.cpu().numpy(), tt.cpu().numpy(), occ.cpu().numpy()
+
+    # the plain per-scene kernels: one ray-bvh scene per call, same device arrays
+    accs = [A.MakeAccelerator("ray-bvh", s["tris"], {"device": dev}) for s in scs]
+    pprim = torch.empty_like(prim)
+    pt, pb1, pb2 = (torch.empty_like(tt) for _ in range(3))
+    pocc = torch.empty_like(occ)
+
+    def per_scene_step():
+        for k, acc in enumerate(accs):
+            a, b = int(near_off[k]), int(near_off[k + 1])
+            if b > a:
+                acc.intersect_device(o4n[a:b], d4n[a:b], pprim[a:b], pt[a:b], pb1[a:b], pb2[a:b],
+                                     stream=stream)
+            a, b = int(occ_off[k]), int(occ_off[k + 1])
+            if b > a:
+                acc.occluded_device(o4s[a:b], d4s[a:b], pocc[a:b], stream=stream)
+
+    with torch.cuda.stream(stream):
+        per_scene_step()
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            per_scene_step()
+        e1.record(stream)
+    e1.synchronize()
+    per_scene_ms = e0.elapsed_time(e1) / 3
+    check = {"rays": rays_per_step,
+             "hit_id_mismatches": int((pprim.cpu().numpy() != got_prim).sum()),
+             "t_bit_mismatches": int((pt.cpu().numpy().view(np.uint32) != got_t.view(np.uint32)).sum()),
+             "occlusion_mismatches": int((pocc.cpu().numpy() != got_occ).sum())}
+
+    # e2e: pinned host rays in, results out, through the public SceneSet call
+    h_prim = torch.empty(nn, dtype=torch.int32, pin_memory=True)
+    h_t, h_b1, h_b2 = (torch.empty(nn, dtype=torch.float32, pin_memory=True) for _ in range(3))
+    h_occ = torch.empty(ns, dtype=torch.uint8, pin_memory=True)
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for h, d in ((h_on, o4n), (h_dn, d4n), (h_os, o4s), (h_ds, d4s)):
+                d.copy_(h, non_blocking=True)
+            sset.trace(**dev_args, stream=stream)
+            for d, h in ((prim, h_prim), (tt, h_t), (b1, h_b1), (b2, h_b2), (occ, h_occ)):
+                h.copy_(d, non_blocking=True)
+        stream.synchronize()
+
+    e2e_step()
+    w0 = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - w0) * 1e3 / max(1, args.steps)
+    h2d = nn * 32 + ns * 32
+    d2h = nn * 16 + ns
+
+    # oracle parity on a ray sample of every scene, and the CPU baseline
+    parity, cpu = None, None
+    if not args.no_parity or not args.no_cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        bvhs = [O.BVH(s["tris"]) for s in scs]
+
+        def cpu_pass(stride, check):
+            nrays, secs, mism, occ_mism = 0, 0.0, 0, 0
+            for k, (s, B) in enumerate(zip(scs, bvhs)):
+                sel_n = np.arange(0, s["near"].shape[1], stride)
+                sel_s = np.arange(0, s["shadow"].shape[1], stride)
+                c0 = time.perf_counter()
+                wp = B.nearest(np.ascontiguousarray(s["near"][:, sel_n]), threads=threads)[0]
+                wo = B.anyhit(np.ascontiguousarray(s["shadow"][:, sel_s]), threads=threads)
+                secs += time.perf_counter() - c0
+                nrays += len(sel_n) + len(sel_s)
+                if check:
+                    mism += int((got_prim[near_off[k] + sel_n] != wp).sum())
+                    occ_mism += int((got_occ[occ_off[k] + sel_s] != wo).sum())
+            return nrays, secs, mism, occ_mism
+
+        sampled, sec97, mism, occ_mism = cpu_pass(97, True)
+        parity = {"sample_rays": sampled, "hit_id_mismatches": mism, "occlusion_mismatches": occ_mism,
+                  "oracle": "SAH BVH + pbrt triangle test (oracle/pbrt_oracle.c)"}
+        if not args.no_cpu and world == 1:
+            # a bounded sample of about 12 s of CPU work
+            stride = max(1, int(round(97 * sec97 / 12.0)))
+            cpu_rays, cpu_s, _, _ = cpu_pass(stride, False)
+            cpu = {"value": round(cpu_rays / cpu_s / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+                   "kind": "port", "seconds": round(cpu_s, 2),
+                   "sample": f"every {stride}th nearest and shadow ray of each of the 64 scenes "
+                             f"({cpu_rays} rays), one scene at a time"}
+
+    hbm, peak_kind = peaks()
+    # algorithmic bytes of one trace launch: rays read once (32 B), results
+    # written once (16 B nearest, 1 B any-hit), every scene's triangle
+    # records read once (48 B)
+    launch_bytes = nn * (32 + 16) + ns * (32 + 1) + tris_total * 48
+    achieved = launch_bytes / (step_ms * 1e-3) / 1e9
+    value = rays_per_step * world / (step_ms * 1e-3) / 1e6
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded terrain + icosphere scenes, seeded camera, path and shadow rays)",
+        "config": {"workload": "batched many-scene: 64 scenes (log-normal triangle counts, median 20k), "
+                               "4k-1M mixed rays each, one persistent launch per step",
+                   "accelerator": "ray-bvh scene set", "scenes": len(scs), "rays_per_step": rays_per_step,
+                   "nearest_rays": nn, "shadow_rays": ns, "triangles": int(tris_total),
+                   "build_s": round(build_s, 2), "autotune_s": round(tune_s, 2), "tuned": tuned,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs > L2 (%.2f GB of rays per step)" % (rays_per_step * 32 / 1e9)},
+        "scene_ms_p50": round(p50, 3), "scene_ms_p99": round(p99, 3),
+        "per_scene_kernels": {"mrays_s": round(rays_per_step / (per_scene_ms * 1e-3) / 1e6, 2),
+                              "ms_per_step": round(per_scene_ms, 3), "launches_per_step": 2 * len(scs)},
+        "check_vs_per_scene_kernels": check,
+        "e2e": {"value": round(rays_per_step / (e2e_ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
+                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "api": "SceneSet.trace (pbg_sceneset_trace) with pinned host rays copied in and results out"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 5), "traffic": None, "kernel": "batch_trace_kernel",
+                     "algorithmic_bytes_per_launch": int(launch_bytes),
+                     "avg_launch_ms": round(step_ms, 4), "peak_source": peak_kind},
+        "gpu_launches": 2 * args.steps,
+        "cpu_baseline": cpu,
+        "parity": parity,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_e2e(args, acc, rays, shadows, hitmask, rays_per_step):
     """Host-buffer frame through the C ABI: pinned arrays in and out."""
     import torch
@@ -530,7 +737,7 @@ def main():
     ap.add_argument("--accel", default="rayhierarchy", choices=["naive", "rayhierarchy", "ray-bvh"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "path"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "path", "batch"])
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--learned", type=int, default=0,
                     help="path workload: 0 plain ordering, 1 learned ordering as the value, "
@@ -549,6 +756,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.workload == "path":
         run_gpu_path(args, rank, world, local)
+    elif args.workload == "batch":
+        run_gpu_batch(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

@@ -240,6 +240,55 @@ int pbg_render(pbg_scene* scene, const pbg_camera* camera, const pbg_light* ligh
                pbg_render_stats* stats);
 
 /* ---------------------------------------------------------------------
+ * Many scenes in one launch.  No counterpart in the reference (one scene,
+ * one batch per call).  A scene set holds up to 4096 ray-bvh scenes; one
+ * trace call answers nearest-hit and any-hit queries of every scene with
+ * one persistent kernel pulling warp-sized work items from a global queue.
+ * The launch sequence is captured once as a CUDA graph and replayed while
+ * the same arrays and parameters are passed; the tile, grid and block
+ * shape come from the built-in autotuner unless given.
+ * ------------------------------------------------------------------- */
+typedef struct pbg_sceneset pbg_sceneset;
+
+typedef struct pbg_batch_params {
+    int32_t tile;        /* rays per work item, multiple of 32 (0 = tuned) */
+    int32_t ctas_per_sm; /* persistent CTAs per SM (0 = tuned) */
+    int32_t threads;     /* threads per CTA, multiple of 32 (0 = tuned) */
+    int32_t use_graph;   /* 1 = capture and replay a CUDA graph (default 1) */
+    int32_t reserved[8];
+} pbg_batch_params;
+
+typedef struct pbg_batch_stats {
+    double ms;                       /* device time of the call's launch sequence */
+    double scene_ms_p50, scene_ms_p99; /* per-scene completion times since launch */
+    uint64_t rays;
+    int32_t tile, ctas_per_sm, threads, graph_replayed;
+} pbg_batch_stats;
+
+int pbg_sceneset_create(int32_t nscenes, const float* const* tri9, const int64_t* ntri,
+                        int32_t device, pbg_sceneset** out);
+void pbg_sceneset_destroy(pbg_sceneset* set);
+/* Scene k's nearest-hit rays are o4n/d4n[near_offsets[k] .. near_offsets[k+1])
+ * (device records as for pbg_intersect_device, offsets host int64 with
+ * nscenes + 1 entries) with results prim/t/b1/b2 at the same indices
+ * (triangle indices local to scene k); likewise any-hit rays o4s/d4s with
+ * occ.  Either query set may be empty (NULL arrays, zero offsets).
+ * scene_ms (host, nscenes entries, may be NULL) receives each scene's
+ * completion time.  params may be NULL (tuned).  Synchronises when stats or
+ * scene_ms are requested. */
+int pbg_sceneset_trace(pbg_sceneset* set, const float* o4n, const float* d4n,
+                       const int64_t* near_offsets, int32_t* prim, float* t, float* b1, float* b2,
+                       const float* o4s, const float* d4s, const int64_t* occ_offsets, uint8_t* occ,
+                       const pbg_batch_params* params, pbg_batch_stats* stats, double* scene_ms,
+                       void* stream);
+/* Times the candidate shapes on these queries and keeps the fastest as the
+ * set's tuned parameters (written to *best if not NULL). */
+int pbg_sceneset_autotune(pbg_sceneset* set, const float* o4n, const float* d4n,
+                          const int64_t* near_offsets, int32_t* prim, float* t, float* b1,
+                          float* b2, const float* o4s, const float* d4s, const int64_t* occ_offsets,
+                          uint8_t* occ, pbg_batch_params* best, void* stream);
+
+/* ---------------------------------------------------------------------
  * Learned traversal ordering (Accelerator "ray-bvh" only).  No counterpart
  * in the reference.  An MLP (105 ray features -> 64 -> 64 -> 256 logits,
  * BF16 weights, FP32 accumulation, tcgen05 kernels) predicts which of the

@@ -324,6 +324,15 @@ int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order)
     return PBG_OK;
 }
 
+int launch_build_tris(const float* tri9_dev, const int32_t* order_dev, int64_t ntri, TriRec* out,
+                      cudaStream_t st) {
+    if (ntri <= 0) return PBG_OK;
+    build_tris_kernel<<<(unsigned)((ntri + 255) / 256), 256, 0, st>>>(tri9_dev, order_dev, ntri, out,
+                                                                      nullptr);
+    PBG_CUDA(cudaGetLastError());
+    return PBG_OK;
+}
+
 // ------------------------------------------------------------- dispatch
 
 static int run_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,

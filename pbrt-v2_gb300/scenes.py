@@ -273,3 +273,89 @@ def config_small_naive() -> dict:
     tris = np.concatenate([uv_sphere(), ground_quad()], 0)
     rays = pinhole_rays(256, 256, (0.0, 1.0, -4.0), (0.0, 0.0, 0.0), 45.0, 1)
     return {"tris": tris, "rays": rays, "light": np.array([2.0, 4.0, -2.0], F32)}
+
+
+# ------------------------------------------------------- many-scene batch
+
+def surface_points(tris: np.ndarray, n: int, rng: np.random.Generator, eps: float = 1e-3):
+    """n uniform points on uniformly chosen triangles, lifted by eps along
+    the geometric normal (turned towards +y), and that normal."""
+    idx = rng.integers(0, tris.shape[0], n)
+    v = tris[idx].astype(np.float64).reshape(n, 3, 3)
+    su = np.sqrt(rng.random(n))
+    b = rng.random(n)
+    p = (1 - su)[:, None] * v[:, 0] + (su * (1 - b))[:, None] * v[:, 1] + (su * b)[:, None] * v[:, 2]
+    nrm = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    ln = np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm = np.where(ln > 0, nrm / np.maximum(ln, 1e-30), np.array([0.0, 1.0, 0.0]))
+    nrm *= np.where(nrm[:, 1:2] < 0, -1.0, 1.0)
+    return p + eps * nrm, nrm
+
+
+def _cosine_dirs(nrm: np.ndarray, rng: np.random.Generator) -> np.ndarray:
+    """Cosine-weighted directions about each normal (Malley's method)."""
+    n = nrm.shape[0]
+    r = np.sqrt(rng.random(n))
+    phi = 2 * np.pi * rng.random(n)
+    lx, ly = r * np.cos(phi), r * np.sin(phi)
+    lz = np.sqrt(np.maximum(0.0, 1 - lx * lx - ly * ly))
+    a = np.where(np.abs(nrm[:, 0:1]) > 0.9, np.array([0.0, 1.0, 0.0]), np.array([1.0, 0.0, 0.0]))
+    t = np.cross(nrm, a)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    s = np.cross(nrm, t)
+    d = lx[:, None] * t + ly[:, None] * s + lz[:, None] * nrm
+    return d / np.linalg.norm(d, axis=1, keepdims=True)
+
+
+def _rays(o: np.ndarray, d: np.ndarray, mint, maxt) -> np.ndarray:
+    rays = np.empty((8, o.shape[0]), F32)
+    rays[0:3] = o.T
+    rays[3:6] = d.T
+    rays[6] = mint
+    rays[7] = maxt
+    return rays
+
+
+def many_scenes(seed: int = 5, n_scenes: int = 64, median_tris: int = 20000, sigma: float = 1.0,
+                tri_range=(1000, 500000), ray_range=(4096, 1 << 20), split=(0.4, 0.3, 0.3)) -> list:
+    """Independent scenes for the batched many-scene pipeline.
+
+    Triangle counts are log-normal (median 20k, sigma 1, clipped to
+    [1k, 500k]); each scene is a terrain + icospheres scene of that size
+    (half terrain, half subdivision-3 icospheres, as terrain_icospheres
+    builds them).  Rays per scene are uniform in [4k, 1M] and mixed:
+    primary camera rays (nearest hit), path rays from surface points in
+    cosine-weighted directions (nearest hit; what bounce-3 rays look like:
+    incoherent, leaving surfaces) and shadow segments from surface points to
+    seeded points on the area light (any hit).  Each entry: tris, near
+    ([8, n] rays), shadow ([8, m] rays), kinds (counts of primary / path /
+    shadow)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_scenes):
+        target = int(np.clip(round(math.exp(rng.normal(math.log(median_tris), sigma))),
+                             tri_range[0], tri_range[1]))
+        n_sph = max(1, int(round(target / 2 / 1280)))
+        grid = max(8, int(round(math.sqrt(max(target - n_sph * 1280, 128) / 2))) + 1)
+        sc = terrain_icospheres(seed=1000 + k, grid=grid, n_spheres=n_sph)
+        tris = sc["tris"]
+        nr = int(rng.integers(ray_range[0], ray_range[1] + 1))
+        n_prim = int(nr * split[0])
+        n_path = int(nr * split[1])
+        n_shad = nr - n_prim - n_path
+        side = int(math.ceil(math.sqrt(n_prim)))
+        prim = pinhole_rays(side, side, (0.0, 9.0, -14.0), (0.0, 0.0, 0.0), 50.0, 1,
+                            jitter_seed=2000 + k)[:, :n_prim]
+        p, nrm = surface_points(tris, n_path, rng)
+        path = _rays(p, _cosine_dirs(nrm, rng), 0.0, np.inf)
+        q, _ = surface_points(tris, n_shad, rng)
+        quad = sc["area_light_quad"].astype(np.float64)
+        u, v = rng.random(n_shad), rng.random(n_shad)
+        lp = quad[0] + u[:, None] * (quad[1] - quad[0]) + v[:, None] * (quad[3] - quad[0])
+        d = lp - q
+        dist = np.linalg.norm(d, axis=1)
+        shad = _rays(q, d / dist[:, None], 1e-3, (dist * (1 - 1e-3)).astype(F32))
+        near = np.ascontiguousarray(np.concatenate([prim, path], 1))
+        out.append({"tris": tris, "near": near, "shadow": np.ascontiguousarray(shad),
+                    "kinds": (n_prim, n_path, n_shad)})
+    return out
