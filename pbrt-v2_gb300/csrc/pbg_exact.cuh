@@ -11,9 +11,12 @@
 //                 the exact test certainly rejects it, using error bounds on
 //                 every quantity it compares (derivation below).
 //   pbg_exact()   pbrt's arithmetic restated with correctly rounded
-//                 intrinsics (__dmul_rn/__dsub_rn for Cross, __fmul_rn/
-//                 __fadd_rn for Dot, __frcp_rn for 1.f/divisor), run only on
-//                 the pairs the filter keeps.
+//                 intrinsics (__fmul_rn/__fadd_rn for Dot, __frcp_rn for
+//                 1.f/divisor), run only on the pairs the filter keeps.  Each
+//                 Cross component comes from xcross_f32() (pbg_xcross.h:
+//                 FP32 error-free transformations with a proof of the
+//                 double-then-float rounding) or, when that proof fails
+//                 (rare), from __dmul_rn/__dsub_rn in FP64.
 //
 // Error bound used by the filter (u = 2^-24):
 //   a Cross component ab - cd: pbrt's value is within 1.01u(|ab|+|cd|) of the
@@ -28,6 +31,8 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+
+#include "pbg_xcross.h"
 
 namespace pbg {
 
@@ -58,18 +63,30 @@ static __device__ __noinline__ bool pbg_exact(float p1x, float p1y, float p1z, f
                                        float e1z, float e2x, float e2y, float e2z, float ox,
                                        float oy, float oz, float dx, float dy, float dz, float mint,
                                        float maxt, float* t_out, float* b1_out, float* b2_out) {
-    float s1x = xcross(dy, e2z, dz, e2y);
-    float s1y = xcross(dz, e2x, dx, e2z);
-    float s1z = xcross(dx, e2y, dy, e2x);
+    bool ok = true;
+    float s1x = xcross_f32(dy, e2z, dz, e2y, ok);
+    float s1y = xcross_f32(dz, e2x, dx, e2z, ok);
+    float s1z = xcross_f32(dx, e2y, dy, e2x, ok);
+    if (!ok) {
+        s1x = xcross(dy, e2z, dz, e2y);
+        s1y = xcross(dz, e2x, dx, e2z);
+        s1z = xcross(dx, e2y, dy, e2x);
+    }
     float divisor = xdot(s1x, s1y, s1z, e1x, e1y, e1z);
     if (divisor == 0.f) return false;
     float inv = __frcp_rn(divisor);
     float vx = __fsub_rn(ox, p1x), vy = __fsub_rn(oy, p1y), vz = __fsub_rn(oz, p1z);
     float b1 = __fmul_rn(xdot(vx, vy, vz, s1x, s1y, s1z), inv);
     if (b1 < 0.f || b1 > 1.f) return false;
-    float s2x = xcross(vy, e1z, vz, e1y);
-    float s2y = xcross(vz, e1x, vx, e1z);
-    float s2z = xcross(vx, e1y, vy, e1x);
+    ok = true;
+    float s2x = xcross_f32(vy, e1z, vz, e1y, ok);
+    float s2y = xcross_f32(vz, e1x, vx, e1z, ok);
+    float s2z = xcross_f32(vx, e1y, vy, e1x, ok);
+    if (!ok) {
+        s2x = xcross(vy, e1z, vz, e1y);
+        s2y = xcross(vz, e1x, vx, e1z);
+        s2z = xcross(vx, e1y, vy, e1x);
+    }
     float b2 = __fmul_rn(xdot(dx, dy, dz, s2x, s2y, s2z), inv);
     if (b2 < 0.f || __fadd_rn(b1, b2) > 1.f) return false;
     float t = __fmul_rn(xdot(e2x, e2y, e2z, s2x, s2y, s2z), inv);
