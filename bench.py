@@ -159,7 +159,7 @@ def run_gpu(args, rank, world, dev):
     sc, rays = make_workload()
     tris = sc["tris"]
     n = rays.shape[1]
-    acc = A.MakeAccelerator(args.accel, tris, {"device": dev})
+    acc = A.MakeAccelerator(args.accel, tris, {"device": dev, "clusterLevels": args.rh_cluster_levels})
     # the breadth-first renderer's ray image: one tile of 1024 x 1024 pixels x 4 spp
     acc.Preprocess(None, 4, 1, 1, xres=1024, yres=1024)
     stream = torch.cuda.Stream()
@@ -739,6 +739,8 @@ def main():
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--workload", default="frame", choices=["frame", "path", "batch"])
     ap.add_argument("--ray-sort", type=int, default=0)
+    ap.add_argument("--rh-cluster-levels", type=int, default=0,
+                    help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")
     ap.add_argument("--learned", type=int, default=0,
                     help="path workload: 0 plain ordering, 1 learned ordering as the value, "
                          "2 plain as the value with the learned comparison attached")

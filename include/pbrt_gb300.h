@@ -69,7 +69,10 @@ typedef struct pbg_params {
     int32_t device;       /* CUDA device ordinal */
     int32_t ray_sort;     /* ray-bvh: 1 = walk each batch in 6-D Morton order
                            * (helps incoherent bounce rays), 0 = caller order */
-    int32_t reserved[9];
+    int32_t rh_cluster_levels; /* rayhierarchy: hierarchy levels walked by clusters of
+                                * 32 triangles before they split (0 = down to the
+                                * leaves' parents, < 0 = no clusters) */
+    int32_t reserved[8];
 } pbg_params;
 
 typedef struct pbg_rays {

@@ -213,6 +213,7 @@ def _params_from(ps: dict | None) -> L.Params:
     p.max_bvh_prim = int(ps.get("maxBVHPrim", 0))
     p.device = int(ps.get("device", 0))
     p.ray_sort = int(ps.get("raySort", 0))
+    p.rh_cluster_levels = int(ps.get("clusterLevels", 0))
     return p
 
 

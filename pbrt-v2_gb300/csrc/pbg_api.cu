@@ -12,6 +12,7 @@
 //     hit geometry.
 // Errors become status codes; nothing aborts (the reference calls Severe(),
 // core/error.cpp:130).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -293,6 +294,41 @@ static void triangle_spheres(const float* tri9, const int32_t* order, int64_t nt
     }
 }
 
+// Bounding sphere of each run of kClusterTris consecutive records (the
+// rayhierarchy's triangle clusters): the centre of the members' box, the
+// radius reaching every member sphere (in double, rounded up), padded by
+// 2^-10 of itself so the node test's distance slop covers every member.
+static void cluster_spheres(const std::vector<float4>& sph, std::vector<float4>* out) {
+    const size_t n = sph.size(), ncl = (n + kClusterTris - 1) / kClusterTris;
+    out->resize(ncl);
+    for (size_t k = 0; k < ncl; ++k) {
+        const size_t b = k * kClusterTris, e = std::min(n, b + kClusterTris);
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        bool inf = false;
+        for (size_t i = b; i < e; ++i) {
+            const float4 q = sph[i];
+            if (!std::isfinite(q.w) || !std::isfinite(q.x) || !std::isfinite(q.y) || !std::isfinite(q.z))
+                inf = true;
+            const double c[3] = {q.x, q.y, q.z};
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], c[a] - (double)q.w);
+                hi[a] = std::max(hi[a], c[a] + (double)q.w);
+            }
+        }
+        const float cx = (float)(0.5 * (lo[0] + hi[0])), cy = (float)(0.5 * (lo[1] + hi[1])),
+                    cz = (float)(0.5 * (lo[2] + hi[2]));
+        double r = 0.0;
+        for (size_t i = b; i < e; ++i) {
+            const float4 q = sph[i];
+            const double dx = (double)q.x - cx, dy = (double)q.y - cy, dz = (double)q.z - cz;
+            r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz) + (double)q.w);
+        }
+        float rf = (float)(r * (1.0 + 0x1p-10) + 0x1p-100);
+        if (inf || !std::isfinite(rf)) rf = INFINITY;
+        (*out)[k] = make_float4(inf ? 0.f : cx, inf ? 0.f : cy, inf ? 0.f : cz, rf);
+    }
+}
+
 int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order) {
     const int64_t ntri = s->ntri;
     const size_t nt = (size_t)(ntri > 0 ? ntri : 1);
@@ -307,6 +343,13 @@ int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order)
     triangle_spheres(tri9_host, order, ntri, &sph);
     PBG_CUDA(cudaMemcpyAsync(s->spheres.ptr, sph.data(), (size_t)ntri * sizeof(float4),
                              cudaMemcpyHostToDevice, s->stream));
+    std::vector<float4> csph;
+    if (s->accel == PBG_ACCEL_RAYHIERARCHY) {
+        cluster_spheres(sph, &csph);
+        if ((rc = ensure(s->clusters, csph.size() * sizeof(float4)))) return rc;
+        PBG_CUDA(cudaMemcpyAsync(s->clusters.ptr, csph.data(), csph.size() * sizeof(float4),
+                                 cudaMemcpyHostToDevice, s->stream));
+    }
     DeviceBuffer dorder;
     if (order) {
         rc = ensure(dorder, (size_t)ntri * sizeof(int32_t));
@@ -518,6 +561,7 @@ void pbg_scene_destroy(pbg_scene* s) {
     release(s->uv6);
     release(s->bvh);
     release(s->spheres);
+    release(s->clusters);
     release(s->tri_pos);
     release(s->err);
     release(s->workc);
@@ -529,7 +573,8 @@ void pbg_scene_destroy(pbg_scene* s) {
     DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.ray_o2, &w.ray_d2, &w.valid, &w.prim,
                            &w.t, &w.b1, &w.b2, &w.occ, &w.keys, &w.stage, &w.perm,
                            &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
-                           &w.leafmask, &w.counters, &w.geo};
+                           &w.leafmask, &w.counters, &w.geo, &w.queue_a, &w.queue_b,
+                           &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt};
     for (DeviceBuffer* b : all) release(*b);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;

@@ -65,11 +65,14 @@ struct HostBvh {
 bool triangle_degenerate(const float* v9);
 void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out);
 
+// Records per rayhierarchy triangle cluster (one warp splits a cluster).
+constexpr int kClusterTris = 32;
+
 // Per-batch device scratch owned by a scene.
 struct Work {
     DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
         perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo, queue_a, queue_b,
-        qcount, scan_sums;
+        qcount, scan_sums, pair_rank, leafcnt;
     int64_t cap = 0;
 };
 
@@ -86,6 +89,7 @@ struct pbg_scene {
     pbg::DeviceBuffer uv6;     // optional per-triangle uvs, float[6*ntri]
     pbg::DeviceBuffer bvh;     // BvhNode[] (ray-bvh)
     pbg::DeviceBuffer spheres; // float4 bounding sphere per record (rayhierarchy)
+    pbg::DeviceBuffer clusters; // float4 sphere per kClusterTris consecutive records (rayhierarchy)
     pbg::DeviceBuffer tri_pos; // original index -> record position
     int64_t bvh_nodes = 0;
     int bvh_depth = 0;

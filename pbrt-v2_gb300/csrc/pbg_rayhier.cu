@@ -19,7 +19,9 @@
 //   traverse  one thread per triangle (triangles sorted by the Morton code of
 //             their centroids, so a warp's triangles are neighbours), private
 //             stack, node test = "can any ray of the node come within R of the
-//             triangle's bounding sphere", leaf test = the exact test per ray.
+//             triangle's bounding sphere", leaf test = the exact test per ray,
+//             with the (triangle, leaf) pairs grouped by leaf first so a
+//             warp loads a leaf's rays once for all its triangles.
 //             Nearest hits merge through a 64-bit atomicMax on (t, index)
 //             keys -- race-free by construction, no repair pass; a thread
 //             reads a ray's current key first and filters with that t.
@@ -35,6 +37,7 @@ namespace pbg {
 
 int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
              const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st);
+int scan_counts(pbg_scene* s, uint32_t* a, int64_t m, cudaStream_t st);
 
 constexpr int kLeafRays = 32;
 constexpr int kFan = 4;
@@ -310,49 +313,138 @@ __global__ void __launch_bounds__(256)
     if (STATS) c_.flush(wc);
 }
 
-// One warp per (triangle, leaf) pair: lane k tests ray k of the leaf, so the
-// 32 rays load as two coalesced 512-byte rows and the triangle record is a
-// broadcast.
-template <bool ANY, bool STATS>
+// (cluster, node) pairs -> (triangle, node) pairs for the cluster's members
+// in [t0, t1) whose own sphere passes the same node test: one warp per pair,
+// lane j = member j.
+template <bool STATS>
 __global__ void __launch_bounds__(256)
-    rh_leaf_kernel(const TriRec* __restrict__ tris, const RayNode* __restrict__ leaves,
-                   const Pair* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t cap,
-                   const float4* __restrict__ so, const float4* __restrict__ sd,
-                   unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
-                   unsigned long long* wc) {
+    rh_split_kernel(const float4* __restrict__ spheres, int32_t t0, int32_t t1,
+                    const RayNode* __restrict__ level_nodes, const Pair* __restrict__ in,
+                    const uint32_t* __restrict__ in_count, Pair* __restrict__ out, uint32_t* out_count,
+                    uint32_t cap, int* status, unsigned long long* wc) {
     const uint32_t nin = min(*in_count, cap);
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     WorkCount c_;
+    // every lane of a warp runs the same number of iterations (warp_append)
     for (int64_t p = warp; p < nin; p += nwarps) {
         const Pair pr = in[p];
-        const int count = __float_as_int(leaves[pr.node].c.z);
-        if (STATS && lane == 0) c_.leaf++;
-        if (lane >= count) continue;
-        const int64_t r = (int64_t)pr.node * kLeafRays + lane;
-        if (ANY && ((leafmask[pr.node] >> lane) & 1u)) continue;
-        const TriRec tr = tris[pr.tri];
-        const float4 o = so[r], d = sd[r];
-        const float nd1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
-        float maxt = d.w;
-        if (STATS) c_.filt++;
-        if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
-        if (!ANY) {
-            const unsigned long long cur = keys[r];
-            if (cur != 0ull) {
-                maxt = fminf(maxt, key_t(cur));
-                if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
+        const int64_t t = (int64_t)pr.tri * kClusterTris + lane;
+        Pair item[1];
+        int k = 0;
+        if (t >= t0 && t < t1) {
+            const RayNode nd = level_nodes[pr.node];
+            if (STATS) c_.node++;
+            if (node_hits_sphere(nd, spheres[t])) item[k++] = Pair{(int32_t)t, pr.node};
+        }
+        warp_append(item, k, out, out_count, cap, status);
+    }
+    if (STATS) c_.flush(wc);
+}
+
+// The final pairs grouped by leaf (a counting sort: count with ranks, scan,
+// scatter), so that a leaf's 32 rays are loaded once for all the triangles
+// that reach it instead of once per pair.
+__global__ void rh_leaf_count_kernel(const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
+                                     uint32_t cap, uint32_t* __restrict__ leafcnt,
+                                     uint32_t* __restrict__ rank) {
+    const uint32_t nin = min(*in_count, cap);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nin; i += stride)
+        rank[i] = atomicAdd(&leafcnt[in[i].node], 1u);
+}
+
+__global__ void rh_leaf_scatter_kernel(const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
+                                       uint32_t cap, const uint32_t* __restrict__ leafoff,
+                                       const uint32_t* __restrict__ rank, Pair* __restrict__ out) {
+    const uint32_t nin = min(*in_count, cap);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nin; i += stride) {
+        const Pair p = in[i];
+        out[leafoff[p.node] + rank[i]] = p;
+    }
+}
+
+constexpr int kLeafChunk = 64;
+
+// One warp per chunk of kLeafChunk leaf-sorted pairs: lane k owns ray k of
+// the current leaf (loaded when the leaf changes), the triangle record of
+// each pair is a broadcast load.  Nearest: each lane keeps its best key and
+// shrinks its maxt as it finds hits, merging with atomicMax when the leaf
+// changes.  Any-hit: an occluded lane stops and sets its bit on leaving.
+template <bool ANY, bool STATS>
+__global__ void __launch_bounds__(256)
+    rh_leaf_sorted_kernel(const TriRec* __restrict__ tris, const RayNode* __restrict__ leaves,
+                          const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
+                          uint32_t cap, const float4* __restrict__ so, const float4* __restrict__ sd,
+                          unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
+                          unsigned long long* wc) {
+    const uint32_t nin = min(*in_count, cap);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    WorkCount c_;
+    for (int64_t c0 = warp * kLeafChunk; c0 < nin; c0 += nwarps * kLeafChunk) {
+        const int64_t c1 = min(c0 + (int64_t)kLeafChunk, (int64_t)nin);
+        int32_t leaf = -1;
+        bool active = false, hit = false;
+        int64_t r = 0;
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+        float nd1 = 0.f, maxt = 0.f;
+        unsigned long long best = 0ull, start = 0ull;
+        for (int64_t p = c0; p < c1; ++p) {
+            const Pair pr = in[p];
+            if (pr.node != leaf) {
+                if (ANY) {
+                    if (hit) atomicOr(&leafmask[leaf], 1u << lane);
+                } else if (best > start) {
+                    atomicMax(&keys[r], best);
+                }
+                leaf = pr.node;
+                if (STATS && lane == 0) c_.leaf++;
+                const int count = __float_as_int(leaves[leaf].c.z);
+                r = (int64_t)leaf * kLeafRays + lane;
+                active = lane < count;
+                if (ANY && active) active = ((leafmask[leaf] >> lane) & 1u) == 0u;
+                hit = false;
+                if (active) {
+                    o = so[r];
+                    d = sd[r];
+                    nd1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+                    maxt = d.w;
+                    if (!ANY) {
+                        start = best = keys[r];
+                        if (start != 0ull) maxt = fminf(maxt, key_t(start));
+                    }
+                } else {
+                    start = best = 0ull;
+                }
+            }
+            if (!active) continue;
+            const TriRec tr = tris[pr.tri];
+            if (STATS) c_.filt++;
+            if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
+            float tt, u1, u2;
+            if (STATS) c_.exact++;
+            if (!pbg_exact_rec(tr, o, d, maxt, &tt, &u1, &u2)) continue;
+            if (STATS) c_.hit++;
+            if (ANY) {
+                hit = true;
+                active = false;
+            } else {
+                const unsigned long long k = hit_key(tt, __float_as_int(tr.c.w));
+                if (k > best) best = k;
+                maxt = tt;
             }
         }
-        float tt, u1, u2;
-        if (STATS) c_.exact++;
-        if (!pbg_exact_rec(tr, o, d, maxt, &tt, &u1, &u2)) continue;
-        if (STATS) c_.hit++;
-        if (ANY)
-            atomicOr(&leafmask[pr.node], 1u << lane);
-        else
-            atomicMax(&keys[r], hit_key(tt, __float_as_int(tr.c.w)));
+        if (leaf >= 0) {
+            if (ANY) {
+                if (hit) atomicOr(&leafmask[leaf], 1u << lane);
+            } else if (best > start) {
+                atomicMax(&keys[r], best);
+            }
+        }
     }
     if (STATS) c_.flush(wc);
 }
@@ -444,8 +536,11 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                        unsigned long long* keys, uint32_t* mask, cudaStream_t st) {
     Work& w = s->work;
     int rc;
+    const int64_t nleaf = lv.cnt[0];
     if ((rc = ensure(w.queue_a, (size_t)kQueueCap * sizeof(Pair))) ||
         (rc = ensure(w.queue_b, (size_t)kQueueCap * sizeof(Pair))) ||
+        (rc = ensure(w.pair_rank, (size_t)kQueueCap * sizeof(uint32_t))) ||
+        (rc = ensure(w.leafcnt, (size_t)nleaf * sizeof(uint32_t))) ||
         (rc = ensure(w.qcount, 64 * sizeof(uint32_t))))
         return rc;
     int sms = 152;
@@ -456,47 +551,87 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
     int* status = (int*)s->err.ptr;
     const RayNode* nodes = (const RayNode*)w.nodes.ptr;
     uint32_t* counts = (uint32_t*)w.qcount.ptr;
+    static_assert(2 * kMaxLevels <= 64, "pair counters");
     int groups = s->rh_groups > 0 ? s->rh_groups : 1;
+    const int top = lv.nlev - 1;
+    // levels walked by 32-triangle clusters before they split into triangles
+    // (default: down to the leaves' parents, the fastest split on the
+    // terrain direct-lighting frame)
+    int kcl = s->params.rh_cluster_levels;
+    if (kcl == 0) kcl = std::max(1, top - 1);
+    if (kcl < 0 || s->clusters.ptr == nullptr) kcl = 0;
+    const int split = std::max(0, top - kcl);
+    const float4* tsph = (const float4*)s->spheres.ptr;
+    const float4* csph = (const float4*)s->clusters.ptr;
     for (int attempt = 0; attempt < 8; ++attempt) {
         PBG_CUDA(cudaMemsetAsync(status + kStatusOverflow, 0, sizeof(int), st));
-        const int64_t per = (s->ntri + groups - 1) / groups;
+        // group boundaries on cluster boundaries
+        const int64_t per = ((s->ntri + groups - 1) / groups + kClusterTris - 1) / kClusterTris * kClusterTris;
         for (int g = 0; g < groups; ++g) {
-            const int32_t t0 = (int32_t)(g * per), t1 = (int32_t)std::min<int64_t>(s->ntri, (g + 1) * per);
+            const int32_t t0 = (int32_t)std::min<int64_t>(s->ntri, g * per),
+                          t1 = (int32_t)std::min<int64_t>(s->ntri, (g + 1) * per);
             if (t0 >= t1) break;
             PBG_CUDA(cudaMemsetAsync(counts, 0, 64 * sizeof(uint32_t), st));
             Pair* qa = (Pair*)w.queue_a.ptr;
             Pair* qb = (Pair*)w.queue_b.ptr;
-            const int top = lv.nlev - 1;
             prof_begin(s, st);
+            // pairs of level l count in counts[l] (clusters: counts[kMaxLevels + l])
+            const bool cl = kcl > 0;
+            const float4* seed_sph = cl ? csph : tsph;
+            const int32_t s0 = cl ? t0 / kClusterTris : t0;
+            const int32_t s1 = cl ? (int32_t)((t1 + kClusterTris - 1) / kClusterTris) : t1;
+            uint32_t* cnt_of[kMaxLevels];
+            for (int l = 0; l < kMaxLevels; ++l) cnt_of[l] = &counts[(cl && l >= split) ? kMaxLevels + l : l];
             if (stats)
-                rh_seed_kernel<true><<<grid, 256, 0, st>>>((const float4*)s->spheres.ptr, t0, t1,
-                                                           nodes + lv.off[top], qa, &counts[top],
-                                                           kQueueCap, status, wc);
+                rh_seed_kernel<true><<<grid, 256, 0, st>>>(seed_sph, s0, s1, nodes + lv.off[top], qa,
+                                                           cnt_of[top], kQueueCap, status, wc);
             else
-                rh_seed_kernel<false><<<grid, 256, 0, st>>>((const float4*)s->spheres.ptr, t0, t1,
-                                                            nodes + lv.off[top], qa, &counts[top],
-                                                            kQueueCap, status, nullptr);
-            for (int l = top; l > 0; --l) {
+                rh_seed_kernel<false><<<grid, 256, 0, st>>>(seed_sph, s0, s1, nodes + lv.off[top], qa,
+                                                            cnt_of[top], kQueueCap, status, nullptr);
+            for (int l = top; l >= 0; --l) {
+                if (cl && l == split) {  // clusters -> triangles, same level
+                    if (stats)
+                        rh_split_kernel<true><<<grid * 2, 256, 0, st>>>(
+                            tsph, t0, t1, nodes + lv.off[l], qa, cnt_of[l], qb, &counts[l], kQueueCap,
+                            status, wc);
+                    else
+                        rh_split_kernel<false><<<grid * 2, 256, 0, st>>>(
+                            tsph, t0, t1, nodes + lv.off[l], qa, cnt_of[l], qb, &counts[l], kQueueCap,
+                            status, nullptr);
+                    Pair* tq = qa;
+                    qa = qb;
+                    qb = tq;
+                    cnt_of[l] = &counts[l];
+                }
+                if (l == 0) break;
+                const float4* sph = (cl && l > split) ? csph : tsph;
                 if (stats)
                     rh_expand_kernel<true><<<grid, 256, 0, st>>>(
-                        (const float4*)s->spheres.ptr, nodes + lv.off[l - 1], lv.cnt[l - 1], qa,
-                        &counts[l], qb, &counts[l - 1], kQueueCap, status, wc);
+                        sph, nodes + lv.off[l - 1], lv.cnt[l - 1], qa, cnt_of[l], qb, cnt_of[l - 1],
+                        kQueueCap, status, wc);
                 else
                     rh_expand_kernel<false><<<grid, 256, 0, st>>>(
-                        (const float4*)s->spheres.ptr, nodes + lv.off[l - 1], lv.cnt[l - 1], qa,
-                        &counts[l], qb, &counts[l - 1], kQueueCap, status, nullptr);
+                        sph, nodes + lv.off[l - 1], lv.cnt[l - 1], qa, cnt_of[l], qb, cnt_of[l - 1],
+                        kQueueCap, status, nullptr);
                 Pair* tq = qa;
                 qa = qb;
                 qb = tq;
             }
+            // group the leaf pairs by leaf: qa -> qb
+            uint32_t* leafcnt = (uint32_t*)w.leafcnt.ptr;
+            uint32_t* rank = (uint32_t*)w.pair_rank.ptr;
+            PBG_CUDA(cudaMemsetAsync(leafcnt, 0, (size_t)nleaf * sizeof(uint32_t), st));
+            rh_leaf_count_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank);
+            if ((rc = scan_counts(s, leafcnt, nleaf, st))) return rc;
+            rh_leaf_scatter_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank, qb);
             if (stats)
-                rh_leaf_kernel<ANY, true><<<grid * 2, 256, 0, st>>>(
-                    (const TriRec*)s->tris.ptr, nodes, qa, &counts[0], kQueueCap, so, sd, keys, mask, wc);
+                rh_leaf_sorted_kernel<ANY, true><<<grid * 2, 256, 0, st>>>(
+                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask, wc);
             else
-                rh_leaf_kernel<ANY, false><<<grid * 2, 256, 0, st>>>(
-                    (const TriRec*)s->tris.ptr, nodes, qa, &counts[0], kQueueCap, so, sd, keys, mask,
+                rh_leaf_sorted_kernel<ANY, false><<<grid * 2, 256, 0, st>>>(
+                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask,
                     nullptr);
-            prof_end(s, st, kStageTraverse, lv.nlev + 1);
+            prof_end(s, st, kStageTraverse, lv.nlev + 6);
             PBG_CUDA(cudaGetLastError());
         }
         // One status read per call: a dropped pair would lose hits.
