@@ -343,6 +343,93 @@ __global__ void __launch_bounds__(256)
     if (STATS) c_.flush(wc);
 }
 
+// warp_append that also stores one rank per item at the item's position.
+__device__ __forceinline__ void warp_append_ranked(const Pair* items, const uint32_t* ranks, int k,
+                                                   Pair* q, uint32_t* rank_out, uint32_t* count,
+                                                   uint32_t cap, int* status) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int incl = k;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(full, incl, off);
+        if (lane >= off) incl += y;
+    }
+    const int total = __shfl_sync(full, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(count, (uint32_t)total);
+    base = __shfl_sync(full, base, 31);
+    const uint32_t start = base + (uint32_t)(incl - k);
+    for (int j = 0; j < k; ++j) {
+        const uint32_t pos = start + (uint32_t)j;
+        if (pos < cap) {
+            q[pos] = items[j];
+            rank_out[pos] = ranks[j];
+        }
+    }
+    if (lane == 31 && total > 0 && base + (uint32_t)total > cap) atomicAdd(&status[kStatusOverflow], 1);
+}
+
+// (cluster, level-1 node) pairs straight to (triangle, leaf) pairs: one warp
+// per pair, lane j = member j, tested against the level-1 node and then its
+// kFan leaves.  All lanes share the candidate leaves, so each leaf's count
+// takes one atomic per warp (ballot), and every item gets its rank among its
+// leaf's pairs for the counting sort.
+template <bool STATS>
+__global__ void __launch_bounds__(256)
+    rh_split_leaf_kernel(const float4* __restrict__ spheres, int32_t t0, int32_t t1,
+                         const RayNode* __restrict__ level1, const RayNode* __restrict__ leaves,
+                         int64_t nleaf, const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
+                         Pair* __restrict__ out, uint32_t* __restrict__ rank_out, uint32_t* out_count,
+                         uint32_t* __restrict__ leafcnt, uint32_t cap, int* status,
+                         unsigned long long* wc) {
+    const unsigned full = 0xffffffffu;
+    const uint32_t nin = min(*in_count, cap);
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    WorkCount c_;
+    for (int64_t p = warp; p < nin; p += nwarps) {
+        const Pair pr = in[p];
+        const int64_t t = (int64_t)pr.tri * kClusterTris + lane;
+        bool pass = false;
+        float4 sph = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (t >= t0 && t < t1) {
+            sph = spheres[t];
+            if (STATS) c_.node++;
+            pass = node_hits_sphere(level1[pr.node], sph);
+        }
+        Pair item[kFan];
+        uint32_t rk[kFan];
+        int k = 0;
+        const int64_t first = (int64_t)pr.node * kFan;
+#pragma unroll
+        for (int c = 0; c < kFan; ++c) {
+            const int64_t leaf = first + c;
+            bool h = false;
+            if (pass && leaf < nleaf) {
+                const RayNode nd = leaves[leaf];
+                if (__float_as_int(nd.c.z) != 0) {
+                    if (STATS) c_.node++;
+                    h = node_hits_sphere(nd, sph);
+                }
+            }
+            const unsigned b = __ballot_sync(full, h);
+            uint32_t base = 0;
+            if (lane == 0 && b) base = atomicAdd(&leafcnt[leaf], (uint32_t)__popc(b));
+            base = __shfl_sync(full, base, 0);
+            if (h) {
+                item[k] = Pair{(int32_t)t, (int32_t)leaf};
+                rk[k] = base + (uint32_t)__popc(b & lt);
+                ++k;
+            }
+        }
+        warp_append_ranked(item, rk, k, out, rank_out, out_count, cap, status);
+    }
+    if (STATS) c_.flush(wc);
+}
+
 // The final pairs grouped by leaf (a counting sort: count with ranks, scan,
 // scatter), so that a leaf's 32 rays are loaded once for all the triangles
 // that reach it instead of once per pair.
@@ -355,46 +442,66 @@ __global__ void rh_leaf_count_kernel(const Pair* __restrict__ in, const uint32_t
         rank[i] = atomicAdd(&leafcnt[in[i].node], 1u);
 }
 
+// After a queue overflow (pairs dropped; the host reruns the batch with more
+// triangle groups) the counts and ranks no longer describe the queue, so the
+// sort and the leaf tests of that attempt do nothing.
 __global__ void rh_leaf_scatter_kernel(const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
                                        uint32_t cap, const uint32_t* __restrict__ leafoff,
-                                       const uint32_t* __restrict__ rank, Pair* __restrict__ out) {
+                                       const uint32_t* __restrict__ rank, Pair* __restrict__ out,
+                                       const int* __restrict__ status) {
+    if (status[kStatusOverflow] != 0) return;
     const uint32_t nin = min(*in_count, cap);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nin; i += stride) {
         const Pair p = in[i];
-        out[leafoff[p.node] + rank[i]] = p;
+        const uint64_t dst = (uint64_t)leafoff[p.node] + rank[i];
+        if (dst < nin) out[dst] = p;
     }
 }
 
 constexpr int kLeafChunk = 64;
+constexpr int kLeafWarps = 8;  // warps per CTA of the leaf kernel
 
-// One warp per chunk of kLeafChunk leaf-sorted pairs: lane k owns ray k of
-// the current leaf (loaded when the leaf changes), the triangle record of
-// each pair is a broadcast load.  Nearest: each lane keeps its best key and
-// shrinks its maxt as it finds hits, merging with atomicMax when the leaf
-// changes.  Any-hit: an occluded lane stops and sets its bit on leaving.
+// One warp per chunk of kLeafChunk leaf-sorted pairs.  The chunk's pairs and
+// triangle records are first staged in shared memory by the whole warp (so
+// the loads overlap), then lane k tests ray k of the current leaf (loaded
+// when the leaf changes) against each record.  Nearest: each lane keeps its
+// best key and shrinks its maxt as it finds hits, merging with atomicMax
+// when the leaf changes.  Any-hit: an occluded lane stops and sets its bit
+// on leaving.
 template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * kLeafWarps)
     rh_leaf_sorted_kernel(const TriRec* __restrict__ tris, const RayNode* __restrict__ leaves,
                           const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
                           uint32_t cap, const float4* __restrict__ so, const float4* __restrict__ sd,
                           unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
-                          unsigned long long* wc) {
+                          const int* __restrict__ status, unsigned long long* wc) {
+    __shared__ float4 s_tri[kLeafWarps][kLeafChunk * 3];
+    __shared__ Pair s_pair[kLeafWarps][kLeafChunk];
+    if (status[kStatusOverflow] != 0) return;  // this attempt is rerun
     const uint32_t nin = min(*in_count, cap);
     const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float4* t4 = reinterpret_cast<const float4*>(tris);
+    Pair* sp = s_pair[wib];
+    float4* st4 = s_tri[wib];
     WorkCount c_;
     for (int64_t c0 = warp * kLeafChunk; c0 < nin; c0 += nwarps * kLeafChunk) {
-        const int64_t c1 = min(c0 + (int64_t)kLeafChunk, (int64_t)nin);
+        const int cnt = (int)min((int64_t)kLeafChunk, (int64_t)nin - c0);
+        for (int j = lane; j < cnt; j += 32) sp[j] = in[c0 + j];
+        __syncwarp();
+        for (int j = lane; j < 3 * cnt; j += 32) st4[j] = t4[(int64_t)sp[j / 3].tri * 3 + j % 3];
+        __syncwarp();
         int32_t leaf = -1;
         bool active = false, hit = false;
         int64_t r = 0;
         float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
         float nd1 = 0.f, maxt = 0.f;
         unsigned long long best = 0ull, start = 0ull;
-        for (int64_t p = c0; p < c1; ++p) {
-            const Pair pr = in[p];
+        for (int p = 0; p < cnt; ++p) {
+            const Pair pr = sp[p];
             if (pr.node != leaf) {
                 if (ANY) {
                     if (hit) atomicOr(&leafmask[leaf], 1u << lane);
@@ -422,7 +529,10 @@ __global__ void __launch_bounds__(256)
                 }
             }
             if (!active) continue;
-            const TriRec tr = tris[pr.tri];
+            TriRec tr;
+            tr.a = st4[3 * p];
+            tr.b = st4[3 * p + 1];
+            tr.c = st4[3 * p + 2];
             if (STATS) c_.filt++;
             if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
             float tt, u1, u2;
@@ -445,6 +555,7 @@ __global__ void __launch_bounds__(256)
                 atomicMax(&keys[r], best);
             }
         }
+        __syncwarp();  // the next chunk overwrites this warp's staging
     }
     if (STATS) c_.flush(wc);
 }
@@ -588,7 +699,26 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             else
                 rh_seed_kernel<false><<<grid, 256, 0, st>>>(seed_sph, s0, s1, nodes + lv.off[top], qa,
                                                             cnt_of[top], kQueueCap, status, nullptr);
+            uint32_t* leafcnt = (uint32_t*)w.leafcnt.ptr;
+            uint32_t* rank = (uint32_t*)w.pair_rank.ptr;
+            PBG_CUDA(cudaMemsetAsync(leafcnt, 0, (size_t)nleaf * sizeof(uint32_t), st));
+            bool counted = false;
             for (int l = top; l >= 0; --l) {
+                if (cl && l == 1 && split == 1) {  // clusters -> (triangle, leaf) pairs, counted
+                    if (stats)
+                        rh_split_leaf_kernel<true><<<grid * 2, 256, 0, st>>>(
+                            tsph, t0, t1, nodes + lv.off[1], nodes + lv.off[0], lv.cnt[0], qa, cnt_of[1],
+                            qb, rank, &counts[0], leafcnt, kQueueCap, status, wc);
+                    else
+                        rh_split_leaf_kernel<false><<<grid * 2, 256, 0, st>>>(
+                            tsph, t0, t1, nodes + lv.off[1], nodes + lv.off[0], lv.cnt[0], qa, cnt_of[1],
+                            qb, rank, &counts[0], leafcnt, kQueueCap, status, nullptr);
+                    Pair* tq = qa;
+                    qa = qb;
+                    qb = tq;
+                    counted = true;
+                    break;
+                }
                 if (cl && l == split) {  // clusters -> triangles, same level
                     if (stats)
                         rh_split_kernel<true><<<grid * 2, 256, 0, st>>>(
@@ -618,18 +748,18 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                 qb = tq;
             }
             // group the leaf pairs by leaf: qa -> qb
-            uint32_t* leafcnt = (uint32_t*)w.leafcnt.ptr;
-            uint32_t* rank = (uint32_t*)w.pair_rank.ptr;
-            PBG_CUDA(cudaMemsetAsync(leafcnt, 0, (size_t)nleaf * sizeof(uint32_t), st));
-            rh_leaf_count_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank);
+            if (!counted)
+                rh_leaf_count_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank);
             if ((rc = scan_counts(s, leafcnt, nleaf, st))) return rc;
-            rh_leaf_scatter_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank, qb);
+            rh_leaf_scatter_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank, qb,
+                                                         status);
             if (stats)
-                rh_leaf_sorted_kernel<ANY, true><<<grid * 2, 256, 0, st>>>(
-                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask, wc);
+                rh_leaf_sorted_kernel<ANY, true><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
+                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask, status,
+                    wc);
             else
-                rh_leaf_sorted_kernel<ANY, false><<<grid * 2, 256, 0, st>>>(
-                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask,
+                rh_leaf_sorted_kernel<ANY, false><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
+                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask, status,
                     nullptr);
             prof_end(s, st, kStageTraverse, lv.nlev + 6);
             PBG_CUDA(cudaGetLastError());
