@@ -65,6 +65,10 @@ struct HostBvh {
 bool triangle_degenerate(const float* v9);
 void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out);
 
+// Ray orders of ray_sort(): the declared ray image if any, else 6-D Morton;
+// or the 3-D Morton code of the origins.
+enum { kOrderDefault = 0, kOrderOrigin = 1 };
+
 // Records per rayhierarchy triangle cluster (one warp splits a cluster).
 constexpr int kClusterTris = 32;
 

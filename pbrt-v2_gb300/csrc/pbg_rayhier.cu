@@ -36,7 +36,7 @@
 namespace pbg {
 
 int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
-             const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st);
+             const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st, int order);
 int scan_counts(pbg_scene* s, uint32_t* a, int64_t m, cudaStream_t st);
 
 constexpr int kLeafRays = 32;
@@ -597,10 +597,11 @@ __global__ void rh_finalize_occluded(const int32_t* __restrict__ perm,
 // ------------------------------------------------------------------ host
 
 static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
-                    const int32_t** perm, float4** so, float4** sd, Levels* lv, cudaStream_t st) {
+                    const int32_t** perm, float4** so, float4** sd, Levels* lv, int order,
+                    cudaStream_t st) {
     Work& w = s->work;
     const uint32_t* skeys = nullptr;
-    int rc = ray_sort(s, o, d, valid, n, perm, &skeys, st);
+    int rc = ray_sort(s, o, d, valid, n, perm, &skeys, st, order);
     if (rc) return rc;
     if ((rc = ensure(w.ray_o2, (size_t)n * sizeof(float4))) ||
         (rc = ensure(w.ray_d2, (size_t)n * sizeof(float4))))
@@ -782,7 +783,7 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
     const int32_t* perm;
     float4 *so, *sd;
     Levels lv;
-    int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, st);
+    int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, kOrderDefault, st);
     if (rc) return rc;
     Work& w = s->work;
     if ((rc = ensure(w.keys, (size_t)n * 8))) return rc;
@@ -803,7 +804,7 @@ int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
     const int32_t* perm;
     float4 *so, *sd;
     Levels lv;
-    int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, st);
+    int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, kOrderOrigin, st);
     if (rc) return rc;
     Work& w = s->work;
     const int64_t nleaf = lv.cnt[0];

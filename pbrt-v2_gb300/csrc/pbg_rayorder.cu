@@ -102,6 +102,43 @@ __global__ void morton_kernel(const float4* __restrict__ ro, const float4* __res
               (spread5(qo0) << 2) | (spread5(qo1) << 1) | spread5(qo2);
 }
 
+// Origin order: the 3-D Morton code of the origin, 10 bits per axis over
+// the batch's origin box.  For shadow batches, whose directions all point at
+// a light, this keeps a leaf's 32 origins close in space (image tiles put
+// silhouette pixels' far-apart hit points together).
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void origin_key_kernel(const float4* __restrict__ ro, const uint8_t* __restrict__ valid,
+                                  int64_t n, const int* __restrict__ bounds, uint32_t* __restrict__ keys,
+                                  int32_t* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vals[i] = (int32_t)i;
+    if (valid && !valid[i]) {
+        keys[i] = 0xffffffffu;
+        return;
+    }
+    const float4 o = ro[i];
+    uint32_t q[3];
+    const float ov[3] = {o.x, o.y, o.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float lo = unord_f(bounds[a]);
+        const float ext = unord_f(bounds[3 + a]) - lo;
+        float v = ext > 0.f ? (ov[a] - lo) / ext * 1024.f : 0.f;
+        v = fminf(fmaxf(v, 0.f), 1023.f);  // NaN -> 0
+        q[a] = (uint32_t)v;
+    }
+    keys[i] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+}
+
 // Ray-image order: when the caller declared its batches as a W x H ray image
 // (Preprocess, accelerators/rayhierarchy.cpp:250-265; ray i at x = i mod W,
 // y = i div W), the key is the 2-D Morton code of (x, y), so a leaf of 32
@@ -355,7 +392,7 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
 // Computes the Morton order of a batch.  *perm (device, n entries) lists ray
 // indices in sorted order; valid rays come first.
 int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
-             const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st) {
+             const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st, int order) {
     Work& w = s->work;
     const int tiles = (int)((n + kSortTile - 1) / kSortTile);
     int rc;
@@ -372,7 +409,15 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     int64_t blocks = (n + 255) / 256;
     if (blocks > 4 * sms) blocks = 4 * sms;
-    if (s->image_w > 0 && n == s->image_w * s->image_h) {
+    if (order == kOrderOrigin) {
+        prof_begin(s, st);
+        origin_bounds_kernel<<<(unsigned)blocks, 256, 0, st>>>(o, valid, n, bounds);
+        prof_end(s, st, kStageSort, 1);
+        prof_begin(s, st);
+        origin_key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            o, valid, n, bounds, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
+        prof_end(s, st, kStageSort, 1);
+    } else if (s->image_w > 0 && n == s->image_w * s->image_h) {
         prof_begin(s, st);
         image_key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
             valid, n, s->image_w, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
@@ -420,7 +465,7 @@ int ray_order(pbg_scene* s, const float4* o, const float4* d, int64_t n, const i
         *perm = nullptr;
         return PBG_OK;
     }
-    return ray_sort(s, o, d, nullptr, n, perm, nullptr, st);
+    return ray_sort(s, o, d, nullptr, n, perm, nullptr, st, kOrderDefault);
 }
 
 }  // namespace pbg
