@@ -219,12 +219,15 @@ __device__ __forceinline__ bool node_hits_sphere(const RayNode& nd, float4 sph) 
     const float R = sph.w + nd.a.w + dist * 0x1p-12f;
     if (!(dist > R)) return true;  // overlapping (or NaN): keep
     if (dist - R > nd.c.y * (1.f + 0x1p-18f)) return false;  // beyond every ray's maxt
-    const float sb = R / dist;
-    const float cb = sqrtf(fmaxf(0.f, 1.f - sb * sb));
+    // With the sphere seen under half-angle beta (sin = R/dist, cos = q/dist)
+    // and the cone's half-angle theta, the test is angle(axis, v) <= theta +
+    // beta, i.e. axis.v >= dist cos(theta + beta) = cos(theta) q - sin(theta) R,
+    // scaled by dist so that no division is needed.
+    const float q = sqrtf(fmaxf(0.f, (dist - R) * (dist + R)));
     const float cth = nd.b.w, sth = nd.c.x;
-    if (cth <= -cb) return true;  // cone half-angle + sphere angle >= pi
-    const float cphi = (vx * nd.b.x + vy * nd.b.y + vz * nd.b.z) / dist;
-    return cphi >= cth * cb - sth * sb - 0x1p-16f;
+    if (cth * dist <= -q) return true;  // cone half-angle + sphere angle >= pi
+    const float dotv = vx * nd.b.x + vy * nd.b.y + vz * nd.b.z;
+    return dotv >= cth * q - sth * R - 0x1p-16f * dist;
 }
 
 // A (triangle record, node) pair that passed its node test.
