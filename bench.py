@@ -110,6 +110,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value: float, world: int) -> float:
+    """The slowest rank's time: all-reduce MAX over the process group (a
+    CUDA tensor under NCCL, a CPU tensor under gloo)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, world: int, ms_max: float) -> float:
+    """Whole-job throughput in millions of units per second: every replica
+    processes units_per_rank, the job takes the slowest rank's time."""
+    return units_per_rank * world / (ms_max * 1e-3) / 1e6
+
+
+def rank_barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
 def make_workload(scale: float = 1.0):
     from pbrt_gb300 import scenes as S
     sc = S.terrain_icospheres(seed=2)
@@ -191,8 +216,7 @@ def run_gpu(args, rank, world, dev):
     launches0 = acc.stats()["kernel_launches"]
     acc.profile(True)
     times = []
-    if world > 1:
-        torch.distributed.barrier()
+    rank_barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
         for _ in range(args.steps):
@@ -206,16 +230,12 @@ def run_gpu(args, rank, world, dev):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    rank_barrier(world)
     st = acc.stats()
     acc.profile(False)
     launches = st["kernel_launches"] - launches0
     step_ms = sum(times) / len(times)
-    if world > 1:
-        t = torch.tensor([step_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(step_ms, world)
 
     # dominant kernel: the traversal stage (event-timed inside the library)
     trav_ms = st["stage_ms"]["traverse"]
@@ -253,7 +273,7 @@ def run_gpu(args, rank, world, dev):
     cpu = cpu_baseline(tris, rays, shadows, hitmask) if (rank == 0 and world == 1 and not args.no_cpu) else None
     if rank == 0:
         clocks = clk.summary()
-        value = rays_per_step * world / (step_ms * 1e-3) / 1e6
+        value = job_rate(rays_per_step, world, step_ms)
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
@@ -314,8 +334,7 @@ def run_gpu_path(args, rank, world, dev):
         l0 = acc.stats()["kernel_launches"]
         acc.profile(True)
         frames, walls = [], []
-        if world > 1:
-            torch.distributed.barrier()
+        rank_barrier(world)
         with ClockSampler(dev) as clk:
             for k in range(args.steps):
                 prm.seed = 1000 + k  # the same frames in every mode
@@ -353,10 +372,7 @@ def run_gpu_path(args, rank, world, dev):
     rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
     frame_ms = sum(f["ms_total"] for f in frames) / len(frames)
     trav_ms = stt["stage_ms"]["traverse"] / args.steps
-    if world > 1:
-        t = torch.tensor([frame_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        frame_ms = float(t.item())
+    frame_ms = max_over_ranks(frame_ms, world)
     if rank != 0:
         return
     hbm, peak_kind = peaks()
@@ -365,7 +381,7 @@ def run_gpu_path(args, rank, world, dev):
     avg_launch_ms = stt["stage_ms"]["traverse"] / n_launch
     achieved = per_launch_bytes / (avg_launch_ms * 1e-3) / 1e9
     line = {
-        "metric": METRIC, "value": round(rays * world / (frame_ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
+        "metric": METRIC, "value": round(job_rate(rays, world, frame_ms), 2), "unit": "Mrays/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(frame_ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded displaced icospheres, counter-hash samples)",
@@ -442,8 +458,7 @@ def run_gpu_batch(args, rank, world, dev):
             sset.trace(**dev_args, stream=stream)
     stream.synchronize()
     times = []
-    if world > 1:
-        torch.distributed.barrier()
+    rank_barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
         for _ in range(args.steps):
@@ -457,10 +472,7 @@ def run_gpu_batch(args, rank, world, dev):
             times.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
     step_ms = sum(times) / len(times)
-    if world > 1:
-        t = torch.tensor([step_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(step_ms, world)
     # per-scene completion: three synchronising calls with the stamps read back
     lat = []
     for _ in range(3):
@@ -566,7 +578,7 @@ def run_gpu_batch(args, rank, world, dev):
     # records read once (48 B)
     launch_bytes = nn * (32 + 16) + ns * (32 + 1) + tris_total * 48
     achieved = launch_bytes / (step_ms * 1e-3) / 1e9
-    value = rays_per_step * world / (step_ms * 1e-3) / 1e6
+    value = job_rate(rays_per_step, world, step_ms)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
