@@ -246,8 +246,12 @@ def run_gpu(args, rank, world, dev):
     # results written once (8 B key nearest, 1 bit any-hit)
     step_bytes = (n * 32 + n * 8 + len(shadows) * (valid_shadow * 32 + valid_shadow / 8)
                   + (1 + len(shadows)) * len(tris) * 64)
+    # one unit = the traversal stage of one batch call (one launch for
+    # ray-bvh and naive; seed, expand, split + leaf tests, leaf sort and leaf
+    # tests for rayhierarchy), event-timed inside the library
+    calls = (1 + len(shadows)) * args.steps
     per_launch_bytes = step_bytes / (1 + len(shadows))
-    avg_launch_ms = trav_ms / max(trav_launches, 1)
+    avg_launch_ms = trav_ms / max(calls, 1)
     hbm, peak_kind = peaks()
     achieved = per_launch_bytes / (avg_launch_ms * 1e-3) / 1e9
     traffic = None
@@ -288,7 +292,8 @@ def run_gpu(args, rank, world, dev):
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
                          "unit": "GB/s", "frac": round(achieved / hbm, 5),
-                         "traffic": traffic, "kernel": "traversal (rh_traverse / bvh / naive)",
+                         "traffic": traffic, "kernel": "traversal stage of one batch call",
+                         "launches_per_unit": round(trav_launches / max(calls, 1), 2),
                          "algorithmic_bytes_per_launch": int(per_launch_bytes),
                          "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind},
             "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in st["stage_ms"].items()},
@@ -566,11 +571,16 @@ def run_gpu_batch(args, rank, world, dev):
         if not args.no_cpu and world == 1:
             # a bounded sample of about 12 s of CPU work
             stride = max(1, int(round(97 * sec97 / 12.0)))
-            cpu_rays, cpu_s, _, _ = cpu_pass(stride, False)
+            cpu_rays, cpu_s, reps = 0, 0.0, 0
+            while cpu_s < 9.6 and (reps == 0 or stride == 1):
+                r_, s_, _, _ = cpu_pass(stride, False)
+                cpu_rays += r_
+                cpu_s += s_
+                reps += 1
             cpu = {"value": round(cpu_rays / cpu_s / 1e6, 3), "unit": "Mrays/s", "cores": threads,
                    "kind": "port", "seconds": round(cpu_s, 2),
-                   "sample": f"every {stride}th nearest and shadow ray of each of the 64 scenes "
-                             f"({cpu_rays} rays), one scene at a time"}
+                   "sample": f"every {stride}th nearest and shadow ray of each of the 64 scenes, "
+                             f"one scene at a time, {reps} pass(es), {cpu_rays} rays"}
 
     hbm, peak_kind = peaks()
     # algorithmic bytes of one trace launch: rays read once (32 B), results
@@ -670,31 +680,41 @@ def cpu_sample(rays, shadows, hitmask, frac):
 
 
 def cpu_baseline(tris, rays, shadows, hitmask, target_s: float = 12.0, threads=None):
-    """Oracle port of pbrt's CPU BVH path, all host cores, bounded sample."""
+    """Oracle port of pbrt's CPU BVH path, all host cores: a stride sample of
+    the frame sized to about target_s seconds, or whole frames repeated until
+    target_s when one frame takes less."""
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
     B = O.BVH(tris)
     n = rays.shape[1]
-    # calibrate on a small slice, then size the sample to ~target_s seconds
+
+    def run(sel):
+        B.nearest(rays[:, sel], threads=threads)
+        nr = len(sel)
+        for s in shadows:
+            B.anyhit(s[:, sel], valid=hitmask[sel], threads=threads)
+            nr += int(hitmask[sel].sum())
+        return nr
+
     sel = np.arange(0, n, 512)
     t0 = time.perf_counter()
-    B.nearest(rays[:, sel], threads=threads)
-    for s in shadows:
-        B.anyhit(s[:, sel], valid=hitmask[sel], threads=threads)
+    run(sel)
     dt = max(time.perf_counter() - t0, 1e-3)
     stride = max(1, int(512 * dt / target_s))
     sel = np.arange(0, n, stride)
+    nr, reps = 0, 0
     t0 = time.perf_counter()
-    B.nearest(rays[:, sel], threads=threads)
-    nr = len(sel)
-    for s in shadows:
-        B.anyhit(s[:, sel], valid=hitmask[sel], threads=threads)
-        nr += int(hitmask[sel].sum())
+    while True:
+        nr += run(sel)
+        reps += 1
+        if time.perf_counter() - t0 >= 0.8 * target_s or stride > 1:
+            break
     dt = time.perf_counter() - t0
+    what = (f"every {stride}th camera ray of the frame ({len(sel)} rays) and its 4 shadow rays"
+            if stride > 1 else f"the whole frame ({n} camera rays + 4 shadow batches) x {reps}")
     return {"value": round(nr / dt / 1e6, 3), "unit": "Mrays/s", "cores": int(threads),
             "kind": "port", "seconds": round(dt, 2),
-            "sample": f"every {stride}th camera ray of the frame ({len(sel)} rays) and its 4 shadow rays; "
-                      "SAH BVH + pbrt's triangle test (oracle/pbrt_oracle.c)"}
+            "sample": what + "; SAH BVH + pbrt's triangle test (oracle/pbrt_oracle.c)"}
 
 
 def run_reference(args):

@@ -72,7 +72,11 @@ typedef struct pbg_params {
     int32_t rh_cluster_levels; /* rayhierarchy: hierarchy levels walked by clusters of
                                 * 32 triangles before they split (0 = down to the
                                 * leaves' parents, < 0 = no clusters) */
-    int32_t reserved[8];
+    int32_t walk;         /* ray-bvh traversal: 0 = automatic (persistent for bounce
+                           * batches: nearest hit with a validity mask, and the
+                           * renderer's bounces >= 1), 1 = one thread per ray,
+                           * 2 = persistent warps refilled from a ray counter */
+    int32_t reserved[7];
 } pbg_params;
 
 typedef struct pbg_rays {

@@ -214,6 +214,7 @@ def _params_from(ps: dict | None) -> L.Params:
     p.device = int(ps.get("device", 0))
     p.ray_sort = int(ps.get("raySort", 0))
     p.rh_cluster_levels = int(ps.get("clusterLevels", 0))
+    p.walk = int(ps.get("walk", 0))
     return p
 
 

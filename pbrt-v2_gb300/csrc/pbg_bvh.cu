@@ -10,6 +10,8 @@
 // it, in the 6-D Morton order of the per-batch ray hierarchy
 // (pbg_rayorder.cu).  With the learned ordering on (pbg_learn.cu) each ray
 // first walks the cluster its model predicts.
+#include <algorithm>
+
 #include "pbg_internal.h"
 #include "pbg_learn.h"
 #include "pbg_tma.cuh"
@@ -65,6 +67,154 @@ __global__ void __launch_bounds__(kBvhThreads)
     b2_out[ray] = h.prim >= 0 ? h.b2 : 0.f;
 }
 
+// Persistent "while-while" form for incoherent batches (one thread per ray
+// leaves most lanes of a warp idle: rays finish at different times and leaf
+// tests run for a few lanes at a time).  Each lane takes a new ray from a
+// global counter as soon as its ray is done, so warps stay full; and each
+// outer iteration first walks inner nodes until the lane holds a leaf (or
+// its ray ends), then runs the leaf tests, so the warp tests leaves
+// together.  The stack keeps leaf children with their triangle counts.
+// Same culling, order-independent merge and results as bvh_kernel.
+constexpr int kPersistThreads = 128;
+
+template <bool ANY>
+__global__ void __launch_bounds__(kPersistThreads)
+    bvh_persistent_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris,
+                          int32_t unculled, const float4* __restrict__ ro, const float4* __restrict__ rd,
+                          const uint8_t* __restrict__ valid, const int32_t* __restrict__ perm, int64_t n,
+                          int32_t* __restrict__ prim_out, float* __restrict__ t_out,
+                          float* __restrict__ b1_out, float* __restrict__ b2_out,
+                          uint8_t* __restrict__ occ, int* status, unsigned long long* next) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    int32_t stack_ref[kStackDepth];
+    int32_t stack_cnt[kStackDepth];
+    float stack_t[kStackDepth];
+    int sp = 0;
+    int64_t ray = 0;
+    bool has = false, exhausted = false, ok = true;
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+    RayInv ri{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float nd = 0.f;
+    WalkHit h{0.f, 0.f, 0.f, -1};
+    int32_t node = -1, leaf_start = 0, leaf_cnt = 0;
+    WorkCount wc;
+
+    auto finish = [&]() {
+        if (ANY) {
+            occ[ray] = h.prim >= 0 ? 1 : 0;
+        } else {
+            const bool hit = h.prim >= 0;
+            prim_out[ray] = h.prim;
+            t_out[ray] = hit ? h.t : 0.f;
+            b1_out[ray] = hit ? h.b1 : 0.f;
+            b2_out[ray] = hit ? h.b2 : 0.f;
+        }
+        if (!ok) atomicAdd(&status[kStatusOverflow], 1);
+        has = false;
+    };
+    // next stack entry that can still hold a hit; false when the stack is empty
+    auto pop = [&]() -> bool {
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= h.t) {
+                if (stack_cnt[sp] == 0) {
+                    node = stack_ref[sp];
+                } else {
+                    node = -1;
+                    leaf_start = ~stack_ref[sp];
+                    leaf_cnt = stack_cnt[sp];
+                }
+                return true;
+            }
+        }
+        return false;
+    };
+
+    for (;;) {
+        // refill the lanes whose ray is done
+        const unsigned need = __ballot_sync(full, !has && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(need));
+            base = __shfl_sync(full, base, leader);
+            if (!has && !exhausted) {
+                const int64_t slot = (int64_t)base + __popc(need & lt);
+                if (slot >= n) {
+                    exhausted = true;
+                } else {
+                    ray = perm ? (int64_t)perm[slot] : slot;
+                    if (valid != nullptr && valid[ray] == 0) {
+                        h = WalkHit{0.f, 0.f, 0.f, -1};
+                        ok = true;
+                        finish();  // invalid: a miss, no walk
+                    } else {
+                        o = ro[ray];
+                        d = rd[ray];
+                        nd = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+                        ri = RayInv{o.x, o.y, o.z, safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+                        h = WalkHit{d.w, 0.f, 0.f, -1};
+                        sp = 0;
+                        node = 0;
+                        ok = true;
+                        leaf_start = 0;
+                        leaf_cnt = unculled;  // degenerate records first
+                        has = true;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(full, has)) {
+            if (__all_sync(full, exhausted)) break;
+            continue;
+        }
+        // inner nodes until this lane holds a leaf or its ray ends
+        while (has && leaf_cnt == 0) {
+            if (node < 0) {
+                if (!pop()) {
+                    finish();
+                    break;
+                }
+                continue;
+            }
+            const BvhNode nn = nodes[node];
+            float tn0, tn1;
+            const bool h0 = slab(ri, nn.n0.x, nn.n0.y, nn.n0.z, nn.n0.w, nn.n2.x, nn.n2.y, o.w, h.t, &tn0);
+            const bool h1 = slab(ri, nn.n1.x, nn.n1.y, nn.n1.z, nn.n1.w, nn.n2.z, nn.n2.w, o.w, h.t, &tn1);
+            node = -1;
+            if (h0 || h1) {
+                const bool near0 = h0 && (!h1 || tn0 <= tn1);
+                const int32_t cn = near0 ? nn.n3.x : nn.n3.y, kn = near0 ? nn.n3.z : nn.n3.w;
+                if (h0 && h1) {
+                    const int32_t cf = near0 ? nn.n3.y : nn.n3.x, kf = near0 ? nn.n3.w : nn.n3.z;
+                    if (sp < kStackDepth) {
+                        stack_ref[sp] = cf;
+                        stack_cnt[sp] = cf >= 0 ? 0 : kf;
+                        stack_t[sp] = near0 ? tn1 : tn0;
+                        ++sp;
+                    } else {
+                        ok = false;
+                    }
+                }
+                if (cn >= 0) {
+                    node = cn;
+                } else {
+                    leaf_start = ~cn;
+                    leaf_cnt = kn;
+                }
+            }
+        }
+        // the leaf tests, converged
+        if (has && leaf_cnt > 0) {
+            const bool done = test_run<ANY, false>(tris, leaf_start, leaf_cnt, o, d, nd, h, wc);
+            leaf_cnt = 0;
+            if (done) finish();
+        }
+    }
+}
+
 int ray_order(pbg_scene* s, const float4* o, const float4* d, int64_t n, const int32_t** perm,
               cudaStream_t st);
 
@@ -88,7 +238,26 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     int* status = (int*)s->err.ptr;
     unsigned long long* wc = (unsigned long long*)s->workc.ptr;
     prof_begin(s, st);
-    if (pred) {
+    // bounce batches are incoherent: the reference's bounce form of Intersect
+    // is the one with a validity mask (rayhierarchy.cpp:602-813)
+    const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
+    const bool persistent = s->params.walk == 2 || (s->params.walk == 0 && hint == 1);
+    if (!pred && s->prof.level < 2 && persistent) {
+        // persistent while-while walk: one counter word, zeroed per launch
+        Work& w = s->work;
+        int rc2 = ensure(w.counters, 64);
+        if (rc2) return rc2;
+        unsigned long long* next = (unsigned long long*)w.counters.ptr;
+        PBG_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_persistent_kernel<ANY>, kPersistThreads, 0);
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+        int64_t blocks = (int64_t)std::max(per_sm, 1) * sms;
+        blocks = std::min<int64_t>(blocks, (n + kPersistThreads - 1) / kPersistThreads);
+        bvh_persistent_kernel<ANY><<<(unsigned)blocks, kPersistThreads, 0, st>>>(
+            nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, next);
+    } else if (pred) {
         if (s->prof.level >= 2)
             bvh_kernel<ANY, true, true><<<grid, kBvhThreads, 0, st>>>(
                 nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, wc, pred, cref);

@@ -99,6 +99,7 @@ struct pbg_scene {
     int bvh_depth = 0;
     int32_t unculled = 0;      // records [0, unculled) are tested by every ray
     int rh_groups = 1;         // triangle groups per rayhierarchy traversal (grows on overflow)
+    int walk_hint = -1;        // ray-bvh: 1 = incoherent batch, 0 = coherent, -1 = infer
     std::vector<pbg::BvhNode> host_nodes;  // ray-bvh tree, kept for the learned clusters
     std::vector<int32_t> host_order;
     struct pbg::Learner* learn = nullptr;

@@ -562,7 +562,13 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     int32_t* qi2 = (int32_t*)B.qidx2.ptr;
     float4* qo2 = (float4*)B.o42.ptr;
     float4* qd2 = (float4*)B.d42.ptr;
+    // camera rays and their shadow rays are coherent, later bounces are not
+    struct HintGuard {
+        pbg_scene* s;
+        ~HintGuard() { s->walk_hint = -1; }
+    } hint_guard{s};
     for (int bounce = 0; nq > 0; ++bounce) {
+        s->walk_hint = bounce > 0 ? 1 : 0;
         if ((r = pbg_intersect_device(s, (const float*)qo, (const float*)qd, nullptr, nq,
                                       (int32_t*)B.prim.ptr, (float*)B.t.ptr, (float*)B.b1.ptr,
                                       (float*)B.b2.ptr, st)))
