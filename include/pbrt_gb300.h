@@ -262,7 +262,9 @@ typedef struct pbg_batch_params {
     int32_t ctas_per_sm; /* persistent CTAs per SM (0 = tuned) */
     int32_t threads;     /* threads per CTA, multiple of 32 (0 = tuned) */
     int32_t use_graph;   /* 1 = capture and replay a CUDA graph (default 1) */
-    int32_t reserved[8];
+    int32_t walk;        /* 1 = warps take work items of `tile` rays, 2 = each lane
+                          * refills from one counter over all rays (0 = tuned) */
+    int32_t reserved[7];
 } pbg_batch_params;
 
 typedef struct pbg_batch_stats {
@@ -270,6 +272,7 @@ typedef struct pbg_batch_stats {
     double scene_ms_p50, scene_ms_p99; /* per-scene completion times since launch */
     uint64_t rays;
     int32_t tile, ctas_per_sm, threads, graph_replayed;
+    int32_t walk, reserved;
 } pbg_batch_stats;
 
 int pbg_sceneset_create(int32_t nscenes, const float* const* tri9, const int64_t* ntri,

@@ -25,13 +25,14 @@ from . import _lib as L
 
 class BatchParams(C.Structure):
     _fields_ = [("tile", C.c_int32), ("ctas_per_sm", C.c_int32), ("threads", C.c_int32),
-                ("use_graph", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("use_graph", C.c_int32), ("walk", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class BatchStats(C.Structure):
     _fields_ = [("ms", C.c_double), ("scene_ms_p50", C.c_double), ("scene_ms_p99", C.c_double),
                 ("rays", C.c_uint64), ("tile", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("threads", C.c_int32), ("graph_replayed", C.c_int32)]
+                ("threads", C.c_int32), ("graph_replayed", C.c_int32), ("walk", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 _bound = False
@@ -100,11 +101,11 @@ class SceneSet:
 
     def trace(self, o4n=None, d4n=None, near_offsets=None, prim=None, t=None, b1=None, b2=None,
               o4s=None, d4s=None, occ_offsets=None, occ=None, tile=0, ctas_per_sm=0, threads=0,
-              use_graph=True, stats=False, stream=None):
+              use_graph=True, walk=0, stats=False, stream=None):
         """One launch over every scene; returns (stats dict, per-scene ms) when
         stats is set (which synchronises), else None."""
         args = self._args(o4n, d4n, near_offsets, prim, t, b1, b2, o4s, d4s, occ_offsets, occ)
-        p = BatchParams(tile, ctas_per_sm, threads, int(bool(use_graph)))
+        p = BatchParams(tile, ctas_per_sm, threads, int(bool(use_graph)), walk)
         st = BatchStats()
         per = np.zeros(self.nscenes, np.float64) if stats else None
         L.check(_bind().pbg_sceneset_trace(
@@ -115,7 +116,8 @@ class SceneSet:
             return None
         return ({"ms": st.ms, "scene_ms_p50": st.scene_ms_p50, "scene_ms_p99": st.scene_ms_p99,
                  "rays": st.rays, "tile": st.tile, "ctas_per_sm": st.ctas_per_sm,
-                 "threads": st.threads, "graph_replayed": bool(st.graph_replayed)}, per)
+                 "threads": st.threads, "graph_replayed": bool(st.graph_replayed),
+                 "walk": st.walk}, per)
 
     def autotune(self, o4n=None, d4n=None, near_offsets=None, prim=None, t=None, b1=None, b2=None,
                  o4s=None, d4s=None, occ_offsets=None, occ=None, stream=None) -> dict:
@@ -124,4 +126,5 @@ class SceneSet:
         L.check(_bind().pbg_sceneset_autotune(
             self.handle, *args, C.byref(best), None if stream is None else stream.cuda_stream),
             "pbg_sceneset_autotune")
-        return {"tile": best.tile, "ctas_per_sm": best.ctas_per_sm, "threads": best.threads}
+        return {"tile": best.tile, "ctas_per_sm": best.ctas_per_sm, "threads": best.threads,
+                "walk": best.walk}

@@ -19,8 +19,11 @@
 //    completion times relative to the stamp of the reset kernel.
 //  * The reset + trace launch pair is captured once as a CUDA graph and
 //    replayed while the caller passes the same arrays and launch shape.
-//  * The autotuner times the candidate (tile, CTAs per SM, threads) shapes on
-//    the caller's queries and keeps the fastest.
+//  * Or, per-lane persistent: every lane refills from a counter over all
+//    rays of the set (batch_persistent_kernel) -- better for incoherent
+//    rays, whose walks end at very different times.
+//  * The autotuner times the candidate (walk, tile, CTAs per SM, threads)
+//    shapes on the caller's queries and keeps the fastest.
 // No kernel here waits on another CTA: the queue is a plain fetch-and-add.
 #include <algorithm>
 #include <atomic>
@@ -51,6 +54,7 @@ struct BatchArgs {
     const int64_t* item_off;  // [2 * nscenes + 1], segment 2k + kind
     const int64_t* ray_off;   // [2 * nscenes]: first ray of each segment
     const int64_t* ray_end;   // [2 * nscenes]
+    const int64_t* rseg_off;  // [2 * nscenes + 1]: rays before each segment
     const float4* o4n;
     const float4* d4n;
     int32_t* prim;
@@ -136,6 +140,152 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_trace_kernel(BatchArgs
     }
 }
 
+// Per-lane persistent form: a lane takes the next ray of the whole set (all
+// scenes' nearest and any-hit rays numbered scene-major) from one counter as
+// soon as its ray is done, walks inner nodes until it holds a leaf, and the
+// warp tests leaves together (the while-while walk of the single-scene
+// persistent kernel, with the scene looked up per ray).  Completion stamps:
+// the lanes that finish a ray in an iteration raise their scene's stamp
+// with one atomicMax per scene per warp.
+__global__ void __launch_bounds__(kBatchMaxThreads) batch_persistent_kernel(BatchArgs a) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nseg = 2 * a.nscenes;
+    const int64_t total = a.rseg_off[nseg];
+    int32_t stack_ref[kStackDepth];
+    int32_t stack_cnt[kStackDepth];
+    float stack_t[kStackDepth];
+    int sp = 0;
+    int64_t r = 0;
+    int k = 0;
+    bool any = false, has = false, exhausted = false, ok = true, fin = false;
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+    RayInv ri{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float nd = 0.f;
+    WalkHit h{0.f, 0.f, 0.f, -1};
+    SceneDesc sd{nullptr, nullptr, 0, 0};
+    int32_t node = -1, leaf_start = 0, leaf_cnt = 0;
+    WorkCount wc;
+
+    auto finish = [&]() {
+        if (any) {
+            a.occ[r] = h.prim >= 0 ? 1 : 0;
+        } else {
+            const bool hit = h.prim >= 0;
+            a.prim[r] = h.prim;
+            a.t[r] = hit ? h.t : 0.f;
+            a.b1[r] = hit ? h.b1 : 0.f;
+            a.b2[r] = hit ? h.b2 : 0.f;
+        }
+        if (!ok) atomicAdd(&a.status[kStatusOverflow], 1);
+        has = false;
+        fin = true;
+    };
+    auto pop = [&]() -> bool {
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= h.t) {
+                if (stack_cnt[sp] == 0) {
+                    node = stack_ref[sp];
+                } else {
+                    node = -1;
+                    leaf_start = ~stack_ref[sp];
+                    leaf_cnt = stack_cnt[sp];
+                }
+                return true;
+            }
+        }
+        return false;
+    };
+
+    for (;;) {
+        fin = false;
+        const unsigned need = __ballot_sync(full, !has && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(a.head, (unsigned long long)__popc(need));
+            base = __shfl_sync(full, base, leader);
+            if (!has && !exhausted) {
+                const int64_t slot = (int64_t)base + __popc(need & lt);
+                if (slot >= total) {
+                    exhausted = true;
+                } else {
+                    int lo = 0, hi = nseg;
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (a.rseg_off[mid] <= slot) lo = mid;
+                        else hi = mid;
+                    }
+                    k = lo >> 1;
+                    any = (lo & 1) != 0;
+                    r = a.ray_off[lo] + (slot - a.rseg_off[lo]);
+                    sd = a.scenes[k];
+                    o = any ? a.o4s[r] : a.o4n[r];
+                    d = any ? a.d4s[r] : a.d4n[r];
+                    nd = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+                    ri = RayInv{o.x, o.y, o.z, safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+                    h = WalkHit{d.w, 0.f, 0.f, -1};
+                    sp = 0;
+                    node = 0;
+                    ok = true;
+                    leaf_start = 0;
+                    leaf_cnt = sd.unculled;
+                    has = true;
+                }
+            }
+        }
+        if (!__any_sync(full, has)) {
+            if (__all_sync(full, exhausted)) break;
+            continue;
+        }
+        while (has && leaf_cnt == 0) {
+            if (node < 0) {
+                if (!pop()) {
+                    finish();
+                    break;
+                }
+                continue;
+            }
+            const BvhNode nn = sd.nodes[node];
+            float tn0, tn1;
+            const bool h0 = slab(ri, nn.n0.x, nn.n0.y, nn.n0.z, nn.n0.w, nn.n2.x, nn.n2.y, o.w, h.t, &tn0);
+            const bool h1 = slab(ri, nn.n1.x, nn.n1.y, nn.n1.z, nn.n1.w, nn.n2.z, nn.n2.w, o.w, h.t, &tn1);
+            node = -1;
+            if (h0 || h1) {
+                const bool near0 = h0 && (!h1 || tn0 <= tn1);
+                const int32_t cn = near0 ? nn.n3.x : nn.n3.y, kn = near0 ? nn.n3.z : nn.n3.w;
+                if (h0 && h1) {
+                    const int32_t cf = near0 ? nn.n3.y : nn.n3.x, kf = near0 ? nn.n3.w : nn.n3.z;
+                    if (sp < kStackDepth) {
+                        stack_ref[sp] = cf;
+                        stack_cnt[sp] = cf >= 0 ? 0 : kf;
+                        stack_t[sp] = near0 ? tn1 : tn0;
+                        ++sp;
+                    } else {
+                        ok = false;
+                    }
+                }
+                if (cn >= 0) {
+                    node = cn;
+                } else {
+                    leaf_start = ~cn;
+                    leaf_cnt = kn;
+                }
+            }
+        }
+        if (has && leaf_cnt > 0) {
+            const bool done = any ? test_run<true, false>(sd.tris, leaf_start, leaf_cnt, o, d, nd, h, wc)
+                                  : test_run<false, false>(sd.tris, leaf_start, leaf_cnt, o, d, nd, h, wc);
+            leaf_cnt = 0;
+            if (done) finish();
+        }
+        const unsigned m = __match_any_sync(full, fin ? k : -1);
+        if (fin && lane == __ffs(m) - 1) atomicMax(&a.done_ns[k], global_ns());
+    }
+}
+
 }  // namespace pbg
 
 using namespace pbg;
@@ -157,32 +307,39 @@ struct pbg_sceneset {
 
 namespace {
 
+// walk: 1 = work items of `tile` rays (batch_trace_kernel), 2 = per-lane
+// persistent refill (batch_persistent_kernel; tile only sizes the items of
+// the completion bookkeeping).
 struct Shape {
-    int tile, ctas_per_sm, threads;
+    int tile, ctas_per_sm, threads, walk;
 };
 
-int max_ctas_per_sm(int threads) {
+int max_ctas_per_sm(int threads, int walk) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_trace_kernel, threads, 0) != cudaSuccess)
-        return 1;
+    const cudaError_t e =
+        walk == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_persistent_kernel, threads, 0)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_trace_kernel, threads, 0);
+    if (e != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
 
 Shape resolve_shape(const pbg_sceneset* set, const pbg_batch_params* p) {
-    Shape s{set->tuned.tile, set->tuned.ctas_per_sm, set->tuned.threads};
+    Shape s{set->tuned.tile, set->tuned.ctas_per_sm, set->tuned.threads, set->tuned.walk};
     if (p && p->tile > 0) s.tile = p->tile;
     if (p && p->threads > 0) s.threads = p->threads;
     if (p && p->ctas_per_sm > 0) s.ctas_per_sm = p->ctas_per_sm;
+    if (p && p->walk > 0) s.walk = p->walk;
     if (s.tile <= 0) s.tile = 64;
     if (s.threads <= 0) s.threads = 128;
-    if (s.ctas_per_sm <= 0) s.ctas_per_sm = max_ctas_per_sm(s.threads);
+    if (s.walk <= 0) s.walk = 1;
+    if (s.ctas_per_sm <= 0) s.ctas_per_sm = max_ctas_per_sm(s.threads, s.walk);
     return s;
 }
 
 bool shape_ok(const Shape& s) {
     return s.tile >= 32 && s.tile <= 8192 && s.tile % 32 == 0 && s.threads >= 32 &&
            s.threads <= kBatchMaxThreads && s.threads % 32 == 0 && s.ctas_per_sm >= 1 &&
-           s.ctas_per_sm <= 64;
+           s.ctas_per_sm <= 64 && (s.walk == 1 || s.walk == 2);
 }
 
 bool offsets_ok(const int64_t* off, int32_t n) {
@@ -193,15 +350,16 @@ bool offsets_ok(const int64_t* off, int32_t n) {
     return true;
 }
 
-// item_off ++ ray_off ++ ray_end for this tile.
+// item_off ++ ray_off ++ ray_end ++ rseg_off for this tile.
 void make_table(int32_t n, const int64_t* near_off, const int64_t* occ_off, int tile,
                 std::vector<int64_t>* out) {
     const int nseg = 2 * n;
-    out->assign((size_t)(nseg + 1 + 2 * nseg), 0);
+    out->assign((size_t)(nseg + 1 + 2 * nseg + nseg + 1), 0);
     int64_t* item = out->data();
     int64_t* roff = item + nseg + 1;
     int64_t* rend = roff + nseg;
-    int64_t acc = 0;
+    int64_t* rseg = rend + nseg;
+    int64_t acc = 0, racc = 0;
     for (int k = 0; k < n; ++k)
         for (int kind = 0; kind < 2; ++kind) {
             const int64_t* off = kind ? occ_off : near_off;
@@ -210,9 +368,12 @@ void make_table(int32_t n, const int64_t* near_off, const int64_t* occ_off, int 
             item[seg] = acc;
             roff[seg] = b;
             rend[seg] = e;
+            rseg[seg] = racc;
             acc += (e - b + tile - 1) / tile;
+            racc += e - b;
         }
     item[nseg] = acc;
+    rseg[nseg] = racc;
 }
 
 struct Call {
@@ -234,6 +395,7 @@ BatchArgs make_args(pbg_sceneset* set, const Call& c, int tile) {
     a.item_off = (const int64_t*)set->item_off.ptr;
     a.ray_off = (const int64_t*)set->item_off.ptr + nseg + 1;
     a.ray_end = (const int64_t*)set->item_off.ptr + nseg + 1 + nseg;
+    a.rseg_off = (const int64_t*)set->item_off.ptr + nseg + 1 + 2 * nseg;
     a.o4n = (const float4*)c.o4n;
     a.d4n = (const float4*)c.d4n;
     a.prim = c.prim;
@@ -255,7 +417,10 @@ int launch_pair(pbg_sceneset* set, const BatchArgs& a, const Shape& s, cudaStrea
     batch_reset_kernel<<<(unsigned)((set->nscenes + 255) / 256), 256, 0, st>>>(a);
     PBG_CUDA(cudaGetLastError());
     const unsigned grid = (unsigned)(s.ctas_per_sm * set->sm_count);
-    batch_trace_kernel<<<grid, (unsigned)s.threads, 0, st>>>(a);
+    if (s.walk == 2)
+        batch_persistent_kernel<<<grid, (unsigned)s.threads, 0, st>>>(a);
+    else
+        batch_trace_kernel<<<grid, (unsigned)s.threads, 0, st>>>(a);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
 }
@@ -317,7 +482,8 @@ int run(pbg_sceneset* set, const Call& c, const Shape& s, bool use_graph, cudaSt
                                   (uintptr_t)c.t,   (uintptr_t)c.b1,  (uintptr_t)c.b2,
                                   (uintptr_t)c.o4s, (uintptr_t)c.d4s, (uintptr_t)c.occ,
                                   (uintptr_t)set->item_off.ptr, (uintptr_t)s.tile,
-                                  (uintptr_t)s.ctas_per_sm, (uintptr_t)s.threads};
+                                  (uintptr_t)s.ctas_per_sm, (uintptr_t)s.threads,
+                                  (uintptr_t)s.walk};
     std::vector<uintptr_t> key(std::begin(key_vals), std::end(key_vals));
     if (set->exec && key == set->graph_key) {
         *replayed = true;
@@ -544,6 +710,7 @@ int pbg_sceneset_trace(pbg_sceneset* set, const float* o4n, const float* d4n,
             stats->ctas_per_sm = s.ctas_per_sm;
             stats->threads = s.threads;
             stats->graph_replayed = replayed ? 1 : 0;
+            stats->walk = s.walk;
         }
     }
     if (e0) cudaEventDestroy(e0);
@@ -568,15 +735,17 @@ int pbg_sceneset_autotune(pbg_sceneset* set, const float* o4n, const float* d4n,
     PBG_CUDA(cudaEventCreate(&e0));
     PBG_CUDA(cudaEventCreate(&e1));
     float best_ms = INFINITY;
-    Shape win{64, 0, 128};
+    Shape win{64, 0, 128, 1};
     int rc = PBG_OK;
+    for (int walk = 1; walk <= 2; ++walk)
     for (int th : threads) {
-        const int full = max_ctas_per_sm(th);
+        const int full = max_ctas_per_sm(th, walk);
         const int ctas[] = {full, std::max(1, full / 2)};
         for (int ci = 0; ci < 2 && rc == PBG_OK; ++ci) {
             if (ci == 1 && ctas[1] == ctas[0]) continue;
             for (int tile : tiles) {
-                const Shape s{tile, ctas[ci], th};
+                if (walk == 2 && tile != 64) continue;  // the persistent walk does not use tiles
+                const Shape s{tile, ctas[ci], th, walk};
                 uint64_t rays = 0;
                 if ((rc = prepare(set, c, s, st, &rays))) break;
                 bool rep = false;
@@ -605,6 +774,7 @@ int pbg_sceneset_autotune(pbg_sceneset* set, const float* o4n, const float* d4n,
     set->tuned.tile = win.tile;
     set->tuned.ctas_per_sm = win.ctas_per_sm;
     set->tuned.threads = win.threads;
+    set->tuned.walk = win.walk;
     set->tuned.use_graph = 1;
     if (best) *best = set->tuned;
     return PBG_OK;
