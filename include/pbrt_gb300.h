@@ -314,7 +314,9 @@ typedef struct pbg_learn_params {
     float lr;                 /* learning rate (0 = 0.05) */
     float momentum;           /* (0 = 0.9) */
     int32_t records;          /* training records kept, ring buffer (0 = 262144) */
-    int32_t reserved0;
+    float margin;             /* a ray walks its predicted cluster first only when the
+                               * top logit leads the second by at least this (0 = 1.0;
+                               * < 0 = always) */
     uint64_t seed;            /* weight initialisation */
     int32_t reserved[8];
 } pbg_learn_params;

@@ -64,7 +64,7 @@ STAGES = ("sort", "build", "traverse", "other")
 
 class LearnParams(C.Structure):
     _fields_ = [("batch", C.c_int32), ("steps_per_train", C.c_int32), ("lr", C.c_float),
-                ("momentum", C.c_float), ("records", C.c_int32), ("reserved0", C.c_int32),
+                ("momentum", C.c_float), ("records", C.c_int32), ("margin", C.c_float),
                 ("seed", C.c_uint64), ("reserved", C.c_int32 * 8)]
 
 

@@ -51,8 +51,10 @@ __global__ void __launch_bounds__(kBvhThreads)
     int32_t fref = INT32_MIN, fcnt = 0;
     if (ORDERED) {
         const int c = pred[ray];
-        fref = cref[2 * c];
-        fcnt = cref[2 * c + 1];
+        if (c != kNoCluster) {
+            fref = cref[2 * c];
+            fcnt = cref[2 * c + 1];
+        }
     }
     const bool ok = bvh_walk<ANY, STATS, ORDERED>(nodes, tris, unculled, o, d, fref, fcnt, h, wc);
     if (!ok) atomicAdd(&status[kStatusOverflow], 1);
@@ -77,14 +79,17 @@ __global__ void __launch_bounds__(kBvhThreads)
 // Same culling, order-independent merge and results as bvh_kernel.
 constexpr int kPersistThreads = 128;
 
-template <bool ANY>
+// ORDERED: the learned ordering's predicted cluster (pred, cref as in
+// bvh_kernel) is walked first, then the whole tree skipping it.
+template <bool ANY, bool ORDERED>
 __global__ void __launch_bounds__(kPersistThreads)
     bvh_persistent_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris,
                           int32_t unculled, const float4* __restrict__ ro, const float4* __restrict__ rd,
                           const uint8_t* __restrict__ valid, const int32_t* __restrict__ perm, int64_t n,
                           int32_t* __restrict__ prim_out, float* __restrict__ t_out,
                           float* __restrict__ b1_out, float* __restrict__ b2_out,
-                          uint8_t* __restrict__ occ, int* status, unsigned long long* next) {
+                          uint8_t* __restrict__ occ, int* status, unsigned long long* next,
+                          const uint16_t* __restrict__ pred, const int32_t* __restrict__ cref) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -98,7 +103,7 @@ __global__ void __launch_bounds__(kPersistThreads)
     RayInv ri{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float nd = 0.f;
     WalkHit h{0.f, 0.f, 0.f, -1};
-    int32_t node = -1, leaf_start = 0, leaf_cnt = 0;
+    int32_t node = -1, leaf_start = 0, leaf_cnt = 0, skip = INT32_MIN;
     WorkCount wc;
 
     auto finish = [&]() {
@@ -162,6 +167,27 @@ __global__ void __launch_bounds__(kPersistThreads)
                         leaf_start = 0;
                         leaf_cnt = unculled;  // degenerate records first
                         has = true;
+                        skip = INT32_MIN;
+                        if (ORDERED) {
+                            const int c = pred[ray];
+                            if (c != kNoCluster) {
+                                // the root after the predicted cluster
+                                skip = cref[2 * c];
+                                stack_ref[0] = 0;
+                                stack_cnt[0] = 0;
+                                stack_t[0] = -INFINITY;
+                                sp = 1;
+                                if (skip >= 0) {
+                                    node = skip;
+                                } else {
+                                    stack_ref[1] = skip;
+                                    stack_cnt[1] = cref[2 * c + 1];
+                                    stack_t[1] = -INFINITY;
+                                    sp = 2;
+                                    node = -1;
+                                }
+                            }
+                        }
                     }
                 }
             }
@@ -181,8 +207,12 @@ __global__ void __launch_bounds__(kPersistThreads)
             }
             const BvhNode nn = nodes[node];
             float tn0, tn1;
-            const bool h0 = slab(ri, nn.n0.x, nn.n0.y, nn.n0.z, nn.n0.w, nn.n2.x, nn.n2.y, o.w, h.t, &tn0);
-            const bool h1 = slab(ri, nn.n1.x, nn.n1.y, nn.n1.z, nn.n1.w, nn.n2.z, nn.n2.w, o.w, h.t, &tn1);
+            bool h0 = slab(ri, nn.n0.x, nn.n0.y, nn.n0.z, nn.n0.w, nn.n2.x, nn.n2.y, o.w, h.t, &tn0);
+            bool h1 = slab(ri, nn.n1.x, nn.n1.y, nn.n1.z, nn.n1.w, nn.n2.z, nn.n2.w, o.w, h.t, &tn1);
+            if (ORDERED) {  // the predicted cluster has been walked already
+                h0 = h0 && nn.n3.x != skip;
+                h1 = h1 && nn.n3.y != skip;
+            }
             node = -1;
             if (h0 || h1) {
                 const bool near0 = h0 && (!h1 || tn0 <= tn1);
@@ -230,7 +260,8 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     }
     const uint16_t* pred = nullptr;
     const int32_t* cref = nullptr;
-    int rc = learn_predict(s, o, d, n, &pred, &cref, st);
+    // the model predicts first-hit clusters: nearest-hit batches only
+    int rc = ANY ? PBG_OK : learn_predict(s, o, d, n, &pred, &cref, st);
     if (rc) return rc;
     const unsigned grid = (unsigned)((n + kBvhThreads - 1) / kBvhThreads);
     const BvhNode* nodes = (const BvhNode*)s->bvh.ptr;
@@ -242,7 +273,7 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // is the one with a validity mask (rayhierarchy.cpp:602-813)
     const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
     const bool persistent = s->params.walk == 2 || (s->params.walk == 0 && hint == 1);
-    if (!pred && s->prof.level < 2 && persistent) {
+    if (s->prof.level < 2 && persistent) {
         // persistent while-while walk: one counter word, zeroed per launch
         Work& w = s->work;
         int rc2 = ensure(w.counters, 64);
@@ -250,13 +281,19 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
         unsigned long long* next = (unsigned long long*)w.counters.ptr;
         PBG_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_persistent_kernel<ANY>, kPersistThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_persistent_kernel<ANY, false>, kPersistThreads, 0);
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
         int64_t blocks = (int64_t)std::max(per_sm, 1) * sms;
         blocks = std::min<int64_t>(blocks, (n + kPersistThreads - 1) / kPersistThreads);
-        bvh_persistent_kernel<ANY><<<(unsigned)blocks, kPersistThreads, 0, st>>>(
-            nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, next);
+        if (pred)
+            bvh_persistent_kernel<ANY, true><<<(unsigned)blocks, kPersistThreads, 0, st>>>(
+                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, next, pred,
+                cref);
+        else
+            bvh_persistent_kernel<ANY, false><<<(unsigned)blocks, kPersistThreads, 0, st>>>(
+                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, next,
+                nullptr, nullptr);
     } else if (pred) {
         if (s->prof.level >= 2)
             bvh_kernel<ANY, true, true><<<grid, kBvhThreads, 0, st>>>(

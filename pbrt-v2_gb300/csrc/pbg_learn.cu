@@ -29,7 +29,8 @@
 namespace pbg {
 
 int tc_gemm(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K, int accumulate,
-            int* status, cudaStream_t st);
+            int* status, cudaStream_t st, float* work);
+size_t tc_gemm_work_floats(int M, int N, int K);
 
 // ------------------------------------------------------------ features
 
@@ -218,7 +219,11 @@ constexpr int kInferThreads = 128;
 constexpr size_t kSmW1 = (size_t)kHidden * kFeat * 2, kSmW2 = (size_t)kHidden * kHidden * 2,
                  kSmW3 = (size_t)kClusters * kHidden * 2, kSmX = 128ull * kFeat * 2,
                  kSmH = 128ull * kHidden * 2;
-constexpr size_t kInferSmem = kSmW1 + kSmW2 + kSmW3 + kSmX + 2 * kSmH + (kHidden * 2 + kClusters) * 4 + 64;
+// H2 reuses the X tile (X is dead once layer 1's MMA has completed), and the
+// three layers share 256 TMEM columns (layer 1 at 0, layer 2 at 64, layer 3
+// at 0 after both have been read), so two CTAs fit on an SM.
+constexpr size_t kInferSmem = kSmW1 + kSmW2 + kSmW3 + kSmX + kSmH + (kHidden * 2 + kClusters) * 4 + 64;
+constexpr uint32_t kInferTmemCols = 256;
 
 // Row-major [rows x K] bf16 from global into the core-matrix layout.
 __device__ __forceinline__ void stage_rows(uint8_t* dst, const uint16_t* src, int rows, int K) {
@@ -256,7 +261,7 @@ __global__ void __launch_bounds__(kInferThreads)
     mlp_infer_kernel(const float4* __restrict__ ro, const float4* __restrict__ rd, int64_t n, LearnBox box,
                      const uint16_t* __restrict__ W1b, const uint16_t* __restrict__ W2b,
                      const uint16_t* __restrict__ W3b, const float* __restrict__ b1,
-                     const float* __restrict__ b2, const float* __restrict__ b3,
+                     const float* __restrict__ b2, const float* __restrict__ b3, float margin,
                      uint16_t* __restrict__ pred, int* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sW1 = smem;
@@ -264,14 +269,14 @@ __global__ void __launch_bounds__(kInferThreads)
     uint8_t* sW3 = sW2 + kSmW2;
     uint8_t* sX = sW3 + kSmW3;
     uint8_t* sH1 = sX + kSmX;
-    uint8_t* sH2 = sH1 + kSmH;
-    float* sb1 = (float*)(sH2 + kSmH);
+    uint8_t* sH2 = sX;
+    float* sb1 = (float*)(sH1 + kSmH);
     float* sb2 = sb1 + kHidden;
     float* sb3 = sb2 + kHidden;
     uint64_t* bar = (uint64_t*)(sb3 + kClusters);
     uint32_t* tslot = (uint32_t*)(bar + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp == 0) tmem_alloc(tslot, 512);
+    if (warp == 0) tmem_alloc(tslot, kInferTmemCols);
     stage_rows(sW1, W1b, kHidden, kFeat);
     stage_rows(sW2, W2b, kHidden, kHidden);
     stage_rows(sW3, W3b, kClusters, kHidden);
@@ -331,27 +336,30 @@ __global__ void __launch_bounds__(kInferThreads)
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-        // layer 3 -> columns 128..383
-        if (threadIdx.x == 0) issue_layer(tbase, 128, sH2, sW3, kClusters, kHidden, bar);
+        // layer 3 -> columns 0..255
+        if (threadIdx.x == 0) issue_layer(tbase, 0, sH2, sW3, kClusters, kHidden, bar);
         ok = mbar_wait_bounded(bar, phase, status);
         phase ^= 1u;
         tc_fence_after();
         if (!ok) break;
-        float best = -INFINITY;
+        float best = -INFINITY, second = -INFINITY;
         int arg = 0;
         for (int c0 = 0; c0 < kClusters; c0 += 16) {
             float z[16];
-            tmem_ld16(tbase + lane_addr + 128u + (uint32_t)c0, z);
+            tmem_ld16(tbase + lane_addr + (uint32_t)c0, z);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const float v = z[j] + sb3[c0 + j];
                 if (v > best) {
+                    second = best;
                     best = v;
                     arg = c0 + j;
+                } else if (v > second) {
+                    second = v;
                 }
             }
         }
-        if (ray < n) pred[ray] = (uint16_t)arg;
+        if (ray < n) pred[ray] = (margin < 0.f || best - second >= margin) ? (uint16_t)arg : kNoCluster;
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
@@ -359,7 +367,7 @@ __global__ void __launch_bounds__(kInferThreads)
     if (!ok && threadIdx.x == 0) mbar_wait_bounded(bar, phase ^ 1u, status);
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_free(tbase, 512);
+    if (warp == 0) tmem_free(tbase, kInferTmemCols);
     (void)lane;
 }
 
@@ -435,7 +443,8 @@ void learn_free(Learner* L) {
                            &L->W3b, &L->W2Tb, &L->W3Tb, &L->recX, &L->recY, &L->X, &L->XT, &L->Z1,
                            &L->Z2, &L->Z3, &L->H1, &L->H2, &L->H1T, &L->H2T, &L->dZ3, &L->dZ3b,
                            &L->dZ3T, &L->dH2, &L->dZ2b, &L->dZ2T, &L->dH1, &L->dZ1b, &L->dZ1T, &L->G1,
-                           &L->G2, &L->G3, &L->gb1, &L->gb2, &L->gb3, &L->acc, &L->feat, &L->pred};
+                           &L->G2, &L->G3, &L->gb1, &L->gb2, &L->gb3, &L->acc, &L->feat, &L->pred,
+                           &L->gemm_work};
     for (DeviceBuffer* b : all) release(*b);
     delete L;
 }
@@ -451,6 +460,7 @@ int learn_init(pbg_scene* s, const pbg_learn_params* p) {
         if (p->batch > 0) L->batch = (p->batch + 127) / 128 * 128;
         if (p->steps_per_train > 0) L->steps_per_train = p->steps_per_train;
         if (p->lr > 0.f) L->lr = p->lr;
+        if (p->margin != 0.f) L->margin = p->margin;
         if (p->momentum > 0.f) L->momentum = p->momentum;
         if (p->records > 0) L->capacity = p->records;
         if (p->seed) L->seed = p->seed;
@@ -553,12 +563,12 @@ int learn_predict(pbg_scene* s, const float4* o, const float4* d, int64_t n, con
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     const int64_t tiles = (n + 127) / 128;
-    const unsigned grid = (unsigned)std::min<int64_t>(tiles, (int64_t)sms);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 2 * (int64_t)sms);  // two CTAs per SM
     prof_begin(s, st);
     mlp_infer_kernel<<<grid, kInferThreads, kInferSmem, st>>>(
         o, d, n, L->box, (const uint16_t*)L->W1b.ptr, (const uint16_t*)L->W2b.ptr, (const uint16_t*)L->W3b.ptr,
-        (const float*)L->b1.ptr, (const float*)L->b2.ptr, (const float*)L->b3.ptr, (uint16_t*)L->pred.ptr,
-        (int*)s->err.ptr);
+        (const float*)L->b1.ptr, (const float*)L->b2.ptr, (const float*)L->b3.ptr, L->margin,
+        (uint16_t*)L->pred.ptr, (int*)s->err.ptr);
     prof_end(s, st, kStageOther, 1);
     PBG_CUDA(cudaGetLastError());
     *pred = (const uint16_t*)L->pred.ptr;
@@ -635,17 +645,22 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
         (rc = ensure(L->gb1, kHidden * 4)) || (rc = ensure(L->gb2, kHidden * 4)) ||
         (rc = ensure(L->gb3, kClusters * 4)) || (rc = ensure(L->acc, 64)))
         return rc;
+    {  // split-K workspace of the weight gradients (K = the batch)
+        const size_t wf = std::max({tc_gemm_work_floats(kClusters, kHidden, B),
+                                    tc_gemm_work_floats(128, kHidden, B), tc_gemm_work_floats(128, kFeat, B)});
+        if ((rc = ensure(L->gemm_work, wf * 4))) return rc;
+    }
     auto blocks = [](size_t n) { return (unsigned)((n + 255) / 256); };
     // forward
-    if ((rc = tc_gemm(X, (const uint16_t*)L->W1b.ptr, (float*)L->Z1.ptr, B, kHidden, kFeat, 0, status, st))) return rc;
+    if ((rc = tc_gemm(X, (const uint16_t*)L->W1b.ptr, (float*)L->Z1.ptr, B, kHidden, kFeat, 0, status, st, nullptr))) return rc;
     bias_relu_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->Z1.ptr, (const float*)L->b1.ptr, B, kHidden, 1,
                                                            (uint16_t*)L->H1.ptr);
     if ((rc = tc_gemm((const uint16_t*)L->H1.ptr, (const uint16_t*)L->W2b.ptr, (float*)L->Z2.ptr, B, kHidden,
-                      kHidden, 0, status, st))) return rc;
+                      kHidden, 0, status, st, nullptr))) return rc;
     bias_relu_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->Z2.ptr, (const float*)L->b2.ptr, B, kHidden, 1,
                                                            (uint16_t*)L->H2.ptr);
     if ((rc = tc_gemm((const uint16_t*)L->H2.ptr, (const uint16_t*)L->W3b.ptr, (float*)L->Z3.ptr, B, kClusters,
-                      kHidden, 0, status, st))) return rc;
+                      kHidden, 0, status, st, nullptr))) return rc;
     bias_relu_kernel<<<blocks(b * kClusters), 256, 0, st>>>((float*)L->Z3.ptr, (const float*)L->b3.ptr, B,
                                                              kClusters, 0, nullptr);
     PBG_CUDA(cudaMemsetAsync(L->acc.ptr, 0, 8, st));
@@ -658,11 +673,11 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
     transpose_bf16_kernel<<<blocks(b * kHidden), 256, 0, st>>>((const uint16_t*)L->H2.ptr, B, kHidden, kHidden,
                                                                 (uint16_t*)L->H2T.ptr);
     if ((rc = tc_gemm((const uint16_t*)L->dZ3T.ptr, (const uint16_t*)L->H2T.ptr, (float*)L->G3.ptr, kClusters,
-                      kHidden, B, 0, status, st))) return rc;
+                      kHidden, B, 0, status, st, (float*)L->gemm_work.ptr))) return rc;
     colsum_kernel<<<kClusters, 256, 0, st>>>((const float*)L->dZ3.ptr, B, kClusters, (float*)L->gb3.ptr);
     // dH2 = dZ3 W3 ; dZ2 = dH2 * relu'
     if ((rc = tc_gemm((const uint16_t*)L->dZ3b.ptr, (const uint16_t*)L->W3Tb.ptr, (float*)L->dH2.ptr, B, kHidden,
-                      kClusters, 0, status, st))) return rc;
+                      kClusters, 0, status, st, nullptr))) return rc;
     relu_grad_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->dH2.ptr, (const float*)L->Z2.ptr, b * kHidden,
                                                            (uint16_t*)L->dZ2b.ptr);
     colsum_kernel<<<kHidden, 256, 0, st>>>((const float*)L->dH2.ptr, B, kHidden, (float*)L->gb2.ptr);
@@ -672,10 +687,10 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
     transpose_bf16_kernel<<<blocks(b * kHidden), 256, 0, st>>>((const uint16_t*)L->H1.ptr, B, kHidden, kHidden,
                                                                 (uint16_t*)L->H1T.ptr);
     if ((rc = tc_gemm((const uint16_t*)L->dZ2T.ptr, (const uint16_t*)L->H1T.ptr, (float*)L->G2.ptr, 128, kHidden,
-                      B, 0, status, st))) return rc;
+                      B, 0, status, st, (float*)L->gemm_work.ptr))) return rc;
     // dH1 = dZ2 W2 ; dZ1 = dH1 * relu'
     if ((rc = tc_gemm((const uint16_t*)L->dZ2b.ptr, (const uint16_t*)L->W2Tb.ptr, (float*)L->dH1.ptr, B, kHidden,
-                      kHidden, 0, status, st))) return rc;
+                      kHidden, 0, status, st, nullptr))) return rc;
     relu_grad_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->dH1.ptr, (const float*)L->Z1.ptr, b * kHidden,
                                                            (uint16_t*)L->dZ1b.ptr);
     colsum_kernel<<<kHidden, 256, 0, st>>>((const float*)L->dH1.ptr, B, kHidden, (float*)L->gb1.ptr);
@@ -684,7 +699,7 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
                                                             (uint16_t*)L->dZ1T.ptr);
     transpose_bf16_kernel<<<blocks(b * kFeat), 256, 0, st>>>(X, B, kFeat, kFeat, (uint16_t*)L->XT.ptr);
     if ((rc = tc_gemm((const uint16_t*)L->dZ1T.ptr, (const uint16_t*)L->XT.ptr, (float*)L->G1.ptr, 128, kFeat, B,
-                      0, status, st))) return rc;
+                      0, status, st, (float*)L->gemm_work.ptr))) return rc;
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;
 }

@@ -23,6 +23,7 @@ struct Learner {
     int batch = 8192;
     int steps_per_train = 8;
     float lr = 0.05f, momentum = 0.9f;
+    float margin = 1.0f;  // logit lead of the top cluster needed to use it
     int64_t capacity = 1 << 18;  // training records kept (ring)
     int64_t count = 0, head = 0;
     uint64_t trained_steps = 0;
@@ -35,7 +36,7 @@ struct Learner {
     DeviceBuffer W1, W2, W3, V1, V2, V3, b1, b2, b3, vb1, vb2, vb3, W1b, W2b, W3b, W2Tb, W3Tb;
     // training scratch
     DeviceBuffer recX, recY, X, XT, Z1, Z2, Z3, H1, H2, H1T, H2T, dZ3, dZ3b, dZ3T, dH2, dZ2b, dZ2T,
-        dH1, dZ1b, dZ1T, G1, G2, G3, gb1, gb2, gb3, acc;
+        dH1, dZ1b, dZ1T, G1, G2, G3, gb1, gb2, gb3, acc, gemm_work;
     // per-batch inference scratch
     DeviceBuffer feat, pred;
     float last_loss = 0.f, last_acc = 0.f;
@@ -45,7 +46,9 @@ struct Learner {
 int learn_init(pbg_scene* s, const pbg_learn_params* p);
 void learn_free(Learner* L);
 // Predicted cluster per ray for the batch (NULL when the learner is off or
-// untrained); *cluster_ref receives the device table of cluster references.
+// untrained; kNoCluster for a ray whose prediction is not confident);
+// *cluster_ref receives the device table of cluster references.
+constexpr uint16_t kNoCluster = 0xffffu;
 int learn_predict(pbg_scene* s, const float4* o, const float4* d, int64_t n, const uint16_t** pred,
                   const int32_t** cluster_ref, cudaStream_t st);
 // Appends training records (features + first-hit cluster) from a finished

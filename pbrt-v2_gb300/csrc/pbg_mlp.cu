@@ -11,10 +11,14 @@ constexpr int kTcKChunk = 128; // K staged per round
 
 // C[M x N] (+)= A[M x K] * B[N x K]^T.  A, B: row-major bf16 (K contiguous,
 // i.e. K-major); C: row-major fp32.  M % 128 == 0, N % 16 == 0 and
-// 16 <= N <= 256, K % 16 == 0.  One CTA of 4 warps per 128-row tile.
+// 16 <= N <= 256, K % 16 == 0.  One CTA of 4 warps per 128-row tile and
+// K slice: blockIdx.y takes K chunks [y * kslice, (y + 1) * kslice); with
+// more than one slice each CTA writes its partial product to
+// work[y][M][N] and tc_reduce_kernel sums the slices in order (split-K for
+// the weight gradients, whose K is the batch).
 __global__ void __launch_bounds__(128)
     tc_gemm_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ B, float* __restrict__ C,
-                   int M, int N, int K, int accumulate_c, int* status) {
+                   int M, int N, int K, int accumulate_c, int* status, int kslice, float* __restrict__ work) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sa = smem;                                 // 128 x 128 bf16 = 32 KB
     uint8_t* sb = smem + kTcRows * kTcKChunk * 2;       // 256 x 128 bf16 = 64 KB
@@ -35,8 +39,9 @@ __global__ void __launch_bounds__(128)
     const uint32_t tbase = *tslot;
     uint32_t phase = 0;
     bool ok = true;
-    for (int k0 = 0; k0 < K && ok; k0 += kTcKChunk) {
-        const int kc = min(kTcKChunk, K - k0);
+    const int kbeg = blockIdx.y * kslice, kend = min(K, kbeg + kslice);
+    for (int k0 = kbeg; k0 < kend && ok; k0 += kTcKChunk) {
+        const int kc = min(kTcKChunk, kend - k0);
         const int kb = kc >> 3;  // 16-byte groups per row
         for (int idx = threadIdx.x; idx < kTcRows * kb; idx += blockDim.x) {
             const int r = idx / kb, g = idx % kb;
@@ -57,7 +62,7 @@ __global__ void __launch_bounds__(128)
             for (int ks = 0; ks < (kc >> 4); ++ks) {
                 const uint64_t ad = smem_desc(sa + ks * 256, 128u, sbo);
                 const uint64_t bd = smem_desc(sb + ks * 256, 128u, sbo);
-                tc_mma(tbase, ad, bd, idesc_bf16(kTcRows, N), (k0 > 0 || ks > 0) ? 1u : 0u);
+                tc_mma(tbase, ad, bd, idesc_bf16(kTcRows, N), (k0 > kbeg || ks > 0) ? 1u : 0u);
             }
             tc_commit(bar);
         }
@@ -70,9 +75,18 @@ __global__ void __launch_bounds__(128)
         for (int c0 = 0; c0 < N; c0 += 16) {
             float v[16];
             tmem_ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            float* out = C + (size_t)row * N + c0;
+            if (kbeg >= kend)  // an empty K slice contributes nothing
 #pragma unroll
-            for (int j = 0; j < 16; ++j) out[j] = accumulate_c ? out[j] + v[j] : v[j];
+                for (int j = 0; j < 16; ++j) v[j] = 0.f;
+            if (gridDim.y > 1) {
+                float* out = work + ((size_t)blockIdx.y * M + row) * N + c0;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) out[j] = v[j];
+            } else {
+                float* out = C + (size_t)row * N + c0;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) out[j] = accumulate_c ? out[j] + v[j] : v[j];
+            }
         }
     } else if (threadIdx.x == 0) {
         // give in-flight MMAs one more bounded window before TMEM is released
@@ -83,10 +97,33 @@ __global__ void __launch_bounds__(128)
     if (warp == 0) tmem_free(tbase, ncols);
 }
 
+// C (+)= the sum of the K slices' partial products, slice by slice.
+__global__ void tc_reduce_kernel(const float* __restrict__ work, int slices, int64_t mn,
+                                 float* __restrict__ C, int accumulate_c) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= mn) return;
+    float acc = accumulate_c ? C[i] : 0.f;
+    for (int y = 0; y < slices; ++y) acc += work[(int64_t)y * mn + i];
+    C[i] = acc;
+}
+
 size_t tc_gemm_smem_bytes() { return (size_t)kTcRows * kTcKChunk * 2 + 256 * kTcKChunk * 2 + 64; }
 
+// K slices for a GEMM given a split-K workspace: powers of two, at most one
+// per K chunk, about one CTA per SM in all.
+int tc_gemm_slices(int M, int K) {
+    const int tiles = M / kTcRows, chunks = (K + kTcKChunk - 1) / kTcKChunk;
+    int slices = 1;
+    while (slices * 2 <= chunks && tiles * slices * 2 <= 152) slices *= 2;
+    return slices;
+}
+
+size_t tc_gemm_work_floats(int M, int N, int K) {
+    return (size_t)tc_gemm_slices(M, K) * (size_t)M * (size_t)N;
+}
+
 int tc_gemm(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K, int accumulate,
-            int* status, cudaStream_t st) {
+            int* status, cudaStream_t st, float* work) {
     if (M <= 0 || M % kTcRows || N < 16 || N > 256 || N % 16 || K <= 0 || K % 16) {
         set_last_error("tc_gemm: M % 128, 16 <= N <= 256 with N % 16, K % 16 required");
         return PBG_ERR_INVALID_ARGUMENT;
@@ -97,8 +134,17 @@ int tc_gemm(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K,
                                       (int)tc_gemm_smem_bytes()));
         attr = true;
     }
-    tc_gemm_kernel<<<M / kTcRows, 128, tc_gemm_smem_bytes(), st>>>(A, B, C, M, N, K, accumulate, status);
+    const int slices = work ? tc_gemm_slices(M, K) : 1;
+    const int chunks = (K + kTcKChunk - 1) / kTcKChunk;
+    const int kslice = ((chunks + slices - 1) / slices) * kTcKChunk;
+    tc_gemm_kernel<<<dim3(M / kTcRows, slices), 128, tc_gemm_smem_bytes(), st>>>(
+        A, B, C, M, N, K, accumulate, status, kslice, work);
     PBG_CUDA(cudaGetLastError());
+    if (slices > 1) {
+        const int64_t mn = (int64_t)M * N;
+        tc_reduce_kernel<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(work, slices, mn, C, accumulate);
+        PBG_CUDA(cudaGetLastError());
+    }
     return PBG_OK;
 }
 
@@ -121,7 +167,7 @@ extern "C" int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, 
         cudaMemset(g_status, 0, 4 * sizeof(int));
     }
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = pbg::tc_gemm(A, B, C, M, N, K, accumulate, g_status, st);
+    int rc = pbg::tc_gemm(A, B, C, M, N, K, accumulate, g_status, st, nullptr);
     if (rc) return rc;
     int h[4] = {0, 0, 0, 0};
     PBG_CUDA(cudaMemcpyAsync(h, g_status, sizeof(h), cudaMemcpyDeviceToHost, st));
