@@ -44,6 +44,9 @@ import pbg_import  # noqa: E402
 pbg_import.load()
 
 METRIC = "Mrays/s nearest+any-hit at exact hit-ID match: plain vs learned-ordered, 1 GB300"
+# dram__bytes_read.sum + dram__bytes_write.sum of one tuned trace launch of
+# the 64-scene batch (ncu --set full, the warm-up launch after autotuning)
+BATCH_LAUNCH_DRAM_BYTES = 1_611_773_000
 L2_BYTES = 129 * 1024 * 1024
 CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)
 
@@ -610,7 +613,9 @@ def run_gpu_batch(args, rank, world, dev):
                 "d2h_bytes_per_step": int(d2h),
                 "api": "SceneSet.trace (pbg_sceneset_trace) with pinned host rays copied in and results out"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 5), "traffic": None, "kernel": "batch_trace_kernel",
+                     "frac": round(achieved / hbm, 5), "traffic": BATCH_LAUNCH_DRAM_BYTES,
+                     "kernel": "batch_persistent_kernel (tuned walk)" if tuned.get("walk") == 2
+                               else "batch_trace_kernel (tuned walk)",
                      "algorithmic_bytes_per_launch": int(launch_bytes),
                      "avg_launch_ms": round(step_ms, 4), "peak_source": peak_kind},
         "gpu_launches": 2 * args.steps,
