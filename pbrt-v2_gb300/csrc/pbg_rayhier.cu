@@ -59,29 +59,26 @@ __device__ __forceinline__ float round_up_rel(float x) { return fmaf(fabsf(x), 0
 
 // ---------------------------------------------------------------- build
 
-__global__ void gather_rays_kernel(const float4* __restrict__ ro, const float4* __restrict__ rd,
-                                   const int32_t* __restrict__ perm, int64_t n,
-                                   float4* __restrict__ so, float4* __restrict__ sd) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int32_t r = perm[i];
-    so[i] = ro[r];
-    sd[i] = rd[r];
-}
-
-// One warp per leaf of 32 sorted rays.
-__global__ void leaf_build_kernel(const float4* __restrict__ so, const float4* __restrict__ sd,
-                                  const uint32_t* __restrict__ skeys, int64_t n, int64_t nleaf,
-                                  RayNode* __restrict__ leaves) {
+// One warp per leaf of 32 sorted rays; the warp also gathers its rays into
+// sorted order (so, sd) for the leaf tests.
+__global__ void leaf_build_kernel(const float4* __restrict__ ro, const float4* __restrict__ rd,
+                                  const int32_t* __restrict__ perm, float4* __restrict__ so,
+                                  float4* __restrict__ sd, const uint32_t* __restrict__ skeys, int64_t n,
+                                  int64_t nleaf, RayNode* __restrict__ leaves) {
     const int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (leaf >= nleaf) return;
     const int64_t i = leaf * kLeafRays + lane;
     const bool ok = i < n && skeys[i] != 0xffffffffu;
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
-    if (ok) {
-        o = so[i];
-        d = sd[i];
+    if (i < n) {
+        const int32_t src = perm[i];
+        so[i] = ro[src];
+        sd[i] = rd[src];
+        if (ok) {
+            o = ro[src];
+            d = rd[src];
+        }
     }
     const unsigned full = 0xffffffffu;
     const int count = __popc(__ballot_sync(full, ok));
@@ -142,10 +139,8 @@ __global__ void leaf_build_kernel(const float4* __restrict__ so, const float4* _
 }
 
 // Parent j merges children kFan*j .. kFan*j+kFan-1.
-__global__ void level_build_kernel(const RayNode* __restrict__ child, int64_t nchild,
-                                   RayNode* __restrict__ parent, int64_t nparent) {
-    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nparent) return;
+__device__ __forceinline__ void build_parent(const RayNode* __restrict__ child, int64_t nchild,
+                                             RayNode* __restrict__ parent, int64_t j) {
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     float sx = 0.f, sy = 0.f, sz = 0.f, reach = 0.f;
     int count = 0;
@@ -204,6 +199,24 @@ __global__ void level_build_kernel(const RayNode* __restrict__ child, int64_t nc
     nd.b = make_float4(ax, ay, az, c);
     nd.c = make_float4(s, reach, __int_as_float(count), 0.f);
     parent[j] = nd;
+}
+
+// Levels l0 + 1 .. l1 of the subtrees above groups of kFan^(l1 - l0) nodes
+// of level l0: CTA g builds its subtree level by level (children written
+// by the same CTA in the previous round), so five levels take one launch.
+constexpr int kLevelsPerLaunch = 5;
+
+__global__ void __launch_bounds__(256) level_build_multi_kernel(RayNode* __restrict__ nodes, Levels lv,
+                                                                 int l0, int l1) {
+    const int64_t span0 = 1ll << (2 * (l1 - l0));
+    for (int l = l0 + 1; l <= l1; ++l) {
+        const int64_t span = span0 >> (2 * (l - l0));
+        const int64_t first = (int64_t)blockIdx.x * span;
+        const int64_t last = min(first + span, lv.cnt[l]);
+        for (int64_t j = first + threadIdx.x; j < last; j += blockDim.x)
+            build_parent(nodes + lv.off[l - 1], lv.cnt[l - 1], nodes + lv.off[l], j);
+        __syncthreads();
+    }
 }
 
 // --------------------------------------------------------------- traverse
@@ -611,9 +624,6 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
         return rc;
     *so = (float4*)w.ray_o2.ptr;
     *sd = (float4*)w.ray_d2.ptr;
-    prof_begin(s, st);
-    gather_rays_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(o, d, *perm, n, *so, *sd);
-    prof_end(s, st, kStageBuild, 1);
     // levels: leaves of 32 rays, parents of 4 children, up to one root
     int64_t cnt = (n + kLeafRays - 1) / kLeafRays, total = 0;
     lv->nlev = 0;
@@ -629,13 +639,15 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     RayNode* nodes = (RayNode*)w.nodes.ptr;
     const int64_t nleaf = lv->cnt[0];
     prof_begin(s, st);
-    leaf_build_kernel<<<(unsigned)((nleaf * 32 + 255) / 256), 256, 0, st>>>(*so, *sd, skeys, n, nleaf,
-                                                                            nodes);
+    leaf_build_kernel<<<(unsigned)((nleaf * 32 + 255) / 256), 256, 0, st>>>(o, d, *perm, *so, *sd, skeys,
+                                                                            n, nleaf, nodes);
     prof_end(s, st, kStageBuild, 1);
-    for (int l = 1; l < lv->nlev; ++l) {
+    for (int l0 = 0; l0 < lv->nlev - 1; l0 += kLevelsPerLaunch) {
+        const int l1 = std::min(l0 + kLevelsPerLaunch, lv->nlev - 1);
+        const int64_t group = 1ll << (2 * (l1 - l0));
         prof_begin(s, st);
-        level_build_kernel<<<(unsigned)((lv->cnt[l] + 127) / 128), 128, 0, st>>>(
-            nodes + lv->off[l - 1], lv->cnt[l - 1], nodes + lv->off[l], lv->cnt[l]);
+        level_build_multi_kernel<<<(unsigned)((lv->cnt[l0] + group - 1) / group), 256, 0, st>>>(nodes, *lv,
+                                                                                               l0, l1);
         prof_end(s, st, kStageBuild, 1);
     }
     PBG_CUDA(cudaGetLastError());

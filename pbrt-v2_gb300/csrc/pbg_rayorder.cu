@@ -23,7 +23,13 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;                         // keys per thread
 constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys per tile
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kRadix = 256;
+constexpr int kDigitBits = 10;                // three passes sort a 30-bit key
+constexpr int kRadix = 1 << kDigitBits;
+constexpr uint32_t kDigitMask = kRadix - 1;
+constexpr int kKeyBits = 30;
+// Valid keys are clamped below 2^30 - 1, so an invalid ray's key 0xffffffff
+// (low 30 bits all ones) sorts after every valid one on the low 30 bits.
+constexpr uint32_t kMaxValidKey = (1u << kKeyBits) - 2u;
 
 __device__ __forceinline__ uint32_t spread5(uint32_t v) {
     // 5 bits -> positions 0, 6, 12, 18, 24
@@ -98,8 +104,8 @@ __global__ void morton_kernel(const float4* __restrict__ ro, const float4* __res
     uint32_t qd0 = quant5(d.x * il, -1.f, 0.5f), qd1 = quant5(d.y * il, -1.f, 0.5f),
              qd2 = quant5(d.z * il, -1.f, 0.5f);
     // Direction bits above origin bits at each level: coherent directions first.
-    keys[i] = (spread5(qd0) << 5) | (spread5(qd1) << 4) | (spread5(qd2) << 3) |
-              (spread5(qo0) << 2) | (spread5(qo1) << 1) | spread5(qo2);
+    keys[i] = min(kMaxValidKey, (spread5(qd0) << 5) | (spread5(qd1) << 4) | (spread5(qd2) << 3) |
+                                    (spread5(qo0) << 2) | (spread5(qo1) << 1) | spread5(qo2));
 }
 
 // Origin order: the 3-D Morton code of the origin, 10 bits per axis over
@@ -136,7 +142,7 @@ __global__ void origin_key_kernel(const float4* __restrict__ ro, const uint8_t* 
         v = fminf(fmaxf(v, 0.f), 1023.f);  // NaN -> 0
         q[a] = (uint32_t)v;
     }
-    keys[i] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+    keys[i] = min(kMaxValidKey, (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]));
 }
 
 // Ray-image order: when the caller declared its batches as a W x H ray image
@@ -164,7 +170,25 @@ __global__ void image_key_kernel(const uint8_t* __restrict__ valid, int64_t n, i
     }
     const uint32_t x = (uint32_t)(i % width), y = (uint32_t)(i / width);
     // 15 bits per axis keeps valid keys below 0xffffffff
-    keys[i] = (spread16(y & 0x7fffu) << 1) | spread16(x & 0x7fffu);
+    keys[i] = min(kMaxValidKey, (spread16(y & 0x7fffu) << 1) | spread16(x & 0x7fffu));
+}
+
+// The same order without a sort, for a fully valid ray image whose width
+// 2^a and height 2^b are powers of two: the Morton code of (x, y) then ranks
+// every pixel densely -- the low min(a, b) bits of x and y interleaved, the
+// longer side's remaining bits on top -- so ray i goes straight to its rank.
+__global__ void image_perm_kernel(int64_t n, int a, int b, int32_t* __restrict__ perm_out,
+                                  uint32_t* __restrict__ keys_out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t x = (uint32_t)(i & ((1ll << a) - 1)), y = (uint32_t)(i >> a);
+    const int c = min(a, b);
+    const uint32_t m = (1u << c) - 1u;
+    const uint32_t low = spread16(x & m) | (spread16(y & m) << 1);
+    const uint32_t high = a > b ? (x >> c) : (y >> c);
+    const uint32_t rank = (high << (2 * c)) | low;
+    perm_out[rank] = (int32_t)i;
+    keys_out[rank] = min(kMaxValidKey, (spread16(y) << 1) | spread16(x));
 }
 
 // Pass 1: digit histogram of each tile, stored digit-major: hist[d * tiles + tile].
@@ -177,7 +201,7 @@ __global__ void __launch_bounds__(kSortThreads)
     const int64_t base = (int64_t)blockIdx.x * kSortTile;
     for (int k = 0; k < kSortItems; ++k) {
         const int64_t i = base + (int64_t)k * kSortThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xff], 1u);
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & kDigitMask], 1u);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < kRadix; k += kSortThreads)
@@ -324,9 +348,9 @@ __global__ void __launch_bounds__(kSortThreads)
         const bool ok = i < n;
         key[k] = ok ? keys[i] : 0xffffffffu;
         val[k] = ok ? vals[i] : 0;
-        const uint32_t dg = (key[k] >> shift) & 0xff;
+        const uint32_t dg = (key[k] >> shift) & kDigitMask;
         const uint32_t inb = __ballot_sync(0xffffffffu, ok);
-        uint32_t peers = __match_any_sync(0xffffffffu, ok ? dg : 0x100u + 0u) & inb;
+        uint32_t peers = __match_any_sync(0xffffffffu, ok ? dg : (uint32_t)kRadix) & inb;
         if (!ok) peers = 0;
         const uint32_t before = wcount[warp][dg];
         __syncwarp();
@@ -350,7 +374,7 @@ __global__ void __launch_bounds__(kSortThreads)
     for (int k = 0; k < kSortItems; ++k) {
         const int64_t i = base + (int64_t)k * 32 + lane;
         if (i >= n) continue;
-        const uint32_t dg = (key[k] >> shift) & 0xff;
+        const uint32_t dg = (key[k] >> shift) & kDigitMask;
         const uint32_t pos = toff[dg] + wcount[warp][dg] + rank[k];
         keys_out[pos] = key[k];
         vals_out[pos] = val[k];
@@ -365,7 +389,7 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
     const int tiles = (int)((n + kSortTile - 1) / kSortTile);
     uint32_t *ka = keys, *kb = keys_tmp;
     int32_t *va = vals, *vb = vals_tmp;
-    for (int shift = 0; shift < bits; shift += 8) {
+    for (int shift = 0; shift < bits; shift += kDigitBits) {
         prof_begin(s, st);
         radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ka, n, shift, tiles, hist);
         prof_end(s, st, kStageSort, 1);
@@ -391,6 +415,8 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
 
 // Computes the Morton order of a batch.  *perm (device, n entries) lists ray
 // indices in sorted order; valid rays come first.
+static bool pow2_le(int64_t v, int64_t cap) { return v > 0 && v <= cap && (v & (v - 1)) == 0; }
+
 int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
              const int32_t** perm, const uint32_t** sorted_keys, cudaStream_t st, int order) {
     Work& w = s->work;
@@ -417,6 +443,19 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
         origin_key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
             o, valid, n, bounds, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
         prof_end(s, st, kStageSort, 1);
+    } else if (s->image_w > 0 && n == s->image_w * s->image_h && valid == nullptr &&
+               pow2_le(s->image_w, 1 << 15) && pow2_le(s->image_h, 1 << 15)) {
+        int a = 0, b = 0;
+        while ((1ll << a) < s->image_w) ++a;
+        while ((1ll << b) < s->image_h) ++b;
+        prof_begin(s, st);
+        image_perm_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            n, a, b, (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.mkeys_tmp.ptr);
+        prof_end(s, st, kStageSort, 1);
+        PBG_CUDA(cudaGetLastError());
+        *perm = (const int32_t*)w.perm_tmp.ptr;
+        if (sorted_keys) *sorted_keys = (const uint32_t*)w.mkeys_tmp.ptr;
+        return PBG_OK;
     } else if (s->image_w > 0 && n == s->image_w * s->image_h) {
         prof_begin(s, st);
         image_key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
@@ -434,10 +473,10 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     PBG_CUDA(cudaGetLastError());
     uint32_t* ko;
     int32_t* vo;
-    // The bounds words sit after the histogram; a 2048-key tile has < 2^16
-    // counts per digit and 32 key bits need four passes.
+    // The bounds words sit after the histogram; the low 30 key bits take
+    // three 10-bit passes (invalid rays last, see kMaxValidKey).
     rc = radix_sort_pairs(s, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr, (uint32_t*)w.mkeys_tmp.ptr,
-                          (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.hist.ptr, n, 32, &ko, &vo, st);
+                          (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.hist.ptr, n, kKeyBits, &ko, &vo, st);
     if (rc) return rc;
     *perm = vo;
     if (sorted_keys) *sorted_keys = ko;
