@@ -23,13 +23,16 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;                         // keys per thread
 constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys per tile
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kDigitBits = 10;                // three passes sort a 30-bit key
+constexpr int kDigitBits = 8;  // 8 keys per digit per 2048-key tile keep the scatter coalesced
 constexpr int kRadix = 1 << kDigitBits;
 constexpr uint32_t kDigitMask = kRadix - 1;
-constexpr int kKeyBits = 30;
-// Valid keys are clamped below 2^30 - 1, so an invalid ray's key 0xffffffff
-// (low 30 bits all ones) sorts after every valid one on the low 30 bits.
+// A sort of the low `bits` key bits: valid keys are clamped below
+// 2^bits - 1, so an invalid ray's key 0xffffffff (low bits all ones) sorts
+// after every valid one.
+constexpr int kKeyBits = 30;                            // image and 6-D keys: 4 passes
+constexpr int kOriginKeyBits = 24;                      // origin keys, 8 bits per axis: 3 passes
 constexpr uint32_t kMaxValidKey = (1u << kKeyBits) - 2u;
+constexpr uint32_t kMaxOriginKey = (1u << kOriginKeyBits) - 2u;
 
 __device__ __forceinline__ uint32_t spread5(uint32_t v) {
     // 5 bits -> positions 0, 6, 12, 18, 24
@@ -108,7 +111,7 @@ __global__ void morton_kernel(const float4* __restrict__ ro, const float4* __res
                                     (spread5(qo0) << 2) | (spread5(qo1) << 1) | spread5(qo2));
 }
 
-// Origin order: the 3-D Morton code of the origin, 10 bits per axis over
+// Origin order: the 3-D Morton code of the origin, 8 bits per axis over
 // the batch's origin box.  For shadow batches, whose directions all point at
 // a light, this keeps a leaf's 32 origins close in space (image tiles put
 // silhouette pixels' far-apart hit points together).
@@ -138,11 +141,11 @@ __global__ void origin_key_kernel(const float4* __restrict__ ro, const uint8_t* 
     for (int a = 0; a < 3; ++a) {
         const float lo = unord_f(bounds[a]);
         const float ext = unord_f(bounds[3 + a]) - lo;
-        float v = ext > 0.f ? (ov[a] - lo) / ext * 1024.f : 0.f;
-        v = fminf(fmaxf(v, 0.f), 1023.f);  // NaN -> 0
+        float v = ext > 0.f ? (ov[a] - lo) / ext * 256.f : 0.f;
+        v = fminf(fmaxf(v, 0.f), 255.f);  // NaN -> 0
         q[a] = (uint32_t)v;
     }
-    keys[i] = min(kMaxValidKey, (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]));
+    keys[i] = min(kMaxOriginKey, (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]));
 }
 
 // Ray-image order: when the caller declared its batches as a W x H ray image
@@ -473,10 +476,11 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     PBG_CUDA(cudaGetLastError());
     uint32_t* ko;
     int32_t* vo;
-    // The bounds words sit after the histogram; the low 30 key bits take
-    // three 10-bit passes (invalid rays last, see kMaxValidKey).
+    // The bounds words sit after the histogram; 8-bit passes over the low
+    // 24 (origin) or 30 key bits, invalid rays last (kMaxValidKey).
     rc = radix_sort_pairs(s, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr, (uint32_t*)w.mkeys_tmp.ptr,
-                          (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.hist.ptr, n, kKeyBits, &ko, &vo, st);
+                          (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.hist.ptr, n,
+                          order == kOrderOrigin ? kOriginKeyBits : kKeyBits, &ko, &vo, st);
     if (rc) return rc;
     *perm = vo;
     if (sorted_keys) *sorted_keys = ko;
