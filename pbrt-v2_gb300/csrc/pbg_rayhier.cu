@@ -227,20 +227,25 @@ __global__ void __launch_bounds__(256) level_build_multi_kernel(RayNode* __restr
 __device__ __forceinline__ bool node_hits_sphere(const RayNode& nd, float4 sph) {
     const float vx = sph.x - nd.a.x, vy = sph.y - nd.a.y, vz = sph.z - nd.a.z;
     const float dist2 = vx * vx + vy * vy + vz * vz;
-    const float dist = sqrtf(dist2);
+    // Square roots by the hardware reciprocal square root (error a few ulp):
+    // dist_lo / dist_hi bracket the distance by 2^-18, far inside the test's
+    // own margins; 0 and inf give NaN, which keeps the pair.
+    const float dist = dist2 * rsqrtf(dist2);
+    const float dist_lo = dist * (1.f - 0x1p-18f), dist_hi = dist * (1.f + 0x1p-18f);
     // slop of pbrt's float test grows with the distance from the ray origin
-    const float R = sph.w + nd.a.w + dist * 0x1p-12f;
-    if (!(dist > R)) return true;  // overlapping (or NaN): keep
-    if (dist - R > nd.c.y * (1.f + 0x1p-18f)) return false;  // beyond every ray's maxt
+    const float R = sph.w + nd.a.w + dist_hi * 0x1p-12f;
+    if (!(dist_lo > R)) return true;  // overlapping (or NaN): keep
+    if (dist_lo - R > nd.c.y * (1.f + 0x1p-18f)) return false;  // beyond every ray's maxt
     // With the sphere seen under half-angle beta (sin = R/dist, cos = q/dist)
     // and the cone's half-angle theta, the test is angle(axis, v) <= theta +
     // beta, i.e. axis.v >= dist cos(theta + beta) = cos(theta) q - sin(theta) R,
     // scaled by dist so that no division is needed.
-    const float q = sqrtf(fmaxf(0.f, (dist - R) * (dist + R)));
+    const float q2 = (dist_hi - R) * (dist_hi + R);  // > 0 here
+    const float q = q2 * rsqrtf(q2);
     const float cth = nd.b.w, sth = nd.c.x;
     if (cth * dist <= -q) return true;  // cone half-angle + sphere angle >= pi
     const float dotv = vx * nd.b.x + vy * nd.b.y + vz * nd.b.z;
-    return dotv >= cth * q - sth * R - 0x1p-16f * dist;
+    return dotv >= cth * q - sth * R - 0x1p-16f * dist_hi;
 }
 
 // A (triangle record, node) pair that passed its node test.
