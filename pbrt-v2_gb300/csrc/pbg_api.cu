@@ -401,10 +401,91 @@ static int run_occluded(pbg_scene* s, const float4* o, const float4* d, const ui
 }
 
 // Copies the caller's host rays into the scene's work buffers.
+// A device-usable address for caller memory, or nullptr: device and managed
+// memory as is, pinned host memory through its mapping, and any host memory
+// when the GPU reads the host's page tables directly (Grace-class hosts,
+// where the coherent chip-to-chip link serves such reads at full rate).
+static const void* device_view(int device, const void* p) {
+    if (!p) return nullptr;
+    static int ats[64] = {0};
+    static bool probed[64] = {false};
+    if (device >= 0 && device < 64 && !probed[device]) {
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+        ats[device] = pageable && host_tables;
+        probed[device] = true;
+    }
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess) {
+        if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+        if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    } else {
+        cudaGetLastError();
+    }
+    return (device >= 0 && device < 64 && ats[device]) ? p : nullptr;
+}
+
+// Caller SoA rows read in place (device-usable addresses) -> 16-byte records,
+// the validity mask copied alongside.
+__global__ void pack_rows_kernel(const float* __restrict__ ox, const float* __restrict__ oy,
+                                 const float* __restrict__ oz, const float* __restrict__ dx,
+                                 const float* __restrict__ dy, const float* __restrict__ dz,
+                                 const float* __restrict__ mint, const float* __restrict__ maxt,
+                                 const uint8_t* __restrict__ valid_in, int64_t n, float4* __restrict__ o,
+                                 float4* __restrict__ d, uint8_t* __restrict__ valid_out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    o[i] = make_float4(ox[i], oy[i], oz[i], mint[i]);
+    d[i] = make_float4(dx[i], dy[i], dz[i], maxt[i]);
+    if (valid_in) valid_out[i] = valid_in[i];
+}
+
+// Results written in place to device-usable caller addresses.
+__global__ void store_hits_kernel(const int32_t* __restrict__ prim, const float* __restrict__ t,
+                                  const float* __restrict__ b1, const float* __restrict__ b2, int64_t n,
+                                  int32_t* __restrict__ prim_out, float* __restrict__ t_out,
+                                  float* __restrict__ b1_out, float* __restrict__ b2_out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    prim_out[i] = prim[i];
+    t_out[i] = t[i];
+    b1_out[i] = b1[i];
+    b2_out[i] = b2[i];
+}
+
+__global__ void store_bytes_kernel(const uint8_t* __restrict__ src, int64_t n, uint8_t* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
 static int stage_rays(pbg_scene* s, const pbg_rays* r, int64_t n, float4** o, float4** d,
                       uint8_t** valid) {
     Work& w = s->work;
     int rc;
+    {  // read the caller's rows in place when the GPU can address them
+        const float* rows[8] = {r->ox, r->oy, r->oz, r->dx, r->dy, r->dz, r->mint, r->maxt};
+        const float* dv[8];
+        bool direct = true;
+        for (int k = 0; k < 8 && direct; ++k) direct = (dv[k] = (const float*)device_view(s->device, rows[k]));
+        const uint8_t* vin = nullptr;
+        if (direct && r->valid) direct = (vin = (const uint8_t*)device_view(s->device, r->valid)) != nullptr;
+        if (direct) {
+            if ((rc = ensure(w.ray_o, (size_t)n * sizeof(float4))) ||
+                (rc = ensure(w.ray_d, (size_t)n * sizeof(float4))) ||
+                (r->valid && (rc = ensure(w.valid, (size_t)n))))
+                return rc;
+            *o = (float4*)w.ray_o.ptr;
+            *d = (float4*)w.ray_d.ptr;
+            *valid = r->valid ? (uint8_t*)w.valid.ptr : nullptr;
+            prof_begin(s, s->stream);
+            pack_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(
+                dv[0], dv[1], dv[2], dv[3], dv[4], dv[5], dv[6], dv[7], vin, n, *o, *d, *valid);
+            prof_end(s, s->stream, kStageOther, 1);
+            PBG_CUDA(cudaGetLastError());
+            return PBG_OK;
+        }
+    }
     if ((rc = ensure(w.stage, (size_t)n * 8 * sizeof(float)))) return rc;
     if ((rc = ensure(w.ray_o, (size_t)n * sizeof(float4)))) return rc;
     if ((rc = ensure(w.ray_d, (size_t)n * sizeof(float4)))) return rc;
@@ -641,10 +722,21 @@ int pbg_intersect(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_hits* out) {
     rc = run_nearest(s, o, d, valid, n, (int32_t*)w.prim.ptr, (float*)w.t.ptr, (float*)w.b1.ptr,
                      (float*)w.b2.ptr, s->stream);
     if (rc) return rc;
-    PBG_CUDA(cudaMemcpyAsync(out->prim, w.prim.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
-    PBG_CUDA(cudaMemcpyAsync(out->t, w.t.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
-    PBG_CUDA(cudaMemcpyAsync(out->b1, w.b1.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
-    PBG_CUDA(cudaMemcpyAsync(out->b2, w.b2.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    int32_t* pp = (int32_t*)device_view(s->device, out->prim);
+    float* pt = (float*)device_view(s->device, out->t);
+    float* p1 = (float*)device_view(s->device, out->b1);
+    float* p2 = (float*)device_view(s->device, out->b2);
+    if (pp && pt && p1 && p2) {
+        store_hits_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(
+            (const int32_t*)w.prim.ptr, (const float*)w.t.ptr, (const float*)w.b1.ptr,
+            (const float*)w.b2.ptr, n, pp, pt, p1, p2);
+        PBG_CUDA(cudaGetLastError());
+    } else {
+        PBG_CUDA(cudaMemcpyAsync(out->prim, w.prim.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+        PBG_CUDA(cudaMemcpyAsync(out->t, w.t.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+        PBG_CUDA(cudaMemcpyAsync(out->b1, w.b1.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+        PBG_CUDA(cudaMemcpyAsync(out->b2, w.b2.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    }
     rc = check_device_status(s, s->stream);
     if (rc) return rc;
     s->counters.rays_nearest += (uint64_t)n;
@@ -667,7 +759,12 @@ int pbg_occluded(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t* occ) {
     if ((rc = ensure(w.occ, (size_t)n))) return rc;
     rc = run_occluded(s, o, d, valid, n, (uint8_t*)w.occ.ptr, s->stream);
     if (rc) return rc;
-    PBG_CUDA(cudaMemcpyAsync(occ, w.occ.ptr, (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    if (uint8_t* po = (uint8_t*)device_view(s->device, occ)) {
+        store_bytes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>((const uint8_t*)w.occ.ptr, n, po);
+        PBG_CUDA(cudaGetLastError());
+    } else {
+        PBG_CUDA(cudaMemcpyAsync(occ, w.occ.ptr, (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    }
     rc = check_device_status(s, s->stream);
     if (rc) return rc;
     s->counters.rays_occluded += (uint64_t)n;
