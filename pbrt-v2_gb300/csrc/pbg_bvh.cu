@@ -104,6 +104,8 @@ __global__ void __launch_bounds__(kPersistThreads)
     float nd = 0.f;
     WalkHit h{0.f, 0.f, 0.f, -1};
     int32_t node = -1, leaf_start = 0, leaf_cnt = 0, skip = INT32_MIN;
+    int32_t leafb_start = 0, leafb_cnt = 0;  // a second, postponed leaf
+    float leafb_t = 0.f;
     WorkCount wc;
 
     auto finish = [&]() {
@@ -119,6 +121,17 @@ __global__ void __launch_bounds__(kPersistThreads)
         if (!ok) atomicAdd(&status[kStatusOverflow], 1);
         has = false;
     };
+    // a leaf reached by the walk: the first pending slot, else the second
+    auto take_leaf = [&](int32_t start, int32_t cnt, float tnear) {
+        if (leaf_cnt == 0) {
+            leaf_start = start;
+            leaf_cnt = cnt;
+        } else {
+            leafb_start = start;
+            leafb_cnt = cnt;
+            leafb_t = tnear;
+        }
+    };
     // next stack entry that can still hold a hit; false when the stack is empty
     auto pop = [&]() -> bool {
         while (sp > 0) {
@@ -128,8 +141,7 @@ __global__ void __launch_bounds__(kPersistThreads)
                     node = stack_ref[sp];
                 } else {
                     node = -1;
-                    leaf_start = ~stack_ref[sp];
-                    leaf_cnt = stack_cnt[sp];
+                    take_leaf(~stack_ref[sp], stack_cnt[sp], stack_t[sp]);
                 }
                 return true;
             }
@@ -166,6 +178,7 @@ __global__ void __launch_bounds__(kPersistThreads)
                         ok = true;
                         leaf_start = 0;
                         leaf_cnt = unculled;  // degenerate records first
+                        leafb_cnt = 0;
                         has = true;
                         skip = INT32_MIN;
                         if (ORDERED) {
@@ -196,13 +209,15 @@ __global__ void __launch_bounds__(kPersistThreads)
             if (__all_sync(full, exhausted)) break;
             continue;
         }
-        // inner nodes until this lane holds a leaf or its ray ends
-        while (has && leaf_cnt == 0) {
+        // Inner nodes until every lane holds a leaf or has ended its ray; a
+        // lane that already holds one keeps walking for a second while others
+        // still search, so the leaf tests below run with fuller warps.
+        for (;;) {
+            const bool searching = has && leaf_cnt == 0;
+            if (!__any_sync(full, searching)) break;
+            if (!has || leafb_cnt > 0) continue;
             if (node < 0) {
-                if (!pop()) {
-                    finish();
-                    break;
-                }
+                if (!pop() && leaf_cnt == 0) finish();  // stack empty, nothing pending: done
                 continue;
             }
             const BvhNode nn = nodes[node];
@@ -231,15 +246,17 @@ __global__ void __launch_bounds__(kPersistThreads)
                 if (cn >= 0) {
                     node = cn;
                 } else {
-                    leaf_start = ~cn;
-                    leaf_cnt = kn;
+                    take_leaf(~cn, kn, near0 ? tn0 : tn1);
                 }
             }
         }
         // the leaf tests, converged
         if (has && leaf_cnt > 0) {
-            const bool done = test_run<ANY, false>(tris, leaf_start, leaf_cnt, o, d, nd, h, wc);
+            bool done = test_run<ANY, false>(tris, leaf_start, leaf_cnt, o, d, nd, h, wc);
             leaf_cnt = 0;
+            if (!done && leafb_cnt > 0 && leafb_t <= h.t)
+                done = test_run<ANY, false>(tris, leafb_start, leafb_cnt, o, d, nd, h, wc);
+            leafb_cnt = 0;
             if (done) finish();
         }
     }
