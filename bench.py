@@ -404,7 +404,8 @@ def run_gpu_path(args, rank, world, dev):
                 "h2d_bytes_per_step": 256, "d2h_bytes_per_step": res * res * 12,
                 "api": "pbg_render (camera and lights in, RGB image out)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 5), "traffic": None, "kernel": "bvh_kernel",
+                     "frac": round(achieved / hbm, 5), "traffic": None,
+                     "kernel": "bvh_kernel (bounce 0) + bvh_persistent_kernel (bounces 1-5)",
                      "algorithmic_bytes_per_launch": int(per_launch_bytes),
                      "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind},
         "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stt["stage_ms"].items()},
