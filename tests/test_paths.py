@@ -1,0 +1,99 @@
+"""Every internal path choice gives the same answers: rayhierarchy with and
+without triangle clusters (and splitting at any level), ray-bvh with one
+thread per ray or persistent warps, the ray image ordered by the direct
+Morton permutation (power-of-two sides) or by sorting (other sides), and
+host buffers read in place (pageable or pinned) or staged through copies.
+All compared bit for bit against the oracle's SAH BVH on the same rays."""
+import numpy as np
+import pytest
+
+from pbrt_gb300 import accel as A
+from pbrt_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_same(got, want, label):
+    prim, t, b1, b2 = got
+    wprim, wt, _, _ = want
+    bad = np.flatnonzero(prim != wprim)
+    assert bad.size == 0, f"{label}: {bad.size} prim mismatches, first {bad[:8]}"
+    h = prim >= 0
+    np.testing.assert_array_equal(t[h].view(np.uint32), wt[h].view(np.uint32), err_msg=label)
+
+
+@pytest.fixture(scope="module")
+def terrain(oracle):
+    sc = S.terrain_icospheres(seed=2, grid=96, n_spheres=12)
+    tris = sc["tris"]
+    cam = S.pinhole_rays(128, 64, (0.0, 9.0, -14.0), (0.0, 0.0, 0.0), 50.0, spp=2, jitter_seed=3)
+    inc = S.random_rays(12000, [-8, -1, -8], [8, 4, 8], seed=21)
+    inc[7, 6000:] = np.random.default_rng(4).uniform(0.1, 4.0, 6000).astype(np.float32)
+    B = oracle.BVH(tris)
+    return {"tris": tris, "cam": cam, "inc": inc, "B": B,
+            "want_cam": B.nearest(cam), "want_inc": B.nearest(inc),
+            "occ_inc": B.anyhit(inc)}
+
+
+@pytest.mark.parametrize("levels", [-1, 1, 2, 4, 99])
+def test_rayhierarchy_cluster_levels(gpu_lib, terrain, levels):
+    acc = A.MakeAccelerator("rayhierarchy", terrain["tris"], {"clusterLevels": levels})
+    assert_same(acc.Intersect(terrain["cam"].copy()), terrain["want_cam"], f"cam, levels {levels}")
+    assert_same(acc.Intersect(terrain["inc"].copy()), terrain["want_inc"], f"inc, levels {levels}")
+    occ = acc.IntersectP(terrain["inc"])
+    np.testing.assert_array_equal(occ == ord("1"), terrain["occ_inc"] == 1)
+
+
+@pytest.mark.parametrize("walk", [1, 2])
+def test_raybvh_walks(gpu_lib, terrain, walk):
+    acc = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": walk})
+    assert_same(acc.Intersect(terrain["cam"].copy()), terrain["want_cam"], f"cam, walk {walk}")
+    assert_same(acc.Intersect(terrain["inc"].copy()), terrain["want_inc"], f"inc, walk {walk}")
+    occ = acc.IntersectP(terrain["inc"])
+    np.testing.assert_array_equal(occ == ord("1"), terrain["occ_inc"] == 1)
+    # the bounce form (a validity mask) selects the persistent walk when automatic
+    hit = (np.arange(terrain["inc"].shape[1]) % 3) != 0
+    got = acc.Intersect(terrain["inc"].copy(), hit=hit.copy(), bounce=1)
+    assert (got[0][~hit] == -1).all()
+    np.testing.assert_array_equal(got[0][hit], terrain["want_inc"][0][hit])
+
+
+@pytest.mark.parametrize("width,height", [(128, 64), (96, 80)])
+def test_image_order_direct_and_sorted(gpu_lib, oracle, terrain, width, height):
+    """A 128 x 64 ray image (power-of-two sides) takes the direct Morton
+    permutation, a 96 x 80 one the sort; both give the oracle's hits, with
+    and without a validity mask."""
+    rays = S.pinhole_rays(width, height, (0.0, 9.0, -14.0), (0.0, 0.0, 0.0), 50.0, spp=1,
+                          jitter_seed=5)
+    want = terrain["B"].nearest(rays)
+    acc = A.MakeAccelerator("rayhierarchy", terrain["tris"])
+    acc.Preprocess(None, 1, 1, 1, xres=width, yres=height)
+    assert_same(acc.Intersect(rays.copy()), want, f"{width}x{height}")
+    hit = (np.arange(rays.shape[1]) % 5) != 2
+    got = acc.Intersect(rays.copy(), hit=hit.copy(), bounce=1)
+    assert (got[0][~hit] == -1).all()
+    np.testing.assert_array_equal(got[0][hit], want[0][hit])
+
+
+def test_host_buffers_pageable_pinned_and_device(gpu_lib, terrain):
+    """The host-buffer call on pageable numpy rows, on pinned rows, and the
+    device-buffer call give identical results."""
+    torch = pytest.importorskip("torch")
+    rays = terrain["inc"]
+    acc = A.MakeAccelerator("ray-bvh", terrain["tris"])
+    pageable = acc.Intersect(rays.copy())
+    pinned = torch.empty(rays.shape, dtype=torch.float32, pin_memory=True).numpy()
+    pinned[...] = rays
+    got_pinned = acc.Intersect(pinned)
+    for a, b in zip(pageable, got_pinned):
+        np.testing.assert_array_equal(a, b)
+    o4 = torch.from_numpy(np.ascontiguousarray(np.stack([rays[0], rays[1], rays[2], rays[6]], 1))).cuda()
+    d4 = torch.from_numpy(np.ascontiguousarray(np.stack([rays[3], rays[4], rays[5], rays[7]], 1))).cuda()
+    n = rays.shape[1]
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    t, b1, b2 = (torch.empty(n, device="cuda") for _ in range(3))
+    acc.intersect_device(o4, d4, prim, t, b1, b2)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(prim.cpu().numpy(), pageable[0])
+    np.testing.assert_array_equal(t.cpu().numpy().view(np.uint32), pageable[1].view(np.uint32))
+    assert_same(pageable, terrain["want_inc"], "pageable")
