@@ -359,7 +359,8 @@ def run_gpu_path(args, rank, world, dev):
     if args.learned:
         plain_rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
         plain_ms = sum(f["ms_total"] for f in frames) / len(frames)
-        acc.learn_enable(True, seed=5)
+        acc.learn_enable(True, seed=5, steps_per_train=args.learn_steps, lr=args.learn_lr,
+                         margin=args.learn_margin)
         lf, lw, lstt, lclocks, llaunch, img_learned = measure("learned")
         ls = acc.learn_stats()
         l_rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in lf) / len(lf)
@@ -779,6 +780,10 @@ def main():
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--rh-cluster-levels", type=int, default=0,
                     help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")
+    ap.add_argument("--learn-steps", type=int, default=0, help="SGD steps per frame (0 = 8)")
+    ap.add_argument("--learn-lr", type=float, default=0.0, help="learning rate (0 = 0.05)")
+    ap.add_argument("--learn-margin", type=float, default=0.0,
+                    help="logit lead needed to walk the predicted cluster first (0 = 1.0)")
     ap.add_argument("--learned", type=int, default=0,
                     help="path workload: 0 plain ordering, 1 learned ordering as the value, "
                          "2 plain as the value with the learned comparison attached")

@@ -160,7 +160,8 @@ class Aggregate:
     # -- learned traversal ordering (ray-bvh) ------------------------------
 
     def learn_enable(self, on: bool = True, batch: int = 0, steps_per_train: int = 0, lr: float = 0.0,
-                     momentum: float = 0.0, records: int = 0, seed: int = 0) -> None:
+                     momentum: float = 0.0, records: int = 0, seed: int = 0,
+                     margin: float = 0.0) -> None:
         """Builds the BVH clusters and the MLP (pbg_learn_enable); the
         accelerator then collects first-hit records from its nearest-hit
         batches, and ordered walks start once the network has trained."""
@@ -168,7 +169,7 @@ class Aggregate:
         lib.pbg_learn_enable.argtypes = [C.c_void_p, C.c_int32, C.POINTER(L.LearnParams)]
         p = L.LearnParams()
         p.batch, p.steps_per_train, p.lr, p.momentum = batch, steps_per_train, lr, momentum
-        p.records, p.seed = records, seed
+        p.records, p.seed, p.margin = records, seed, margin
         L.check(lib.pbg_learn_enable(self.handle, int(on), C.byref(p)), "pbg_learn_enable")
 
     def learn_train(self, steps: int = 0) -> None:
