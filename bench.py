@@ -187,7 +187,8 @@ def run_gpu(args, rank, world, dev):
     sc, rays = make_workload()
     tris = sc["tris"]
     n = rays.shape[1]
-    acc = A.MakeAccelerator(args.accel, tris, {"device": dev, "clusterLevels": args.rh_cluster_levels})
+    acc = A.MakeAccelerator(args.accel, tris, {"device": dev, "clusterLevels": args.rh_cluster_levels,
+                                               "walk": args.walk})
     # the breadth-first renderer's ray image: one tile of 1024 x 1024 pixels x 4 spp
     acc.Preprocess(None, 4, 1, 1, xres=1024, yres=1024)
     stream = torch.cuda.Stream()
@@ -780,6 +781,8 @@ def main():
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--rh-cluster-levels", type=int, default=0,
                     help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")
+    ap.add_argument("--walk", type=int, default=0,
+                    help="ray-bvh: 0 automatic, 1 one thread per ray, 2 persistent warps")
     ap.add_argument("--learn-steps", type=int, default=0, help="SGD steps per frame (0 = 8)")
     ap.add_argument("--learn-lr", type=float, default=0.0, help="learning rate (0 = 0.05)")
     ap.add_argument("--learn-margin", type=float, default=0.0,
