@@ -13,6 +13,7 @@
 // Errors become status codes; nothing aborts (the reference calls Severe(),
 // core/error.cpp:130).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -407,14 +408,13 @@ static int run_occluded(pbg_scene* s, const float4* o, const float4* d, const ui
 // where the coherent chip-to-chip link serves such reads at full rate).
 static const void* device_view(int device, const void* p) {
     if (!p) return nullptr;
-    static int ats[64] = {0};
-    static bool probed[64] = {false};
-    if (device >= 0 && device < 64 && !probed[device]) {
+    // per device: 0 not probed yet, 1 no host page-table access, 2 access
+    static std::atomic<int> ats[64];
+    if (device >= 0 && device < 64 && ats[device].load() == 0) {
         int pageable = 0, host_tables = 0;
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
         cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
-        ats[device] = pageable && host_tables;
-        probed[device] = true;
+        ats[device].store(pageable && host_tables ? 2 : 1);
     }
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) == cudaSuccess) {
@@ -423,7 +423,7 @@ static const void* device_view(int device, const void* p) {
     } else {
         cudaGetLastError();
     }
-    return (device >= 0 && device < 64 && ats[device]) ? p : nullptr;
+    return (device >= 0 && device < 64 && ats[device].load() == 2) ? p : nullptr;
 }
 
 // Caller SoA rows read in place (device-usable addresses) -> 16-byte records,

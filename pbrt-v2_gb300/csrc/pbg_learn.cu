@@ -554,12 +554,9 @@ int learn_predict(pbg_scene* s, const float4* o, const float4* d, int64_t n, con
     if (!L || !L->enabled || L->trained_steps == 0 || n <= 0) return PBG_OK;
     int rc = ensure(L->pred, (size_t)n * 2);
     if (rc) return rc;
-    static bool attr = false;
-    if (!attr) {
-        PBG_CUDA(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)kInferSmem));
-        attr = true;
-    }
+    // a per-device setting (cheap, idempotent): set on every call so that each
+    // device the library launches on has it
+    PBG_CUDA(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     const int64_t tiles = (n + 127) / 128;

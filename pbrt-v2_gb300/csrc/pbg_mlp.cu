@@ -1,6 +1,8 @@
 // pbg_mlp.cu -- tensor-core (tcgen05) kernels of the learned traversal
 // ordering: a generic BF16 GEMM with FP32 accumulation in TMEM (the training
 // passes are built from it) and, in pbg_learn.cu, the fused inference MLP.
+#include <mutex>
+
 #include "pbg_internal.h"
 #include "pbg_tc.cuh"
 
@@ -128,12 +130,9 @@ int tc_gemm(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K,
         set_last_error("tc_gemm: M % 128, 16 <= N <= 256 with N % 16, K % 16 required");
         return PBG_ERR_INVALID_ARGUMENT;
     }
-    static bool attr = false;
-    if (!attr) {
-        PBG_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)tc_gemm_smem_bytes()));
-        attr = true;
-    }
+    // a per-device setting (cheap, idempotent): set on every call so that each
+    // device the library launches on has it
+    PBG_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_gemm_smem_bytes()));
     const int slices = work ? tc_gemm_slices(M, K) : 1;
     const int chunks = (K + kTcKChunk - 1) / kTcKChunk;
     const int kslice = ((chunks + slices - 1) / slices) * kTcKChunk;
@@ -152,8 +151,10 @@ int tc_gemm(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K,
 
 using namespace pbg;
 
-// Status words for library-level launches that have no scene.
-static int* g_status = nullptr;
+// Status words for library-level launches that have no scene, one block per
+// device (allocated on that device the first time it is used).
+static int* g_status[64] = {nullptr};
+static std::mutex g_status_mu;
 
 extern "C" int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t M, int32_t N,
                                 int32_t K, int32_t accumulate, void* stream) {
@@ -161,19 +162,29 @@ extern "C" int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, 
         pbg::set_last_error("pbg_tc_gemm_bf16: null pointer");
         return PBG_ERR_INVALID_ARGUMENT;
     }
-    if (!g_status) {
-        cudaError_t e = cudaMalloc(&g_status, 4 * sizeof(int));
-        if (e != cudaSuccess) return pbg::cuda_status(e, "cudaMalloc(status)");
-        cudaMemset(g_status, 0, 4 * sizeof(int));
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        pbg::set_last_error("pbg_tc_gemm_bf16: no current CUDA device");
+        return PBG_ERR_NO_DEVICE;
+    }
+    int* status = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_status_mu);
+        if (!g_status[dev]) {
+            cudaError_t e = cudaMalloc(&g_status[dev], 4 * sizeof(int));
+            if (e != cudaSuccess) return pbg::cuda_status(e, "cudaMalloc(status)");
+            cudaMemset(g_status[dev], 0, 4 * sizeof(int));
+        }
+        status = g_status[dev];
     }
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = pbg::tc_gemm(A, B, C, M, N, K, accumulate, g_status, st, nullptr);
+    int rc = pbg::tc_gemm(A, B, C, M, N, K, accumulate, status, st, nullptr);
     if (rc) return rc;
     int h[4] = {0, 0, 0, 0};
-    PBG_CUDA(cudaMemcpyAsync(h, g_status, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PBG_CUDA(cudaMemcpyAsync(h, status, sizeof(h), cudaMemcpyDeviceToHost, st));
     PBG_CUDA(cudaStreamSynchronize(st));
     if (h[pbg::kStatusTimeout]) {
-        cudaMemset(g_status, 0, 4 * sizeof(int));
+        cudaMemset(status, 0, 4 * sizeof(int));
         pbg::set_last_error("pbg_tc_gemm_bf16: bounded mbarrier wait expired");
         return PBG_ERR_DEVICE_TIMEOUT;
     }
