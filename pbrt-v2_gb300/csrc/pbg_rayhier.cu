@@ -20,8 +20,11 @@
 //             their centroids, so a warp's triangles are neighbours), private
 //             stack, node test = "can any ray of the node come within R of the
 //             triangle's bounding sphere", leaf test = the exact test per ray,
-//             with the (triangle, leaf) pairs grouped by leaf first so a
-//             warp loads a leaf's rays once for all its triangles.
+//             32-triangle clusters walk the upper levels; at the leaves'
+//             parents a warp splits its cluster and tests the reaching
+//             members against each leaf's rays directly; other split levels
+//             group the (triangle, leaf) pairs by leaf first so a warp
+//             loads a leaf's rays once for all its triangles.
 //             Nearest hits merge through a 64-bit atomicMax on (t, index)
 //             keys -- race-free by construction, no repair pass; a thread
 //             reads a ray's current key first and filters with that t.
@@ -364,50 +367,28 @@ __global__ void __launch_bounds__(256)
     if (STATS) c_.flush(wc);
 }
 
-// warp_append that also stores one rank per item at the item's position.
-__device__ __forceinline__ void warp_append_ranked(const Pair* items, const uint32_t* ranks, int k,
-                                                   Pair* q, uint32_t* rank_out, uint32_t* count,
-                                                   uint32_t cap, int* status) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    int incl = k;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const int y = __shfl_up_sync(full, incl, off);
-        if (lane >= off) incl += y;
-    }
-    const int total = __shfl_sync(full, incl, 31);
-    uint32_t base = 0;
-    if (lane == 31 && total > 0) base = atomicAdd(count, (uint32_t)total);
-    base = __shfl_sync(full, base, 31);
-    const uint32_t start = base + (uint32_t)(incl - k);
-    for (int j = 0; j < k; ++j) {
-        const uint32_t pos = start + (uint32_t)j;
-        if (pos < cap) {
-            q[pos] = items[j];
-            rank_out[pos] = ranks[j];
-        }
-    }
-    if (lane == 31 && total > 0 && base + (uint32_t)total > cap) atomicAdd(&status[kStatusOverflow], 1);
-}
-
-// (cluster, level-1 node) pairs straight to (triangle, leaf) pairs: one warp
-// per pair, lane j = member j, tested against the level-1 node and then its
-// kFan leaves.  All lanes share the candidate leaves, so each leaf's count
-// takes one atomic per warp (ballot), and every item gets its rank among its
-// leaf's pairs for the counting sort.
-template <bool STATS>
+// The last two levels and the leaf tests in one pass, no pair queue: one
+// warp per (cluster, leaves' parent) pair.  Lane j first stands for member
+// triangle j (parent test, then each of the kFan leaves: a ballot gives the
+// members that reach the leaf); then, leaf by leaf, lane k stands for ray k
+// of the leaf and tests the reaching members one after another, their
+// records broadcast from the owning lanes by shuffles.  A leaf's rays are
+// loaded once per cluster that reaches it (from L2), instead of going
+// through a written, counted, sorted and re-read list of (triangle, leaf)
+// pairs.  Nearest: per-lane best key, atomicMax per leaf; any-hit: the
+// leaf's occlusion bits are read first and set when a ray is blocked.
+template <bool ANY, bool STATS>
 __global__ void __launch_bounds__(256)
-    rh_split_leaf_kernel(const float4* __restrict__ spheres, int32_t t0, int32_t t1,
-                         const RayNode* __restrict__ level1, const RayNode* __restrict__ leaves,
+    rh_split_test_kernel(const float4* __restrict__ spheres, const TriRec* __restrict__ tris, int32_t t0,
+                         int32_t t1, const RayNode* __restrict__ level1, const RayNode* __restrict__ leaves,
                          int64_t nleaf, const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
-                         Pair* __restrict__ out, uint32_t* __restrict__ rank_out, uint32_t* out_count,
-                         uint32_t* __restrict__ leafcnt, uint32_t cap, int* status,
-                         unsigned long long* wc) {
+                         uint32_t cap, const float4* __restrict__ so, const float4* __restrict__ sd,
+                         unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
+                         const int* __restrict__ status, unsigned long long* wc) {
+    if (status[kStatusOverflow] != 0) return;  // pairs were dropped upstream: this attempt is rerun
     const unsigned full = 0xffffffffu;
     const uint32_t nin = min(*in_count, cap);
     const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     WorkCount c_;
@@ -421,32 +402,76 @@ __global__ void __launch_bounds__(256)
             if (STATS) c_.node++;
             pass = node_hits_sphere(level1[pr.node], sph);
         }
-        Pair item[kFan];
-        uint32_t rk[kFan];
-        int k = 0;
+        if (!__any_sync(full, pass)) continue;
+        TriRec own;
+        own.a = own.b = own.c = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (pass) own = tris[t];
         const int64_t first = (int64_t)pr.node * kFan;
-#pragma unroll
+#pragma unroll 1
         for (int c = 0; c < kFan; ++c) {
             const int64_t leaf = first + c;
-            bool h = false;
-            if (pass && leaf < nleaf) {
-                const RayNode nd = leaves[leaf];
-                if (__float_as_int(nd.c.z) != 0) {
-                    if (STATS) c_.node++;
-                    h = node_hits_sphere(nd, sph);
+            if (leaf >= nleaf) break;
+            const RayNode nd = leaves[leaf];
+            const int count = __float_as_int(nd.c.z);
+            if (count == 0) continue;
+            bool reach = false;
+            if (pass) {
+                if (STATS) c_.node++;
+                reach = node_hits_sphere(nd, sph);
+            }
+            unsigned m = __ballot_sync(full, reach);
+            if (!m) continue;
+            if (STATS && lane == 0) c_.leaf++;
+            const int64_t r = leaf * kLeafRays + lane;
+            bool active = lane < count;
+            if (ANY && active) active = ((leafmask[leaf] >> lane) & 1u) == 0u;
+            if (!__any_sync(full, active)) continue;
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+            float nd1 = 0.f, maxt = 0.f;
+            unsigned long long best = 0ull, start = 0ull;
+            if (active) {
+                o = so[r];
+                d = sd[r];
+                nd1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+                maxt = d.w;
+                if (!ANY) {
+                    start = best = keys[r];
+                    if (start != 0ull) maxt = fminf(maxt, key_t(start));
                 }
             }
-            const unsigned b = __ballot_sync(full, h);
-            uint32_t base = 0;
-            if (lane == 0 && b) base = atomicAdd(&leafcnt[leaf], (uint32_t)__popc(b));
-            base = __shfl_sync(full, base, 0);
-            if (h) {
-                item[k] = Pair{(int32_t)t, (int32_t)leaf};
-                rk[k] = base + (uint32_t)__popc(b & lt);
-                ++k;
+            bool hit = false;
+            while (m) {
+                const int j = __ffs(m) - 1;
+                m &= m - 1;
+                TriRec tr;
+                tr.a = make_float4(__shfl_sync(full, own.a.x, j), __shfl_sync(full, own.a.y, j),
+                                   __shfl_sync(full, own.a.z, j), __shfl_sync(full, own.a.w, j));
+                tr.b = make_float4(__shfl_sync(full, own.b.x, j), __shfl_sync(full, own.b.y, j),
+                                   __shfl_sync(full, own.b.z, j), __shfl_sync(full, own.b.w, j));
+                tr.c = make_float4(__shfl_sync(full, own.c.x, j), __shfl_sync(full, own.c.y, j),
+                                   __shfl_sync(full, own.c.z, j), __shfl_sync(full, own.c.w, j));
+                if (!active) continue;
+                if (STATS) c_.filt++;
+                if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
+                float tt, u1, u2;
+                if (STATS) c_.exact++;
+                if (!pbg_exact_rec(tr, o, d, maxt, &tt, &u1, &u2)) continue;
+                if (STATS) c_.hit++;
+                if (ANY) {
+                    hit = true;
+                    active = false;
+                } else {
+                    const unsigned long long k = hit_key(tt, __float_as_int(tr.c.w));
+                    if (k > best) best = k;
+                    maxt = tt;
+                }
+            }
+            if (ANY) {
+                if (hit) atomicOr(&leafmask[leaf], 1u << lane);
+            } else if (best > start) {
+                atomicMax(&keys[r], best);
             }
         }
-        warp_append_ranked(item, rk, k, out, rank_out, out_count, cap, status);
     }
     if (STATS) c_.flush(wc);
 }
@@ -723,21 +748,18 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             uint32_t* leafcnt = (uint32_t*)w.leafcnt.ptr;
             uint32_t* rank = (uint32_t*)w.pair_rank.ptr;
             PBG_CUDA(cudaMemsetAsync(leafcnt, 0, (size_t)nleaf * sizeof(uint32_t), st));
-            bool counted = false;
+            bool fused = false;
             for (int l = top; l >= 0; --l) {
-                if (cl && l == 1 && split == 1) {  // clusters -> (triangle, leaf) pairs, counted
+                if (cl && l == 1 && split == 1) {  // clusters straight into the leaf tests
                     if (stats)
-                        rh_split_leaf_kernel<true><<<grid * 2, 256, 0, st>>>(
-                            tsph, t0, t1, nodes + lv.off[1], nodes + lv.off[0], lv.cnt[0], qa, cnt_of[1],
-                            qb, rank, &counts[0], leafcnt, kQueueCap, status, wc);
+                        rh_split_test_kernel<ANY, true><<<grid * 2, 256, 0, st>>>(
+                            tsph, (const TriRec*)s->tris.ptr, t0, t1, nodes + lv.off[1], nodes + lv.off[0],
+                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, status, wc);
                     else
-                        rh_split_leaf_kernel<false><<<grid * 2, 256, 0, st>>>(
-                            tsph, t0, t1, nodes + lv.off[1], nodes + lv.off[0], lv.cnt[0], qa, cnt_of[1],
-                            qb, rank, &counts[0], leafcnt, kQueueCap, status, nullptr);
-                    Pair* tq = qa;
-                    qa = qb;
-                    qb = tq;
-                    counted = true;
+                        rh_split_test_kernel<ANY, false><<<grid * 2, 256, 0, st>>>(
+                            tsph, (const TriRec*)s->tris.ptr, t0, t1, nodes + lv.off[1], nodes + lv.off[0],
+                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, status, nullptr);
+                    fused = true;
                     break;
                 }
                 if (cl && l == split) {  // clusters -> triangles, same level
@@ -768,20 +790,21 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                 qa = qb;
                 qb = tq;
             }
-            // group the leaf pairs by leaf: qa -> qb
-            if (!counted)
+            // group the leaf pairs by leaf (qa -> qb), then the leaf tests
+            if (!fused) {
                 rh_leaf_count_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank);
-            if ((rc = scan_counts(s, leafcnt, nleaf, st))) return rc;
-            rh_leaf_scatter_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank, qb,
-                                                         status);
-            if (stats)
-                rh_leaf_sorted_kernel<ANY, true><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
-                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask, status,
-                    wc);
-            else
-                rh_leaf_sorted_kernel<ANY, false><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
-                    (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask, status,
-                    nullptr);
+                if ((rc = scan_counts(s, leafcnt, nleaf, st))) return rc;
+                rh_leaf_scatter_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank, qb,
+                                                             status);
+                if (stats)
+                    rh_leaf_sorted_kernel<ANY, true><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
+                        (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask,
+                        status, wc);
+                else
+                    rh_leaf_sorted_kernel<ANY, false><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
+                        (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask,
+                        status, nullptr);
+            }
             prof_end(s, st, kStageTraverse, lv.nlev + 6);
             PBG_CUDA(cudaGetLastError());
         }
