@@ -377,8 +377,10 @@ __global__ void __launch_bounds__(256)
 // through a written, counted, sorted and re-read list of (triangle, leaf)
 // pairs.  Nearest: per-lane best key, atomicMax per leaf; any-hit: the
 // leaf's occlusion bits are read first and set when a ray is blocked.
+constexpr int kSplitTestMinBlocks = 4;  // CTAs per SM: 5-8 force spills and measured no faster
+
 template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, kSplitTestMinBlocks)
     rh_split_test_kernel(const float4* __restrict__ spheres, const TriRec* __restrict__ tris, int32_t t0,
                          int32_t t1, const RayNode* __restrict__ level1, const RayNode* __restrict__ leaves,
                          int64_t nleaf, const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
