@@ -372,12 +372,12 @@ __global__ void __launch_bounds__(256)
 // triangle j (parent test, then each of the kFan leaves: a ballot gives the
 // members that reach the leaf); then, leaf by leaf, lane k stands for ray k
 // of the leaf and tests the reaching members one after another, their
-// records broadcast from the owning lanes by shuffles.  A leaf's rays are
+// records staged in shared memory by the owning lanes.  A leaf's rays are
 // loaded once per cluster that reaches it (from L2), instead of going
 // through a written, counted, sorted and re-read list of (triangle, leaf)
 // pairs.  Nearest: per-lane best key, atomicMax per leaf; any-hit: the
 // leaf's occlusion bits are read first and set when a ray is blocked.
-constexpr int kSplitTestMinBlocks = 4;  // CTAs per SM: 5-8 force spills and measured no faster
+constexpr int kSplitTestMinBlocks = 5;  // CTAs per SM: measured best of 4-8 (5-7 equal, 5 spills least)
 
 template <bool ANY, bool STATS>
 __global__ void __launch_bounds__(256, kSplitTestMinBlocks)
@@ -387,8 +387,10 @@ __global__ void __launch_bounds__(256, kSplitTestMinBlocks)
                          uint32_t cap, const float4* __restrict__ so, const float4* __restrict__ sd,
                          unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
                          const int* __restrict__ status, unsigned long long* wc) {
+    __shared__ float4 s_rec[8][kClusterTris * 3];  // this warp's member records (256 threads)
     if (status[kStatusOverflow] != 0) return;  // pairs were dropped upstream: this attempt is rerun
     const unsigned full = 0xffffffffu;
+    float4* rec = s_rec[threadIdx.x >> 5];
     const uint32_t nin = min(*in_count, cap);
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -405,9 +407,14 @@ __global__ void __launch_bounds__(256, kSplitTestMinBlocks)
             pass = node_hits_sphere(level1[pr.node], sph);
         }
         if (!__any_sync(full, pass)) continue;
-        TriRec own;
-        own.a = own.b = own.c = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (pass) own = tris[t];
+        __syncwarp();  // the previous pair's records are no longer read
+        if (pass) {
+            const TriRec own = tris[t];
+            rec[3 * lane] = own.a;
+            rec[3 * lane + 1] = own.b;
+            rec[3 * lane + 2] = own.c;
+        }
+        __syncwarp();
         const int64_t first = (int64_t)pr.node * kFan;
 #pragma unroll 1
         for (int c = 0; c < kFan; ++c) {
@@ -445,14 +452,11 @@ __global__ void __launch_bounds__(256, kSplitTestMinBlocks)
             while (m) {
                 const int j = __ffs(m) - 1;
                 m &= m - 1;
-                TriRec tr;
-                tr.a = make_float4(__shfl_sync(full, own.a.x, j), __shfl_sync(full, own.a.y, j),
-                                   __shfl_sync(full, own.a.z, j), __shfl_sync(full, own.a.w, j));
-                tr.b = make_float4(__shfl_sync(full, own.b.x, j), __shfl_sync(full, own.b.y, j),
-                                   __shfl_sync(full, own.b.z, j), __shfl_sync(full, own.b.w, j));
-                tr.c = make_float4(__shfl_sync(full, own.c.x, j), __shfl_sync(full, own.c.y, j),
-                                   __shfl_sync(full, own.c.z, j), __shfl_sync(full, own.c.w, j));
                 if (!active) continue;
+                TriRec tr;
+                tr.a = rec[3 * j];
+                tr.b = rec[3 * j + 1];
+                tr.c = rec[3 * j + 2];
                 if (STATS) c_.filt++;
                 if (!pbg_filter(tr, o, d, nd1, maxt)) continue;
                 float tt, u1, u2;
