@@ -20,9 +20,10 @@
 namespace pbg {
 
 constexpr int kBvhThreads = 128;
+constexpr int kBvhMinBlocks = 8;  // CTAs per SM: measured best of 8, 12, 16
 
 template <bool ANY, bool STATS, bool ORDERED>
-__global__ void __launch_bounds__(kBvhThreads)
+__global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
     bvh_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris, int32_t unculled,
                const float4* __restrict__ ro, const float4* __restrict__ rd,
                const uint8_t* __restrict__ valid, const int32_t* __restrict__ perm, int64_t n,
@@ -78,11 +79,12 @@ __global__ void __launch_bounds__(kBvhThreads)
 // together.  The stack keeps leaf children with their triangle counts.
 // Same culling, order-independent merge and results as bvh_kernel.
 constexpr int kPersistThreads = 128;
+constexpr int kPersistMinBlocks = 8;  // CTAs per SM: measured best of 8, 12, 16
 
 // ORDERED: the learned ordering's predicted cluster (pred, cref as in
 // bvh_kernel) is walked first, then the whole tree skipping it.
 template <bool ANY, bool ORDERED>
-__global__ void __launch_bounds__(kPersistThreads)
+__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
     bvh_persistent_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris,
                           int32_t unculled, const float4* __restrict__ ro, const float4* __restrict__ rd,
                           const uint8_t* __restrict__ valid, const int32_t* __restrict__ perm, int64_t n,
