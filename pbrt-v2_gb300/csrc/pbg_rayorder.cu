@@ -30,7 +30,8 @@ constexpr uint32_t kDigitMask = kRadix - 1;
 // 2^bits - 1, so an invalid ray's key 0xffffffff (low bits all ones) sorts
 // after every valid one.
 constexpr int kKeyBits = 30;                            // image and 6-D keys: 4 passes
-constexpr int kOriginKeyBits = 24;                      // origin keys, 8 bits per axis: 3 passes
+constexpr int kOriginAxisBits = 8;  // origin keys: bits per axis (measured best of 5, 7, 8)
+constexpr int kOriginKeyBits = 3 * kOriginAxisBits;     // 24 bits: 3 passes
 constexpr uint32_t kMaxValidKey = (1u << kKeyBits) - 2u;
 constexpr uint32_t kMaxOriginKey = (1u << kOriginKeyBits) - 2u;
 
@@ -141,8 +142,9 @@ __global__ void origin_key_kernel(const float4* __restrict__ ro, const uint8_t* 
     for (int a = 0; a < 3; ++a) {
         const float lo = unord_f(bounds[a]);
         const float ext = unord_f(bounds[3 + a]) - lo;
-        float v = ext > 0.f ? (ov[a] - lo) / ext * 256.f : 0.f;
-        v = fminf(fmaxf(v, 0.f), 255.f);  // NaN -> 0
+        constexpr float kCells = (float)(1 << kOriginAxisBits);
+        float v = ext > 0.f ? (ov[a] - lo) / ext * kCells : 0.f;
+        v = fminf(fmaxf(v, 0.f), kCells - 1.f);  // NaN -> 0
         q[a] = (uint32_t)v;
     }
     keys[i] = min(kMaxOriginKey, (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]));
