@@ -436,9 +436,17 @@ __global__ void pack_rows_kernel(const float* __restrict__ ox, const float* __re
                                  float4* __restrict__ d, uint8_t* __restrict__ valid_out) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (valid_in) {  // an invalid ray's row entries are never read: skip them on the link
+        const uint8_t v = valid_in[i];
+        valid_out[i] = v;
+        if (v == 0) {
+            o[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            d[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            return;
+        }
+    }
     o[i] = make_float4(ox[i], oy[i], oz[i], mint[i]);
     d[i] = make_float4(dx[i], dy[i], dz[i], maxt[i]);
-    if (valid_in) valid_out[i] = valid_in[i];
 }
 
 // Results written in place to device-usable caller addresses.
