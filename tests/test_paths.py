@@ -97,3 +97,32 @@ def test_host_buffers_pageable_pinned_and_device(gpu_lib, terrain):
     np.testing.assert_array_equal(prim.cpu().numpy(), pageable[0])
     np.testing.assert_array_equal(t.cpu().numpy().view(np.uint32), pageable[1].view(np.uint32))
     assert_same(pageable, terrain["want_inc"], "pageable")
+
+
+def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
+    """Shadow batches from the same points (one per light sample) reuse the
+    cached origin sort; a batch that moves one origin, changes validity or
+    changes size sorts again.  Every batch matches the oracle."""
+    B = terrain["B"]
+    base = terrain["inc"].copy()
+    rng = np.random.default_rng(11)
+    acc = A.MakeAccelerator("rayhierarchy", terrain["tris"])
+    n = base.shape[1]
+    all_valid = np.ones(n, bool)
+    cases = []
+    for k in range(3):  # same origins, new directions and lengths
+        r = base.copy()
+        r[3:6] = rng.normal(size=(3, n)).astype(np.float32)
+        r[7] = rng.uniform(0.5, 6.0, n).astype(np.float32)
+        cases.append((r, all_valid))
+    moved = cases[-1][0].copy()
+    moved[0, n // 2] += 0.75
+    cases.append((moved, all_valid))
+    some = (np.arange(n) % 7) != 3
+    cases.append((moved, some))
+    cases.append((moved, some))
+    cases.append((moved[:, : n - 64].copy(), some[: n - 64].copy()))
+    for i, (r, v) in enumerate(cases):
+        got = acc.IntersectP(r, hit=v) if not v.all() else acc.IntersectP(r)
+        want = B.anyhit(r) == 1
+        np.testing.assert_array_equal((got == ord("1"))[v], want[v], err_msg=f"batch {i}")
