@@ -663,7 +663,7 @@ void pbg_scene_destroy(pbg_scene* s) {
                            &w.t, &w.b1, &w.b2, &w.occ, &w.keys, &w.stage, &w.perm,
                            &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
                            &w.leafmask, &w.counters, &w.geo, &w.queue_a, &w.queue_b,
-                           &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt, &w.okey_cache,
+                           &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt, &w.origin_cache,
                            &w.osort_keys, &w.osort_perm, &w.osort_same};
     for (DeviceBuffer* b : all) release(*b);
     if (s->stream) cudaStreamDestroy(s->stream);

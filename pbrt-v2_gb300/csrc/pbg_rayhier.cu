@@ -829,6 +829,10 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
 int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
     if (n <= 0) return PBG_OK;
+    // A nearest-hit batch yields new hit points: the origin order kept for
+    // the shadow batches that leave from the previous ones is dropped, so
+    // only shadow batches between two nearest-hit batches share a sort.
+    s->origin_sort_n = -1;
     const int32_t* perm;
     float4 *so, *sd;
     Levels lv;

@@ -199,8 +199,7 @@ __global__ void image_perm_kernel(int64_t n, int a, int b, int32_t* __restrict__
 // Pass 1: digit histogram of each tile, stored digit-major: hist[d * tiles + tile].
 __global__ void __launch_bounds__(kSortThreads)
     radix_hist_kernel(const uint32_t* __restrict__ keys, int64_t n, int shift, int tiles,
-                      uint32_t* __restrict__ hist, const int* __restrict__ skip) {
-    if (skip && *skip) return;
+                      uint32_t* __restrict__ hist) {
     __shared__ uint32_t h[kRadix];
     for (int k = threadIdx.x; k < kRadix; k += kSortThreads) h[k] = 0;
     __syncthreads();
@@ -245,9 +244,7 @@ __device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t* w
 }
 
 __global__ void __launch_bounds__(1024) scan_chunk_sums(const uint32_t* __restrict__ a, int64_t m,
-                                                        uint32_t* __restrict__ sums,
-                                                        const int* __restrict__ skip = nullptr) {
-    if (skip && *skip) return;
+                                                        uint32_t* __restrict__ sums) {
     __shared__ uint32_t ws[32];
     const int64_t base = (int64_t)blockIdx.x * kScanChunk + threadIdx.x * 4;
     uint32_t v = 0;
@@ -259,9 +256,7 @@ __global__ void __launch_bounds__(1024) scan_chunk_sums(const uint32_t* __restri
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(1024) scan_top(uint32_t* __restrict__ sums, int nchunks,
-                                                 const int* __restrict__ skip = nullptr) {
-    if (skip && *skip) return;
+__global__ void __launch_bounds__(1024) scan_top(uint32_t* __restrict__ sums, int nchunks) {
     __shared__ uint32_t ws[32];
     __shared__ uint32_t carry;
     if (threadIdx.x == 0) carry = 0;
@@ -279,9 +274,7 @@ __global__ void __launch_bounds__(1024) scan_top(uint32_t* __restrict__ sums, in
 }
 
 __global__ void __launch_bounds__(1024) scan_chunks(uint32_t* __restrict__ a, int64_t m,
-                                                    const uint32_t* __restrict__ sums,
-                                                    const int* __restrict__ skip = nullptr) {
-    if (skip && *skip) return;
+                                                    const uint32_t* __restrict__ sums) {
     __shared__ uint32_t ws[32];
     const int64_t base = (int64_t)blockIdx.x * kScanChunk + threadIdx.x * 4;
     uint32_t v[4], s = 0;
@@ -340,9 +333,7 @@ __global__ void __launch_bounds__(1024) scan_kernel(uint32_t* __restrict__ a, in
 __global__ void __launch_bounds__(kSortThreads)
     radix_scatter_kernel(const uint32_t* __restrict__ keys, const int32_t* __restrict__ vals,
                          int64_t n, int shift, int tiles, const uint32_t* __restrict__ offs,
-                         uint32_t* __restrict__ keys_out, int32_t* __restrict__ vals_out,
-                         const int* __restrict__ skip) {
-    if (skip && *skip) return;
+                         uint32_t* __restrict__ keys_out, int32_t* __restrict__ vals_out) {
     __shared__ uint32_t wcount[kSortWarps][kRadix];  // per-warp digit counts, then prefixes
     __shared__ uint32_t toff[kRadix];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -397,28 +388,26 @@ __global__ void __launch_bounds__(kSortThreads)
 
 // Sorts (keys, vals) of length n in place through the tmp buffers; returns
 // pointers to the sorted arrays (which alternate between the two buffers).
-// skip (device word, may be null): when it holds non-zero at run time every
-// pass returns at once, leaving the arrays as they are.
 int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp,
                      uint32_t* hist, int64_t n, int bits, uint32_t** keys_out, int32_t** vals_out,
-                     cudaStream_t st, const int* skip) {
+                     cudaStream_t st) {
     const int tiles = (int)((n + kSortTile - 1) / kSortTile);
     uint32_t *ka = keys, *kb = keys_tmp;
     int32_t *va = vals, *vb = vals_tmp;
     for (int shift = 0; shift < bits; shift += kDigitBits) {
         prof_begin(s, st);
-        radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ka, n, shift, tiles, hist, skip);
+        radix_hist_kernel<<<tiles, kSortThreads, 0, st>>>(ka, n, shift, tiles, hist);
         prof_end(s, st, kStageSort, 1);
         const int64_t m = (int64_t)tiles * kRadix;
         const int nchunks = (int)((m + kScanChunk - 1) / kScanChunk);
         uint32_t* sums = hist + m + 8;  // after the histogram and the bounds words
         prof_begin(s, st);
-        scan_chunk_sums<<<nchunks, 1024, 0, st>>>(hist, m, sums, skip);
-        scan_top<<<1, 1024, 0, st>>>(sums, nchunks, skip);
-        scan_chunks<<<nchunks, 1024, 0, st>>>(hist, m, sums, skip);
+        scan_chunk_sums<<<nchunks, 1024, 0, st>>>(hist, m, sums);
+        scan_top<<<1, 1024, 0, st>>>(sums, nchunks);
+        scan_chunks<<<nchunks, 1024, 0, st>>>(hist, m, sums);
         prof_end(s, st, kStageSort, 3);
         prof_begin(s, st);
-        radix_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(ka, va, n, shift, tiles, hist, kb, vb, skip);
+        radix_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(ka, va, n, shift, tiles, hist, kb, vb);
         prof_end(s, st, kStageSort, 1);
         PBG_CUDA(cudaGetLastError());
         uint32_t* tk = ka; ka = kb; kb = tk;
@@ -432,25 +421,31 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
 // Computes the Morton order of a batch.  *perm (device, n entries) lists ray
 // indices in sorted order; valid rays come first.
 // Shadow batches of one frame (one per light sample) leave from the same
-// points with the same validity, so their origin keys -- and the sorted
-// order -- repeat.  compare_keys_kernel clears *same at the first key that
-// differs from the cached ones and stores the new keys in the cache;
-// store_sorted_kernel keeps a fresh sort's result unless *same held.
-__global__ void compare_keys_kernel(const uint32_t* __restrict__ keys, int64_t n,
-                                    uint32_t* __restrict__ cache, int* __restrict__ same) {
+// points with the same validity, so their origin order repeats.
+// compare_origins_kernel clears *same at any ray whose validity, or whose
+// origin while valid, differs bit for bit from the cached batch, and stores
+// the new entry (x, y, z, valid) in the cache; store_sorted_kernel keeps a
+// fresh sort's order for the next batch.
+__global__ void compare_origins_kernel(const float4* __restrict__ ro, const uint8_t* __restrict__ valid,
+                                       int64_t n, uint4* __restrict__ cache, int* __restrict__ same) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t k = keys[i];
-    if (cache[i] != k) {
+    const uint32_t v = valid ? (valid[i] != 0) : 1u;
+    uint4 e = make_uint4(0u, 0u, 0u, 0u);
+    if (v) {
+        const float4 o = ro[i];
+        e = make_uint4(__float_as_uint(o.x), __float_as_uint(o.y), __float_as_uint(o.z), 1u);
+    }
+    const uint4 c = cache[i];
+    if (c.x != e.x || c.y != e.y || c.z != e.z || c.w != e.w) {
         *same = 0;
-        cache[i] = k;
+        cache[i] = e;
     }
 }
 
 __global__ void store_sorted_kernel(const uint32_t* __restrict__ skeys, const int32_t* __restrict__ perm,
-                                    int64_t n, const int* __restrict__ same,
-                                    uint32_t* __restrict__ skeys_cache, int32_t* __restrict__ perm_cache) {
-    if (*same) return;
+                                    int64_t n, uint32_t* __restrict__ skeys_cache,
+                                    int32_t* __restrict__ perm_cache) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     skeys_cache[i] = skeys[i];
@@ -478,6 +473,33 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     int64_t blocks = (n + 255) / 256;
     if (blocks > 4 * sms) blocks = 4 * sms;
     if (order == kOrderOrigin) {
+        // reuse the previous origin order when origins and validity repeat
+        const void* before[3] = {w.origin_cache.ptr, w.osort_keys.ptr, w.osort_perm.ptr};
+        const bool was_cached = s->origin_sort_n == n;
+        s->origin_sort_n = -1;  // set again only once the cache is consistent
+        if ((rc = ensure(w.origin_cache, (size_t)n * 16)) || (rc = ensure(w.osort_keys, (size_t)n * 4)) ||
+            (rc = ensure(w.osort_perm, (size_t)n * 4)) || (rc = ensure(w.osort_same, 16)))
+            return rc;
+        const bool comparable = was_cached && before[0] == w.origin_cache.ptr &&
+                                before[1] == w.osort_keys.ptr && before[2] == w.osort_perm.ptr;
+        int* same = (int*)w.osort_same.ptr;
+        PBG_CUDA(cudaMemsetAsync(same, comparable ? 1 : 0, sizeof(int), st));
+        prof_begin(s, st);
+        compare_origins_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            o, valid, n, (uint4*)w.origin_cache.ptr, same);
+        prof_end(s, st, kStageSort, 1);
+        PBG_CUDA(cudaGetLastError());
+        int hsame = 0;
+        if (comparable) {  // one flag read; the sort below is 15 launches
+            PBG_CUDA(cudaMemcpyAsync(&hsame, same, sizeof(int), cudaMemcpyDeviceToHost, st));
+            PBG_CUDA(cudaStreamSynchronize(st));
+        }
+        if (hsame) {
+            s->origin_sort_n = n;
+            *perm = (const int32_t*)w.osort_perm.ptr;
+            if (sorted_keys) *sorted_keys = (const uint32_t*)w.osort_keys.ptr;
+            return PBG_OK;
+        }
         prof_begin(s, st);
         origin_bounds_kernel<<<(unsigned)blocks, 256, 0, st>>>(o, valid, n, bounds);
         prof_end(s, st, kStageSort, 1);
@@ -515,33 +537,16 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     PBG_CUDA(cudaGetLastError());
     uint32_t* ko;
     int32_t* vo;
-    int* same = nullptr;
-    if (order == kOrderOrigin) {  // reuse the last origin sort when the keys repeat
-        const void* before[3] = {w.okey_cache.ptr, w.osort_keys.ptr, w.osort_perm.ptr};
-        const bool was_cached = s->origin_sort_n == n;
-        s->origin_sort_n = -1;  // set again only once the cache is consistent
-        if ((rc = ensure(w.okey_cache, (size_t)n * 4)) || (rc = ensure(w.osort_keys, (size_t)n * 4)) ||
-            (rc = ensure(w.osort_perm, (size_t)n * 4)) || (rc = ensure(w.osort_same, 16)))
-            return rc;
-        const bool comparable = was_cached && before[0] == w.okey_cache.ptr &&
-                                before[1] == w.osort_keys.ptr && before[2] == w.osort_perm.ptr;
-        same = (int*)w.osort_same.ptr;
-        PBG_CUDA(cudaMemsetAsync(same, comparable ? 1 : 0, sizeof(int), st));
-        prof_begin(s, st);
-        compare_keys_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            (const uint32_t*)w.mkeys.ptr, n, (uint32_t*)w.okey_cache.ptr, same);
-        prof_end(s, st, kStageSort, 1);
-    }
     // The bounds words sit after the histogram; 8-bit passes over the low
     // 24 (origin) or 30 key bits, invalid rays last (kMaxValidKey).
     rc = radix_sort_pairs(s, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr, (uint32_t*)w.mkeys_tmp.ptr,
                           (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.hist.ptr, n,
-                          order == kOrderOrigin ? kOriginKeyBits : kKeyBits, &ko, &vo, st, same);
+                          order == kOrderOrigin ? kOriginKeyBits : kKeyBits, &ko, &vo, st);
     if (rc) return rc;
-    if (same) {
+    if (order == kOrderOrigin) {
         prof_begin(s, st);
         store_sorted_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            ko, vo, n, same, (uint32_t*)w.osort_keys.ptr, (int32_t*)w.osort_perm.ptr);
+            ko, vo, n, (uint32_t*)w.osort_keys.ptr, (int32_t*)w.osort_perm.ptr);
         prof_end(s, st, kStageSort, 1);
         PBG_CUDA(cudaGetLastError());
         ko = (uint32_t*)w.osort_keys.ptr;

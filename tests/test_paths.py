@@ -101,8 +101,9 @@ def test_host_buffers_pageable_pinned_and_device(gpu_lib, terrain):
 
 def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
     """Shadow batches from the same points (one per light sample) reuse the
-    cached origin sort; a batch that moves one origin, changes validity or
-    changes size sorts again.  Every batch matches the oracle."""
+    kept origin order; a batch that moves one origin, changes validity or
+    changes size, or follows a nearest-hit batch, sorts again.  Every batch
+    matches the oracle."""
     B = terrain["B"]
     base = terrain["inc"].copy()
     rng = np.random.default_rng(11)
@@ -123,6 +124,8 @@ def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
     cases.append((moved, some))
     cases.append((moved[:, : n - 64].copy(), some[: n - 64].copy()))
     for i, (r, v) in enumerate(cases):
+        if i == 2:  # a nearest-hit batch in between drops the kept order
+            assert_same(acc.Intersect(terrain["inc"].copy()), terrain["want_inc"], "nearest")
         got = acc.IntersectP(r, hit=v) if not v.all() else acc.IntersectP(r)
         want = B.anyhit(r) == 1
         np.testing.assert_array_equal((got == ord("1"))[v], want[v], err_msg=f"batch {i}")
