@@ -664,7 +664,7 @@ void pbg_scene_destroy(pbg_scene* s) {
                            &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
                            &w.leafmask, &w.counters, &w.geo, &w.queue_a, &w.queue_b,
                            &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt, &w.origin_cache,
-                           &w.osort_keys, &w.osort_perm, &w.osort_same};
+                           &w.osort_keys, &w.osort_perm, &w.osort_same, &w.reach};
     for (DeviceBuffer* b : all) release(*b);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;

@@ -76,7 +76,7 @@ constexpr int kClusterTris = 32;
 struct Work {
     DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
         perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo, queue_a, queue_b,
-        qcount, scan_sums, pair_rank, leafcnt, origin_cache, osort_keys, osort_perm, osort_same;
+        qcount, scan_sums, pair_rank, leafcnt, origin_cache, osort_keys, osort_perm, osort_same, reach;
     int64_t cap = 0;
 };
 

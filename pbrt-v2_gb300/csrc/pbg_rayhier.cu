@@ -378,14 +378,32 @@ __global__ void __launch_bounds__(256)
 // pairs.  Nearest: per-lane best key, atomicMax per leaf; any-hit: the
 // leaf's occlusion bits are read first and set when a ray is blocked.
 constexpr int kSplitTestMinBlocks = 5;  // CTAs per SM: measured best of 4-8 (5-7 equal, 5 spills least)
+constexpr int kNearestMinBlocks = 4;     // nearest-hit variant, resident grid: best of 4-6
+
+// Nearest-hit batches also keep a live reach bound per leaf and per leaves'
+// parent: an upper bound on maxt x |d| over the node's rays, where each
+// ray's maxt has shrunk to its best hit so far (hits are only replaced by
+// nearer ones, or by the higher index at equal t, which the node test's
+// strict comparison keeps).  A member whose sphere lies wholly beyond the
+// bound cannot become any of the node's nearest hits, so it is culled like
+// one beyond the rays' own maxt.  Stored as 0x7f800000 - bits(bound), so
+// zeroed memory reads +inf and atomicMax lowers the bound.
+__device__ __forceinline__ float live_reach(const uint32_t* b) {
+    return __uint_as_float(0x7f800000u - __ldcg(b));
+}
+__device__ __forceinline__ void lower_reach(uint32_t* b, float x) {
+    x = (x == x) ? fmaxf(x, 0.f) : INFINITY;  // NaN reads as unbounded
+    atomicMax(b, 0x7f800000u - __float_as_uint(x));
+}
 
 template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(256, kSplitTestMinBlocks)
+__global__ void __launch_bounds__(256, ANY ? kSplitTestMinBlocks : kNearestMinBlocks)
     rh_split_test_kernel(const float4* __restrict__ spheres, const TriRec* __restrict__ tris, int32_t t0,
                          int32_t t1, const RayNode* __restrict__ level1, const RayNode* __restrict__ leaves,
                          int64_t nleaf, const Pair* __restrict__ in, const uint32_t* __restrict__ in_count,
                          uint32_t cap, const float4* __restrict__ so, const float4* __restrict__ sd,
                          unsigned long long* __restrict__ keys, uint32_t* __restrict__ leafmask,
+                         uint32_t* __restrict__ leaf_reach, uint32_t* __restrict__ parent_reach,
                          const int* __restrict__ status, unsigned long long* wc) {
     __shared__ float4 s_rec[8][kClusterTris * 3];  // this warp's member records (256 threads)
     if (status[kStatusOverflow] != 0) return;  // pairs were dropped upstream: this attempt is rerun
@@ -401,10 +419,16 @@ __global__ void __launch_bounds__(256, kSplitTestMinBlocks)
         const int64_t t = (int64_t)pr.tri * kClusterTris + lane;
         bool pass = false;
         float4 sph = make_float4(0.f, 0.f, 0.f, 0.f);
+        float parent_now = INFINITY;
         if (t >= t0 && t < t1) {
             sph = spheres[t];
             if (STATS) c_.node++;
-            pass = node_hits_sphere(level1[pr.node], sph);
+            RayNode pn = level1[pr.node];
+            if (!ANY) {
+                pn.c.y = fminf(pn.c.y, live_reach(parent_reach + pr.node));
+                parent_now = pn.c.y;
+            }
+            pass = node_hits_sphere(pn, sph);
         }
         if (!__any_sync(full, pass)) continue;
         __syncwarp();  // the previous pair's records are no longer read
@@ -416,20 +440,25 @@ __global__ void __launch_bounds__(256, kSplitTestMinBlocks)
         }
         __syncwarp();
         const int64_t first = (int64_t)pr.node * kFan;
+        float parent_new = 0.f;  // max of the leaves' bounds after this pair
 #pragma unroll 1
         for (int c = 0; c < kFan; ++c) {
             const int64_t leaf = first + c;
             if (leaf >= nleaf) break;
-            const RayNode nd = leaves[leaf];
+            RayNode nd = leaves[leaf];
             const int count = __float_as_int(nd.c.z);
             if (count == 0) continue;
+            if (!ANY) nd.c.y = fminf(nd.c.y, live_reach(leaf_reach + leaf));
             bool reach = false;
             if (pass) {
                 if (STATS) c_.node++;
                 reach = node_hits_sphere(nd, sph);
             }
             unsigned m = __ballot_sync(full, reach);
-            if (!m) continue;
+            if (!m) {
+                if (!ANY) parent_new = fmaxf(parent_new, nd.c.y);
+                continue;
+            }
             if (STATS && lane == 0) c_.leaf++;
             const int64_t r = leaf * kLeafRays + lane;
             bool active = lane < count;
@@ -474,12 +503,87 @@ __global__ void __launch_bounds__(256, kSplitTestMinBlocks)
             }
             if (ANY) {
                 if (hit) atomicOr(&leafmask[leaf], 1u << lane);
-            } else if (best > start) {
-                atomicMax(&keys[r], best);
+            } else {
+                if (best > start) atomicMax(&keys[r], best);
+                // the leaf's bound from its rays' maxt after this cluster
+                // (2^-20 covers the rounding of |d|; lanes past count hold
+                // no ray)
+                const float len = sqrtf(fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z)));
+                float b = lane < count ? maxt * len * (1.f + 0x1p-20f) : 0.f;
+                if (!(b == b)) b = INFINITY;
+#pragma unroll
+                for (int off = 16; off; off >>= 1) b = fmaxf(b, __shfl_xor_sync(full, b, off));
+                if (lane == 0 && b < nd.c.y) lower_reach(leaf_reach + leaf, b);
+                parent_new = fmaxf(parent_new, fminf(b, nd.c.y));
             }
         }
+        if (!ANY && lane == 0 && parent_new < parent_now) lower_reach(parent_reach + pr.node, parent_new);
     }
     if (STATS) c_.flush(wc);
+}
+
+// Front-to-back order for the pairs of a nearest-hit batch: a counting sort
+// of the (cluster, leaves' parent) pairs on the distance from the root's
+// origin ball to the cluster's sphere, so that the leaf tests, which take
+// the pairs in queue order over time, meet the near clusters first and
+// their hits lower the live reach bounds before the far clusters arrive.
+// Buckets: the top bits of the float distance, 64 per octave.  The order
+// only changes how much is culled, never a result.
+constexpr int kOrderBuckets = 16384;
+
+__device__ __forceinline__ uint32_t pair_bucket(float4 c, float4 root) {
+    const float dx = c.x - root.x, dy = c.y - root.y, dz = c.z - root.z;
+    float dist = sqrtf(dx * dx + dy * dy + dz * dz) - c.w - root.w;
+    if (!(dist > 0.f)) dist = 0.f;  // overlapping, or NaN
+    return min(__float_as_uint(dist) >> 17, (uint32_t)kOrderBuckets - 1u);
+}
+
+__global__ void __launch_bounds__(256)
+    rh_order_count_kernel(const float4* __restrict__ csph, const RayNode* __restrict__ root,
+                          const Pair* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t cap,
+                          uint32_t* __restrict__ hist, const int* __restrict__ status) {
+    if (status[kStatusOverflow] != 0) return;  // this attempt is rerun
+    const uint32_t nin = min(*in_count, cap);
+    const float4 r = root->a;
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nin; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const bool ok = i < nin;
+        const uint32_t key = ok ? pair_bucket(csph[in[i].tri], r) : (uint32_t)kOrderBuckets;
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        if (ok && lane == __ffs(peers) - 1) atomicAdd(&hist[key], (uint32_t)__popc(peers));
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    rh_order_scatter_kernel(const float4* __restrict__ csph, const RayNode* __restrict__ root,
+                            const Pair* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t cap,
+                            uint32_t* __restrict__ cursor, Pair* __restrict__ out,
+                            const int* __restrict__ status) {
+    if (status[kStatusOverflow] != 0) return;
+    const uint32_t nin = min(*in_count, cap);
+    const float4 r = root->a;
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nin; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const bool ok = i < nin;
+        Pair pr = Pair{0, 0};
+        uint32_t key = (uint32_t)kOrderBuckets;
+        if (ok) {
+            pr = in[i];
+            key = pair_bucket(csph[pr.tri], r);
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t first = 0;
+        if (ok && lane == leader) first = atomicAdd(&cursor[key], (uint32_t)__popc(peers));
+        first = __shfl_sync(0xffffffffu, first, leader);
+        const uint64_t dst = (uint64_t)first + __popc(peers & lt);
+        if (ok && dst < nin) out[dst] = pr;
+    }
 }
 
 // The final pairs grouped by leaf (a counting sort: count with ranks, scan,
@@ -726,6 +830,15 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
     const int split = std::max(0, top - kcl);
     const float4* tsph = (const float4*)s->spheres.ptr;
     const float4* csph = (const float4*)s->clusters.ptr;
+    uint32_t *leaf_reach = nullptr, *parent_reach = nullptr, *order_hist = nullptr;
+    if (!ANY && lv.nlev > 1) {  // live reach bounds, +inf to start (zeroed)
+        const size_t nb = (size_t)(lv.cnt[0] + lv.cnt[1]);
+        if ((rc = ensure(w.reach, (nb + kOrderBuckets) * sizeof(uint32_t)))) return rc;
+        leaf_reach = (uint32_t*)w.reach.ptr;
+        parent_reach = leaf_reach + lv.cnt[0];
+        order_hist = parent_reach + lv.cnt[1];
+        PBG_CUDA(cudaMemsetAsync(leaf_reach, 0, nb * sizeof(uint32_t), st));
+    }
     for (int attempt = 0; attempt < 8; ++attempt) {
         PBG_CUDA(cudaMemsetAsync(status + kStatusOverflow, 0, sizeof(int), st));
         // group boundaries on cluster boundaries
@@ -738,6 +851,7 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             Pair* qa = (Pair*)w.queue_a.ptr;
             Pair* qb = (Pair*)w.queue_b.ptr;
             prof_begin(s, st);
+            int nl = 1;  // kernels launched below (scan_counts counts its own)
             // pairs of level l count in counts[l] (clusters: counts[kMaxLevels + l])
             const bool cl = kcl > 0;
             const float4* seed_sph = cl ? csph : tsph;
@@ -757,15 +871,33 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             bool fused = false;
             for (int l = top; l >= 0; --l) {
                 if (cl && l == 1 && split == 1) {  // clusters straight into the leaf tests
+                    unsigned tgrid = grid * 2;
+                    if (order_hist) {  // nearest: front-to-back pairs, taken in order
+                        PBG_CUDA(cudaMemsetAsync(order_hist, 0, kOrderBuckets * sizeof(uint32_t), st));
+                        rh_order_count_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[top], qa, cnt_of[1],
+                                                                    kQueueCap, order_hist, status);
+                        if ((rc = scan_counts(s, order_hist, kOrderBuckets, st))) return rc;
+                        rh_order_scatter_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[top], qa,
+                                                                      cnt_of[1], kQueueCap, order_hist, qb,
+                                                                      status);
+                        Pair* tq = qa;
+                        qa = qb;
+                        qb = tq;
+                        tgrid = (unsigned)(sms * kNearestMinBlocks);  // resident CTAs only
+                        nl += 2;
+                    }
                     if (stats)
-                        rh_split_test_kernel<ANY, true><<<grid * 2, 256, 0, st>>>(
+                        rh_split_test_kernel<ANY, true><<<tgrid, 256, 0, st>>>(
                             tsph, (const TriRec*)s->tris.ptr, t0, t1, nodes + lv.off[1], nodes + lv.off[0],
-                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, status, wc);
+                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, leaf_reach,
+                            parent_reach, status, wc);
                     else
-                        rh_split_test_kernel<ANY, false><<<grid * 2, 256, 0, st>>>(
+                        rh_split_test_kernel<ANY, false><<<tgrid, 256, 0, st>>>(
                             tsph, (const TriRec*)s->tris.ptr, t0, t1, nodes + lv.off[1], nodes + lv.off[0],
-                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, status, nullptr);
+                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, leaf_reach,
+                            parent_reach, status, nullptr);
                     fused = true;
+                    ++nl;
                     break;
                 }
                 if (cl && l == split) {  // clusters -> triangles, same level
@@ -781,6 +913,7 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                     qa = qb;
                     qb = tq;
                     cnt_of[l] = &counts[l];
+                    ++nl;
                 }
                 if (l == 0) break;
                 const float4* sph = (cl && l > split) ? csph : tsph;
@@ -795,6 +928,7 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                 Pair* tq = qa;
                 qa = qb;
                 qb = tq;
+                ++nl;
             }
             // group the leaf pairs by leaf (qa -> qb), then the leaf tests
             if (!fused) {
@@ -810,8 +944,9 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                     rh_leaf_sorted_kernel<ANY, false><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
                         (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask,
                         status, nullptr);
+                nl += 3;
             }
-            prof_end(s, st, kStageTraverse, lv.nlev + 6);
+            prof_end(s, st, kStageTraverse, nl);
             PBG_CUDA(cudaGetLastError());
         }
         // One status read per call: a dropped pair would lose hits.
