@@ -252,10 +252,25 @@ static void prof_collect(pbg_scene* s) {
     }
 }
 
+__global__ void publish_words_kernel(const int* __restrict__ src, int count, int* dst) {
+    if ((int)threadIdx.x < count) ((volatile int*)dst)[threadIdx.x] = src[threadIdx.x];
+}
+
+int read_device_words(pbg_scene* s, const int* dev, int count, int* out, cudaStream_t st) {
+    if (count > 16 || !s->mbox_dev) return PBG_ERR_INVALID_ARGUMENT;
+    publish_words_kernel<<<1, 32, 0, st>>>(dev, count, s->mbox_dev);
+    s->counters.kernel_launches++;
+    PBG_CUDA(cudaGetLastError());
+    PBG_CUDA(cudaStreamSynchronize(st));
+    const volatile int* h = s->mbox_host;
+    for (int k = 0; k < count; ++k) out[k] = h[k];
+    return PBG_OK;
+}
+
 int check_device_status(pbg_scene* s, cudaStream_t st) {
     int h[4] = {0, 0, 0, 0};
-    PBG_CUDA(cudaMemcpyAsync(h, s->err.ptr, sizeof(h), cudaMemcpyDeviceToHost, st));
-    PBG_CUDA(cudaStreamSynchronize(st));
+    int rc = read_device_words(s, (const int*)s->err.ptr, 4, h, st);
+    if (rc) return rc;
     if (h[kStatusTimeout] != 0 || h[kStatusOverflow] != 0) {
         PBG_CUDA(cudaMemsetAsync(s->err.ptr, 0, sizeof(h), st));
         char buf[160];
@@ -596,6 +611,11 @@ int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t 
         if (e != cudaSuccess) return fail(cuda_status(e, "cudaStreamCreate"));
     }
     if ((rc = ensure(s->err, 4 * sizeof(int)))) return fail(rc);
+    {
+        cudaError_t e = cudaHostAlloc((void**)&s->mbox_host, 16 * sizeof(int), cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&s->mbox_dev, s->mbox_host, 0);
+        if (e != cudaSuccess) return fail(cuda_status(e, "cudaHostAlloc(status words)"));
+    }
     if (cudaMemset(s->err.ptr, 0, 4 * sizeof(int)) != cudaSuccess)
         return fail(cuda_status(cudaGetLastError(), "cudaMemset"));
     for (int64_t i = 0; i < ntri; ++i)
@@ -667,6 +687,7 @@ void pbg_scene_destroy(pbg_scene* s) {
                            &w.osort_keys, &w.osort_perm, &w.osort_same, &w.reach};
     for (DeviceBuffer* b : all) release(*b);
     if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->mbox_host) cudaFreeHost(s->mbox_host);
     delete s;
 }
 

@@ -951,8 +951,7 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
         }
         // One status read per call: a dropped pair would lose hits.
         int ovf = 0;
-        PBG_CUDA(cudaMemcpyAsync(&ovf, status + kStatusOverflow, sizeof(int), cudaMemcpyDeviceToHost, st));
-        PBG_CUDA(cudaStreamSynchronize(st));
+        if ((rc = read_device_words(s, status + kStatusOverflow, 1, &ovf, st))) return rc;
         if (ovf == 0) return PBG_OK;
         groups *= 4;  // rerun: atomicMax / atomicOr merges make a rerun idempotent
         s->rh_groups = groups;

@@ -82,6 +82,11 @@ __global__ void origin_bounds_kernel(const float4* __restrict__ ro, const uint8_
     }
 }
 
+// Empty bounds for origin_bounds_kernel's atomics: lo = max, hi = min.
+__global__ void init_bounds_kernel(int* __restrict__ bounds) {
+    if (threadIdx.x < 6) bounds[threadIdx.x] = threadIdx.x < 3 ? 0x7fffffff : (int)0x80000000;
+}
+
 __global__ void morton_kernel(const float4* __restrict__ ro, const float4* __restrict__ rd,
                               const uint8_t* __restrict__ valid, int64_t n,
                               const int* __restrict__ bounds, uint32_t* __restrict__ keys,
@@ -465,9 +470,6 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
                               ((size_t)tiles * kRadix + kScanChunk - 1) / kScanChunk + 8) * 4)))
         return rc;
     int* bounds = (int*)((uint32_t*)w.hist.ptr + (size_t)tiles * kRadix);
-    const int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000,
-                         (int)0x80000000};
-    PBG_CUDA(cudaMemcpyAsync(bounds, init, sizeof(init), cudaMemcpyHostToDevice, st));
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     int64_t blocks = (n + 255) / 256;
@@ -491,8 +493,7 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
         PBG_CUDA(cudaGetLastError());
         int hsame = 0;
         if (comparable) {  // one flag read; the sort below is 15 launches
-            PBG_CUDA(cudaMemcpyAsync(&hsame, same, sizeof(int), cudaMemcpyDeviceToHost, st));
-            PBG_CUDA(cudaStreamSynchronize(st));
+            if ((rc = read_device_words(s, same, 1, &hsame, st))) return rc;
         }
         if (hsame) {
             s->origin_sort_n = n;
@@ -501,8 +502,9 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
             return PBG_OK;
         }
         prof_begin(s, st);
+        init_bounds_kernel<<<1, 32, 0, st>>>(bounds);
         origin_bounds_kernel<<<(unsigned)blocks, 256, 0, st>>>(o, valid, n, bounds);
-        prof_end(s, st, kStageSort, 1);
+        prof_end(s, st, kStageSort, 2);
         prof_begin(s, st);
         origin_key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
             o, valid, n, bounds, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);
@@ -527,8 +529,9 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
         prof_end(s, st, kStageSort, 1);
     } else {
         prof_begin(s, st);
+        init_bounds_kernel<<<1, 32, 0, st>>>(bounds);
         origin_bounds_kernel<<<(unsigned)blocks, 256, 0, st>>>(o, valid, n, bounds);
-        prof_end(s, st, kStageSort, 1);
+        prof_end(s, st, kStageSort, 2);
         prof_begin(s, st);
         morton_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
             o, d, valid, n, bounds, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr);

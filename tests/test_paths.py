@@ -102,8 +102,8 @@ def test_host_buffers_pageable_pinned_and_device(gpu_lib, terrain):
 def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
     """Shadow batches from the same points (one per light sample) reuse the
     kept origin order; a batch that moves one origin, changes validity or
-    changes size, or follows a nearest-hit batch, sorts again.  Every batch
-    matches the oracle."""
+    size, or follows a nearest-hit batch, sorts again.  Every batch matches
+    the oracle."""
     B = terrain["B"]
     base = terrain["inc"].copy()
     rng = np.random.default_rng(11)
@@ -116,6 +116,10 @@ def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
         r[3:6] = rng.normal(size=(3, n)).astype(np.float32)
         r[7] = rng.uniform(0.5, 6.0, n).astype(np.float32)
         cases.append((r, all_valid))
+    near = cases[-1][0].copy()  # nearby directions
+    near[3:6] += (0.02 * rng.normal(size=(3, n))).astype(np.float32)
+    cases.append((near, all_valid))
+    cases.append((near, all_valid))  # the same batch again
     moved = cases[-1][0].copy()
     moved[0, n // 2] += 0.75
     cases.append((moved, all_valid))
