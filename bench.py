@@ -47,6 +47,10 @@ METRIC = "Mrays/s nearest+any-hit at exact hit-ID match: plain vs learned-ordere
 # dram__bytes_read.sum + dram__bytes_write.sum of one tuned trace launch of
 # the 64-scene batch (ncu --set full, the warm-up launch after autotuning)
 BATCH_LAUNCH_DRAM_BYTES = 1_611_773_000
+# dram__bytes_read.sum + dram__bytes_write.sum of the traversal stage of one
+# batch call of the terrain frame (every traversal kernel of the warm-up
+# frame's nearest batch and four shadow batches, averaged over the five)
+FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 207_000_000, "ray-bvh": 116_000_000}
 L2_BYTES = 129 * 1024 * 1024
 CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)
 
@@ -258,10 +262,7 @@ def run_gpu(args, rank, world, dev):
     avg_launch_ms = trav_ms / max(calls, 1)
     hbm, peak_kind = peaks()
     achieved = per_launch_bytes / (avg_launch_ms * 1e-3) / 1e9
-    traffic = None
-    tj = os.path.join(ROOT, "profiles", f"traffic_{args.accel}.json")
-    if os.path.exists(tj):
-        traffic = json.load(open(tj)).get("bytes_per_launch")
+    traffic = FRAME_TRAVERSAL_DRAM_BYTES.get(args.accel)
 
     # parity sample: hit IDs of a ray sample against the oracle port (CPU)
     parity = None
