@@ -283,24 +283,31 @@ __device__ __forceinline__ void warp_append(const Pair* items, int k, Pair* q, u
 }
 
 // Level-synchronous descent.  Pairs of level `lvl` (already tested) produce
-// the pairs of their children that pass; the root level is seeded from the
-// triangles [t0, t1).
+// the pairs of their children that pass.  The descent is seeded at a level
+// of at most kSeedNodes nodes: every (cluster or triangle in [t0, t1), node)
+// pair there is tested directly, which replaces the launches of the nearly
+// empty levels above it.
+constexpr int64_t kSeedNodes = 256;
+
 template <bool STATS>
 __global__ void __launch_bounds__(256)
     rh_seed_kernel(const float4* __restrict__ spheres, int32_t t0, int32_t t1,
-                   const RayNode* __restrict__ root, Pair* __restrict__ out, uint32_t* count,
-                   uint32_t cap, int* status, unsigned long long* wc) {
+                   const RayNode* __restrict__ level_nodes, int64_t nnodes, Pair* __restrict__ out,
+                   uint32_t* count, uint32_t cap, int* status, unsigned long long* wc) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const RayNode nd = *root;
-    const int rc = __float_as_int(nd.c.z);
+    const int64_t total = (int64_t)(t1 - t0) * nnodes;
     WorkCount c_;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + t0; base < t1; base += stride) {
-        const int64_t t = base + (threadIdx.x);
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
+        const int64_t i = base + threadIdx.x;
         Pair item[1];
         int k = 0;
-        if (t < t1 && rc > 0) {
-            if (STATS) c_.node++;
-            if (node_hits_sphere(nd, spheres[t])) item[k++] = Pair{(int32_t)t, 0};
+        if (i < total) {
+            const int64_t t = t0 + i / nnodes, node = i % nnodes;
+            const RayNode nd = level_nodes[node];
+            if (__float_as_int(nd.c.z) > 0) {
+                if (STATS) c_.node++;
+                if (node_hits_sphere(nd, spheres[t])) item[k++] = Pair{(int32_t)t, (int32_t)node};
+            }
         }
         warp_append(item, k, out, count, cap, status);
     }
@@ -859,17 +866,25 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             const int32_t s1 = cl ? (int32_t)((t1 + kClusterTris - 1) / kClusterTris) : t1;
             uint32_t* cnt_of[kMaxLevels];
             for (int l = 0; l < kMaxLevels; ++l) cnt_of[l] = &counts[(cl && l >= split) ? kMaxLevels + l : l];
+            // seed level: the lowest with at most kSeedNodes nodes, not below
+            // the level where clusters split
+            int ls = top;
+            while (ls > std::max(split, 1) && lv.cnt[ls - 1] <= kSeedNodes) --ls;
+            const int64_t seed_grid = std::min<int64_t>(
+                grid, ((int64_t)(s1 - s0) * lv.cnt[ls] + 255) / 256);
             if (stats)
-                rh_seed_kernel<true><<<grid, 256, 0, st>>>(seed_sph, s0, s1, nodes + lv.off[top], qa,
-                                                           cnt_of[top], kQueueCap, status, wc);
+                rh_seed_kernel<true><<<(unsigned)seed_grid, 256, 0, st>>>(
+                    seed_sph, s0, s1, nodes + lv.off[ls], lv.cnt[ls], qa, cnt_of[ls], kQueueCap, status, wc);
             else
-                rh_seed_kernel<false><<<grid, 256, 0, st>>>(seed_sph, s0, s1, nodes + lv.off[top], qa,
-                                                            cnt_of[top], kQueueCap, status, nullptr);
+                rh_seed_kernel<false><<<(unsigned)seed_grid, 256, 0, st>>>(
+                    seed_sph, s0, s1, nodes + lv.off[ls], lv.cnt[ls], qa, cnt_of[ls], kQueueCap, status,
+                    nullptr);
             uint32_t* leafcnt = (uint32_t*)w.leafcnt.ptr;
             uint32_t* rank = (uint32_t*)w.pair_rank.ptr;
-            PBG_CUDA(cudaMemsetAsync(leafcnt, 0, (size_t)nleaf * sizeof(uint32_t), st));
+            if (!(cl && split == 1))  // the leaf-pair counting sort runs
+                PBG_CUDA(cudaMemsetAsync(leafcnt, 0, (size_t)nleaf * sizeof(uint32_t), st));
             bool fused = false;
-            for (int l = top; l >= 0; --l) {
+            for (int l = ls; l >= 0; --l) {
                 if (cl && l == 1 && split == 1) {  // clusters straight into the leaf tests
                     unsigned tgrid = grid * 2;
                     if (order_hist) {  // nearest: front-to-back pairs, taken in order
