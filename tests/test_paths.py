@@ -133,3 +133,40 @@ def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
         got = acc.IntersectP(r, hit=v) if not v.all() else acc.IntersectP(r)
         want = B.anyhit(r) == 1
         np.testing.assert_array_equal((got == ord("1"))[v], want[v], err_msg=f"batch {i}")
+
+
+def test_exact_ties_across_clusters(gpu_lib, oracle):
+    """Ties at scale for the front-to-back order with live reach bounds:
+    a 48 x 48 grid of quads laid down twice (the second copy after every
+    other triangle, so tied triangles sit in different clusters), rays
+    straight down onto grid vertices and edge midpoints.  Every ray hits
+    several triangles at the same t; the highest index must win, as in the
+    in-order loop, although the first cluster reached already set the
+    leaf's bound to that t."""
+    k = 48
+    xs = np.arange(k + 1, dtype=np.float32)
+    tris = []
+    for i in range(k):
+        for j in range(k):
+            a = (xs[i], 0.0, xs[j])
+            b = (xs[i + 1], 0.0, xs[j])
+            c = (xs[i + 1], 0.0, xs[j + 1])
+            d = (xs[i], 0.0, xs[j + 1])
+            tris.append(a + b + c)
+            tris.append(a + c + d)
+    tris = np.asarray(tris, np.float32)
+    tris = np.concatenate([tris, tris[::-1]])  # each triangle twice, far apart in index
+    g = np.random.default_rng(8)
+    px = np.concatenate([g.integers(1, k, 6000).astype(np.float32),
+                         g.integers(1, k, 3000).astype(np.float32) + 0.5])
+    pz = np.concatenate([g.integers(1, k, 6000).astype(np.float32),
+                         g.integers(1, k, 3000).astype(np.float32)])
+    n = px.size
+    rays = np.zeros((8, n), np.float32)
+    rays[0], rays[1], rays[2] = px, 3.0, pz
+    rays[4] = -1.0
+    rays[7] = np.inf
+    want = oracle.nearest(tris, rays)
+    for kind in ("rayhierarchy", "ray-bvh"):
+        acc = A.MakeAccelerator(kind, tris)
+        assert_same(acc.Intersect(rays.copy()), want, kind)
