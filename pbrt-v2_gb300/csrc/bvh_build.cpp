@@ -4,8 +4,9 @@
 // The reference builds pbrt's BVHAccel per triangle part on the CPU
 // (accelerators/bvh.cpp:209-283 with gpu=true, flattened breadth-first by
 // GPUbufferWide, bvh.cpp:154-206, into 32-byte GPUNode records,
-// accelerators/bvh.h:75-79).  Here one binned-SAH tree covers the whole
-// scene (no 60k-triangle parts) and is stored as two-wide nodes that carry
+// accelerators/bvh.h:75-79).  Here one binned-SAH tree (32 bins on each
+// axis, leaves of at most 4 triangles) covers the whole scene (no
+// 60k-triangle parts) and is stored as two-wide nodes that carry
 // both children's boxes (BvhNode, 64 bytes), which halves the dependent node
 // fetches of a traversal step.
 //
@@ -63,7 +64,7 @@ struct Task {
     int32_t begin, end, depth;
 };
 
-constexpr int kBins = 16;
+constexpr int kBins = 32;
 
 float pad_of(float lo, float hi, float global_pad) {
     float mag = std::max(std::fabs(lo), std::fabs(hi));
@@ -184,42 +185,46 @@ void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out) {
         int32_t mid = -1;
         bool leaf = np <= max_leaf || !(ext > 0.f) || tk.depth >= 48;
         if (!leaf) {
-            int cnt[kBins] = {0};
-            Box bb[kBins];
-            for (int k = 0; k < kBins; ++k) bb[k].reset();
-            const float scale = kBins / ext;
-            auto bin_of = [&](const Item& it) {
-                int b = (int)((it.c[axis] - cb.lo[axis]) * scale);
-                return b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
-            };
-            for (int32_t i = tk.begin; i < tk.end; ++i) {
-                int b = bin_of(items[i]);
-                cnt[b]++;
-                bb[b].grow(items[i].box);
-            }
-            float rarea[kBins];
-            int rcnt[kBins];
-            Box acc;
-            acc.reset();
-            int c = 0;
-            for (int k = kBins - 1; k > 0; --k) {
-                acc.grow(bb[k]);
-                c += cnt[k];
-                rarea[k] = acc.area();
-                rcnt[k] = c;
-            }
-            acc.reset();
-            c = 0;
+            // binned SAH over every axis with a centroid extent; the lowest
+            // cost wins
             float best = INFINITY;
-            int best_split = -1;
-            for (int k = 0; k < kBins - 1; ++k) {
-                acc.grow(bb[k]);
-                c += cnt[k];
-                if (c == 0 || rcnt[k + 1] == 0) continue;
-                float cost = acc.area() * c + rarea[k + 1] * rcnt[k + 1];
-                if (cost < best) {
-                    best = cost;
-                    best_split = k;
+            int best_axis = -1, best_split = -1;
+            for (int a = 0; a < 3; ++a) {
+                const float ea = cb.hi[a] - cb.lo[a];
+                if (!(ea > 0.f)) continue;
+                int cnt[kBins] = {0};
+                Box bb[kBins];
+                for (int k = 0; k < kBins; ++k) bb[k].reset();
+                const float scale = kBins / ea;
+                for (int32_t i = tk.begin; i < tk.end; ++i) {
+                    int b = (int)((items[i].c[a] - cb.lo[a]) * scale);
+                    b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+                    cnt[b]++;
+                    bb[b].grow(items[i].box);
+                }
+                float rarea[kBins];
+                int rcnt[kBins];
+                Box acc;
+                acc.reset();
+                int c = 0;
+                for (int k = kBins - 1; k > 0; --k) {
+                    acc.grow(bb[k]);
+                    c += cnt[k];
+                    rarea[k] = acc.area();
+                    rcnt[k] = c;
+                }
+                acc.reset();
+                c = 0;
+                for (int k = 0; k < kBins - 1; ++k) {
+                    acc.grow(bb[k]);
+                    c += cnt[k];
+                    if (c == 0 || rcnt[k + 1] == 0) continue;
+                    const float cost = acc.area() * c + rarea[k + 1] * rcnt[k + 1];
+                    if (cost < best) {
+                        best = cost;
+                        best_axis = a;
+                        best_split = k;
+                    }
                 }
             }
             if (best_split < 0) {
@@ -232,8 +237,15 @@ void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out) {
                                      });
                 }
             } else {
+                const int a = best_axis;
+                const float scale = kBins / (cb.hi[a] - cb.lo[a]);
+                const float lo = cb.lo[a];
                 auto it = std::partition(items.begin() + tk.begin, items.begin() + tk.end,
-                                         [&](const Item& x) { return bin_of(x) <= best_split; });
+                                         [&](const Item& x) {
+                                             int b = (int)((x.c[a] - lo) * scale);
+                                             b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+                                             return b <= best_split;
+                                         });
                 mid = (int32_t)(it - items.begin());
                 if (mid == tk.begin || mid == tk.end) mid = tk.begin + np / 2;
             }
