@@ -51,6 +51,11 @@ BATCH_LAUNCH_DRAM_BYTES = 1_611_773_000
 # batch call of the terrain frame (every traversal kernel of the warm-up
 # frame's nearest batch and four shadow batches, averaged over the five)
 FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 207_000_000, "ray-bvh": 116_000_000}
+# The traversal is bound by instruction issue, not by HBM: ncu's issue-active
+# fraction of the dominant kernel (smsp__issue_active, --set full capture of
+# the frame's camera and first shadow batch)
+FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, nearest)": 0.69,
+                                       "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.74}}
 L2_BYTES = 129 * 1024 * 1024
 CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)
 
@@ -300,7 +305,8 @@ def run_gpu(args, rank, world, dev):
                          "traffic": traffic, "kernel": "traversal stage of one batch call",
                          "launches_per_unit": round(trav_launches / max(calls, 1), 2),
                          "algorithmic_bytes_per_launch": int(per_launch_bytes),
-                         "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind},
+                         "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind,
+                         "issue_active": FRAME_ISSUE_ACTIVE.get(args.accel)},
             "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in st["stage_ms"].items()},
             "gpu_launches": int(launches),
             "cpu_baseline": cpu,
