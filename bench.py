@@ -681,7 +681,10 @@ def run_e2e(args, acc, rays, shadows, hitmask, rays_per_step):
         frame()
     torch.cuda.synchronize()
     ms = (time.perf_counter() - t0) * 1e3 / k
-    h2d = n * 32 + len(shadows) * (n * 32 + n)
+    # bytes that cross the host link: a shadow batch's invalid rays are not
+    # read (only their validity byte), the results of every ray are written
+    nvalid = int(np.count_nonzero(hitmask))
+    h2d = n * 32 + len(shadows) * (nvalid * 32 + n)
     d2h = n * 16 + len(shadows) * n
     return {"value": round(rays_per_step / (ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
             "ms_per_step": round(ms, 3), "h2d_bytes_per_step": int(h2d),
