@@ -684,7 +684,8 @@ void pbg_scene_destroy(pbg_scene* s) {
                            &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
                            &w.leafmask, &w.counters, &w.geo, &w.queue_a, &w.queue_b,
                            &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt, &w.origin_cache,
-                           &w.osort_keys, &w.osort_perm, &w.osort_same, &w.reach};
+                           &w.osort_keys, &w.osort_perm, &w.osort_same, &w.reach,
+                           &w.origin_valid};
     for (DeviceBuffer* b : all) release(*b);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->mbox_host) cudaFreeHost(s->mbox_host);

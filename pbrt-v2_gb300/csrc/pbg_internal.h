@@ -76,7 +76,7 @@ constexpr int kClusterTris = 32;
 struct Work {
     DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
         perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo, queue_a, queue_b,
-        qcount, scan_sums, pair_rank, leafcnt, origin_cache, osort_keys, osort_perm, osort_same, reach;
+        qcount, scan_sums, pair_rank, leafcnt, origin_cache, osort_keys, osort_perm, osort_same, reach, origin_valid;
     int64_t cap = 0;
 };
 
@@ -101,6 +101,9 @@ struct pbg_scene {
     int rh_groups = 1;         // triangle groups per rayhierarchy traversal (grows on overflow)
     int walk_hint = -1;        // ray-bvh: 1 = incoherent batch, 0 = coherent, -1 = infer
     int64_t origin_sort_n = -1;  // rays of the cached origin sort (-1 = none)
+    bool origin_reused = false;      // the last origin-ordered sort reused the kept order
+    bool sorted_origins_ok = false;  // the work buffers hold the last origin-ordered build's
+                                     // sorted origins and leaf spheres
     std::vector<pbg::BvhNode> host_nodes;  // ray-bvh tree, kept for the learned clusters
     std::vector<int32_t> host_order;
     struct pbg::Learner* learn = nullptr;

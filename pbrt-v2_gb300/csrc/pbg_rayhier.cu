@@ -64,10 +64,14 @@ __device__ __forceinline__ float round_up_rel(float x) { return fmaf(fabsf(x), 0
 
 // One warp per leaf of 32 sorted rays; the warp also gathers its rays into
 // sorted order (so, sd) for the leaf tests.
+// keep_o: the batch leaves from the same origins (bit for bit, mint
+// included) in the same order as the previous one, whose sorted origins and
+// leaf spheres are still in so / leaves: only the directions are gathered
+// and only the cones rebuilt.
 __global__ void leaf_build_kernel(const float4* __restrict__ ro, const float4* __restrict__ rd,
                                   const int32_t* __restrict__ perm, float4* __restrict__ so,
                                   float4* __restrict__ sd, const uint32_t* __restrict__ skeys, int64_t n,
-                                  int64_t nleaf, RayNode* __restrict__ leaves) {
+                                  int64_t nleaf, RayNode* __restrict__ leaves, bool keep_o) {
     const int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (leaf >= nleaf) return;
@@ -76,11 +80,11 @@ __global__ void leaf_build_kernel(const float4* __restrict__ ro, const float4* _
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
     if (i < n) {
         const int32_t src = perm[i];
-        so[i] = ro[src];
         sd[i] = rd[src];
-        if (ok) {
-            o = ro[src];
-            d = rd[src];
+        if (ok) d = rd[src];
+        if (!keep_o) {
+            so[i] = ro[src];
+            if (ok) o = ro[src];
         }
     }
     const unsigned full = 0xffffffffu;
@@ -133,7 +137,7 @@ __global__ void leaf_build_kernel(const float4* __restrict__ ro, const float4* _
             float c = fmaxf(cosv - 0x1p-18f, -1.f);
             if (c > 1.f) c = 1.f;
             const float s = fminf(sqrtf(fmaxf(0.f, 1.f - c * c)) + 0x1p-18f, 1.f);
-            nd.a = make_float4(cx, cy, cz, ro_);
+            nd.a = keep_o ? leaves[leaf].a : make_float4(cx, cy, cz, ro_);
             nd.b = make_float4(ax, ay, az, c);
             nd.c = make_float4(s, reach, __int_as_float(count), 0.f);
         }
@@ -764,6 +768,9 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
                     cudaStream_t st) {
     Work& w = s->work;
     const uint32_t* skeys = nullptr;
+    const bool had_origins = s->sorted_origins_ok;
+    s->sorted_origins_ok = false;  // set again once this build has written them
+    const void* before[2] = {w.ray_o2.ptr, w.nodes.ptr};
     int rc = ray_sort(s, o, d, valid, n, perm, &skeys, st, order);
     if (rc) return rc;
     if ((rc = ensure(w.ray_o2, (size_t)n * sizeof(float4))) ||
@@ -785,9 +792,13 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     if ((rc = ensure(w.nodes, (size_t)total * sizeof(RayNode)))) return rc;
     RayNode* nodes = (RayNode*)w.nodes.ptr;
     const int64_t nleaf = lv->cnt[0];
+    // the previous batch's sorted origins and leaf spheres still apply when
+    // its order was reused and neither buffer moved
+    const bool keep_o = order == kOrderOrigin && s->origin_reused && had_origins &&
+                        before[0] == w.ray_o2.ptr && before[1] == w.nodes.ptr;
     prof_begin(s, st);
     leaf_build_kernel<<<(unsigned)((nleaf * 32 + 255) / 256), 256, 0, st>>>(o, d, *perm, *so, *sd, skeys,
-                                                                            n, nleaf, nodes);
+                                                                            n, nleaf, nodes, keep_o);
     prof_end(s, st, kStageBuild, 1);
     for (int l0 = 0; l0 < lv->nlev - 1; l0 += kLevelsPerLaunch) {
         const int l1 = std::min(l0 + kLevelsPerLaunch, lv->nlev - 1);
@@ -798,6 +809,7 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
         prof_end(s, st, kStageBuild, 1);
     }
     PBG_CUDA(cudaGetLastError());
+    s->sorted_origins_ok = order == kOrderOrigin;
     return PBG_OK;
 }
 

@@ -426,25 +426,27 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
 // Computes the Morton order of a batch.  *perm (device, n entries) lists ray
 // indices in sorted order; valid rays come first.
 // Shadow batches of one frame (one per light sample) leave from the same
-// points with the same validity, so their origin order repeats.
-// compare_origins_kernel clears *same at any ray whose validity, or whose
-// origin while valid, differs bit for bit from the cached batch, and stores
-// the new entry (x, y, z, valid) in the cache; store_sorted_kernel keeps a
-// fresh sort's order for the next batch.
+// points (the same origin and mint) with the same validity, so their origin
+// order repeats.  compare_origins_kernel clears *same at any ray whose
+// validity, or whose (origin, mint) while valid, differs bit for bit from
+// the cached batch, and stores the new entry in the cache;
+// store_sorted_kernel keeps a fresh sort's order for the next batch.
 __global__ void compare_origins_kernel(const float4* __restrict__ ro, const uint8_t* __restrict__ valid,
-                                       int64_t n, uint4* __restrict__ cache, int* __restrict__ same) {
+                                       int64_t n, uint4* __restrict__ cache, uint8_t* __restrict__ vcache,
+                                       int* __restrict__ same) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t v = valid ? (valid[i] != 0) : 1u;
+    const uint8_t v = valid ? (valid[i] != 0) : 1;
     uint4 e = make_uint4(0u, 0u, 0u, 0u);
     if (v) {
         const float4 o = ro[i];
-        e = make_uint4(__float_as_uint(o.x), __float_as_uint(o.y), __float_as_uint(o.z), 1u);
+        e = make_uint4(__float_as_uint(o.x), __float_as_uint(o.y), __float_as_uint(o.z), __float_as_uint(o.w));
     }
     const uint4 c = cache[i];
-    if (c.x != e.x || c.y != e.y || c.z != e.z || c.w != e.w) {
+    if (vcache[i] != v || c.x != e.x || c.y != e.y || c.z != e.z || c.w != e.w) {
         *same = 0;
         cache[i] = e;
+        vcache[i] = v;
     }
 }
 
@@ -474,21 +476,25 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     int64_t blocks = (n + 255) / 256;
     if (blocks > 4 * sms) blocks = 4 * sms;
+    s->origin_reused = false;
     if (order == kOrderOrigin) {
         // reuse the previous origin order when origins and validity repeat
-        const void* before[3] = {w.origin_cache.ptr, w.osort_keys.ptr, w.osort_perm.ptr};
+        const void* before[4] = {w.origin_cache.ptr, w.osort_keys.ptr, w.osort_perm.ptr,
+                                 w.origin_valid.ptr};
         const bool was_cached = s->origin_sort_n == n;
         s->origin_sort_n = -1;  // set again only once the cache is consistent
         if ((rc = ensure(w.origin_cache, (size_t)n * 16)) || (rc = ensure(w.osort_keys, (size_t)n * 4)) ||
-            (rc = ensure(w.osort_perm, (size_t)n * 4)) || (rc = ensure(w.osort_same, 16)))
+            (rc = ensure(w.osort_perm, (size_t)n * 4)) || (rc = ensure(w.osort_same, 16)) ||
+            (rc = ensure(w.origin_valid, (size_t)n)))
             return rc;
         const bool comparable = was_cached && before[0] == w.origin_cache.ptr &&
-                                before[1] == w.osort_keys.ptr && before[2] == w.osort_perm.ptr;
+                                before[1] == w.osort_keys.ptr && before[2] == w.osort_perm.ptr &&
+                                before[3] == w.origin_valid.ptr;
         int* same = (int*)w.osort_same.ptr;
         PBG_CUDA(cudaMemsetAsync(same, comparable ? 1 : 0, sizeof(int), st));
         prof_begin(s, st);
         compare_origins_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            o, valid, n, (uint4*)w.origin_cache.ptr, same);
+            o, valid, n, (uint4*)w.origin_cache.ptr, (uint8_t*)w.origin_valid.ptr, same);
         prof_end(s, st, kStageSort, 1);
         PBG_CUDA(cudaGetLastError());
         int hsame = 0;
@@ -497,6 +503,7 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
         }
         if (hsame) {
             s->origin_sort_n = n;
+            s->origin_reused = true;
             *perm = (const int32_t*)w.osort_perm.ptr;
             if (sorted_keys) *sorted_keys = (const uint32_t*)w.osort_keys.ptr;
             return PBG_OK;
