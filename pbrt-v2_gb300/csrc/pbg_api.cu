@@ -630,7 +630,7 @@ int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t 
     std::vector<int32_t> morder;
     const int32_t* order = nullptr;
     if (accel == PBG_ACCEL_RAYHIERARCHY) {
-        morton_triangle_order(tri9, ntri, &morder);
+        cluster_triangle_order(tri9, ntri, &morder);
         order = morder.empty() ? nullptr : morder.data();
     }
     if (accel == PBG_ACCEL_RAYBVH) {

@@ -142,7 +142,7 @@ int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order)
 // TriRec[i] from device vertices tri9_dev[order_dev[i]] (record index = local triangle index).
 int launch_build_tris(const float* tri9_dev, const int32_t* order_dev, int64_t ntri, TriRec* out,
                       cudaStream_t st);
-void morton_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order);
+void cluster_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order);
 int check_device_status(pbg_scene* s, cudaStream_t st);
 // Copies count (<= 16) device words to the host: a one-warp kernel stores
 // them into mapped pinned memory and the host waits for the stream.  No
