@@ -118,7 +118,9 @@ __global__ void morton_kernel(const float4* __restrict__ ro, const float4* __res
 }
 
 // Origin order: the 3-D Morton code of the origin, 8 bits per axis over
-// the batch's origin box.  For shadow batches, whose directions all point at
+// the batch's origin box in cubic cells (the box's largest extent on every
+// axis, so that a flat spread of origins is not cut finer across its thin
+// axis).  For shadow batches, whose directions all point at
 // a light, this keeps a leaf's 32 origins close in space (image tiles put
 // silhouette pixels' far-apart hit points together).
 __device__ __forceinline__ uint32_t spread10(uint32_t v) {
@@ -143,10 +145,13 @@ __global__ void origin_key_kernel(const float4* __restrict__ ro, const uint8_t* 
     const float4 o = ro[i];
     uint32_t q[3];
     const float ov[3] = {o.x, o.y, o.z};
+    float cube = 0.f;  // cubic cells: the largest extent on every axis
+#pragma unroll
+    for (int a = 0; a < 3; ++a) cube = fmaxf(cube, unord_f(bounds[3 + a]) - unord_f(bounds[a]));
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float lo = unord_f(bounds[a]);
-        const float ext = unord_f(bounds[3 + a]) - lo;
+        const float ext = cube;
         constexpr float kCells = (float)(1 << kOriginAxisBits);
         float v = ext > 0.f ? (ov[a] - lo) / ext * kCells : 0.f;
         v = fminf(fmaxf(v, 0.f), kCells - 1.f);  // NaN -> 0
