@@ -117,12 +117,14 @@ __global__ void morton_kernel(const float4* __restrict__ ro, const float4* __res
                                     (spread5(qo0) << 2) | (spread5(qo1) << 1) | spread5(qo2));
 }
 
-// Origin order: the 3-D Morton code of the origin, 8 bits per axis over
-// the batch's origin box in cubic cells (the box's largest extent on every
-// axis, so that a flat spread of origins is not cut finer across its thin
-// axis).  For shadow batches, whose directions all point at
+// Origin order: the origin's position along a 3-D Hilbert curve, 8 bits
+// per axis over the batch's origin box in cubic cells (the box's largest
+// extent on every axis, so that a flat spread of origins is not cut finer
+// across its thin axis).  For shadow batches, whose directions all point at
 // a light, this keeps a leaf's 32 origins close in space (image tiles put
-// silhouette pixels' far-apart hit points together).
+// silhouette pixels' far-apart hit points together); unlike a Morton code,
+// consecutive cells of the curve are always neighbours, so no leaf spans a
+// jump.
 __device__ __forceinline__ uint32_t spread10(uint32_t v) {
     v &= 0x3ffu;
     v = (v | (v << 16)) & 0x030000ffu;
@@ -130,6 +132,36 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
     v = (v | (v << 4)) & 0x030c30c3u;
     v = (v | (v << 2)) & 0x09249249u;
     return v;
+}
+
+// 3-D Hilbert index in transposed form (J. Skilling, "Programming the
+// Hilbert curve", AIP Conf. Proc. 707, 2004): the coordinates are rewritten
+// in place so that interleaving their bits, as for a Morton code, gives the
+// cell's position along the Hilbert curve, whose consecutive cells are
+// always face neighbours.
+__device__ __forceinline__ void hilbert3(uint32_t x[3], int bits) {
+    const uint32_t top = 1u << (bits - 1);
+    for (uint32_t q = top; q > 1; q >>= 1) {
+        const uint32_t p = q - 1;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (x[a] & q) {
+                x[0] ^= p;
+            } else {
+                const uint32_t t = (x[0] ^ x[a]) & p;
+                x[0] ^= t;
+                x[a] ^= t;
+            }
+        }
+    }
+    x[1] ^= x[0];
+    x[2] ^= x[1];
+    uint32_t t = 0;
+    for (uint32_t q = top; q > 1; q >>= 1)
+        if (x[2] & q) t ^= q - 1;
+    x[0] ^= t;
+    x[1] ^= t;
+    x[2] ^= t;
 }
 
 __global__ void origin_key_kernel(const float4* __restrict__ ro, const uint8_t* __restrict__ valid,
@@ -157,6 +189,7 @@ __global__ void origin_key_kernel(const float4* __restrict__ ro, const uint8_t* 
         v = fminf(fmaxf(v, 0.f), kCells - 1.f);  // NaN -> 0
         q[a] = (uint32_t)v;
     }
+    hilbert3(q, kOriginAxisBits);
     keys[i] = min(kMaxOriginKey, (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]));
 }
 
