@@ -50,11 +50,11 @@ BATCH_LAUNCH_DRAM_BYTES = 1_611_773_000
 # dram__bytes_read.sum + dram__bytes_write.sum of the traversal stage of one
 # batch call of the terrain frame (every traversal kernel of the warm-up
 # frame's nearest batch and four shadow batches, averaged over the five)
-FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 207_000_000, "ray-bvh": 116_000_000}
+FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 147_000_000, "ray-bvh": 116_000_000}
 # The traversal is bound by instruction issue, not by HBM: ncu's issue-active
 # fraction of the dominant kernel (smsp__issue_active, --set full capture of
 # the frame's camera and first shadow batch)
-FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, nearest)": 0.69,
+FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, nearest)": 0.72,
                                        "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.74}}
 L2_BYTES = 129 * 1024 * 1024
 CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)

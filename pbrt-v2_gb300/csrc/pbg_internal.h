@@ -66,7 +66,7 @@ bool triangle_degenerate(const float* v9);
 void build_bvh(const float* tri9, int64_t ntri, int max_leaf, HostBvh* out);
 
 // Ray orders of ray_sort(): the declared ray image if any, else 6-D Morton;
-// or the 3-D Morton code of the origins.
+// or the origins along a 3-D Hilbert curve.
 enum { kOrderDefault = 0, kOrderOrigin = 1 };
 
 // Records per rayhierarchy triangle cluster (one warp splits a cluster).

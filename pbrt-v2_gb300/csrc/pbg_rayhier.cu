@@ -10,17 +10,20 @@
 // extra passes (yetAnotherIntersection6DB.cl).
 //
 // Here:
-//   build     rays sorted by 6-D Morton code (pbg_rayorder.cu) and gathered;
-//             a leaf is 32 consecutive rays (one warp builds it with shuffle
+//   build     rays ordered (pbg_rayorder.cu: the declared ray image in 2-D
+//             Morton order, shadow batches along a 3-D Hilbert curve of their
+//             origins, otherwise a 6-D Morton code) and gathered; a leaf is
+//             32 consecutive rays (one warp builds it with shuffle
 //             reductions); parents merge 4 children.  A node is bounded by an
 //             origin sphere (centre, radius), a direction cone (unit axis,
 //             cos/sin of the half-angle) and the farthest reach of its rays
 //             (max maxt*|d|).
-//   traverse  one thread per triangle (triangles sorted by the Morton code of
-//             their centroids, so a warp's triangles are neighbours), private
-//             stack, node test = "can any ray of the node come within R of the
-//             triangle's bounding sphere", leaf test = the exact test per ray,
-//             32-triangle clusters walk the upper levels; at the leaves'
+//   traverse  triangle records in clusters of 32 (SAH-style splits on whole
+//             clusters, bvh_build.cpp), node test = "can any ray of the node
+//             come within R of the triangle's or cluster's bounding sphere",
+//             leaf test = the exact test per ray; the clusters walk the
+//             levels level by level, seeded at the first level of at most
+//             256 nodes; at the leaves'
 //             parents a warp splits its cluster and tests the reaching
 //             members against each leaf's rays directly; other split levels
 //             group the (triangle, leaf) pairs by leaf first so a warp

@@ -461,7 +461,7 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
     return PBG_OK;
 }
 
-// Computes the Morton order of a batch.  *perm (device, n entries) lists ray
+// Computes the order of a batch (image, Hilbert origin or 6-D Morton).  *perm (device, n entries) lists ray
 // indices in sorted order; valid rays come first.
 // Shadow batches of one frame (one per light sample) leave from the same
 // points (the same origin and mint) with the same validity, so their origin
