@@ -88,6 +88,8 @@ struct pbg_scene {
     pbg_params params{};
     int64_t ntri = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t io_stream = nullptr;          // host-link copies of two-half calls
+    cudaEvent_t io_events[4] = {nullptr, nullptr, nullptr, nullptr};
     pbg::DeviceBuffer tris;    // TriRec[ntri], in traversal order (c.w = original index)
     pbg::DeviceBuffer tri9;    // original vertices, float[9*ntri]
     pbg::DeviceBuffer uv6;     // optional per-triangle uvs, float[6*ntri]

@@ -170,3 +170,47 @@ def test_exact_ties_across_clusters(gpu_lib, oracle):
     for kind in ("rayhierarchy", "ray-bvh"):
         acc = A.MakeAccelerator(kind, tris)
         assert_same(acc.Intersect(rays.copy()), want, kind)
+
+
+@pytest.mark.parametrize("kind", ["rayhierarchy", "ray-bvh"])
+def test_host_call_in_two_halves(gpu_lib, kind):
+    """A nearest-hit call of 2^21 rays on pinned rows and pinned outputs runs
+    as two halves whose copies overlap the other half's traversal; with and
+    without a declared ray image and with a validity mask, it answers
+    exactly like the device-buffer call."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from pbrt_gb300 import _lib as L
+    sc = S.terrain_icospheres(seed=2, grid=96, n_spheres=12)
+    rays = S.pinhole_rays(1024, 1024, (0.0, 9.0, -14.0), (0.0, 0.0, 0.0), 50.0, spp=2, jitter_seed=9)
+    n = rays.shape[1]
+    assert n >= 1 << 21
+    hit = ((np.arange(n) % 9) != 4).astype(np.uint8)
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    hr = pinned((8, n), torch.float32)
+    hr[...] = rays
+    hv = pinned((n,), torch.uint8)
+    hv[...] = hit
+    outs = [pinned((n,), torch.int32)] + [pinned((n,), torch.float32) for _ in range(3)]
+    o4 = torch.from_numpy(np.ascontiguousarray(np.stack([rays[0], rays[1], rays[2], rays[6]], 1))).cuda()
+    d4 = torch.from_numpy(np.ascontiguousarray(np.stack([rays[3], rays[4], rays[5], rays[7]], 1))).cuda()
+    vd = torch.from_numpy(hit).cuda()
+    for image in (True, False):
+        acc = A.MakeAccelerator(kind, sc["tris"])
+        if image:
+            acc.Preprocess(None, 2, 1, 1, xres=1024, yres=1024)
+        for valid in (None, hv):
+            prim = torch.empty(n, dtype=torch.int32, device="cuda")
+            t, b1, b2 = (torch.empty(n, device="cuda") for _ in range(3))
+            acc.intersect_device(o4, d4, prim, t, b1, b2, valid=None if valid is None else vd)
+            torch.cuda.synchronize()
+            want = [x.cpu().numpy() for x in (prim, t, b1, b2)]
+            h = L.Hits(outs[0].ctypes.data_as(C.POINTER(C.c_int32)),
+                       *(o.ctypes.data_as(C.POINTER(C.c_float)) for o in outs[1:]))
+            rs = acc._rays_struct(hr, valid)
+            L.check(L.lib().pbg_intersect(acc.handle, C.byref(rs), n, C.byref(h)), "pbg_intersect")
+            for a, b in zip(outs, want):
+                np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
