@@ -214,3 +214,54 @@ def test_host_call_in_two_halves(gpu_lib, kind):
             L.check(L.lib().pbg_intersect(acc.handle, C.byref(rs), n, C.byref(h)), "pbg_intersect")
             for a, b in zip(outs, want):
                 np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_randomised_scenes_against_oracle(gpu_lib, oracle, seed):
+    """Randomised scenes (terrain with icospheres at random sizes, a grid of
+    shared-edge quads laid over it, a random soup) and ray sets (a declared
+    camera image with jitter, masked shadow batches from its hits reused
+    across light samples, incoherent segments): rayhierarchy and ray-bvh
+    against the oracle, bit for bit."""
+    rng = np.random.default_rng(100 + seed)
+    sc = S.terrain_icospheres(seed=seed, grid=int(rng.integers(32, 96)), n_spheres=int(rng.integers(2, 20)))
+    k = 24
+    xs = np.linspace(-4, 4, k + 1, dtype=np.float32)
+    quads = []
+    for i in range(k):
+        for j in range(k):
+            a = (xs[i], 1.5, xs[j]); b = (xs[i + 1], 1.5, xs[j]); c = (xs[i + 1], 1.5, xs[j + 1]); d = (xs[i], 1.5, xs[j + 1])
+            quads.append(a + b + c)
+            quads.append(a + c + d)
+    soup = rng.uniform(-6, 6, (500, 9)).astype(np.float32)
+    soup[:, 3:] = soup[:, :3].repeat(2, 0).reshape(-1, 6) + rng.normal(0, 0.3, (500, 6)).astype(np.float32)
+    tris = np.concatenate([sc["tris"], np.asarray(quads, np.float32), soup])
+    tris = tris[rng.permutation(len(tris))]
+    B = oracle.BVH(tris)
+    w, h = 128, 64
+    cam = S.pinhole_rays(w, h, tuple(rng.uniform([-3, 5, -12], [3, 10, -8])), (0.0, 0.0, 0.0),
+                         float(rng.uniform(30, 70)), spp=2, jitter_seed=seed)
+    inc = S.random_rays(8000, [-8, -1, -8], [8, 5, 8], seed=seed)
+    inc[7, ::2] = rng.uniform(0.05, 6.0, 4000).astype(np.float32)
+    for kind in ("rayhierarchy", "ray-bvh"):
+        acc = A.MakeAccelerator(kind, tris)
+        acc.Preprocess(None, 2, 1, 1, xres=w, yres=h)
+        want = B.nearest(cam)
+        assert_same(acc.Intersect(cam.copy()), want, f"{kind} camera {seed}")
+        hitm = want[0] >= 0
+        p = cam[0:3] + cam[3:6] * np.where(hitm, want[1], 0)[None]
+        for q in range(3):
+            lp = rng.uniform([-1, 8, -1], [1, 9, 1], (cam.shape[1], 3)).T
+            d = lp - p
+            dist = np.sqrt((d ** 2).sum(0))
+            dist = np.where(dist > 0, dist, 1.0)
+            r = np.empty((8, cam.shape[1]), np.float32)
+            r[0:3] = p
+            r[3:6] = d / dist[None]
+            r[6] = np.where(hitm, 1e-3 * want[1], 0.0)
+            r[7] = dist * (1 - 1e-3)
+            occ = acc.IntersectP(r, hit=hitm)
+            want_occ = B.anyhit(r, valid=hitm.astype(np.uint8)) == 1
+            np.testing.assert_array_equal((occ == ord("1"))[hitm], want_occ[hitm], err_msg=f"{kind} shadow {seed}/{q}")
+        assert_same(acc.Intersect(inc.copy()), B.nearest(inc), f"{kind} incoherent {seed}")
+        np.testing.assert_array_equal(acc.IntersectP(inc) == ord("1"), B.anyhit(inc) == 1)
