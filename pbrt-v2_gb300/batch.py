@@ -119,6 +119,57 @@ class SceneSet:
                  "threads": st.threads, "graph_replayed": bool(st.graph_replayed),
                  "walk": st.walk}, per)
 
+    def trace_host(self, host: dict, dev: dict, near_offsets, occ_offsets, stream, copy_stream,
+                   split: int | None = None):
+        """Pinned host rays in and results out, in two halves of the scenes:
+        the second half's rays are copied while the first half is traced, and
+        the first half's results while the second is.  `host` and `dev` map
+        o4n, d4n, o4s, d4s, prim, t, b1, b2, occ to pinned host tensors and
+        device tensors of the same shapes.  Each half is one trace call over
+        every scene, the other half's scenes given empty ranges, so the
+        results are those of one call (the graph cache keeps both halves'
+        segment tables).  `split` = the first scene of the second half
+        (default: where half of the rays are)."""
+        import torch
+        n = self.nscenes
+        no = _offsets(near_offsets, n)
+        so = _offsets(occ_offsets, n)
+        tot = no + so
+        k = split if split is not None else int(np.searchsorted(tot, tot[-1] / 2))
+        k = min(max(k, 1), n - 1) if n > 1 else n
+        parts = []
+        for lo_s, hi_s in ((0, k), (k, n)):
+            nb, ne = int(no[lo_s]), int(no[hi_s])
+            sb, se = int(so[lo_s]), int(so[hi_s])
+            # this part's scenes keep their ranges, relative to its first ray
+            pn = np.clip(no - nb, 0, ne - nb)
+            ps = np.clip(so - sb, 0, se - sb)
+            parts.append((nb, ne, sb, se, pn, ps))
+        ev_in = [torch.cuda.Event() for _ in parts]
+        ev_done = [torch.cuda.Event() for _ in parts]
+        with torch.cuda.stream(copy_stream):
+            for (nb, ne, sb, se, _, _), ev in zip(parts, ev_in):
+                for key in ("o4n", "d4n"):
+                    dev[key][nb:ne].copy_(host[key][nb:ne], non_blocking=True)
+                for key in ("o4s", "d4s"):
+                    dev[key][sb:se].copy_(host[key][sb:se], non_blocking=True)
+                ev.record(copy_stream)
+        for (nb, ne, sb, se, pn, ps), ei, ed in zip(parts, ev_in, ev_done):
+            stream.wait_event(ei)
+            with torch.cuda.stream(stream):
+                self.trace(o4n=dev["o4n"][nb:], d4n=dev["d4n"][nb:], near_offsets=pn,
+                           prim=dev["prim"][nb:], t=dev["t"][nb:], b1=dev["b1"][nb:], b2=dev["b2"][nb:],
+                           o4s=dev["o4s"][sb:], d4s=dev["d4s"][sb:], occ_offsets=ps, occ=dev["occ"][sb:],
+                           stream=stream)
+            ed.record(stream)
+            copy_stream.wait_event(ed)
+            with torch.cuda.stream(copy_stream):
+                for key in ("prim", "t", "b1", "b2"):
+                    host[key][nb:ne].copy_(dev[key][nb:ne], non_blocking=True)
+                host["occ"][sb:se].copy_(dev["occ"][sb:se], non_blocking=True)
+        copy_stream.synchronize()
+        stream.synchronize()
+
     def autotune(self, o4n=None, d4n=None, near_offsets=None, prim=None, t=None, b1=None, b2=None,
                  o4s=None, d4s=None, occ_offsets=None, occ=None, stream=None) -> dict:
         args = self._args(o4n, d4n, near_offsets, prim, t, b1, b2, o4s, d4s, occ_offsets, occ)

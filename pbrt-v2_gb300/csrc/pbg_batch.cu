@@ -295,14 +295,22 @@ struct pbg_sceneset {
     int32_t nscenes = 0;
     cudaStream_t capture_stream = nullptr;
     DeviceBuffer nodes, tris, descs, err;
-    DeviceBuffer item_off, head, remaining, done_ns, start_ns;  // item_off holds the whole segment table
+    DeviceBuffer head, remaining, done_ns, start_ns;
     std::vector<int64_t> ntri;
-    std::vector<int64_t> host_table;  // item_off ++ ray_off ++ ray_end last uploaded
+    // Segment tables (item_off ++ ray_off ++ ray_end ++ rseg_off) with the
+    // graph captured over each: two, so that a caller alternating between
+    // two sets of offsets (two halves of the scenes) replays both.
+    struct Slot {
+        std::vector<int64_t> host;
+        DeviceBuffer dev;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<uintptr_t> key;
+        uint64_t used = 0;
+    } slot[2];
+    int cur = 0;       // the slot of the call in progress
+    uint64_t tick = 0;
     pbg_batch_params tuned{};
     int sm_count = 0;
-    // cached graph
-    cudaGraphExec_t exec = nullptr;
-    std::vector<uintptr_t> graph_key;
 };
 
 namespace {
@@ -392,10 +400,11 @@ BatchArgs make_args(pbg_sceneset* set, const Call& c, int tile) {
     a.nscenes = set->nscenes;
     a.tile = tile;
     const int nseg = 2 * set->nscenes;
-    a.item_off = (const int64_t*)set->item_off.ptr;
-    a.ray_off = (const int64_t*)set->item_off.ptr + nseg + 1;
-    a.ray_end = (const int64_t*)set->item_off.ptr + nseg + 1 + nseg;
-    a.rseg_off = (const int64_t*)set->item_off.ptr + nseg + 1 + 2 * nseg;
+    const int64_t* table = (const int64_t*)set->slot[set->cur].dev.ptr;
+    a.item_off = table;
+    a.ray_off = table + nseg + 1;
+    a.ray_end = table + nseg + 1 + nseg;
+    a.rseg_off = table + nseg + 1 + 2 * nseg;
     a.o4n = (const float4*)c.o4n;
     a.d4n = (const float4*)c.d4n;
     a.prim = c.prim;
@@ -454,23 +463,35 @@ int prepare(pbg_sceneset* set, const Call& c, const Shape& s, cudaStream_t st, u
             set_last_error("pbg_sceneset_trace: too many work items in one scene");
             return PBG_ERR_INVALID_ARGUMENT;
         }
-    if (table != set->host_table) {
-        int rc = ensure(set->item_off, table.size() * sizeof(int64_t));
+    int hit = -1;
+    for (int k = 0; k < 2; ++k)
+        if (set->slot[k].host == table) hit = k;
+    if (hit < 0) {  // upload into the least recently used slot
+        hit = set->slot[0].used <= set->slot[1].used ? 0 : 1;
+        auto& sl = set->slot[hit];
+        if (sl.exec) cudaGraphExecDestroy(sl.exec);
+        sl.exec = nullptr;
+        sl.key.clear();
+        int rc = ensure(sl.dev, table.size() * sizeof(int64_t));
         if (rc) return rc;
-        PBG_CUDA(cudaMemcpyAsync(set->item_off.ptr, table.data(), table.size() * sizeof(int64_t),
+        PBG_CUDA(cudaMemcpyAsync(sl.dev.ptr, table.data(), table.size() * sizeof(int64_t),
                                  cudaMemcpyHostToDevice, st));
         // the host vector must outlive the (possibly asynchronous) copy
         PBG_CUDA(cudaStreamSynchronize(st));
-        set->host_table.swap(table);
+        sl.host.swap(table);
     }
+    set->cur = hit;
+    set->slot[hit].used = ++set->tick;
     *rays = (uint64_t)(nn + ns);
     return PBG_OK;
 }
 
 void destroy_graph(pbg_sceneset* set) {
-    if (set->exec) cudaGraphExecDestroy(set->exec);
-    set->exec = nullptr;
-    set->graph_key.clear();
+    for (auto& sl : set->slot) {
+        if (sl.exec) cudaGraphExecDestroy(sl.exec);
+        sl.exec = nullptr;
+        sl.key.clear();
+    }
 }
 
 int run(pbg_sceneset* set, const Call& c, const Shape& s, bool use_graph, cudaStream_t st,
@@ -481,14 +502,17 @@ int run(pbg_sceneset* set, const Call& c, const Shape& s, bool use_graph, cudaSt
     const uintptr_t key_vals[] = {(uintptr_t)c.o4n, (uintptr_t)c.d4n, (uintptr_t)c.prim,
                                   (uintptr_t)c.t,   (uintptr_t)c.b1,  (uintptr_t)c.b2,
                                   (uintptr_t)c.o4s, (uintptr_t)c.d4s, (uintptr_t)c.occ,
-                                  (uintptr_t)set->item_off.ptr, (uintptr_t)s.tile,
+                                  (uintptr_t)set->slot[set->cur].dev.ptr, (uintptr_t)s.tile,
                                   (uintptr_t)s.ctas_per_sm, (uintptr_t)s.threads,
                                   (uintptr_t)s.walk};
     std::vector<uintptr_t> key(std::begin(key_vals), std::end(key_vals));
-    if (set->exec && key == set->graph_key) {
+    auto& sl = set->slot[set->cur];
+    if (sl.exec && key == sl.key) {
         *replayed = true;
     } else {
-        destroy_graph(set);
+        if (sl.exec) cudaGraphExecDestroy(sl.exec);
+        sl.exec = nullptr;
+        sl.key.clear();
         cudaGraph_t g = nullptr;
         PBG_CUDA(cudaStreamBeginCapture(set->capture_stream, cudaStreamCaptureModeThreadLocal));
         int rc = launch_pair(set, a, s, set->capture_stream);
@@ -498,15 +522,15 @@ int run(pbg_sceneset* set, const Call& c, const Shape& s, bool use_graph, cudaSt
             return rc;
         }
         if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&set->exec, g, 0);
+        e = cudaGraphInstantiate(&sl.exec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) {
-            set->exec = nullptr;
+            sl.exec = nullptr;
             return cuda_status(e, "cudaGraphInstantiate");
         }
-        set->graph_key = key;
+        sl.key = key;
     }
-    PBG_CUDA(cudaGraphLaunch(set->exec, st));
+    PBG_CUDA(cudaGraphLaunch(sl.exec, st));
     return PBG_OK;
 }
 
@@ -640,8 +664,8 @@ void pbg_sceneset_destroy(pbg_sceneset* set) {
     cudaSetDevice(set->device);
     cudaDeviceSynchronize();
     destroy_graph(set);
-    DeviceBuffer* all[] = {&set->nodes, &set->tris,      &set->descs,   &set->err,      &set->item_off,
-                           &set->head,  &set->remaining, &set->done_ns, &set->start_ns};
+    DeviceBuffer* all[] = {&set->nodes, &set->tris,      &set->descs,   &set->err,      &set->slot[0].dev,
+                           &set->slot[1].dev, &set->head, &set->remaining, &set->done_ns, &set->start_ns};
     for (DeviceBuffer* b : all) release(*b);
     if (set->capture_stream) cudaStreamDestroy(set->capture_stream);
     delete set;
@@ -690,7 +714,8 @@ int pbg_sceneset_trace(pbg_sceneset* set, const float* o4n, const float* d4n,
         if (e != cudaSuccess) rc = cuda_status(e, "pbg_sceneset_trace readback");
         std::vector<double> busy;
         for (int32_t k = 0; k < n && rc == PBG_OK; ++k) {
-            const bool work = set->host_table[(size_t)(2 * k + 2)] > set->host_table[(size_t)(2 * k)];
+            const std::vector<int64_t>& ht = set->slot[set->cur].host;
+            const bool work = ht[(size_t)(2 * k + 2)] > ht[(size_t)(2 * k)];
             const double v = work && done[(size_t)k] >= t0 ? (double)(done[(size_t)k] - t0) * 1e-6 : 0.0;
             if (scene_ms) scene_ms[k] = v;
             if (work) busy.push_back(v);

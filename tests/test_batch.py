@@ -144,6 +144,36 @@ def test_matches_per_scene_kernels(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_trace_host_in_two_halves(gpu_lib):
+    """trace_host: pinned host rays in and results out, in two halves of the
+    scenes whose copies overlap the other half's trace; both halves' graphs
+    stay cached; bit for bit the answers of one device-buffer trace, for
+    several split points."""
+    from pbrt_gb300.batch import SceneSet
+    scs = small_set()
+    sset = SceneSet([s["tris"] for s in scs])
+    pk = Packed([s["near"] for s in scs], [s["shadow"] for s in scs])
+    sset.trace(**pk.args())
+    want = pk.results()
+    pin = lambda x: x.cpu().pin_memory()
+    host = dict(o4n=pin(pk.o4n), d4n=pin(pk.d4n), o4s=pin(pk.o4s), d4s=pin(pk.d4s),
+                prim=pin(pk.prim), t=pin(pk.t), b1=pin(pk.b1), b2=pin(pk.b2), occ=pin(pk.occ))
+    stream, copy_stream = torch.cuda.Stream(), torch.cuda.Stream(priority=-1)
+    for split in (None, 1, len(scs) - 1):
+        for key in ("prim", "t", "b1", "b2", "occ"):
+            host[key].fill_(0)
+        dev = dict(o4n=torch.zeros_like(pk.o4n), d4n=torch.zeros_like(pk.d4n), o4s=torch.zeros_like(pk.o4s),
+                   d4s=torch.zeros_like(pk.d4s), prim=torch.full_like(pk.prim, -7), t=torch.full_like(pk.t, -7.0),
+                   b1=torch.full_like(pk.b1, -7.0), b2=torch.full_like(pk.b2, -7.0), occ=torch.full_like(pk.occ, 7))
+        for _ in range(2):  # the second call replays both halves' graphs
+            sset.trace_host(host, dev, pk.near_off, pk.occ_off, stream, copy_stream, split=split)
+            got = tuple(host[k].numpy() for k in ("prim", "t", "b1", "b2", "occ"))
+            for a, b in zip(got, want):
+                np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8), err_msg=f"split {split}")
+    sset.close()
+
+
+@pytest.mark.gpu
 def test_empty_and_ragged(gpu_lib):
     """Scenes with no triangles, scenes with no rays of one kind, one-ray
     scenes, and a call with no any-hit rays at all."""
