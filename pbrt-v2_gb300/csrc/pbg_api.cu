@@ -14,6 +14,7 @@
 // core/error.cpp:130).
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -252,17 +253,42 @@ static void prof_collect(pbg_scene* s) {
     }
 }
 
-__global__ void publish_words_kernel(const int* __restrict__ src, int count, int* dst) {
-    if ((int)threadIdx.x < count) ((volatile int*)dst)[threadIdx.x] = src[threadIdx.x];
+// Stores the words, then (after a system-scope fence) the sequence number
+// in the last word: a host that sees the number sees the words.
+__global__ void publish_words_kernel(const int* __restrict__ src, int count, int* dst, int seq) {
+    if (threadIdx.x != 0) return;
+    volatile int* d = dst;
+    for (int k = 0; k < count; ++k) d[k] = src[k];
+    __threadfence_system();
+    d[kMailboxWords - 1] = seq;
 }
 
 int read_device_words(pbg_scene* s, const int* dev, int count, int* out, cudaStream_t st) {
-    if (count > 16 || !s->mbox_dev) return PBG_ERR_INVALID_ARGUMENT;
-    publish_words_kernel<<<1, 32, 0, st>>>(dev, count, s->mbox_dev);
+    if (count > kMailboxWords - 1 || !s->mbox_dev) return PBG_ERR_INVALID_ARGUMENT;
+    const int seq = (int)++s->mbox_seq;  // compared as bits; wraps harmlessly
+    publish_words_kernel<<<1, 32, 0, st>>>(dev, count, s->mbox_dev, seq);
     s->counters.kernel_launches++;
     PBG_CUDA(cudaGetLastError());
-    PBG_CUDA(cudaStreamSynchronize(st));
+    // The host polls the mapped word instead of sleeping in a stream
+    // synchronisation: it sees the kernel's store within microseconds, where
+    // a blocking wait adds tens of microseconds of wake-up latency to every
+    // call.  After 20 ms it waits on the stream instead (a long batch, or an
+    // earlier failure, which the synchronisation then reports).
     const volatile int* h = s->mbox_host;
+    const auto t0 = std::chrono::steady_clock::now();
+    unsigned spins = 0;
+    while (h[kMailboxWords - 1] != seq) {
+        if ((++spins & 1023u) == 0 &&
+            std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(20)) {
+            PBG_CUDA(cudaStreamSynchronize(st));
+            if (h[kMailboxWords - 1] != seq) {
+                set_last_error("read_device_words: the status kernel did not publish");
+                return PBG_ERR_INTERNAL;
+            }
+            break;
+        }
+    }
+    std::atomic_thread_fence(std::memory_order_acquire);
     for (int k = 0; k < count; ++k) out[k] = h[k];
     return PBG_OK;
 }
@@ -712,7 +738,8 @@ int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t 
     }
     if ((rc = ensure(s->err, 4 * sizeof(int)))) return fail(rc);
     {
-        cudaError_t e = cudaHostAlloc((void**)&s->mbox_host, 16 * sizeof(int), cudaHostAllocMapped);
+        cudaError_t e = cudaHostAlloc((void**)&s->mbox_host, kMailboxWords * sizeof(int), cudaHostAllocMapped);
+        if (e == cudaSuccess) memset(s->mbox_host, 0, kMailboxWords * sizeof(int));
         if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&s->mbox_dev, s->mbox_host, 0);
         if (e != cudaSuccess) return fail(cuda_status(e, "cudaHostAlloc(status words)"));
     }

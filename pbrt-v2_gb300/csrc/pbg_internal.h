@@ -114,6 +114,7 @@ struct pbg_scene {
     pbg::DeviceBuffer err;     // int[4] device status words
     int* mbox_host = nullptr;  // mapped pinned words the host reads status through
     int* mbox_dev = nullptr;   // the same words as the device addresses them
+    uint32_t mbox_seq = 0;     // sequence number of the last publication
     pbg::DeviceBuffer workc;   // uint64[8] traversal work counters (profiling level 2)
     pbg::Work work;
     pbg_counters counters{};
@@ -146,10 +147,11 @@ int launch_build_tris(const float* tri9_dev, const int32_t* order_dev, int64_t n
                       cudaStream_t st);
 void cluster_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order);
 int check_device_status(pbg_scene* s, cudaStream_t st);
-// Copies count (<= 16) device words to the host: a one-warp kernel stores
-// them into mapped pinned memory and the host waits for the stream.  No
-// copy-engine transfer is involved, so the read never queues behind large
-// transfers the caller has in flight.
+// Copies count (< kMailboxWords) device words to the host: a one-warp
+// kernel stores them into mapped pinned memory and the host polls for them.
+// No copy-engine transfer is involved, so the read never queues behind
+// large transfers the caller has in flight.
+constexpr int kMailboxWords = 16;
 int read_device_words(pbg_scene* s, const int* dev, int count, int* out, cudaStream_t st);
 
 // Stage timing around one launch (no-ops unless profiling is on); stages:
