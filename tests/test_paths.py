@@ -116,6 +116,9 @@ def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
         r[3:6] = rng.normal(size=(3, n)).astype(np.float32)
         r[7] = rng.uniform(0.5, 6.0, n).astype(np.float32)
         cases.append((r, all_valid))
+    other_mint = cases[-1][0].copy()  # the same origins with another mint: no reuse
+    other_mint[6] = rng.uniform(0.0, 0.05, n).astype(np.float32)
+    cases.append((other_mint, all_valid))
     near = cases[-1][0].copy()  # nearby directions
     near[3:6] += (0.02 * rng.normal(size=(3, n))).astype(np.float32)
     cases.append((near, all_valid))
