@@ -20,7 +20,7 @@
 namespace pbg {
 
 constexpr int kBvhThreads = 128;
-constexpr int kBvhMinBlocks = 8;  // CTAs per SM: measured best of 8, 12, 16
+constexpr int kBvhMinBlocks = 4;  // CTAs per SM: measured best of 4, 5, 6, 8, 12, 16
 
 template <bool ANY, bool STATS, bool ORDERED>
 __global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
 // together.  The stack keeps leaf children with their triangle counts.
 // Same culling, order-independent merge and results as bvh_kernel.
 constexpr int kPersistThreads = 128;
-constexpr int kPersistMinBlocks = 8;  // CTAs per SM: measured best of 8, 12, 16
+constexpr int kPersistMinBlocks = 10;  // CTAs per SM: measured best of 6, 8, 9, 10, 12, 16
 
 // ORDERED: the learned ordering's predicted cluster (pred, cref as in
 // bvh_kernel) is walked first, then the whole tree skipping it.
