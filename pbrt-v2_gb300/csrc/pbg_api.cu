@@ -581,6 +581,8 @@ static bool is_pinned(const void* p) {
 // from the traversal.  The host link moves about 210 GB/s each way, which
 // for a 4 M-ray camera batch is 0.64 ms in and 0.35 ms out against about
 // 0.9 ms of traversal.  *done = false: not applicable, nothing was started.
+constexpr int kHostParts = 2;  // measured: 4 parts cost the rayhierarchy frame 2.6 % of e2e
+
 static int intersect_two_halves(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_hits* out,
                                 bool* done) {
     *done = false;
@@ -592,10 +594,12 @@ static int intersect_two_halves(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_
     void* outs[4] = {out->prim, out->t, out->b1, out->b2};
     for (void* q : outs)
         if (!is_pinned(q)) return PBG_OK;
-    // halves on whole image rows when a ray image of this size is declared
+    // parts on whole image rows when a ray image of this size is declared
+    constexpr int P = kHostParts;
     const bool image = s->image_w > 0 && n == s->image_w * s->image_h;
-    if (image && (s->image_h % 2) != 0) return PBG_OK;
-    const int64_t half = image ? (s->image_h / 2) * s->image_w : n / 2;
+    if (image && (s->image_h % P) != 0) return PBG_OK;
+    int64_t lo_of[P + 1];
+    for (int c = 0; c <= P; ++c) lo_of[c] = image ? (s->image_h / P) * c * s->image_w : n * c / P;
     Work& w = s->work;
     int rc;
     if ((rc = ensure(w.stage, (size_t)n * 8 * sizeof(float))) ||
@@ -613,9 +617,8 @@ static int intersect_two_halves(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_
     }
     float* stage = (float*)w.stage.ptr;
     uint8_t* vdev = r->valid ? (uint8_t*)w.valid.ptr : nullptr;
-    const int64_t lo_of[2] = {0, half}, hi_of[2] = {half, n};
-    for (int c = 0; c < 2; ++c) {  // both halves' rays in, in order
-        const int64_t lo = lo_of[c], cnt = hi_of[c] - lo_of[c];
+    for (int c = 0; c < P; ++c) {  // every part's rays in, in order
+        const int64_t lo = lo_of[c], cnt = lo_of[c + 1] - lo_of[c];
         for (int k = 0; k < 8; ++k)
             PBG_CUDA(cudaMemcpyAsync(stage + (size_t)k * n + lo, rows[k] + lo, (size_t)cnt * 4,
                                      cudaMemcpyHostToDevice, s->io_stream));
@@ -625,13 +628,13 @@ static int intersect_two_halves(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_
         PBG_CUDA(cudaEventRecord(s->io_events[c], s->io_stream));
     }
     const int64_t image_h = s->image_h;
-    if (image) s->image_h = image_h / 2;  // each half is a ray image of half the rows
+    if (image) s->image_h = image_h / P;  // each part is a ray image of 1/P of the rows
     float4* o = (float4*)w.ray_o.ptr;
     float4* d = (float4*)w.ray_d.ptr;
     int32_t* prim = (int32_t*)w.prim.ptr;
     float *t = (float*)w.t.ptr, *b1 = (float*)w.b1.ptr, *b2 = (float*)w.b2.ptr;
-    for (int c = 0; c < 2 && rc == PBG_OK; ++c) {
-        const int64_t lo = lo_of[c], cnt = hi_of[c] - lo_of[c];
+    for (int c = 0; c < P && rc == PBG_OK; ++c) {
+        const int64_t lo = lo_of[c], cnt = lo_of[c + 1] - lo_of[c];
         cudaStreamWaitEvent(s->stream, s->io_events[c], 0);
         const float* sr[8];
         for (int k = 0; k < 8; ++k) sr[k] = stage + (size_t)k * n + lo;
@@ -647,8 +650,8 @@ static int intersect_two_halves(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_
         rc = run_nearest(s, o + lo, d + lo, vdev ? vdev + lo : nullptr, cnt, prim + lo, t + lo, b1 + lo,
                          b2 + lo, s->stream);
         if (rc) break;
-        cudaEventRecord(s->io_events[2 + c], s->stream);
-        cudaStreamWaitEvent(s->io_stream, s->io_events[2 + c], 0);
+        cudaEventRecord(s->io_events[P + c], s->stream);
+        cudaStreamWaitEvent(s->io_stream, s->io_events[P + c], 0);
         const void* src[4] = {prim + lo, t + lo, b1 + lo, b2 + lo};
         for (int k = 0; k < 4; ++k)
             if (cudaMemcpyAsync((char*)outs[k] + lo * 4, src[k], (size_t)cnt * 4, cudaMemcpyDeviceToHost,

@@ -89,7 +89,7 @@ struct pbg_scene {
     int64_t ntri = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t io_stream = nullptr;          // host-link copies of two-half calls
-    cudaEvent_t io_events[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t io_events[8] = {};
     pbg::DeviceBuffer tris;    // TriRec[ntri], in traversal order (c.w = original index)
     pbg::DeviceBuffer tri9;    // original vertices, float[9*ntri]
     pbg::DeviceBuffer uv6;     // optional per-triangle uvs, float[6*ntri]
