@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(256, ANY ? kSplitTestMinBlocks : kNearestMinBl
 }
 
 // Front-to-back order for the pairs of a nearest-hit batch: a counting sort
-// of the (cluster, leaves' parent) pairs on the distance from the root's
+// of the (cluster, leaves' parent) pairs on the distance from the parent's
 // origin ball to the cluster's sphere, so that the leaf tests, which take
 // the pairs in queue order over time, meet the near clusters first and
 // their hits lower the live reach bounds before the far clusters arrive.
@@ -545,39 +545,41 @@ __global__ void __launch_bounds__(256, ANY ? kSplitTestMinBlocks : kNearestMinBl
 // only changes how much is culled, never a result.
 constexpr int kOrderBuckets = 16384;
 
-__device__ __forceinline__ uint32_t pair_bucket(float4 c, float4 root) {
-    const float dx = c.x - root.x, dy = c.y - root.y, dz = c.z - root.z;
-    float dist = sqrtf(dx * dx + dy * dy + dz * dz) - c.w - root.w;
+__device__ __forceinline__ uint32_t pair_bucket(float4 c, float4 ball) {
+    const float dx = c.x - ball.x, dy = c.y - ball.y, dz = c.z - ball.z;
+    float dist = sqrtf(dx * dx + dy * dy + dz * dz) - c.w - ball.w;
     if (!(dist > 0.f)) dist = 0.f;  // overlapping, or NaN
     return min(__float_as_uint(dist) >> 17, (uint32_t)kOrderBuckets - 1u);
 }
 
 __global__ void __launch_bounds__(256)
-    rh_order_count_kernel(const float4* __restrict__ csph, const RayNode* __restrict__ root,
+    rh_order_count_kernel(const float4* __restrict__ csph, const RayNode* __restrict__ level1,
                           const Pair* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t cap,
                           uint32_t* __restrict__ hist, const int* __restrict__ status) {
     if (status[kStatusOverflow] != 0) return;  // this attempt is rerun
     const uint32_t nin = min(*in_count, cap);
-    const float4 r = root->a;
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nin; base += stride) {
         const int64_t i = base + threadIdx.x;
         const bool ok = i < nin;
-        const uint32_t key = ok ? pair_bucket(csph[in[i].tri], r) : (uint32_t)kOrderBuckets;
+        uint32_t key = (uint32_t)kOrderBuckets;
+        if (ok) {
+            const Pair pr = in[i];
+            key = pair_bucket(csph[pr.tri], level1[pr.node].a);
+        }
         const uint32_t peers = __match_any_sync(0xffffffffu, key);
         if (ok && lane == __ffs(peers) - 1) atomicAdd(&hist[key], (uint32_t)__popc(peers));
     }
 }
 
 __global__ void __launch_bounds__(256)
-    rh_order_scatter_kernel(const float4* __restrict__ csph, const RayNode* __restrict__ root,
+    rh_order_scatter_kernel(const float4* __restrict__ csph, const RayNode* __restrict__ level1,
                             const Pair* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t cap,
                             uint32_t* __restrict__ cursor, Pair* __restrict__ out,
                             const int* __restrict__ status) {
     if (status[kStatusOverflow] != 0) return;
     const uint32_t nin = min(*in_count, cap);
-    const float4 r = root->a;
     const int lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -588,7 +590,7 @@ __global__ void __launch_bounds__(256)
         uint32_t key = (uint32_t)kOrderBuckets;
         if (ok) {
             pr = in[i];
-            key = pair_bucket(csph[pr.tri], r);
+            key = pair_bucket(csph[pr.tri], level1[pr.node].a);
         }
         const uint32_t peers = __match_any_sync(0xffffffffu, key);
         const int leader = __ffs(peers) - 1;
@@ -766,6 +768,28 @@ __global__ void rh_finalize_occluded(const int32_t* __restrict__ perm,
 
 // ------------------------------------------------------------------ host
 
+// The levels the traversal reads: clusters split into triangles at level
+// `split`, and the descent is seeded at `seed`, the lowest level of at most
+// kSeedNodes nodes not below max(split, 1).  No level above the seed is
+// read, so the build stops there.
+struct Descent {
+    int split, seed;
+};
+static Descent descent_levels(const pbg_scene* s, const Levels& lv) {
+    const int top = lv.nlev - 1;
+    // levels walked by 32-triangle clusters before they split into triangles
+    // (default: down to the leaves' parents, the fastest split on the
+    // terrain direct-lighting frame)
+    int kcl = s->params.rh_cluster_levels;
+    if (kcl == 0) kcl = std::max(1, top - 1);
+    if (kcl < 0 || s->clusters.ptr == nullptr) kcl = 0;
+    Descent d;
+    d.split = std::max(0, top - kcl);
+    d.seed = top;
+    while (d.seed > std::max(d.split, 1) && lv.cnt[d.seed - 1] <= kSeedNodes) --d.seed;
+    return d;
+}
+
 static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                     const int32_t** perm, float4** so, float4** sd, Levels* lv, int order,
                     cudaStream_t st) {
@@ -803,8 +827,9 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     leaf_build_kernel<<<(unsigned)((nleaf * 32 + 255) / 256), 256, 0, st>>>(o, d, *perm, *so, *sd, skeys,
                                                                             n, nleaf, nodes, keep_o);
     prof_end(s, st, kStageBuild, 1);
-    for (int l0 = 0; l0 < lv->nlev - 1; l0 += kLevelsPerLaunch) {
-        const int l1 = std::min(l0 + kLevelsPerLaunch, lv->nlev - 1);
+    const int built = descent_levels(s, *lv).seed;  // the levels above are never read
+    for (int l0 = 0; l0 < built; l0 += kLevelsPerLaunch) {
+        const int l1 = std::min(l0 + kLevelsPerLaunch, built);
         const int64_t group = 1ll << (2 * (l1 - l0));
         prof_begin(s, st);
         level_build_multi_kernel<<<(unsigned)((lv->cnt[l0] + group - 1) / group), 256, 0, st>>>(nodes, *lv,
@@ -843,13 +868,9 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
     static_assert(2 * kMaxLevels <= 64, "pair counters");
     int groups = s->rh_groups > 0 ? s->rh_groups : 1;
     const int top = lv.nlev - 1;
-    // levels walked by 32-triangle clusters before they split into triangles
-    // (default: down to the leaves' parents, the fastest split on the
-    // terrain direct-lighting frame)
-    int kcl = s->params.rh_cluster_levels;
-    if (kcl == 0) kcl = std::max(1, top - 1);
-    if (kcl < 0 || s->clusters.ptr == nullptr) kcl = 0;
-    const int split = std::max(0, top - kcl);
+    const Descent dsc = descent_levels(s, lv);
+    const int split = dsc.split;
+    const int kcl = top - split;  // levels walked by clusters (0: none)
     const float4* tsph = (const float4*)s->spheres.ptr;
     const float4* csph = (const float4*)s->clusters.ptr;
     uint32_t *leaf_reach = nullptr, *parent_reach = nullptr, *order_hist = nullptr;
@@ -883,8 +904,7 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             for (int l = 0; l < kMaxLevels; ++l) cnt_of[l] = &counts[(cl && l >= split) ? kMaxLevels + l : l];
             // seed level: the lowest with at most kSeedNodes nodes, not below
             // the level where clusters split
-            int ls = top;
-            while (ls > std::max(split, 1) && lv.cnt[ls - 1] <= kSeedNodes) --ls;
+            const int ls = dsc.seed;
             const int64_t seed_grid = std::min<int64_t>(
                 grid, ((int64_t)(s1 - s0) * lv.cnt[ls] + 255) / 256);
             if (stats)
@@ -904,10 +924,10 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                     unsigned tgrid = grid * 2;
                     if (order_hist) {  // nearest: front-to-back pairs, taken in order
                         PBG_CUDA(cudaMemsetAsync(order_hist, 0, kOrderBuckets * sizeof(uint32_t), st));
-                        rh_order_count_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[top], qa, cnt_of[1],
+                        rh_order_count_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[1], qa, cnt_of[1],
                                                                     kQueueCap, order_hist, status);
                         if ((rc = scan_counts(s, order_hist, kOrderBuckets, st))) return rc;
-                        rh_order_scatter_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[top], qa,
+                        rh_order_scatter_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[1], qa,
                                                                       cnt_of[1], kQueueCap, order_hist, qb,
                                                                       status);
                         Pair* tq = qa;
