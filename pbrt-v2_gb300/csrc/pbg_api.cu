@@ -475,19 +475,63 @@ __global__ void pack_rows_kernel(const float* __restrict__ ox, const float* __re
                                  const float* __restrict__ mint, const float* __restrict__ maxt,
                                  const uint8_t* __restrict__ valid_in, int64_t n, float4* __restrict__ o,
                                  float4* __restrict__ d, uint8_t* __restrict__ valid_out) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (valid_in) {  // an invalid ray's row entries are never read: skip them on the link
-        const uint8_t v = valid_in[i];
-        valid_out[i] = v;
-        if (v == 0) {
-            o[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            d[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            return;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (valid_in) {  // an invalid ray's row entries are never read: skip them on the link
+            const uint8_t v = valid_in[i];
+            valid_out[i] = v;
+            if (v == 0) {
+                o[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                d[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                continue;
+            }
+        }
+        o[i] = make_float4(ox[i], oy[i], oz[i], mint[i]);
+        d[i] = make_float4(dx[i], dy[i], dz[i], maxt[i]);
+    }
+}
+
+// The same gather in CTAs of 64 threads, four rays in flight per thread:
+// small enough to sit beside a traversal kernel's resident CTAs (a 256-thread
+// CTA does not fit beside five 256-thread CTAs of 48 registers), with enough
+// loads in flight to keep the host link busy from one CTA per SM.
+constexpr int kNarrowThreads = 64, kNarrowRays = 4;
+
+__global__ void __launch_bounds__(kNarrowThreads)
+    pack_rows_narrow_kernel(const float* __restrict__ ox, const float* __restrict__ oy,
+                            const float* __restrict__ oz, const float* __restrict__ dx,
+                            const float* __restrict__ dy, const float* __restrict__ dz,
+                            const float* __restrict__ mint, const float* __restrict__ maxt,
+                            const uint8_t* __restrict__ valid_in, int64_t n, float4* __restrict__ o,
+                            float4* __restrict__ d, uint8_t* __restrict__ valid_out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kNarrowRays * stride) {
+        uint8_t v[kNarrowRays];
+#pragma unroll
+        for (int k = 0; k < kNarrowRays; ++k) {
+            const int64_t i = base + k * stride;
+            v[k] = i < n ? (valid_in ? valid_in[i] : (uint8_t)1) : (uint8_t)0;
+        }
+        float4 a[kNarrowRays], b[kNarrowRays];
+#pragma unroll
+        for (int k = 0; k < kNarrowRays; ++k) {
+            const int64_t i = base + k * stride;
+            a[k] = b[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (v[k]) {  // an invalid ray's row entries are never read
+                a[k] = make_float4(ox[i], oy[i], oz[i], mint[i]);
+                b[k] = make_float4(dx[i], dy[i], dz[i], maxt[i]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kNarrowRays; ++k) {
+            const int64_t i = base + k * stride;
+            if (i < n) {
+                o[i] = a[k];
+                d[i] = b[k];
+                if (valid_in) valid_out[i] = v[k];
+            }
         }
     }
-    o[i] = make_float4(ox[i], oy[i], oz[i], mint[i]);
-    d[i] = make_float4(dx[i], dy[i], dz[i], maxt[i]);
 }
 
 // Results written in place to device-usable caller addresses.
@@ -573,6 +617,16 @@ static bool is_pinned(const void* p) {
     return a.type == cudaMemoryTypeHost;
 }
 
+// The high-priority stream (and its events) of the host-link copies.
+static int ensure_io_stream(pbg_scene* s) {
+    if (s->io_stream) return PBG_OK;
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    PBG_CUDA(cudaStreamCreateWithPriority(&s->io_stream, cudaStreamNonBlocking, hi));
+    for (cudaEvent_t& e : s->io_events) PBG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return PBG_OK;
+}
+
 // Host-buffer nearest-hit calls of at least 2^21 rays on pinned memory run
 // as two halves (of the declared ray image's rows, when there is one): the
 // second half's rays cross the host link while the first half is traced,
@@ -609,12 +663,7 @@ static int intersect_two_halves(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_
         (rc = ensure(w.t, (size_t)n * 4)) || (rc = ensure(w.b1, (size_t)n * 4)) ||
         (rc = ensure(w.b2, (size_t)n * 4)))
         return rc;
-    if (!s->io_stream) {
-        int lo = 0, hi = 0;
-        cudaDeviceGetStreamPriorityRange(&lo, &hi);
-        PBG_CUDA(cudaStreamCreateWithPriority(&s->io_stream, cudaStreamNonBlocking, hi));
-        for (cudaEvent_t& e : s->io_events) PBG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    }
+    if ((rc = ensure_io_stream(s))) return rc;
     float* stage = (float*)w.stage.ptr;
     uint8_t* vdev = r->valid ? (uint8_t*)w.valid.ptr : nullptr;
     for (int c = 0; c < P; ++c) {  // every part's rays in, in order
@@ -662,6 +711,96 @@ static int intersect_two_halves(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_
     const cudaError_t e = cudaStreamSynchronize(s->io_stream);
     if (rc) return rc;
     if (e != cudaSuccess) return cuda_status(e, "intersect_two_halves");
+    *done = true;
+    return check_device_status(s, s->stream);
+}
+
+void release_work(Work& w) {
+    DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.ray_o2, &w.ray_d2, &w.valid, &w.prim,
+                           &w.t, &w.b1, &w.b2, &w.occ, &w.keys, &w.stage, &w.perm,
+                           &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
+                           &w.leafmask, &w.counters, &w.geo, &w.queue_a, &w.queue_b,
+                           &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt, &w.origin_cache,
+                           &w.osort_keys, &w.osort_perm, &w.osort_same, &w.reach,
+                           &w.origin_valid};
+    for (DeviceBuffer* b : all) release(*b);
+    w.origin_sort_n = -1;
+    w.origin_reused = false;
+    w.sorted_origins_ok = false;
+}
+
+// Host-buffer shadow calls of at least 2^21 rays whose rows and result the
+// GPU addresses in place (pinned, or host page tables) run as two parts,
+// each with its own work buffers and so its own kept origin order: the
+// second part's rows cross the host link, read by a narrow gather kernel of
+// one 64-thread CTA per SM on the high-priority stream, while the first part
+// is traced.  Only
+// valid rays' rows are read.  *done = false: not applicable, nothing was
+// started.
+constexpr int kShadowParts = 2;
+
+static int occluded_in_parts(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t* occ, bool* done) {
+    *done = false;
+    if (n < (int64_t(1) << 21)) return PBG_OK;
+    const float* rows[8] = {r->ox, r->oy, r->oz, r->dx, r->dy, r->dz, r->mint, r->maxt};
+    const float* dv[8];
+    for (int k = 0; k < 8; ++k)
+        if (!(dv[k] = (const float*)device_view(s->device, rows[k]))) return PBG_OK;
+    const uint8_t* vin = nullptr;
+    if (r->valid && !(vin = (const uint8_t*)device_view(s->device, r->valid))) return PBG_OK;
+    uint8_t* po = (uint8_t*)device_view(s->device, occ);
+    if (!po) return PBG_OK;
+    constexpr int P = kShadowParts;
+    int64_t lo_of[P + 1];
+    for (int c = 0; c <= P; ++c) lo_of[c] = n * c / P;
+    Work* wp[P] = {&s->work, &s->alt};
+    int rc;
+    for (int c = 0; c < P; ++c) {
+        const size_t cnt = (size_t)(lo_of[c + 1] - lo_of[c]);
+        if ((rc = ensure(wp[c]->ray_o, cnt * sizeof(float4))) ||
+            (rc = ensure(wp[c]->ray_d, cnt * sizeof(float4))) || (rc = ensure(wp[c]->occ, cnt)) ||
+            (vin && (rc = ensure(wp[c]->valid, cnt))))
+            return rc;
+    }
+    if ((rc = ensure_io_stream(s))) return rc;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    for (int c = 0; c < P; ++c) {  // every part's rows in, in order
+        const int64_t lo = lo_of[c], cnt = lo_of[c + 1] - lo_of[c];
+        Work& w = *wp[c];
+        if (c == 0) {
+            pack_rows_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s->io_stream>>>(
+                dv[0] + lo, dv[1] + lo, dv[2] + lo, dv[3] + lo, dv[4] + lo, dv[5] + lo, dv[6] + lo,
+                dv[7] + lo, vin ? vin + lo : nullptr, cnt, (float4*)w.ray_o.ptr, (float4*)w.ray_d.ptr,
+                vin ? (uint8_t*)w.valid.ptr : nullptr);
+        } else {  // beside the first part's traversal: one narrow CTA per SM
+            pack_rows_narrow_kernel<<<(unsigned)sms, kNarrowThreads, 0, s->io_stream>>>(
+                dv[0] + lo, dv[1] + lo, dv[2] + lo, dv[3] + lo, dv[4] + lo, dv[5] + lo, dv[6] + lo,
+                dv[7] + lo, vin ? vin + lo : nullptr, cnt, (float4*)w.ray_o.ptr, (float4*)w.ray_d.ptr,
+                vin ? (uint8_t*)w.valid.ptr : nullptr);
+        }
+        PBG_CUDA(cudaGetLastError());
+        PBG_CUDA(cudaEventRecord(s->io_events[c], s->io_stream));
+    }
+    rc = PBG_OK;
+    for (int c = 0; c < P && rc == PBG_OK; ++c) {
+        const int64_t lo = lo_of[c], cnt = lo_of[c + 1] - lo_of[c];
+        cudaStreamWaitEvent(s->stream, s->io_events[c], 0);
+        Work& w = *wp[c];
+        const float4* o = (const float4*)w.ray_o.ptr;
+        const float4* d = (const float4*)w.ray_d.ptr;
+        const uint8_t* v = vin ? (const uint8_t*)w.valid.ptr : nullptr;
+        uint8_t* oc = (uint8_t*)w.occ.ptr;
+        if (c > 0) std::swap(s->work, s->alt);  // the part's own buffers and kept order
+        rc = run_occluded(s, o, d, v, cnt, oc, s->stream);
+        if (c > 0) std::swap(s->work, s->alt);
+        if (rc) break;
+        store_bytes_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s->stream>>>(oc, cnt, po + lo);
+        if (cudaGetLastError() != cudaSuccess) rc = PBG_ERR_INTERNAL;
+    }
+    const cudaError_t e = cudaStreamSynchronize(s->io_stream);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_status(e, "occluded_in_parts");
     *done = true;
     return check_device_status(s, s->stream);
 }
@@ -808,15 +947,8 @@ void pbg_scene_destroy(pbg_scene* s) {
         learn_free(s->learn);
         s->learn = nullptr;
     }
-    Work& w = s->work;
-    DeviceBuffer* all[] = {&w.ray_o, &w.ray_d, &w.ray_o2, &w.ray_d2, &w.valid, &w.prim,
-                           &w.t, &w.b1, &w.b2, &w.occ, &w.keys, &w.stage, &w.perm,
-                           &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
-                           &w.leafmask, &w.counters, &w.geo, &w.queue_a, &w.queue_b,
-                           &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt, &w.origin_cache,
-                           &w.osort_keys, &w.osort_perm, &w.osort_same, &w.reach,
-                           &w.origin_valid};
-    for (DeviceBuffer* b : all) release(*b);
+    release_work(s->work);
+    release_work(s->alt);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->io_stream) {
         cudaStreamDestroy(s->io_stream);
@@ -925,9 +1057,17 @@ int pbg_occluded(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t* occ) {
     }
     if (n == 0) return PBG_OK;
     cudaSetDevice(s->device);
+    bool done = false;
+    int rc = occluded_in_parts(s, r, n, occ, &done);
+    if (rc) return rc;
+    if (done) {
+        s->counters.rays_occluded += (uint64_t)n;
+        s->counters.calls++;
+        return PBG_OK;
+    }
     float4 *o, *d;
     uint8_t* valid;
-    int rc = stage_rays(s, r, n, &o, &d, &valid);
+    rc = stage_rays(s, r, n, &o, &d, &valid);
     if (rc) return rc;
     Work& w = s->work;
     if ((rc = ensure(w.occ, (size_t)n))) return rc;

@@ -78,7 +78,12 @@ struct Work {
         perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo, queue_a, queue_b,
         qcount, scan_sums, pair_rank, leafcnt, origin_cache, osort_keys, osort_perm, osort_same, reach, origin_valid;
     int64_t cap = 0;
+    int64_t origin_sort_n = -1;      // rays of the cached origin sort (-1 = none)
+    bool origin_reused = false;      // the last origin-ordered sort reused the kept order
+    bool sorted_origins_ok = false;  // ray_o2 and the leaves hold the last origin-ordered
+                                     // build's sorted origins and leaf spheres
 };
+void release_work(Work& w);
 
 }  // namespace pbg
 
@@ -102,10 +107,6 @@ struct pbg_scene {
     int32_t unculled = 0;      // records [0, unculled) are tested by every ray
     int rh_groups = 1;         // triangle groups per rayhierarchy traversal (grows on overflow)
     int walk_hint = -1;        // ray-bvh: 1 = incoherent batch, 0 = coherent, -1 = infer
-    int64_t origin_sort_n = -1;  // rays of the cached origin sort (-1 = none)
-    bool origin_reused = false;      // the last origin-ordered sort reused the kept order
-    bool sorted_origins_ok = false;  // the work buffers hold the last origin-ordered build's
-                                     // sorted origins and leaf spheres
     std::vector<pbg::BvhNode> host_nodes;  // ray-bvh tree, kept for the learned clusters
     std::vector<int32_t> host_order;
     struct pbg::Learner* learn = nullptr;
@@ -117,6 +118,7 @@ struct pbg_scene {
     uint32_t mbox_seq = 0;     // sequence number of the last publication
     pbg::DeviceBuffer workc;   // uint64[8] traversal work counters (profiling level 2)
     pbg::Work work;
+    pbg::Work alt;             // the second part's buffers in two-part host shadow calls
     pbg_counters counters{};
     pbg::Profiler prof;
 };

@@ -795,8 +795,8 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
                     cudaStream_t st) {
     Work& w = s->work;
     const uint32_t* skeys = nullptr;
-    const bool had_origins = s->sorted_origins_ok;
-    s->sorted_origins_ok = false;  // set again once this build has written them
+    const bool had_origins = w.sorted_origins_ok;
+    w.sorted_origins_ok = false;  // set again once this build has written them
     const void* before[2] = {w.ray_o2.ptr, w.nodes.ptr};
     int rc = ray_sort(s, o, d, valid, n, perm, &skeys, st, order);
     if (rc) return rc;
@@ -821,7 +821,7 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     const int64_t nleaf = lv->cnt[0];
     // the previous batch's sorted origins and leaf spheres still apply when
     // its order was reused and neither buffer moved
-    const bool keep_o = order == kOrderOrigin && s->origin_reused && had_origins &&
+    const bool keep_o = order == kOrderOrigin && w.origin_reused && had_origins &&
                         before[0] == w.ray_o2.ptr && before[1] == w.nodes.ptr;
     prof_begin(s, st);
     leaf_build_kernel<<<(unsigned)((nleaf * 32 + 255) / 256), 256, 0, st>>>(o, d, *perm, *so, *sd, skeys,
@@ -837,7 +837,7 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
         prof_end(s, st, kStageBuild, 1);
     }
     PBG_CUDA(cudaGetLastError());
-    s->sorted_origins_ok = order == kOrderOrigin;
+    w.sorted_origins_ok = order == kOrderOrigin;
     return PBG_OK;
 }
 
@@ -1016,7 +1016,8 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
     // A nearest-hit batch yields new hit points: the origin order kept for
     // the shadow batches that leave from the previous ones is dropped, so
     // only shadow batches between two nearest-hit batches share a sort.
-    s->origin_sort_n = -1;
+    s->work.origin_sort_n = -1;
+    s->alt.origin_sort_n = -1;
     const int32_t* perm;
     float4 *so, *sd;
     Levels lv;

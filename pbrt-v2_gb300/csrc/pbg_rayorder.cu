@@ -514,13 +514,13 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     int64_t blocks = (n + 255) / 256;
     if (blocks > 4 * sms) blocks = 4 * sms;
-    s->origin_reused = false;
+    w.origin_reused = false;
     if (order == kOrderOrigin) {
         // reuse the previous origin order when origins and validity repeat
         const void* before[4] = {w.origin_cache.ptr, w.osort_keys.ptr, w.osort_perm.ptr,
                                  w.origin_valid.ptr};
-        const bool was_cached = s->origin_sort_n == n;
-        s->origin_sort_n = -1;  // set again only once the cache is consistent
+        const bool was_cached = w.origin_sort_n == n;
+        w.origin_sort_n = -1;  // set again only once the cache is consistent
         if ((rc = ensure(w.origin_cache, (size_t)n * 16)) || (rc = ensure(w.osort_keys, (size_t)n * 4)) ||
             (rc = ensure(w.osort_perm, (size_t)n * 4)) || (rc = ensure(w.osort_same, 16)) ||
             (rc = ensure(w.origin_valid, (size_t)n)))
@@ -540,8 +540,8 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
             if ((rc = read_device_words(s, same, 1, &hsame, st))) return rc;
         }
         if (hsame) {
-            s->origin_sort_n = n;
-            s->origin_reused = true;
+            w.origin_sort_n = n;
+            w.origin_reused = true;
             *perm = (const int32_t*)w.osort_perm.ptr;
             if (sorted_keys) *sorted_keys = (const uint32_t*)w.osort_keys.ptr;
             return PBG_OK;
@@ -599,7 +599,7 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
         PBG_CUDA(cudaGetLastError());
         ko = (uint32_t*)w.osort_keys.ptr;
         vo = (int32_t*)w.osort_perm.ptr;
-        s->origin_sort_n = n;
+        w.origin_sort_n = n;
     }
     *perm = vo;
     if (sorted_keys) *sorted_keys = ko;

@@ -219,6 +219,67 @@ def test_host_call_in_two_halves(gpu_lib, kind):
                 np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
+@pytest.mark.parametrize("kind", ["rayhierarchy", "ray-bvh"])
+def test_host_shadow_call_in_two_parts(gpu_lib, kind):
+    """A shadow call of 2^21 rays on pinned rows and a pinned result runs as
+    two parts with their own work buffers and kept origin orders; through
+    repeated light samples (both parts reuse their order), a validity change
+    in the second part only, a nearest-hit call in between and a call
+    without a mask, it answers exactly like the device-buffer call of a
+    separate accelerator."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from pbrt_gb300 import _lib as L
+    sc = S.terrain_icospheres(seed=3, grid=96, n_spheres=12)
+    cam = S.pinhole_rays(1024, 1024, (0.0, 9.0, -14.0), (0.0, 0.0, 0.0), 50.0, spp=2, jitter_seed=4)
+    n = cam.shape[1]
+    assert n >= 1 << 21
+    acc = A.MakeAccelerator(kind, sc["tris"])
+    ref = A.MakeAccelerator(kind, sc["tris"])
+    prim, t, _, _ = acc.Intersect(cam.copy())
+    hitm = prim >= 0
+    p = cam[0:3] + cam[3:6] * np.where(hitm, t, 0)[None]
+    rng = np.random.default_rng(5)
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    def shadow(q):
+        lp = np.array([[0.6 * q - 1.0], [8.5], [0.3 * q]], np.float32) + rng.uniform(-0.2, 0.2, (3, n)).astype(np.float32)
+        d = lp - p
+        out = np.empty((8, n), np.float32)
+        out[0:3] = p
+        out[3:6] = d
+        out[6] = 1e-3
+        out[7] = 0.999
+        return out
+
+    hr = pinned((8, n), torch.float32)
+    hv = pinned((n,), torch.uint8)
+    ho = pinned((n,), torch.uint8)
+    mask = hitm.astype(np.uint8)
+    moved = mask.copy()
+    moved[n - 1000:n - 990] ^= 1  # second part only
+    steps = [(0, mask), (1, mask), (2, mask), (2, moved), ("cam", None), (3, mask), (3, None)]
+    for q, m in steps:
+        if q == "cam":
+            acc.Intersect(cam.copy())
+            continue
+        hr[...] = shadow(q)
+        if m is not None:
+            hv[...] = m
+        rs = acc._rays_struct(hr, None if m is None else hv)
+        L.check(L.lib().pbg_occluded(acc.handle, C.byref(rs), n, ho.ctypes.data), "pbg_occluded")
+        o4 = torch.from_numpy(np.ascontiguousarray(np.stack([hr[0], hr[1], hr[2], hr[6]], 1))).cuda()
+        d4 = torch.from_numpy(np.ascontiguousarray(np.stack([hr[3], hr[4], hr[5], hr[7]], 1))).cuda()
+        occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+        ref.occluded_device(o4, d4, occ, valid=None if m is None else torch.from_numpy(m).cuda())
+        torch.cuda.synchronize()
+        want = occ.cpu().numpy()
+        np.testing.assert_array_equal(ho != 0, want != 0, err_msg=f"{kind} step {q}")
+        assert 0 < int(np.count_nonzero(want)) < n
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_randomised_scenes_against_oracle(gpu_lib, oracle, seed):
     """Randomised scenes (terrain with icospheres at random sizes, a grid of
