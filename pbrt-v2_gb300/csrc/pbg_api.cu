@@ -721,11 +721,12 @@ void release_work(Work& w) {
                            &w.perm_tmp, &w.mkeys, &w.mkeys_tmp, &w.hist, &w.nodes,
                            &w.leafmask, &w.counters, &w.geo, &w.queue_a, &w.queue_b,
                            &w.qcount, &w.scan_sums, &w.pair_rank, &w.leafcnt, &w.origin_cache,
-                           &w.osort_keys, &w.osort_perm, &w.osort_same, &w.reach,
+                           &w.osort_keys, &w.osort_perm, &w.reach,
                            &w.origin_valid};
     for (DeviceBuffer* b : all) release(*b);
     w.origin_sort_n = -1;
     w.origin_reused = false;
+    w.origin_speculative = false;
     w.sorted_origins_ok = false;
 }
 

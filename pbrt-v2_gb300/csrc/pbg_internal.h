@@ -76,10 +76,11 @@ constexpr int kClusterTris = 32;
 struct Work {
     DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
         perm_tmp, mkeys, mkeys_tmp, hist, nodes, leafmask, counters, geo, queue_a, queue_b,
-        qcount, scan_sums, pair_rank, leafcnt, origin_cache, osort_keys, osort_perm, osort_same, reach, origin_valid;
+        qcount, scan_sums, pair_rank, leafcnt, origin_cache, osort_keys, osort_perm, reach, origin_valid;
     int64_t cap = 0;
     int64_t origin_sort_n = -1;      // rays of the cached origin sort (-1 = none)
     bool origin_reused = false;      // the last origin-ordered sort reused the kept order
+    bool origin_speculative = false; // ... before the comparison's answer was read
     bool sorted_origins_ok = false;  // ray_o2 and the leaves hold the last origin-ordered
                                      // build's sorted origins and leaf spheres
 };

@@ -847,7 +847,7 @@ constexpr uint32_t kQueueCap = 1u << 25;
 
 template <bool ANY>
 static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const float4* sd,
-                       unsigned long long* keys, uint32_t* mask, cudaStream_t st) {
+                       unsigned long long* keys, uint32_t* mask, cudaStream_t st, int* moved) {
     Work& w = s->work;
     int rc;
     const int64_t nleaf = lv.cnt[0];
@@ -999,10 +999,16 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             prof_end(s, st, kStageTraverse, nl);
             PBG_CUDA(cudaGetLastError());
         }
-        // One status read per call: a dropped pair would lose hits.
-        int ovf = 0;
-        if ((rc = read_device_words(s, status + kStatusOverflow, 1, &ovf, st))) return rc;
-        if (ovf == 0) return PBG_OK;
+        // One status read per call: a dropped pair would lose hits.  With
+        // *moved, the word after it too: the batch's origins differ from
+        // the kept order it was traced in, and the caller traces it again.
+        int h[2] = {0, 0};
+        if ((rc = read_device_words(s, status + kStatusOverflow, moved ? 2 : 1, h, st))) return rc;
+        if (moved && h[1] != 0) {
+            *moved = 1;
+            return PBG_OK;
+        }
+        if (h[0] == 0) return PBG_OK;
         groups *= 4;  // rerun: atomicMax / atomicOr merges make a rerun idempotent
         s->rh_groups = groups;
     }
@@ -1027,7 +1033,7 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
     if ((rc = ensure(w.keys, (size_t)n * 8))) return rc;
     unsigned long long* keys = (unsigned long long*)w.keys.ptr;
     PBG_CUDA(cudaMemsetAsync(keys, 0, (size_t)n * 8, st));
-    if (s->ntri > 0 && (rc = rh_traverse<false>(s, lv, so, sd, keys, nullptr, st))) return rc;
+    if (s->ntri > 0 && (rc = rh_traverse<false>(s, lv, so, sd, keys, nullptr, st, nullptr))) return rc;
     prof_begin(s, st);
     rh_finalize_nearest<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
         (const TriRec*)s->tris.ptr, (const int32_t*)s->tri_pos.ptr, so, sd, perm, keys, n, prim, t, b1, b2);
@@ -1039,22 +1045,42 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
 int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                 uint8_t* occ, cudaStream_t st) {
     if (n <= 0) return PBG_OK;
-    const int32_t* perm;
-    float4 *so, *sd;
-    Levels lv;
-    int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, kOrderOrigin, st);
-    if (rc) return rc;
-    Work& w = s->work;
-    const int64_t nleaf = lv.cnt[0];
-    if ((rc = ensure(w.leafmask, (size_t)nleaf * 4))) return rc;
-    uint32_t* mask = (uint32_t*)w.leafmask.ptr;
-    PBG_CUDA(cudaMemsetAsync(mask, 0, (size_t)nleaf * 4, st));
-    if (s->ntri > 0 && (rc = rh_traverse<true>(s, lv, so, sd, nullptr, mask, st))) return rc;
-    prof_begin(s, st);
-    rh_finalize_occluded<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(perm, mask, n, occ);
-    prof_end(s, st, kStageOther, 1);
-    PBG_CUDA(cudaGetLastError());
-    return PBG_OK;
+    // Two attempts at most: one in the kept origin order, taken before the
+    // comparison's answer, and, when the origins moved, one in a fresh order
+    // (the kept order is dropped, so that attempt cannot speculate).
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const int32_t* perm;
+        float4 *so, *sd;
+        Levels lv;
+        int rc = rh_build(s, o, d, valid, n, &perm, &so, &sd, &lv, kOrderOrigin, st);
+        if (rc) return rc;
+        Work& w = s->work;
+        const bool speculative = w.origin_speculative;
+        const int64_t nleaf = lv.cnt[0];
+        if ((rc = ensure(w.leafmask, (size_t)nleaf * 4))) return rc;
+        uint32_t* mask = (uint32_t*)w.leafmask.ptr;
+        PBG_CUDA(cudaMemsetAsync(mask, 0, (size_t)nleaf * 4, st));
+        int moved = 0;
+        if (s->ntri > 0) {
+            rc = rh_traverse<true>(s, lv, so, sd, nullptr, mask, st, speculative ? &moved : nullptr);
+            if (rc) return rc;
+        } else if (speculative) {
+            rc = read_device_words(s, (const int*)s->err.ptr + kStatusOriginMoved, 1, &moved, st);
+            if (rc) return rc;
+        }
+        if (moved) {
+            w.origin_sort_n = -1;
+            w.origin_reused = w.origin_speculative = false;
+            continue;
+        }
+        prof_begin(s, st);
+        rh_finalize_occluded<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(perm, mask, n, occ);
+        prof_end(s, st, kStageOther, 1);
+        PBG_CUDA(cudaGetLastError());
+        return PBG_OK;
+    }
+    set_last_error("rayhierarchy: the origin order changed under a fresh sort");
+    return PBG_ERR_INTERNAL;
 }
 
 }  // namespace pbg

@@ -16,6 +16,7 @@
 // which each warp ranks its 32 keys per digit with __match_any_sync and the
 // tile's warps are combined through shared-memory prefix sums.
 #include "pbg_internal.h"
+#include "pbg_tma.cuh"
 
 namespace pbg {
 
@@ -465,13 +466,13 @@ int radix_sort_pairs(pbg_scene* s, uint32_t* keys, int32_t* vals, uint32_t* keys
 // indices in sorted order; valid rays come first.
 // Shadow batches of one frame (one per light sample) leave from the same
 // points (the same origin and mint) with the same validity, so their origin
-// order repeats.  compare_origins_kernel clears *same at any ray whose
+// order repeats.  compare_origins_kernel sets *moved at any ray whose
 // validity, or whose (origin, mint) while valid, differs bit for bit from
 // the cached batch, and stores the new entry in the cache;
 // store_sorted_kernel keeps a fresh sort's order for the next batch.
 __global__ void compare_origins_kernel(const float4* __restrict__ ro, const uint8_t* __restrict__ valid,
                                        int64_t n, uint4* __restrict__ cache, uint8_t* __restrict__ vcache,
-                                       int* __restrict__ same) {
+                                       int* __restrict__ moved) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint8_t v = valid ? (valid[i] != 0) : 1;
@@ -482,7 +483,7 @@ __global__ void compare_origins_kernel(const float4* __restrict__ ro, const uint
     }
     const uint4 c = cache[i];
     if (vcache[i] != v || c.x != e.x || c.y != e.y || c.z != e.z || c.w != e.w) {
-        *same = 0;
+        *moved = 1;
         cache[i] = e;
         vcache[i] = v;
     }
@@ -515,6 +516,7 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     int64_t blocks = (n + 255) / 256;
     if (blocks > 4 * sms) blocks = 4 * sms;
     w.origin_reused = false;
+    w.origin_speculative = false;
     if (order == kOrderOrigin) {
         // reuse the previous origin order when origins and validity repeat
         const void* before[4] = {w.origin_cache.ptr, w.osort_keys.ptr, w.osort_perm.ptr,
@@ -522,26 +524,25 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
         const bool was_cached = w.origin_sort_n == n;
         w.origin_sort_n = -1;  // set again only once the cache is consistent
         if ((rc = ensure(w.origin_cache, (size_t)n * 16)) || (rc = ensure(w.osort_keys, (size_t)n * 4)) ||
-            (rc = ensure(w.osort_perm, (size_t)n * 4)) || (rc = ensure(w.osort_same, 16)) ||
-            (rc = ensure(w.origin_valid, (size_t)n)))
+            (rc = ensure(w.osort_perm, (size_t)n * 4)) || (rc = ensure(w.origin_valid, (size_t)n)))
             return rc;
         const bool comparable = was_cached && before[0] == w.origin_cache.ptr &&
                                 before[1] == w.osort_keys.ptr && before[2] == w.osort_perm.ptr &&
                                 before[3] == w.origin_valid.ptr;
-        int* same = (int*)w.osort_same.ptr;
-        PBG_CUDA(cudaMemsetAsync(same, comparable ? 1 : 0, sizeof(int), st));
+        int* moved = (int*)s->err.ptr + kStatusOriginMoved;
+        PBG_CUDA(cudaMemsetAsync(moved, 0, sizeof(int), st));
         prof_begin(s, st);
         compare_origins_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            o, valid, n, (uint4*)w.origin_cache.ptr, (uint8_t*)w.origin_valid.ptr, same);
+            o, valid, n, (uint4*)w.origin_cache.ptr, (uint8_t*)w.origin_valid.ptr, moved);
         prof_end(s, st, kStageSort, 1);
         PBG_CUDA(cudaGetLastError());
-        int hsame = 0;
-        if (comparable) {  // one flag read; the sort below is 15 launches
-            if ((rc = read_device_words(s, same, 1, &hsame, st))) return rc;
-        }
-        if (hsame) {
+        if (comparable) {
+            // The kept order is taken without waiting for the comparison:
+            // the batch's closing status read carries *moved, and a batch
+            // whose origins moved is traced again with a fresh sort.
             w.origin_sort_n = n;
             w.origin_reused = true;
+            w.origin_speculative = true;
             *perm = (const int32_t*)w.osort_perm.ptr;
             if (sorted_keys) *sorted_keys = (const uint32_t*)w.osort_keys.ptr;
             return PBG_OK;

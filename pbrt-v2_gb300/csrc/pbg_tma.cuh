@@ -13,8 +13,9 @@ namespace pbg {
 
 constexpr uint32_t kSpinLimit = 1u << 24;
 
-// Device status words (global int[4]); [0] = timeout count.
-enum : int { kStatusTimeout = 0, kStatusOverflow = 1 };
+// Device status words (global int[4]); [0] = timeout count, [1] = queue or
+// stack overflows, [2] = a shadow batch's origins differ from the kept order's.
+enum : int { kStatusTimeout = 0, kStatusOverflow = 1, kStatusOriginMoved = 2 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
