@@ -104,7 +104,12 @@ typedef struct pbg_counters {
      * (or box) tests, [1] leaves visited, [2] ray/triangle filter tests,
      * [3] exact tests, [4] exact tests that hit.  Zero otherwise. */
     uint64_t work[5];
-    uint64_t reserved[2];
+    /* rayhierarchy shadow batches traced in the kept origin order of the
+     * previous batch, and batches traced again because their origins or
+     * validity differed from it (the kept order is taken before the
+     * comparison's answer is read). */
+    uint64_t origin_reuses;
+    uint64_t origin_reruns;
     /* Device time per stage in ms while profiling is on (CUDA events around
      * each launch on its stream): [0] ray sort, [1] hierarchy build,
      * [2] traversal (the intersection kernels), [3] finalize / other. */

@@ -155,6 +155,7 @@ class Aggregate:
                 "timed_launches": dict(zip(L.STAGES, list(c.timed_launches))),
                 "work": dict(zip(("node_tests", "leaves", "filter_tests", "exact_tests",
                                   "exact_hits"), list(c.work))),
+                "origin_reuses": c.origin_reuses, "origin_reruns": c.origin_reruns,
                 "stage_ms": dict(zip(L.STAGES, list(c.stage_ms)))}
 
     # -- learned traversal ordering (ray-bvh) ------------------------------

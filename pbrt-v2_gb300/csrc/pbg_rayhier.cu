@@ -1071,8 +1071,10 @@ int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
         if (moved) {
             w.origin_sort_n = -1;
             w.origin_reused = w.origin_speculative = false;
+            s->counters.origin_reruns++;
             continue;
         }
+        if (speculative) s->counters.origin_reuses++;
         prof_begin(s, st);
         rh_finalize_occluded<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(perm, mask, n, occ);
         prof_end(s, st, kStageOther, 1);

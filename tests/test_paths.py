@@ -130,12 +130,19 @@ def test_repeated_shadow_origins_reuse_sort(gpu_lib, terrain):
     cases.append((moved, some))
     cases.append((moved, some))
     cases.append((moved[:, : n - 64].copy(), some[: n - 64].copy()))
+    # per batch: traced in the kept order (reuse), or taken in it and traced
+    # again because origins, mint or validity moved (rerun), or sorted afresh
+    expect = ["sort", "reuse", "sort", "rerun", "reuse", "reuse", "rerun", "rerun", "reuse", "sort"]
     for i, (r, v) in enumerate(cases):
         if i == 2:  # a nearest-hit batch in between drops the kept order
             assert_same(acc.Intersect(terrain["inc"].copy()), terrain["want_inc"], "nearest")
+        before = acc.stats()
         got = acc.IntersectP(r, hit=v) if not v.all() else acc.IntersectP(r)
+        after = acc.stats()
         want = B.anyhit(r) == 1
         np.testing.assert_array_equal((got == ord("1"))[v], want[v], err_msg=f"batch {i}")
+        seen = (after["origin_reuses"] - before["origin_reuses"], after["origin_reruns"] - before["origin_reruns"])
+        assert seen == {"sort": (0, 0), "reuse": (1, 0), "rerun": (0, 1)}[expect[i]], (i, seen)
 
 
 def test_exact_ties_across_clusters(gpu_lib, oracle):
@@ -261,6 +268,7 @@ def test_host_shadow_call_in_two_parts(gpu_lib, kind):
     moved = mask.copy()
     moved[n - 1000:n - 990] ^= 1  # second part only
     steps = [(0, mask), (1, mask), (2, mask), (2, moved), ("cam", None), (3, mask), (3, None)]
+    reuses = acc.stats()["origin_reuses"]
     for q, m in steps:
         if q == "cam":
             acc.Intersect(cam.copy())
@@ -278,6 +286,8 @@ def test_host_shadow_call_in_two_parts(gpu_lib, kind):
         want = occ.cpu().numpy()
         np.testing.assert_array_equal(ho != 0, want != 0, err_msg=f"{kind} step {q}")
         assert 0 < int(np.count_nonzero(want)) < n
+    if kind == "rayhierarchy":  # light samples 1 and 2 in both parts, 2 with the moved mask in part one
+        assert acc.stats()["origin_reuses"] - reuses == 5
 
 
 @pytest.mark.parametrize("seed", range(6))
