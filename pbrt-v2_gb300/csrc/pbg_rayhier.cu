@@ -14,10 +14,15 @@
 //             Morton order, shadow batches along a 3-D Hilbert curve of their
 //             origins, otherwise a 6-D Morton code) and gathered; a leaf is
 //             32 consecutive rays (one warp builds it with shuffle
-//             reductions); parents merge 4 children.  A node is bounded by an
-//             origin sphere (centre, radius), a direction cone (unit axis,
-//             cos/sin of the half-angle) and the farthest reach of its rays
-//             (max maxt*|d|).
+//             reductions); parents merge 4 children, up to the level the
+//             descent is seeded at (no level above it is built).  A node is
+//             bounded by an origin sphere (centre, radius), a direction cone
+//             (unit axis, cos/sin of the half-angle) and the farthest reach
+//             of its rays (max maxt*|d|).  A shadow batch whose origins and
+//             validity repeat the previous batch's takes the kept order and
+//             sorted origins at once; the comparison's answer is read with
+//             the batch's closing status word and a batch whose origins moved
+//             is traced again in a fresh order.
 //   traverse  triangle records in clusters of 32 (SAH-style splits on whole
 //             clusters, bvh_build.cpp), node test = "can any ray of the node
 //             come within R of the triangle's or cluster's bounding sphere",
@@ -31,6 +36,9 @@
 //             Nearest hits merge through a 64-bit atomicMax on (t, index)
 //             keys -- race-free by construction, no repair pass; a thread
 //             reads a ray's current key first and filters with that t.
+//             Nearest-hit batches take the final (cluster, leaves' parent)
+//             pairs front to back (by distance from the parent's origin
+//             ball) and cull with live reach bounds per leaf and parent.
 //             Any-hit keeps one occlusion bit per ray (a 32-bit mask per
 //             leaf) and skips leaves whose rays are all occluded.
 #include <algorithm>
@@ -796,7 +804,7 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     Work& w = s->work;
     const uint32_t* skeys = nullptr;
     const bool had_origins = w.sorted_origins_ok;
-    w.sorted_origins_ok = false;  // set again once this build has written them
+    w.sorted_origins_ok = false;  // set again once this hierarchy build has written them
     const void* before[2] = {w.ray_o2.ptr, w.nodes.ptr};
     int rc = ray_sort(s, o, d, valid, n, perm, &skeys, st, order);
     if (rc) return rc;
