@@ -587,19 +587,25 @@ int ray_sort(pbg_scene* s, const float4* o, const float4* d, const uint8_t* vali
     uint32_t* ko;
     int32_t* vo;
     // The bounds words sit after the histogram; 8-bit passes over the low
-    // 24 (origin) or 30 key bits, invalid rays last (kMaxValidKey).
-    rc = radix_sort_pairs(s, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr, (uint32_t*)w.mkeys_tmp.ptr,
-                          (int32_t*)w.perm_tmp.ptr, (uint32_t*)w.hist.ptr, n,
-                          order == kOrderOrigin ? kOriginKeyBits : kKeyBits, &ko, &vo, st);
+    // 24 (origin) or 30 key bits, invalid rays last (kMaxValidKey).  An
+    // origin order alternates with the kept-order buffers, so that its odd
+    // number of passes ends in them.
+    const bool origin = order == kOrderOrigin;
+    rc = radix_sort_pairs(s, (uint32_t*)w.mkeys.ptr, (int32_t*)w.perm.ptr,
+                          (uint32_t*)(origin ? w.osort_keys.ptr : w.mkeys_tmp.ptr),
+                          (int32_t*)(origin ? w.osort_perm.ptr : w.perm_tmp.ptr), (uint32_t*)w.hist.ptr, n,
+                          origin ? kOriginKeyBits : kKeyBits, &ko, &vo, st);
     if (rc) return rc;
-    if (order == kOrderOrigin) {
-        prof_begin(s, st);
-        store_sorted_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            ko, vo, n, (uint32_t*)w.osort_keys.ptr, (int32_t*)w.osort_perm.ptr);
-        prof_end(s, st, kStageSort, 1);
-        PBG_CUDA(cudaGetLastError());
-        ko = (uint32_t*)w.osort_keys.ptr;
-        vo = (int32_t*)w.osort_perm.ptr;
+    if (origin) {
+        if (ko != (uint32_t*)w.osort_keys.ptr) {  // an even number of passes
+            prof_begin(s, st);
+            store_sorted_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                ko, vo, n, (uint32_t*)w.osort_keys.ptr, (int32_t*)w.osort_perm.ptr);
+            prof_end(s, st, kStageSort, 1);
+            PBG_CUDA(cudaGetLastError());
+            ko = (uint32_t*)w.osort_keys.ptr;
+            vo = (int32_t*)w.osort_perm.ptr;
+        }
         w.origin_sort_n = n;
     }
     *perm = vo;
