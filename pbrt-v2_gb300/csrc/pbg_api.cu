@@ -777,6 +777,7 @@ static int occluded_in_parts(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t
     for (int c = 0; c < P; ++c) {  // every part's rows in, in order
         const int64_t lo = lo_of[c], cnt = lo_of[c + 1] - lo_of[c];
         Work& w = *wp[c];
+        prof_begin(s, s->io_stream);
         if (c == 0) {
             pack_rows_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s->io_stream>>>(
                 dv[0] + lo, dv[1] + lo, dv[2] + lo, dv[3] + lo, dv[4] + lo, dv[5] + lo, dv[6] + lo,
@@ -788,6 +789,7 @@ static int occluded_in_parts(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t
                 dv[7] + lo, vin ? vin + lo : nullptr, cnt, (float4*)w.ray_o.ptr, (float4*)w.ray_d.ptr,
                 vin ? (uint8_t*)w.valid.ptr : nullptr);
         }
+        prof_end(s, s->io_stream, kStageOther, 1);
         PBG_CUDA(cudaGetLastError());
         PBG_CUDA(cudaEventRecord(s->io_events[c], s->io_stream));
     }

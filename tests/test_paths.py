@@ -288,6 +288,25 @@ def test_host_shadow_call_in_two_parts(gpu_lib, kind):
         assert 0 < int(np.count_nonzero(want)) < n
     if kind == "rayhierarchy":  # light samples 1 and 2 in both parts, 2 with the moved mask in part one
         assert acc.stats()["origin_reuses"] - reuses == 5
+    # a size that is no multiple of 4,096: the part boundary is rounded down
+    # to one, and the second part ends on a ragged tail
+    extra = 3001
+    rows = np.concatenate([shadow(4), shadow(5)[:, :extra]], 1)
+    m2 = np.concatenate([mask, mask[:extra]])
+    n2 = rows.shape[1]
+    hr2 = pinned((8, n2), torch.float32)
+    hr2[...] = rows
+    hv2 = pinned((n2,), torch.uint8)
+    hv2[...] = m2
+    ho2 = pinned((n2,), torch.uint8)
+    rs = acc._rays_struct(hr2, hv2)
+    L.check(L.lib().pbg_occluded(acc.handle, C.byref(rs), n2, ho2.ctypes.data), "pbg_occluded")
+    o4 = torch.from_numpy(np.ascontiguousarray(np.stack([rows[0], rows[1], rows[2], rows[6]], 1))).cuda()
+    d4 = torch.from_numpy(np.ascontiguousarray(np.stack([rows[3], rows[4], rows[5], rows[7]], 1))).cuda()
+    occ = torch.empty(n2, dtype=torch.uint8, device="cuda")
+    ref.occluded_device(o4, d4, occ, valid=torch.from_numpy(m2).cuda())
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(ho2 != 0, occ.cpu().numpy() != 0, err_msg=f"{kind} ragged size")
 
 
 @pytest.mark.parametrize("seed", range(6))
