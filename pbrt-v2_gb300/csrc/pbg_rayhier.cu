@@ -89,13 +89,13 @@ __global__ void leaf_build_kernel(const float4* __restrict__ ro, const float4* _
     const int64_t i = leaf * kLeafRays + lane;
     const bool ok = i < n && skeys[i] != 0xffffffffu;
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
-    if (i < n) {
+    if (ok) {  // invalid rays sort last and are never read back: not gathered
         const int32_t src = perm[i];
-        sd[i] = rd[src];
-        if (ok) d = rd[src];
+        d = rd[src];
+        sd[i] = d;
         if (!keep_o) {
-            so[i] = ro[src];
-            if (ok) o = ro[src];
+            o = ro[src];
+            so[i] = o;
         }
     }
     const unsigned full = 0xffffffffu;
