@@ -263,12 +263,24 @@ __global__ void publish_words_kernel(const int* __restrict__ src, int count, int
     d[kMailboxWords - 1] = seq;
 }
 
-int read_device_words(pbg_scene* s, const int* dev, int count, int* out, cudaStream_t st) {
+int publish_device_words(pbg_scene* s, const int* dev, int count, int* seq_out, cudaStream_t st) {
     if (count > kMailboxWords - 1 || !s->mbox_dev) return PBG_ERR_INVALID_ARGUMENT;
     const int seq = (int)++s->mbox_seq;  // compared as bits; wraps harmlessly
     publish_words_kernel<<<1, 32, 0, st>>>(dev, count, s->mbox_dev, seq);
     s->counters.kernel_launches++;
     PBG_CUDA(cudaGetLastError());
+    *seq_out = seq;
+    return PBG_OK;
+}
+
+int read_device_words(pbg_scene* s, const int* dev, int count, int* out, cudaStream_t st) {
+    int seq = 0;
+    const int rc = publish_device_words(s, dev, count, &seq, st);
+    if (rc) return rc;
+    return wait_device_words(s, seq, count, out, st);
+}
+
+int wait_device_words(pbg_scene* s, int seq, int count, int* out, cudaStream_t st) {
     // The host polls the mapped word instead of sleeping in a stream
     // synchronisation: it sees the kernel's store within microseconds, where
     // a blocking wait adds tens of microseconds of wake-up latency to every

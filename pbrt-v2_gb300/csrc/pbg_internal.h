@@ -156,6 +156,10 @@ int check_device_status(pbg_scene* s, cudaStream_t st);
 // large transfers the caller has in flight.
 constexpr int kMailboxWords = 16;
 int read_device_words(pbg_scene* s, const int* dev, int count, int* out, cudaStream_t st);
+// The two halves of read_device_words: work enqueued between them runs while
+// the host waits for the words.
+int publish_device_words(pbg_scene* s, const int* dev, int count, int* seq, cudaStream_t st);
+int wait_device_words(pbg_scene* s, int seq, int count, int* out, cudaStream_t st);
 
 // Stage timing around one launch (no-ops unless profiling is on); stages:
 // 0 ray sort, 1 hierarchy build, 2 traversal, 3 finalize / other.

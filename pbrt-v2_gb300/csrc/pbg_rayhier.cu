@@ -42,6 +42,7 @@
 //             Any-hit keeps one occlusion bit per ray (a 32-bit mask per
 //             leaf) and skips leaves whose rays are all occluded.
 #include <algorithm>
+#include <functional>
 
 #include "pbg_internal.h"
 #include "pbg_count.cuh"
@@ -855,7 +856,8 @@ constexpr uint32_t kQueueCap = 1u << 25;
 
 template <bool ANY>
 static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const float4* sd,
-                       unsigned long long* keys, uint32_t* mask, cudaStream_t st, int* moved) {
+                       unsigned long long* keys, uint32_t* mask, cudaStream_t st, int* moved,
+                       const std::function<int()>& tail) {
     Work& w = s->work;
     int rc;
     const int64_t nleaf = lv.cnt[0];
@@ -1010,8 +1012,14 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
         // One status read per call: a dropped pair would lose hits.  With
         // *moved, the word after it too: the batch's origins differ from
         // the kept order it was traced in, and the caller traces it again.
+        // The caller's tail (the finalize kernel) is enqueued behind the
+        // publication, so the GPU runs it while the host waits; an attempt
+        // that is rerun enqueues it again.
+        int seq = 0;
+        if ((rc = publish_device_words(s, status + kStatusOverflow, moved ? 2 : 1, &seq, st))) return rc;
+        if ((rc = tail())) return rc;
         int h[2] = {0, 0};
-        if ((rc = read_device_words(s, status + kStatusOverflow, moved ? 2 : 1, h, st))) return rc;
+        if ((rc = wait_device_words(s, seq, moved ? 2 : 1, h, st))) return rc;
         if (moved && h[1] != 0) {
             *moved = 1;
             return PBG_OK;
@@ -1041,13 +1049,17 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
     if ((rc = ensure(w.keys, (size_t)n * 8))) return rc;
     unsigned long long* keys = (unsigned long long*)w.keys.ptr;
     PBG_CUDA(cudaMemsetAsync(keys, 0, (size_t)n * 8, st));
-    if (s->ntri > 0 && (rc = rh_traverse<false>(s, lv, so, sd, keys, nullptr, st, nullptr))) return rc;
-    prof_begin(s, st);
-    rh_finalize_nearest<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        (const TriRec*)s->tris.ptr, (const int32_t*)s->tri_pos.ptr, so, sd, perm, keys, n, prim, t, b1, b2);
-    prof_end(s, st, kStageOther, 1);
-    PBG_CUDA(cudaGetLastError());
-    return PBG_OK;
+    const std::function<int()> finalize = [&]() -> int {
+        prof_begin(s, st);
+        rh_finalize_nearest<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            (const TriRec*)s->tris.ptr, (const int32_t*)s->tri_pos.ptr, so, sd, perm, keys, n, prim, t, b1,
+            b2);
+        prof_end(s, st, kStageOther, 1);
+        PBG_CUDA(cudaGetLastError());
+        return PBG_OK;
+    };
+    if (s->ntri > 0) return rh_traverse<false>(s, lv, so, sd, keys, nullptr, st, nullptr, finalize);
+    return finalize();
 }
 
 int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
@@ -1068,13 +1080,24 @@ int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
         if ((rc = ensure(w.leafmask, (size_t)nleaf * 4))) return rc;
         uint32_t* mask = (uint32_t*)w.leafmask.ptr;
         PBG_CUDA(cudaMemsetAsync(mask, 0, (size_t)nleaf * 4, st));
+        const std::function<int()> finalize = [&]() -> int {
+            prof_begin(s, st);
+            rh_finalize_occluded<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(perm, mask, n, occ);
+            prof_end(s, st, kStageOther, 1);
+            PBG_CUDA(cudaGetLastError());
+            return PBG_OK;
+        };
         int moved = 0;
         if (s->ntri > 0) {
-            rc = rh_traverse<true>(s, lv, so, sd, nullptr, mask, st, speculative ? &moved : nullptr);
+            // the finalize runs behind the status publication; a moved
+            // batch's answers are overwritten by the next attempt's
+            rc = rh_traverse<true>(s, lv, so, sd, nullptr, mask, st, speculative ? &moved : nullptr, finalize);
             if (rc) return rc;
-        } else if (speculative) {
-            rc = read_device_words(s, (const int*)s->err.ptr + kStatusOriginMoved, 1, &moved, st);
-            if (rc) return rc;
+        } else {
+            if ((rc = finalize())) return rc;
+            if (speculative &&
+                (rc = read_device_words(s, (const int*)s->err.ptr + kStatusOriginMoved, 1, &moved, st)))
+                return rc;
         }
         if (moved) {
             w.origin_sort_n = -1;
@@ -1083,10 +1106,6 @@ int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
             continue;
         }
         if (speculative) s->counters.origin_reuses++;
-        prof_begin(s, st);
-        rh_finalize_occluded<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(perm, mask, n, occ);
-        prof_end(s, st, kStageOther, 1);
-        PBG_CUDA(cudaGetLastError());
         return PBG_OK;
     }
     set_last_error("rayhierarchy: the origin order changed under a fresh sort");
