@@ -38,3 +38,43 @@ def test_make_accelerator_names():
     from pbrt_gb300 import accel as A
     with pytest.raises(ValueError):
         A.MakeAccelerator("kdtree", [[0, 0, 0, 1, 0, 0, 0, 1, 0]])
+
+
+def test_struct_mirrors_match_the_header(tmp_path):
+    """Every ctypes mirror of a header struct has the header's size and, field
+    by field, the header's offsets (a C program compiled by gcc against
+    include/pbrt_gb300.h prints them)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    import pytest
+    from pbrt_gb300 import batch as Bt
+    from pbrt_gb300 import render as R
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    mirrors = {"pbg_params": L.Params, "pbg_rays": L.Rays, "pbg_hits": L.Hits, "pbg_counters": L.Counters,
+               "pbg_learn_params": L.LearnParams, "pbg_learn_stats": L.LearnStats,
+               "pbg_batch_params": Bt.BatchParams, "pbg_batch_stats": Bt.BatchStats,
+               "pbg_camera": R.Camera, "pbg_light": R.Light, "pbg_render_params": R.RenderParams,
+               "pbg_render_stats": R.RenderStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "pbrt_gb300.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append(f'printf("{cname} :size %zu\\n", sizeof({cname}));')
+        for name, *_ in cls._fields_:
+            lines.append(f'printf("{cname} {name} %zu\\n", offsetof({cname}, {name}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = Path(__file__).resolve().parents[1] / "include"
+    subprocess.run(["gcc", "-std=c11", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {}
+    for line in out.splitlines():
+        cname, name, value = line.split()
+        got[(cname, name)] = int(value)
+    for cname, cls in mirrors.items():
+        assert got[(cname, ":size")] == ctypes.sizeof(cls), cname
+        for name, *_ in cls._fields_:
+            assert got[(cname, name)] == getattr(cls, name).offset, (cname, name)
