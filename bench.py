@@ -55,7 +55,7 @@ FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 148_000_000, "ray-bvh": 116_000_00
 # fraction of the dominant kernel (smsp__issue_active, --set full capture of
 # the frame's camera and first shadow batch)
 FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, nearest)": 0.72,
-                                       "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.74}}
+                                       "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.73}}
 L2_BYTES = 129 * 1024 * 1024
 CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)
 
