@@ -560,8 +560,8 @@ __global__ void store_hits_kernel(const int32_t* __restrict__ prim, const float*
 }
 
 __global__ void store_bytes_kernel(const uint8_t* __restrict__ src, int64_t n, uint8_t* __restrict__ dst) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = src[i];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
 }
 
 static int stage_rays(pbg_scene* s, const pbg_rays* r, int64_t n, float4** o, float4** d,
@@ -818,7 +818,13 @@ static int occluded_in_parts(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t
         rc = run_occluded(s, o, d, v, cnt, oc, s->stream);
         if (c > 0) std::swap(s->work, s->alt);
         if (rc) break;
-        store_bytes_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s->stream>>>(oc, cnt, po + lo);
+        if (c + 1 < P) {  // beside the next part's traversal: narrow CTAs on the copy stream
+            cudaEventRecord(s->io_events[P + c], s->stream);
+            cudaStreamWaitEvent(s->io_stream, s->io_events[P + c], 0);
+            store_bytes_kernel<<<(unsigned)sms, kNarrowThreads, 0, s->io_stream>>>(oc, cnt, po + lo);
+        } else {
+            store_bytes_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s->stream>>>(oc, cnt, po + lo);
+        }
         if (cudaGetLastError() != cudaSuccess) rc = PBG_ERR_INTERNAL;
     }
     const cudaError_t e = cudaStreamSynchronize(s->io_stream);
