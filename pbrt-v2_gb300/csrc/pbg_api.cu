@@ -749,9 +749,9 @@ void release_work(Work& w) {
 // each with its own work buffers and so its own kept origin order: the
 // second part's rows cross the host link, read by a narrow gather kernel of
 // one 64-thread CTA per SM on the high-priority stream, while the first part
-// is traced.  Only
-// valid rays' rows are read.  *done = false: not applicable, nothing was
-// started.
+// is traced, and the first part's results cross back the same way while the
+// second part is traced.  Only valid rays' rows are read.  *done = false:
+// not applicable, nothing was started.
 constexpr int kShadowParts = 2;
 // Share of the first part, whose rows cross the link with nothing to hide
 // them behind: measured best of 40, 45 and 50 (a smaller first part leaves
