@@ -1,28 +1,39 @@
 """Benchmark of the ray-batch intersection path (one JSON line on rank 0).
 
-Workload (default): the ray-hierarchy direct-lighting frame -- 1024x1024,
-4 spp jittered camera rays (4,194,304) into the 181,250-triangle terrain +
-40 icospheres scene, nearest hit through Accelerator "rayhierarchy", then
-4 shadow batches (one per area-light sample, as DirectLightingIntegrator's
-batch path issues them, core/integrator.cpp:358-455) of any-hit rays from
-every hit point to seeded points on the 1x1 area light.  One step = that
-frame's five batch calls (1 nearest + 4 any-hit), hierarchy rebuilt per call.
+Workload (default, --workload path): the 1M-triangle path-tracing frame --
+1024x1024, 8 spp (2x4 jittered), 800 displaced icospheres (1,024,000
+triangles) through Accelerator "ray-bvh", path integrator to depth 5
+(Russian roulette after bounce 3, integrators/path.cpp:43-157) with one
+area-light shadow ray per vertex; every camera, bounce and shadow batch of
+the frame runs on the device (pbg_render).  One step = one frame.
 
-value     rays completed per second with rays and shadow rays resident in HBM
-          (device-pointer entry points), CUDA-event time per step, L2 flushed
-          between steps (outside the timed region).
-e2e       the same frame through the host-buffer C ABI calls (pbg_intersect /
-          pbg_occluded) with pinned host arrays: H2D of rays, D2H of results.
-roofline  the dominant kernel (the traversal kernels), algorithmic bytes over
-          their event-timed duration, against the measured HBM peak.
-cpu_baseline  the oracle's SAH-BVH port of pbrt's CPU path on the host cores,
-          on a bounded sample of the same rays.
+value     nearest-hit + any-hit rays per second of the frame with the plain
+          cluster order, CUDA-event time of the whole frame on the device
+          (ray generation, traversal, shading, queue compaction, film).
+learned_vs_plain  the same frames with the learned ordering on (online
+          training and inference inside each frame's time), their ratio, the
+          work counters per ray of both, and whether the images are equal.
+e2e       the same frame through the host call pbg_render: camera, light and
+          parameters in, the RGB image read back; wall time of the call.
+roofline  the traversal launches: algorithmic bytes against the measured HBM
+          copy peak, and algorithmic FP32 work (box and triangle tests
+          counted by the kernels' counting variants on one extra frame)
+          against the nominal FP32 rate.
+cpu_baseline  the oracle's restatement of the same frame (same samples,
+          SAH BVH + pbrt's triangle test) on all host cores and on one, a
+          bounded strided sample of the frame's paths.
+parity    the whole frame against the oracle's render of the same seed.
 
---impl reference runs the reference's CPU path (the oracle port: the
-reference's own build needs its source tree, which the GPU host lacks) on
-all host cores and prints the same line with "impl": "reference".
---gpus N under torchrun: one replica of the frame per GPU ("replicas only":
-rays are independent, nothing is exchanged).
+Other workloads: --workload frame (the rayhierarchy direct-lighting frame,
+181,250 triangles, 1 camera + 4 shadow batches through the per-batch C ABI)
+and --workload batch (64 scenes, one persistent launch per step).
+
+--impl reference runs the reference's CPU path on the same workload (the
+oracle port: the reference's own build needs its source tree, which the GPU
+host lacks) on all host cores and prints the same line with
+"impl": "reference".
+--gpus N under torchrun: one replica per GPU ("replicas only": rays are
+independent, nothing is exchanged).
 """
 from __future__ import annotations
 
@@ -54,6 +65,12 @@ FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 148_000_000, "ray-bvh": 116_000_00
 # The traversal is bound by instruction issue, not by HBM: ncu's issue-active
 # fraction of the dominant kernel (smsp__issue_active, --set full capture of
 # the frame's camera and first shadow batch)
+# dram__bytes_read.sum + dram__bytes_write.sum per traversal launch of the
+# path frame (None until captured)
+PATH_LAUNCH_DRAM_BYTES = None
+# smsp__issue_active of the persistent walk on the path frame's bounces
+# (ncu --set full, bounce 2 of the warm-up frame: nearest, any-hit)
+PATH_ISSUE_ACTIVE = {"bvh_persistent_kernel (nearest)": 0.67, "bvh_persistent_kernel (any-hit)": 0.66}
 FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, nearest)": 0.72,
                                        "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.73}}
 L2_BYTES = 129 * 1024 * 1024
@@ -318,31 +335,94 @@ def run_gpu(args, rank, world, dev):
 
 PATH_CAMERA = dict(eye=(0.0, 6.0, -62.0), look=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fov=42.0)
 PATH_LIGHT = np.array([[-12, 32, -12], [12, 32, -12], [12, 32, 12], [-12, 32, 12]], np.float32)
+PATH_LIGHT_L = (12.0, 12.0, 12.0)
+PATH_RES, PATH_SPP, PATH_DEPTH = 1024, (2, 4), 5
+PATH_WORKLOAD = ("ray-bvh path tracing 1024x1024x8spp (2x4 jittered), 1,024,000 triangles "
+                 "(800 displaced icospheres), depth 5, one area-light sample per vertex, "
+                 "whole frame on device")
+# Algorithmic FP32 work per counted unit (an FMA counts as 2 FLOP): a slab
+# test of one child box with the ray's reciprocal direction precomputed is
+# 6 subtractions + 6 multiplications; a ray/triangle test by Moller-Trumbore
+# stage is 24 FLOP (s1 = d x e2, divisor, 1/divisor, o - p1, b1), then 15
+# (s2 = v x e1, b2) and 6 (t); pbrt's exact test is all three stages.
+FLOP_BOX, FLOP_STAGE1, FLOP_STAGE23, FLOP_EXACT = 12, 24, 21, 45
+
+
+def fp32_peak_tflops(sm_mhz):
+    """Nominal dense FP32 rate: SMs x 128 FP32 lanes x 2 FLOP (FMA) x clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    return sms * 128 * 2 * sm_mhz * 1e6 / 1e12, sms
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def path_setup():
+    from pbrt_gb300 import render as R
+    from pbrt_gb300 import scenes as S
+    sc = S.displaced_icospheres(seed=3)
+    r2c, c2w = R.perspective_camera(PATH_RES, PATH_RES, PATH_CAMERA["eye"], PATH_CAMERA["look"],
+                                    PATH_CAMERA["up"], PATH_CAMERA["fov"])
+    return sc, r2c, c2w
+
+
+def path_cpu_counter(tris, r2c, c2w, seed):
+    from oracle import oracle as O
+    lights = [{"type": "quad", "quad": PATH_LIGHT, "L": PATH_LIGHT_L, "nsamples": 1}]
+    return O.RenderCounter(tris, r2c, c2w, PATH_RES, PATH_RES, lights, "path", PATH_SPP, True,
+                           PATH_DEPTH, seed)
+
+
+def timed_cpu_sample(rc, threads, target_s, seed):
+    """Traces a strided subset of the frame's samples sized to about target_s
+    seconds on `threads` host threads; returns (rays, seconds, stride)."""
+    probe = 8192
+    t0 = time.perf_counter()
+    n0, s0 = rc.count(0, probe, threads, seed)
+    dt = max(time.perf_counter() - t0, 1e-4)
+    per_sample = dt / max(1, (rc.samples + probe - 1) // probe)
+    stride = max(1, int(rc.samples * per_sample / target_s))
+    t0 = time.perf_counter()
+    n, s = rc.count(1, stride, threads, seed)
+    return n + s, time.perf_counter() - t0, stride
 
 
 def run_gpu_path(args, rank, world, dev):
     """The ray-bvh path-tracing frame: 1024x1024 x 8 spp (2x4 jittered) on
     800 displaced icospheres (1,024,000 triangles), path integrator to depth
     5 with Russian roulette after bounce 3, one area-light shadow ray per
-    vertex; the whole frame runs on the device (pbg_render)."""
+    vertex; the whole frame runs on the device (pbg_render).  value = the
+    plain ordering; the learned ordering is measured on the same frames."""
     import torch
     from pbrt_gb300 import accel as A
     from pbrt_gb300 import render as R
-    from pbrt_gb300 import scenes as S
     torch.cuda.set_device(dev)
-    sc = S.displaced_icospheres(seed=3)
+    sc, r2c, c2w = path_setup()
     tris = sc["tris"]
     t0 = time.perf_counter()
     acc = A.MakeAccelerator("ray-bvh", tris, {"device": dev, "raySort": int(args.ray_sort)})
     build_s = time.perf_counter() - t0
-    res = 1024
-    r2c, c2w = R.perspective_camera(res, res, PATH_CAMERA["eye"], PATH_CAMERA["look"],
-                                    PATH_CAMERA["up"], PATH_CAMERA["fov"])
-    cam = R.camera_struct(r2c, c2w, res, res)
-    light = R.quad_light(PATH_LIGHT, (12.0, 12.0, 12.0), 1)
-    prm = R.render_params("path", spp=(2, 4), jitter=True, max_depth=5, seed=17)
+    cam = R.camera_struct(r2c, c2w, PATH_RES, PATH_RES)
+    light = R.quad_light(PATH_LIGHT, PATH_LIGHT_L, 1)
+    prm = R.render_params("path", spp=PATH_SPP, jitter=True, max_depth=PATH_DEPTH, seed=17)
 
-    def measure(label):
+    def measure():
         for k in range(args.warmup):
             prm.seed = 500 + k
             R.render(acc, cam, [light], prm)
@@ -351,6 +431,7 @@ def run_gpu_path(args, rank, world, dev):
         acc.profile(True)
         frames, walls = [], []
         rank_barrier(world)
+        torch.cuda.synchronize()
         with ClockSampler(dev) as clk:
             for k in range(args.steps):
                 prm.seed = 1000 + k  # the same frames in every mode
@@ -358,69 +439,141 @@ def run_gpu_path(args, rank, world, dev):
                 img, st = R.render(acc, cam, [light], prm)
                 walls.append(time.perf_counter() - w0)
                 frames.append(st)
+        torch.cuda.synchronize()
+        rank_barrier(world)
         stt = acc.stats()
         acc.profile(False)
         return frames, walls, stt, clk.summary(), stt["kernel_launches"] - l0, img
 
+    def count_work(seed):
+        """One more frame with the counting kernels (profiling level 2)."""
+        acc.profile(2)
+        prm.seed = seed
+        _, st = R.render(acc, cam, [light], prm)
+        w = acc.stats()["work"]
+        acc.profile(False)
+        return w, st
+
+    def rate(frames):
+        rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
+        ms = sum(f["ms_total"] for f in frames) / len(frames)
+        return rays, ms
+
+    frames, walls, stt, clocks, launches, img_plain = measure()
+    rays, frame_ms = rate(frames)
+    work, wst = count_work(1000)
     learned_line = None
-    frames, walls, stt, clocks, launches, img_plain = measure("plain")
     if args.learned:
-        plain_rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
-        plain_ms = sum(f["ms_total"] for f in frames) / len(frames)
         acc.learn_enable(True, seed=5, steps_per_train=args.learn_steps, lr=args.learn_lr,
                          margin=args.learn_margin)
-        lf, lw, lstt, lclocks, llaunch, img_learned = measure("learned")
+        lf, lw, lstt, lclocks, llaunch, img_learned = measure()
+        lwork, _ = count_work(1000)
         ls = acc.learn_stats()
-        l_rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in lf) / len(lf)
-        l_ms = sum(f["ms_total"] for f in lf) / len(lf)
+        l_rays, l_ms = rate(lf)
         learned_line = {
-            "plain_mrays_s": round(plain_rays / (plain_ms * 1e-3) / 1e6, 2),
+            "plain_mrays_s": round(rays / (frame_ms * 1e-3) / 1e6, 2),
             "learned_mrays_s": round(l_rays / (l_ms * 1e-3) / 1e6, 2),
-            "learned_over_plain": round((l_rays / l_ms) / (plain_rays / plain_ms), 3),
+            "learned_over_plain": round((l_rays / l_ms) / (rays / frame_ms), 3),
             "learned_traversal_ms_per_step": round(lstt["stage_ms"]["traverse"] / args.steps, 3),
             "plain_traversal_ms_per_step": round(stt["stage_ms"]["traverse"] / args.steps, 3),
             "images_identical": bool(np.array_equal(img_plain, img_learned)),
+            "work_per_ray": {
+                "plain": {k: round(v / (wst["nearest_rays"] + wst["shadow_rays"]), 3) for k, v in work.items()},
+                "learned": {k: round(v / (wst["nearest_rays"] + wst["shadow_rays"]), 3) for k, v in lwork.items()}},
             "mlp": {"trained_steps": ls["trained_steps"], "records": ls["records"],
                     "last_loss": round(ls["last_loss"], 4), "top1_accuracy": round(ls["last_accuracy"], 4),
-                    "train_ms_total": round(ls["train_ms"], 2)},
+                    "train_ms_total": round(ls["train_ms"], 2), "infer_ms_total": round(ls["infer_ms"], 2)},
         }
-        if args.learned == 1:  # report the learned-ordered form as the value
+        if args.learned == 1:  # the learned-ordered form as the value
             frames, walls, stt, clocks, launches = lf, lw, lstt, lclocks, llaunch
-    rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
-    frame_ms = sum(f["ms_total"] for f in frames) / len(frames)
-    trav_ms = stt["stage_ms"]["traverse"] / args.steps
+            rays, frame_ms = l_rays, l_ms
+            work = lwork
     frame_ms = max_over_ranks(frame_ms, world)
     if rank != 0:
         return
+    trav_ms = stt["stage_ms"]["traverse"] / args.steps
     hbm, peak_kind = peaks()
     n_launch = max(stt["timed_launches"]["traverse"], 1)
-    per_launch_bytes = (rays * 32 + rays * 8) / (n_launch / args.steps) + len(tris) * 48
+    launches_per_frame = n_launch / args.steps
+    # HBM: every traced ray read once (32 B) and its result written once
+    # (16 B nearest, 1 B any-hit), the triangle records read once per launch
+    near_rays = sum(f["nearest_rays"] for f in frames) / len(frames)
+    sh_rays = sum(f["shadow_rays"] for f in frames) / len(frames)
+    per_launch_bytes = (near_rays * 48 + sh_rays * 33) / launches_per_frame + len(tris) * 48
     avg_launch_ms = stt["stage_ms"]["traverse"] / n_launch
     achieved = per_launch_bytes / (avg_launch_ms * 1e-3) / 1e9
+    # FP32: the counted frame's work over its own traversal share of the frame
+    flops_frame = (work["node_tests"] * FLOP_BOX + work["filter_tests"] * FLOP_STAGE1
+                   + work["filter_stage2"] * FLOP_STAGE23 + work["exact_tests"] * FLOP_EXACT)
+    flops_per_launch = flops_frame / launches_per_frame
+    fp32_achieved = flops_per_launch / (avg_launch_ms * 1e-3) / 1e12
+    fp32_peak, sms = fp32_peak_tflops(clocks.get("sm_max_mhz") or 2070.0)
+    # CPU baseline: the oracle's restatement of the same frame (same seed,
+    # same samples) on the host cores, a bounded strided sample
+    cpu = None
+    if not args.no_cpu and world == 1:
+        rc = path_cpu_counter(tris, r2c, c2w, 1000)
+        threads = os.cpu_count() or 1
+        r_all, s_all, stride_all = timed_cpu_sample(rc, threads, 10.0, 1000)
+        r_one, s_one, stride_one = timed_cpu_sample(rc, 1, 3.0, 1000)
+        cpu = {"value": round(r_all / s_all / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "seconds": round(s_all, 2), "cpu_model": cpu_model(),
+               "sample": (f"every {stride_all}th sample of the same frame" if stride_all > 1 else "the whole frame")
+                         + f" ({r_all} nearest + shadow rays), depth-first path per sample, "
+                           "SAH BVH + pbrt's triangle test (oracle/render_oracle.c)",
+               "single_core": {"value": round(r_one / s_one / 1e6, 3), "cores": 1, "seconds": round(s_one, 2),
+                               "sample": f"every {stride_one}th sample ({r_one} rays)"}}
+        del rc
+    parity = None
+    if not args.no_parity and world == 1:
+        # the whole frame against the oracle's render of the same seed
+        from oracle import oracle as O
+        lights = [{"type": "quad", "quad": PATH_LIGHT, "L": PATH_LIGHT_L, "nsamples": 1}]
+        prm.seed = 1000
+        img_gpu, _ = R.render(acc, cam, [light], prm)
+        c0 = time.perf_counter()
+        img_cpu = O.render(tris, r2c, c2w, PATH_RES, PATH_RES, lights, "path", PATH_SPP, True, PATH_DEPTH,
+                           1000)
+        diff = img_gpu.astype(np.float64) - img_cpu.astype(np.float64)
+        parity = {"image": f"{PATH_RES}x{PATH_RES}x{PATH_SPP[0] * PATH_SPP[1]}spp frame, seed 1000",
+                  "rmse_vs_oracle": float(np.sqrt(np.mean(diff ** 2))),
+                  "pixels_differing": int(np.count_nonzero(np.any(diff != 0, axis=2))),
+                  "tolerance": "RMSE <= 1e-4", "oracle_seconds": round(time.perf_counter() - c0, 2)}
     line = {
         "metric": METRIC, "value": round(job_rate(rays, world, frame_ms), 2), "unit": "Mrays/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(frame_ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded displaced icospheres, counter-hash samples)",
-        "config": {"workload": "ray-bvh path tracing 1024x1024x8spp, 1,024,000 triangles, depth 5, "
-                               "one light sample per vertex (whole frame on device)",
-                   "accelerator": "ray-bvh", "rays_per_step": int(rays), "triangles": int(len(tris)),
-                   "bvh_build_s": round(build_s, 2), "ray_sort": bool(args.ray_sort),
-                   "parallelism": f"replicas x{world}",
+        "config": {"workload": PATH_WORKLOAD, "accelerator": "ray-bvh",
+                   "ordering": "learned" if args.learned == 1 else "plain",
+                   "rays_per_step": int(rays), "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays),
+                   "triangles": int(len(tris)), "bvh_build_s": round(build_s, 2),
+                   "ray_sort": bool(args.ray_sort), "parallelism": f"replicas x{world}",
                    "l2": "inputs > L2 (8.4M paths x 32 B rays per bounce)"},
         "traversal_mrays_s": round(rays / (trav_ms * 1e-3) / 1e6, 2),
         "e2e": {"value": round(rays / (sum(walls) / len(walls)) / 1e6, 2), "unit": "Mrays/s",
-                "h2d_bytes_per_step": 256, "d2h_bytes_per_step": res * res * 12,
-                "api": "pbg_render (camera and lights in, RGB image out)"},
+                "ms_per_step": round(sum(walls) / len(walls) * 1e3, 3),
+                "h2d_bytes_per_step": 256 + 112, "d2h_bytes_per_step": PATH_RES * PATH_RES * 12,
+                "api": "pbg_render (camera, light and parameters in, RGB image out; wall time of the host call)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 5), "traffic": None,
-                     "kernel": "bvh_kernel (bounce 0) + bvh_persistent_kernel (bounces 1-5)",
+                     "frac": round(achieved / hbm, 5), "traffic": PATH_LAUNCH_DRAM_BYTES,
+                     "kernel": "traversal launch (bvh_kernel on bounce 0, bvh_persistent_kernel on bounces 1-5)",
+                     "launches_per_step": round(launches_per_frame, 2),
                      "algorithmic_bytes_per_launch": int(per_launch_bytes),
-                     "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind},
+                     "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind + " (of measured copy)",
+                     "fp32": {"achieved_tflops": round(fp32_achieved, 3), "peak_tflops": round(fp32_peak, 1),
+                              "frac": round(fp32_achieved / fp32_peak, 5),
+                              "flops_per_launch": int(flops_per_launch),
+                              "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 x max SM clock",
+                              "counted": {k: int(v) for k, v in work.items()},
+                              "flop_per_unit": {"box_test": FLOP_BOX, "tri_stage1": FLOP_STAGE1,
+                                                "tri_stage2_3": FLOP_STAGE23, "exact_test": FLOP_EXACT}},
+                     "issue_active": PATH_ISSUE_ACTIVE},
         "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stt["stage_ms"].items()},
         "gpu_launches": int(launches),
-        "ordering": "learned" if args.learned == 1 else "plain",
         "learned_vs_plain": learned_line,
+        "cpu_baseline": cpu,
+        "parity": parity,
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -734,44 +887,84 @@ def cpu_baseline(tris, rays, shadows, hitmask, target_s: float = 12.0, threads=N
             "sample": what + "; SAH BVH + pbrt's triangle test (oracle/pbrt_oracle.c)"}
 
 
-def run_reference(args):
-    """The reference's CPU path for this frame on the host cores."""
+def run_reference_frame(args):
+    """The reference's CPU path for the rayhierarchy frame on the host cores:
+    the shadow batches come from the CPU path's own hits, generated once
+    before the timed steps; each step traces a strided subset of the GPU
+    frame's rays (camera rays and their 4 shadow rays)."""
     sc, rays = make_workload()
     tris = sc["tris"]
-    # hit points for the shadow batches come from the CPU path itself
     from oracle import oracle as O
     B = O.BVH(tris)
     n = rays.shape[1]
     threads = os.cpu_count() or 1
-    stride = 64
-    sel = np.arange(0, n, stride)
-    sub = np.ascontiguousarray(rays[:, sel])
-    times = []
-    nrays = 0
+    prim, t, _, _ = B.nearest(rays, threads=threads)
+    shadows, hit = shadow_batches(rays, prim, t, sc["area_light_quad"])
+    stride = 8
+    times, nrays = [], 0
     for it in range(args.warmup + args.steps):
+        sel = np.arange(it % stride, n, stride)
+        sub = np.ascontiguousarray(rays[:, sel])
+        subs = [np.ascontiguousarray(sh[:, sel]) for sh in shadows]
+        hv = np.ascontiguousarray(hit[sel])
         t0 = time.perf_counter()
-        prim, t, _, _ = B.nearest(sub, threads=threads)
-        shadows, hit = shadow_batches(sub, prim, t, sc["area_light_quad"])
+        B.nearest(sub, threads=threads)
         nr = sub.shape[1]
-        for s in shadows:
-            B.anyhit(s, valid=hit, threads=threads)
-            nr += int(hit.sum())
+        for sh in subs:
+            B.anyhit(sh, valid=hv, threads=threads)
+            nr += int(hv.sum())
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             times.append(dt)
-            nrays = nr
-    sec = sum(times) / len(times)
-    value = nrays / sec / 1e6
+            nrays += nr
+    value = nrays / sum(times) / 1e6
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sum(times) / len(times) * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded terrain + icospheres)", "impl": "reference",
             "config": {"workload": "rayhierarchy direct lighting 1024x1024x4spp, 181,250 triangles, "
                                    "1 nearest + 4 shadow batches per frame",
-                       "sample": f"every {stride}th camera ray per step"},
-            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads,
-                             "kind": "port",
-                             "sample": f"every {stride}th camera ray ({len(sel)}) + 4 shadow rays each"},
+                       "sample": f"1/{stride} of the camera rays per step (a different eighth each step) "
+                                 "and their 4 shadow rays"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
+                             "sample": f"1/{stride} of the frame's rays per step"},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_path(args):
+    """The reference's CPU path for the path-tracing frame on all host cores:
+    the oracle's restatement of the breadth-first path integrator over its
+    SAH BVH and pbrt's triangle test, the same frame and samples as the GPU
+    arm; each step traces a strided 1/16 of the frame's paths (a different
+    subset each step), timed whole (camera rays, shading, bounce and shadow
+    rays)."""
+    from pbrt_gb300 import scenes  # noqa: F401  (package import for the scene generator)
+    sc, r2c, c2w = path_setup()
+    rc = path_cpu_counter(sc["tris"], r2c, c2w, 1000)
+    threads = os.cpu_count() or 1
+    stride = 16
+    times, nrays = [], 0
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        a, b = rc.count(it % stride, stride, threads, 1000)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            nrays += a + b
+    value = nrays / sum(times) / 1e6
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sum(times) / len(times) * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded displaced icospheres, counter-hash samples)", "impl": "reference",
+            "config": {"workload": PATH_WORKLOAD, "accelerator": "ray-bvh",
+                       "sample": f"1/{stride} of the frame's paths per step"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
+                             "sample": f"every {stride}th sample of the frame per step, seed 1000 "
+                                       "(oracle/render_oracle.c)"},
             "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -786,7 +979,7 @@ def main():
     ap.add_argument("--accel", default="rayhierarchy", choices=["naive", "rayhierarchy", "ray-bvh"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "path", "batch"])
+    ap.add_argument("--workload", default="path", choices=["path", "frame", "batch"])
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--rh-cluster-levels", type=int, default=0,
                     help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")
@@ -796,7 +989,7 @@ def main():
     ap.add_argument("--learn-lr", type=float, default=0.0, help="learning rate (0 = 0.05)")
     ap.add_argument("--learn-margin", type=float, default=0.0,
                     help="logit lead needed to walk the predicted cluster first (0 = 1.0)")
-    ap.add_argument("--learned", type=int, default=0,
+    ap.add_argument("--learned", type=int, default=2,
                     help="path workload: 0 plain ordering, 1 learned ordering as the value, "
                          "2 plain as the value with the learned comparison attached")
     args = ap.parse_args()
@@ -805,7 +998,13 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         if rank == 0:
-            run_reference(args)
+            if args.workload == "path":
+                run_reference_path(args)
+            elif args.workload == "frame":
+                run_reference_frame(args)
+            else:
+                print(json.dumps({"impl": "reference", "unavailable": "the 64-scene batch has no reference arm; "
+                                  "its CPU baseline is in the GPU line"}), flush=True)
         return
     if world > 1:
         import torch

@@ -102,8 +102,9 @@ typedef struct pbg_counters {
     uint64_t timed_launches[4]; /* launches timed per stage (profiling on) */
     /* Work counted by the traversal kernels at profiling level 2: [0] node
      * (or box) tests, [1] leaves visited, [2] ray/triangle filter tests,
-     * [3] exact tests, [4] exact tests that hit.  Zero otherwise. */
-    uint64_t work[5];
+     * [3] exact tests, [4] exact tests that hit, [5] filter tests that went
+     * past the first barycentric check (ray-bvh walks).  Zero otherwise. */
+    uint64_t work[6];
     /* rayhierarchy shadow batches traced in the kept origin order of the
      * previous batch, and batches traced again because their origins or
      * validity differed from it (the kept order is taken before the

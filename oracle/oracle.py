@@ -193,12 +193,7 @@ class _Params(C.Structure):
                 ("max_depth", C.c_int), ("seed", C.c_uint64), ("albedo", C.c_float * 3)]
 
 
-def render(tris, r2c, c2w, xres, yres, lights, integrator="directlighting", spp=(1, 1),
-           jitter=False, max_depth=5, seed=1, albedo=(0.7, 0.7, 0.7), threads=None):
-    """The CPU restatement of the renderer (oracle/render_oracle.c).  lights:
-    dicts {"type": "point", "pos", "I"} or {"type": "quad", "quad", "L",
-    "nsamples"}.  Returns rgb [yres, xres, 3]."""
-    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+def _render_structs(r2c, c2w, xres, yres, lights, integrator, spp, jitter, max_depth, seed, albedo):
     cam = _Cam()
     cam.r2c[:] = [float(x) for x in np.asarray(r2c, np.float32).reshape(16)]
     cam.c2w[:] = [float(x) for x in np.asarray(c2w, np.float32).reshape(16)]
@@ -220,6 +215,17 @@ def render(tris, r2c, c2w, xres, yres, lights, integrator="directlighting", spp=
     p.max_depth = max_depth
     p.seed = seed
     p.albedo[:] = [float(a) for a in albedo]
+    return cam, arr, p
+
+
+def render(tris, r2c, c2w, xres, yres, lights, integrator="directlighting", spp=(1, 1),
+           jitter=False, max_depth=5, seed=1, albedo=(0.7, 0.7, 0.7), threads=None):
+    """The CPU restatement of the renderer (oracle/render_oracle.c).  lights:
+    dicts {"type": "point", "pos", "I"} or {"type": "quad", "quad", "L",
+    "nsamples"}.  Returns rgb [yres, xres, 3]."""
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    cam, arr, p = _render_structs(r2c, c2w, xres, yres, lights, integrator, spp, jitter, max_depth,
+                                  seed, albedo)
     L = lib()
     L.orc_render.argtypes = [_fp, C.c_int64, C.POINTER(_Cam), C.POINTER(_Light), C.c_int,
                              C.POINTER(_Params), _fp, C.c_int]
@@ -227,6 +233,44 @@ def render(tris, r2c, c2w, xres, yres, lights, integrator="directlighting", spp=
     L.orc_render(_f(tris), tris.shape[0], C.byref(cam), arr, len(lights), C.byref(p), _f(img),
                  threads or os.cpu_count() or 1)
     return img
+
+
+class RenderCounter:
+    """The CPU restatement of a frame, for timing: the BVH is built once;
+    count(first, stride) traces the samples first, first + stride, ... of the
+    frame (every ray a whole path of the GPU frame would trace) and returns
+    (nearest-hit rays, shadow rays)."""
+
+    def __init__(self, tris, r2c, c2w, xres, yres, lights, integrator="path", spp=(1, 1),
+                 jitter=True, max_depth=5, seed=1, albedo=(0.7, 0.7, 0.7)):
+        self.tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        self.cam, self.arr, self.p = _render_structs(r2c, c2w, xres, yres, lights, integrator, spp,
+                                                     jitter, max_depth, seed, albedo)
+        self.nlights = len(lights)
+        self.samples = int(xres) * int(yres) * int(spp[0]) * int(spp[1])
+        L = lib()
+        L.orc_render_bvh.restype = C.c_void_p
+        L.orc_render_bvh.argtypes = [_fp, C.c_int64]
+        L.orc_render_bvh_free.argtypes = [C.c_void_p]
+        L.orc_render_count.argtypes = [_fp, C.c_void_p, C.POINTER(_Cam), C.POINTER(_Light), C.c_int,
+                                       C.POINTER(_Params), C.c_int64, C.c_int64, C.c_int,
+                                       C.POINTER(C.c_uint64)]
+        self._L = L
+        self.h = L.orc_render_bvh(_f(self.tris), self.tris.shape[0])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.orc_render_bvh_free(self.h)
+            self.h = None
+
+    def count(self, first: int, stride: int, threads: int | None = None, seed: int | None = None):
+        if seed is not None:
+            self.p.seed = int(seed)
+        out = (C.c_uint64 * 2)()
+        self._L.orc_render_count(_f(self.tris), self.h, C.byref(self.cam), self.arr, self.nlights,
+                                 C.byref(self.p), int(first), int(stride),
+                                 threads or os.cpu_count() or 1, out)
+        return int(out[0]), int(out[1])
 
 
 def ref_camera(xres, yres, eye, look, up, fov, xy):

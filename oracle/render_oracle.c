@@ -123,17 +123,20 @@ typedef struct {
     const orc_light* lights;
     int nlights;
     const orc_params* prm;
-    float* L; /* [n][3] per sample */
-    int64_t begin, end;
+    float* L; /* [n][3] per sample (NULL: counting only) */
+    int64_t begin, end;   /* sample slots [begin, end) ... */
+    int64_t stride, first; /* ... are samples first + slot * stride */
+    uint64_t nearest, shadow; /* rays traced by this job */
 } job_t;
 
-static int occluded(void* bvh, vec o, vec d, float mint, float maxt) {
+static int occluded(job_t* j, vec o, vec d, float mint, float maxt) {
     float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
-    return orc_bvh_trace(bvh, oo, dd, mint, maxt, 1, NULL, NULL, NULL) >= 0;
+    j->shadow++;
+    return orc_bvh_trace(j->bvh, oo, dd, mint, maxt, 1, NULL, NULL, NULL) >= 0;
 }
 
 /* EstimateDirect for one light sample (u1, u2); 0 if occluded or black. */
-static vec estimate_direct(const job_t* j, const orc_light* lt, vec p, float eps, vec nn, vec ng,
+static vec estimate_direct(job_t* j, const orc_light* lt, vec p, float eps, vec nn, vec ng,
                            vec wo, const vec fr[3], vec fR, float u1, float u2) {
     vec zero = V(0.f, 0.f, 0.f);
     vec target, wi, Li;
@@ -172,7 +175,7 @@ static vec estimate_direct(const job_t* j, const orc_light* lt, vec p, float eps
     /* VisibilityTester::SetSegment */
     float dist = length(sub(p, target));
     vec dn = scl(sub(target, p), 1.f / dist);
-    if (occluded(j->bvh, p, dn, eps, dist * (1.f - eps2))) return zero;
+    if (occluded(j, p, dn, eps, dist * (1.f - eps2))) return zero;
     float absdot = fabsf(dot(wi, nn));
     float w;
     if (lt->type == 0) {
@@ -194,7 +197,8 @@ static void* render_worker(void* arg) {
     const orc_params* prm = j->prm;
     const int spp = prm->spp_x * prm->spp_y;
     const vec fR = V(prm->albedo[0] * INV_PI, prm->albedo[1] * INV_PI, prm->albedo[2] * INV_PI);
-    for (int64_t s = j->begin; s < j->end; ++s) {
+    for (int64_t slot = j->begin; slot < j->end; ++slot) {
+        const int64_t s = j->first + slot * j->stride;
         int64_t pix = s / spp;
         int k = (int)(s % spp);
         int px = (int)(pix % cam->xres), py = (int)(pix / cam->xres);
@@ -213,6 +217,7 @@ static void* render_worker(void* arg) {
             float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
             float t, b1, b2;
             int32_t prim = orc_bvh_trace(j->bvh, oo, dd, mint, INFINITY, 0, &t, &b1, &b2);
+            j->nearest++;
             if (prim < 0) break;
             float g[14];
             orc_hit_geometry(j->tris + 9 * (int64_t)prim, NULL, oo, dd, t, b1, b2, g);
@@ -289,11 +294,55 @@ static void* render_worker(void* arg) {
             d = wi;
             mint = eps;
         }
-        j->L[3 * s] = L.x;
-        j->L[3 * s + 1] = L.y;
-        j->L[3 * s + 2] = L.z;
+        if (j->L) {
+            j->L[3 * s] = L.x;
+            j->L[3 * s + 1] = L.y;
+            j->L[3 * s + 2] = L.z;
+        }
     }
     return NULL;
+}
+
+/* Runs nslots samples (first + k * stride, k < nslots) on nthreads threads
+ * over a prebuilt BVH; out receives the radiance when non-NULL (indexed by
+ * sample), counts[0] / counts[1] the nearest-hit and shadow rays traced. */
+static void run_samples(const float* tris, void* bvh, const orc_camera* cam, const orc_light* lights,
+                        int nlights, const orc_params* prm, float* L, int64_t first, int64_t stride,
+                        int64_t nslots, int nthreads, uint64_t counts[2]) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    job_t jobs[256];
+    pthread_t th[256];
+    int64_t chunk = (nslots + nthreads - 1) / nthreads;
+    int started = 0;
+    for (int k = 0; k < nthreads; ++k) {
+        job_t jb = {tris, bvh, cam, lights, nlights, prm, L, k * chunk,
+                    (k + 1) * chunk < nslots ? (k + 1) * chunk : nslots, stride, first, 0, 0};
+        jobs[k] = jb;
+        if (jobs[k].begin >= jobs[k].end) break;
+        pthread_create(&th[k], NULL, render_worker, &jobs[k]);
+        started = k + 1;
+    }
+    counts[0] = counts[1] = 0;
+    for (int k = 0; k < started; ++k) {
+        pthread_join(th[k], NULL);
+        counts[0] += jobs[k].nearest;
+        counts[1] += jobs[k].shadow;
+    }
+}
+
+/* The CPU baseline's bounded sample of a frame: the BVH is built once
+ * (orc_render_bvh), then orc_render_count traces the samples first,
+ * first + stride, ... of the image and returns only the ray counts. */
+void* orc_render_bvh(const float* tris, int64_t ntri) { return orc_bvh_build(tris, ntri, 4); }
+void orc_render_bvh_free(void* bvh) { orc_bvh_free(bvh); }
+void orc_render_count(const float* tris, void* bvh, const orc_camera* cam, const orc_light* lights,
+                      int nlights, const orc_params* prm, int64_t first, int64_t stride, int nthreads,
+                      uint64_t* counts) {
+    const int64_t n = (int64_t)cam->xres * cam->yres * prm->spp_x * prm->spp_y;
+    if (stride < 1) stride = 1;
+    const int64_t nslots = first < n ? (n - first + stride - 1) / stride : 0;
+    run_samples(tris, bvh, cam, lights, nlights, prm, NULL, first, stride, nslots, nthreads, counts);
 }
 
 /* rgb: [yres][xres][3].  nthreads host threads over the samples. */
@@ -303,20 +352,8 @@ void orc_render(const float* tris, int64_t ntri, const orc_camera* cam, const or
     const int64_t npix = (int64_t)cam->xres * cam->yres, n = npix * spp;
     float* L = (float*)malloc((size_t)(n > 0 ? n : 1) * 3 * sizeof(float));
     void* bvh = orc_bvh_build(tris, ntri, 4);
-    if (nthreads < 1) nthreads = 1;
-    if (nthreads > 256) nthreads = 256;
-    job_t jobs[256];
-    pthread_t th[256];
-    int64_t chunk = (n + nthreads - 1) / nthreads;
-    int started = 0;
-    for (int k = 0; k < nthreads; ++k) {
-        job_t jb = {tris, bvh, cam, lights, nlights, prm, L, k * chunk, (k + 1) * chunk < n ? (k + 1) * chunk : n};
-        jobs[k] = jb;
-        if (jobs[k].begin >= jobs[k].end) break;
-        pthread_create(&th[k], NULL, render_worker, &jobs[k]);
-        started = k + 1;
-    }
-    for (int k = 0; k < started; ++k) pthread_join(th[k], NULL);
+    uint64_t counts[2];
+    run_samples(tris, bvh, cam, lights, nlights, prm, L, 0, 1, n, nthreads, counts);
     for (int64_t p = 0; p < npix; ++p) {
         float X = 0.f, Y = 0.f, Z = 0.f, w = 0.f;
         for (int k = 0; k < spp; ++k) {

@@ -54,7 +54,7 @@ class Hits(C.Structure):
 class Counters(C.Structure):
     _fields_ = [("rays_nearest", C.c_uint64), ("rays_occluded", C.c_uint64),
                 ("calls", C.c_uint64), ("bvh_nodes", C.c_uint64), ("kernel_launches", C.c_uint64),
-                ("timed_launches", C.c_uint64 * 4), ("work", C.c_uint64 * 5),
+                ("timed_launches", C.c_uint64 * 4), ("work", C.c_uint64 * 6),
                 ("origin_reuses", C.c_uint64), ("origin_reruns", C.c_uint64),
                 ("stage_ms", C.c_double * 4)]
 

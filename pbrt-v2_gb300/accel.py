@@ -154,7 +154,7 @@ class Aggregate:
                 "calls": c.calls, "bvh_nodes": c.bvh_nodes, "kernel_launches": c.kernel_launches,
                 "timed_launches": dict(zip(L.STAGES, list(c.timed_launches))),
                 "work": dict(zip(("node_tests", "leaves", "filter_tests", "exact_tests",
-                                  "exact_hits"), list(c.work))),
+                                  "exact_hits", "filter_stage2"), list(c.work))),
                 "origin_reuses": c.origin_reuses, "origin_reruns": c.origin_reruns,
                 "stage_ms": dict(zip(L.STAGES, list(c.stage_ms)))}
 

@@ -247,7 +247,7 @@ static void prof_collect(pbg_scene* s) {
     if (s->prof.level >= 2 && s->workc.ptr) {
         unsigned long long h[8];
         if (cudaMemcpy(h, s->workc.ptr, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess)
-            for (int k = 0; k < 5; ++k) s->counters.work[k] = h[k];
+            for (int k = 0; k < 6; ++k) s->counters.work[k] = h[k];
         else
             cudaGetLastError();
     }
@@ -978,6 +978,7 @@ void pbg_scene_destroy(pbg_scene* s) {
     }
     release_work(s->work);
     release_work(s->alt);
+    render_free(s);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->io_stream) {
         cudaStreamDestroy(s->io_stream);
@@ -1185,7 +1186,7 @@ int pbg_profile(pbg_scene* s, int on) {
         s->counters.stage_ms[k] = 0.0;
         s->counters.timed_launches[k] = 0;
     }
-    for (int k = 0; k < 5; ++k) s->counters.work[k] = 0;
+    for (int k = 0; k < 6; ++k) s->counters.work[k] = 0;
     if (on >= 2) {
         int rc = ensure(s->workc, 8 * sizeof(unsigned long long));
         if (rc) return rc;

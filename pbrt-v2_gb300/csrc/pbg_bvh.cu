@@ -82,8 +82,10 @@ constexpr int kPersistThreads = 128;
 constexpr int kPersistMinBlocks = 10;  // CTAs per SM: measured best of 6, 8, 9, 10, 12, 16
 
 // ORDERED: the learned ordering's predicted cluster (pred, cref as in
-// bvh_kernel) is walked first, then the whole tree skipping it.
-template <bool ANY, bool ORDERED>
+// bvh_kernel) is walked first, then the whole tree skipping it.  STATS: the
+// counting variant (profiling level 2) tallies node tests, leaves and
+// triangle tests into wcount.
+template <bool ANY, bool ORDERED, bool STATS>
 __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
     bvh_persistent_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris,
                           int32_t unculled, const float4* __restrict__ ro, const float4* __restrict__ rd,
@@ -91,7 +93,8 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
                           int32_t* __restrict__ prim_out, float* __restrict__ t_out,
                           float* __restrict__ b1_out, float* __restrict__ b2_out,
                           uint8_t* __restrict__ occ, int* status, unsigned long long* next,
-                          const uint16_t* __restrict__ pred, const int32_t* __restrict__ cref) {
+                          const uint16_t* __restrict__ pred, const int32_t* __restrict__ cref,
+                          unsigned long long* wcount) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -223,6 +226,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
                 continue;
             }
             const BvhNode nn = nodes[node];
+            if (STATS) wc.node += 2;
             float tn0, tn1;
             bool h0 = slab(ri, nn.n0.x, nn.n0.y, nn.n0.z, nn.n0.w, nn.n2.x, nn.n2.y, o.w, h.t, &tn0);
             bool h1 = slab(ri, nn.n1.x, nn.n1.y, nn.n1.z, nn.n1.w, nn.n2.z, nn.n2.w, o.w, h.t, &tn1);
@@ -254,14 +258,18 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
         }
         // the leaf tests, converged
         if (has && leaf_cnt > 0) {
-            bool done = test_run<ANY, false>(tris, leaf_start, leaf_cnt, o, d, nd, h, wc);
+            if (STATS) wc.leaf++;
+            bool done = test_run<ANY, STATS>(tris, leaf_start, leaf_cnt, o, d, nd, h, wc);
             leaf_cnt = 0;
-            if (!done && leafb_cnt > 0 && leafb_t <= h.t)
-                done = test_run<ANY, false>(tris, leafb_start, leafb_cnt, o, d, nd, h, wc);
+            if (!done && leafb_cnt > 0 && leafb_t <= h.t) {
+                if (STATS) wc.leaf++;
+                done = test_run<ANY, STATS>(tris, leafb_start, leafb_cnt, o, d, nd, h, wc);
+            }
             leafb_cnt = 0;
             if (done) finish();
         }
     }
+    if (STATS) wc.flush(wcount);
 }
 
 int ray_order(pbg_scene* s, const float4* o, const float4* d, int64_t n, const int32_t** perm,
@@ -292,7 +300,7 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // is the one with a validity mask (rayhierarchy.cpp:602-813)
     const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
     const bool persistent = s->params.walk == 2 || (s->params.walk == 0 && hint == 1);
-    if (s->prof.level < 2 && persistent) {
+    if (persistent) {
         // persistent while-while walk: one counter word, zeroed per launch
         Work& w = s->work;
         int rc2 = ensure(w.counters, 64);
@@ -300,19 +308,18 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
         unsigned long long* next = (unsigned long long*)w.counters.ptr;
         PBG_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_persistent_kernel<ANY, false>, kPersistThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_persistent_kernel<ANY, false, false>,
+                                                      kPersistThreads, 0);
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
         int64_t blocks = (int64_t)std::max(per_sm, 1) * sms;
         blocks = std::min<int64_t>(blocks, (n + kPersistThreads - 1) / kPersistThreads);
-        if (pred)
-            bvh_persistent_kernel<ANY, true><<<(unsigned)blocks, kPersistThreads, 0, st>>>(
-                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, next, pred,
-                cref);
-        else
-            bvh_persistent_kernel<ANY, false><<<(unsigned)blocks, kPersistThreads, 0, st>>>(
-                nodes, tris, s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ, status, next,
-                nullptr, nullptr);
+        const bool stats = s->prof.level >= 2;
+        auto kern = pred ? (stats ? bvh_persistent_kernel<ANY, true, true> : bvh_persistent_kernel<ANY, true, false>)
+                         : (stats ? bvh_persistent_kernel<ANY, false, true> : bvh_persistent_kernel<ANY, false, false>);
+        kern<<<(unsigned)blocks, kPersistThreads, 0, st>>>(nodes, tris, s->unculled, o, d, valid, perm, n,
+                                                           prim, t, b1, b2, occ, status, next, pred, cref,
+                                                           stats ? wc : nullptr);
     } else if (pred) {
         if (s->prof.level >= 2)
             bvh_kernel<ANY, true, true><<<grid, kBvhThreads, 0, st>>>(

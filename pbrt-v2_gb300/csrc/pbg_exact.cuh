@@ -110,8 +110,10 @@ __device__ __forceinline__ float flip_sign(float v, float s) {
 // Conservative FP32 filter.  o.w = mint, maxt = current upper bound (the
 // best exact t so far, which the exact test accepts when equal).  nd = |d|_1.
 // Returns false only when pbg_exact() would return false for the same maxt.
+// stage2 (counting kernels only): incremented when the test goes past the
+// first barycentric check.
 __device__ __forceinline__ bool pbg_filter(const TriRec& tr, float4 o, float4 d, float nd,
-                                           float maxt) {
+                                           float maxt, uint32_t* stage2 = nullptr) {
     const float e1x = tr.b.x, e1y = tr.b.y, e1z = tr.b.z;
     const float e2x = tr.c.x, e2y = tr.c.y, e2z = tr.c.z;
     const float ne1 = tr.a.w, ne2 = tr.b.w;
@@ -130,6 +132,7 @@ __device__ __forceinline__ bool pbg_filter(const TriRec& tr, float4 o, float4 d,
     float a1 = flip_sign(n1, div);
     float top = fmaf(D, 1.f + kFilterR, ediv);
     if (a1 < -e1b || a1 > top + e1b) return false;
+    if (stage2) ++*stage2;
     float s2x = fmaf(vy, e1z, -(vz * e1y));
     float s2y = fmaf(vz, e1x, -(vx * e1z));
     float s2z = fmaf(vx, e1y, -(vy * e1x));

@@ -12,6 +12,7 @@
 namespace pbg {
 
 struct Learner;
+struct RenderBuffers;
 
 // Two-wide BVH node (64 bytes): both children's boxes, so one node fetch
 // decides both children.  A child index >= 0 is an inner node; a negative
@@ -111,6 +112,7 @@ struct pbg_scene {
     std::vector<pbg::BvhNode> host_nodes;  // ray-bvh tree, kept for the learned clusters
     std::vector<int32_t> host_order;
     struct pbg::Learner* learn = nullptr;
+    struct pbg::RenderBuffers* render_bufs = nullptr;  // pbg_render's frame buffers, kept across frames
     int64_t image_w = 0, image_h = 0;  // ray-image layout from pbg_preprocess (0 = none)
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     pbg::DeviceBuffer err;     // int[4] device status words
@@ -150,6 +152,7 @@ int launch_build_tris(const float* tri9_dev, const int32_t* order_dev, int64_t n
                       cudaStream_t st);
 void cluster_triangle_order(const float* tri9, int64_t ntri, std::vector<int32_t>* order);
 int check_device_status(pbg_scene* s, cudaStream_t st);
+void render_free(pbg_scene* s);
 // Copies count (< kMailboxWords) device words to the host: a one-warp
 // kernel stores them into mapped pinned memory and the host polls for them.
 // No copy-engine transfer is involved, so the read never queues behind

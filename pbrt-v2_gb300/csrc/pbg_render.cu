@@ -458,6 +458,11 @@ struct RenderBuffers {
     }
 };
 
+void render_free(pbg_scene* s) {
+    delete s->render_bufs;
+    s->render_bufs = nullptr;
+}
+
 static int compact_count(pbg_scene* s, const uint8_t* flag, int64_t n, uint32_t* counts, int64_t* total,
                          cudaStream_t st) {
     const int64_t blocks = (n + 255) / 256;
@@ -531,7 +536,8 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
         return PBG_ERR_INVALID_ARGUMENT;
     }
     cudaStream_t st = s->stream;
-    RenderBuffers B;
+    if (!s->render_bufs) s->render_bufs = new RenderBuffers();
+    RenderBuffers& B = *s->render_bufs;  // grown on demand, kept for the next frame
     int r;
     const size_t nk = (size_t)n * kslots;
     if ((r = ensure(B.o4, n * 16)) || (r = ensure(B.d4, n * 16)) || (r = ensure(B.qidx, n * 4)) ||
@@ -552,6 +558,7 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
         rc, n, (float4*)B.o4.ptr, (float4*)B.d4.ptr, (int32_t*)B.qidx.ptr, (float*)B.L.ptr,
         (float*)B.beta.ptr);
     PBG_CUDA(cudaGetLastError());
+    s->counters.kernel_launches += 1;
     pbg_render_stats stt{};
     stt.camera_rays = (uint64_t)n;
     int64_t nq = n;
@@ -582,6 +589,7 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
             (float*)B.scontrib.ptr, (uint8_t*)B.sflag.ptr, (float4*)B.no.ptr, (float4*)B.nd.ptr,
             (uint8_t*)B.nflag.ptr);
         PBG_CUDA(cudaGetLastError());
+        s->counters.kernel_launches += 1;
         // shadow queue
         int64_t nsh = 0;
         if ((r = compact_count(s, (const uint8_t*)B.sflag.ptr, nslots, (uint32_t*)B.counts.ptr, &nsh, st)))
@@ -590,6 +598,7 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
             (const uint8_t*)B.sflag.ptr, nslots, (const uint32_t*)B.counts.ptr, (const float4*)B.so.ptr,
             (const float4*)B.sd.ptr, (float4*)B.sqo.ptr, (float4*)B.sqd.ptr, (int32_t*)B.spos.ptr);
         PBG_CUDA(cudaGetLastError());
+        s->counters.kernel_launches += 1;
         if (nsh > 0 && (r = pbg_occluded_device(s, (const float*)B.sqo.ptr, (const float*)B.sqd.ptr,
                                                 nullptr, nsh, (uint8_t*)B.occ.ptr, st)))
             return r;
@@ -598,6 +607,7 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
             rc, nq, kslots, qi, (const uint8_t*)B.sflag.ptr, (const int32_t*)B.spos.ptr,
             (const uint8_t*)B.occ.ptr, (const float*)B.scontrib.ptr, (float*)B.L.ptr);
         PBG_CUDA(cudaGetLastError());
+        s->counters.kernel_launches += 1;
         if (rc.integrator != PBG_INTEGRATOR_PATH) break;
         // bounce queue
         int64_t nn = 0;
@@ -607,6 +617,7 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
             (const uint8_t*)B.nflag.ptr, nq, (const uint32_t*)B.counts.ptr, qi, (const float4*)B.no.ptr,
             (const float4*)B.nd.ptr, qi2, qo2, qd2);
         PBG_CUDA(cudaGetLastError());
+        s->counters.kernel_launches += 1;
         std::swap(qi, qi2);
         std::swap(qo, qo2);
         std::swap(qd, qd2);
@@ -618,6 +629,7 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     film_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(npix, rc.spp, (const float*)B.L.ptr,
                                                                  (float*)B.rgb.ptr);
     PBG_CUDA(cudaGetLastError());
+    s->counters.kernel_launches += 1;
     cudaEventRecord(e1, st);
     PBG_CUDA(cudaMemcpyAsync(rgb_host, B.rgb.ptr, npix * 12, cudaMemcpyDeviceToHost, st));
     PBG_CUDA(cudaStreamSynchronize(st));

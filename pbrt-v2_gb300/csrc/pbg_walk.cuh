@@ -50,7 +50,7 @@ __device__ __forceinline__ bool test_run(const TriRec* __restrict__ tris, int32_
     for (int32_t k = 0; k < cnt; ++k) {
         const TriRec tr = tris[start + k];
         if (STATS) wc.filt++;
-        if (!pbg_filter(tr, o, d, nd, h.t)) continue;
+        if (!pbg_filter(tr, o, d, nd, h.t, STATS ? &wc.filt2 : nullptr)) continue;
         float tt, u1, u2;
         if (STATS) wc.exact++;
         if (!pbg_exact_rec(tr, o, d, h.t, &tt, &u1, &u2)) continue;
