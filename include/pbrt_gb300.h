@@ -216,15 +216,20 @@ typedef struct pbg_camera {
     int32_t xres, yres;
 } pbg_camera;
 
-#define PBG_LIGHT_POINT 0 /* lights/point.cpp PointLight            */
-#define PBG_LIGHT_QUAD 1  /* lights/diffuse.cpp on a parallelogram  */
+#define PBG_LIGHT_POINT 0 /* lights/point.cpp PointLight                         */
+#define PBG_LIGHT_QUAD 1  /* an emitter on a parallelogram, sampled by area      */
+#define PBG_LIGHT_MESH 2  /* lights/diffuse.cpp DiffuseAreaLight on scene triangles */
 typedef struct pbg_light {
     int32_t type;
     int32_t nsamples;  /* "nsamples" of the area light (directlighting) */
     float pos[3];      /* point light position */
     float intensity[3];/* point light I, RGB */
-    float quad[12];    /* area light corners p0, p1, p2, p3 (p2 = p1 + p3 - p0) */
-    float radiance[3]; /* area light L, RGB; emits on the side of (p1-p0)x(p3-p0) */
+    float quad[12];    /* parallelogram corners p0, p1, p2, p3 (p2 = p1 + p3 - p0) */
+    float radiance[3]; /* area light L, RGB; a parallelogram emits on the side of
+                          (p1-p0)x(p3-p0), a triangle on the side of its
+                          DifferentialGeometry normal */
+    int32_t first_tri; /* PBG_LIGHT_MESH: the emitter is the scene's triangles */
+    int32_t ntri;      /* [first_tri, first_tri + ntri), 1..64 (its ShapeSet)  */
 } pbg_light;
 
 #define PBG_INTEGRATOR_DIRECT 0 /* SurfaceIntegrator "directlighting" */
@@ -247,10 +252,48 @@ typedef struct pbg_render_stats {
 
 /* Renders the image; rgb receives [yres][xres][3] floats (host memory),
  * ImageFilm's XYZ accumulation and box filter (film/image.cpp).  stats may
- * be NULL. */
+ * be NULL.  Sample values come from a counter-based hash of
+ * (params->seed, sample, dimension). */
 int pbg_render(pbg_scene* scene, const pbg_camera* camera, const pbg_light* lights,
                int32_t nlights, const pbg_render_params* params, float* rgb,
                pbg_render_stats* stats);
+
+/* One breadth-first task's sample values as the reference draws them
+ * (renderers/breadth-first.cpp:18-48): the samples its StratifiedSampler
+ * produced and the continuation of the task's RNG.  Host arrays.
+ *   image_xy  [count][2]  Sample::imageX, imageY, in the task's order
+ *   dims      [count][ndims], per sample:
+ *             directlighting: 6 values per light sample, lights in order and
+ *               each light's nsamples in order: LightSample uPos[0], uPos[1],
+ *               uComponent, BSDFSample uDir[0], uDir[1], uComponent (the
+ *               integrator's arrays, integrators/directlighting.cpp:45-62)
+ *             path: 10 values for each of the bounces 0-2: light choice,
+ *               LightSample uPos[0..1], uComponent, BSDFSample uDir[0..1],
+ *               uComponent, the path's BSDFSample uDir[0..1], uComponent
+ *               (integrators/path.cpp:31-38)
+ *   rng       [nrng] the task RNG's RandomFloat draws after the sampler's;
+ *             path bounces from 3 on consume them as the batch integrator
+ *             does: 7 per ray of the task for UniformSampleOneLight, then 3
+ *             per ray that hit (4 after bounce 3, Russian roulette)
+ * count camera rays are traced; a sample adds to the pixels of ImageFilm's
+ * box-filter footprint around (imageX, imageY).  A path vertex whose sampled
+ * direction the BSDF rejects ends the render with PBG_ERR_UNSUPPORTED (the
+ * reference would trace that ray again unchanged). */
+typedef struct pbg_sample_stream {
+    int64_t count;
+    const float* image_xy;
+    const float* dims;
+    int32_t ndims;
+    int32_t reserved;
+    const float* rng;
+    int64_t nrng;
+} pbg_sample_stream;
+
+/* pbg_render with the reference's sample stream instead of the hash (no
+ * counterpart in the reference: its renderer draws these values itself). */
+int pbg_render_stream(pbg_scene* scene, const pbg_camera* camera, const pbg_light* lights,
+                      int32_t nlights, const pbg_render_params* params,
+                      const pbg_sample_stream* stream, float* rgb, pbg_render_stats* stats);
 
 /* ---------------------------------------------------------------------
  * Many scenes in one launch.  No counterpart in the reference (one scene,

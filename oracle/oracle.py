@@ -185,7 +185,8 @@ class _Cam(C.Structure):
 
 class _Light(C.Structure):
     _fields_ = [("type", C.c_int), ("nsamples", C.c_int), ("pos", C.c_float * 3),
-                ("I", C.c_float * 3), ("quad", C.c_float * 12), ("L", C.c_float * 3)]
+                ("I", C.c_float * 3), ("quad", C.c_float * 12), ("L", C.c_float * 3),
+                ("first_tri", C.c_int), ("ntri", C.c_int)]
 
 
 class _Params(C.Structure):
@@ -204,6 +205,10 @@ def _render_structs(r2c, c2w, xres, yres, lights, integrator, spp, jitter, max_d
             arr[k].type, arr[k].nsamples = 0, 1
             arr[k].pos[:] = [float(x) for x in lt["pos"]]
             arr[k].I[:] = [float(x) for x in lt["I"]]
+        elif lt["type"] == "mesh":
+            arr[k].type, arr[k].nsamples = 2, int(lt.get("nsamples", 1))
+            arr[k].first_tri, arr[k].ntri = int(lt["first"]), int(lt["ntri"])
+            arr[k].L[:] = [float(x) for x in lt["L"]]
         else:
             arr[k].type, arr[k].nsamples = 1, int(lt.get("nsamples", 4))
             arr[k].quad[:] = [float(x) for x in np.asarray(lt["quad"], np.float32).reshape(12)]
@@ -221,8 +226,10 @@ def _render_structs(r2c, c2w, xres, yres, lights, integrator, spp, jitter, max_d
 def render(tris, r2c, c2w, xres, yres, lights, integrator="directlighting", spp=(1, 1),
            jitter=False, max_depth=5, seed=1, albedo=(0.7, 0.7, 0.7), threads=None):
     """The CPU restatement of the renderer (oracle/render_oracle.c).  lights:
-    dicts {"type": "point", "pos", "I"} or {"type": "quad", "quad", "L",
-    "nsamples"}.  Returns rgb [yres, xres, 3]."""
+    dicts {"type": "point", "pos", "I"}, {"type": "quad", "quad", "L",
+    "nsamples"} or {"type": "mesh", "first", "ntri", "L", "nsamples"} (the
+    scene's triangles [first, first + ntri) as an area light).  Returns rgb
+    [yres, xres, 3]."""
     tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
     cam, arr, p = _render_structs(r2c, c2w, xres, yres, lights, integrator, spp, jitter, max_depth,
                                   seed, albedo)
@@ -232,6 +239,29 @@ def render(tris, r2c, c2w, xres, yres, lights, integrator="directlighting", spp=
     img = np.empty((yres, xres, 3), np.float32)
     L.orc_render(_f(tris), tris.shape[0], C.byref(cam), arr, len(lights), C.byref(p), _f(img),
                  threads or os.cpu_count() or 1)
+    return img
+
+
+def render_stream(tris, r2c, c2w, xres, yres, lights, integrator, image_xy, dims, rng, max_depth=5,
+                  albedo=(0.7, 0.7, 0.7), threads=None):
+    """The renderer restatement fed one task's reference sample values
+    (orc_render_stream; the layout of pbg_sample_stream)."""
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    image_xy = np.ascontiguousarray(image_xy, np.float32)
+    dims = np.ascontiguousarray(dims, np.float32)
+    rng = np.ascontiguousarray(rng, np.float32)
+    cam, arr, p = _render_structs(r2c, c2w, xres, yres, lights, integrator, (1, 1), True, max_depth, 0, albedo)
+    L = lib()
+    L.orc_render_stream.restype = C.c_int
+    L.orc_render_stream.argtypes = [_fp, C.c_int64, C.POINTER(_Cam), C.POINTER(_Light), C.c_int,
+                                    C.POINTER(_Params), C.c_int64, _fp, _fp, C.c_int, _fp, C.c_int64, _fp,
+                                    C.c_int]
+    img = np.empty((yres, xres, 3), np.float32)
+    rc = L.orc_render_stream(_f(tris), tris.shape[0], C.byref(cam), arr, len(lights), C.byref(p),
+                             image_xy.shape[0], _f(image_xy), _f(dims), dims.shape[1], _f(rng), rng.shape[0],
+                             _f(img), threads or os.cpu_count() or 1)
+    if rc != 0:
+        raise ValueError("orc_render_stream: bad stream")
     return img
 
 
@@ -271,6 +301,50 @@ class RenderCounter:
                                  C.byref(self.p), int(first), int(stride),
                                  threads or os.cpu_count() or 1, out)
         return int(out[0]), int(out[1])
+
+
+def pbrt_task_samples(extent, spp, n1d, n2d, count, nrng, jitter=True, task=0, reference=False):
+    """One breadth-first render task's samples as pbrt draws them: RNG(task),
+    the stratified sampler over the pixel extent (x0, x1, y0, y1), spp =
+    (xsamples, ysamples), the integrators' 1-D / 2-D array sizes n1d / n2d
+    in request order; then nrng further RandomFloat draws.  reference=True
+    runs pbrt's own sampler (oracle/_ref), else the restatement
+    (oracle/pbrt_sampler.c).  Returns (image_xy [n, 2], oned [n, sum n1d],
+    twod [n, sum n2d, 2], rng [nrng])."""
+    n1d = np.ascontiguousarray(n1d, np.int32)
+    n2d = np.ascontiguousarray(n2d, np.int32)
+    img = np.zeros((count, 2), np.float32)
+    o1 = np.zeros((count, max(1, int(n1d.sum()))), np.float32)
+    o2 = np.zeros((count, max(1, int(n2d.sum())), 2), np.float32)
+    rr = np.zeros(max(1, nrng), np.float32)
+    if reference:
+        L = ref()
+        fn = L.ref_task_samples
+    else:
+        L = lib()
+        fn = L.orc_pbrt_task_samples
+    fn.restype = C.c_int64
+    fn.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _ip, C.c_int,
+                   _ip, C.c_int, C.c_int64, _fp, _fp, _fp, C.c_int64, _fp]
+    x0, x1, y0, y1 = extent
+    got = fn(task, x0, x1, y0, y1, spp[0], spp[1], int(bool(jitter)), _i(n1d), len(n1d), _i(n2d), len(n2d),
+             count, _f(img), _f(o1), _f(o2), nrng, _f(rr))
+    return img[:got], o1[:got, :int(n1d.sum())], o2[:got, :int(n2d.sum())], rr[:nrng]
+
+
+def area_light_sample(tris, L, q, reference=False):
+    """DiffuseAreaLight::Sample_L over the emitter triangles tris [n, 9] for
+    rows q [m, 7] = (p.xyz, pEpsilon, uPos[0], uPos[1], uComponent): rows of
+    (L.rgb, wi.xyz, pdf, shadow ray o.xyz, d.xyz, mint, maxt, 0).  reference=
+    True runs pbrt's own light (oracle/_ref), else the restatement."""
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    q = np.ascontiguousarray(q, np.float32).reshape(-1, 7)
+    L3 = np.ascontiguousarray(L, np.float32)
+    out = np.zeros((q.shape[0], 16), np.float32)
+    fn = ref().ref_area_light_sample if reference else lib().orc_area_light_sample
+    fn.argtypes = [_fp, C.c_int, _fp, _fp, C.c_int64, _fp]
+    fn(_f(tris), tris.shape[0], _f(L3), _f(q), q.shape[0], _f(out))
+    return out
 
 
 def ref_camera(xres, yres, eye, look, up, fov, xy):

@@ -226,3 +226,94 @@ void ref_camera(int xres, int yres, const float* eye, const float* look, const f
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ samples
+// One breadth-first task's samples from pbrt's own StratifiedSampler and RNG
+// (renderers/breadth-first.cpp:18-48, samplers/stratified.cpp:60-105), in
+// the layout of orc_pbrt_task_samples (oracle/pbrt_sampler.c), which it pins.
+#include "sampler.h"
+#include "samplers/stratified.h"
+#include "rng.h"
+
+extern "C" {
+
+int64_t ref_task_samples(uint32_t task, int x0, int x1, int y0, int y1, int spx, int spy, int jitter,
+                         const int* n1d, int k1, const int* n2d, int k2, int64_t count, float* image_xy,
+                         float* oned, float* twod, int64_t nrng, float* rng_out) {
+    StratifiedSampler sampler(x0, x1, y0, y1, spx, spy, jitter != 0, 0.f, 1.f);
+    Sample proto(NULL, NULL, NULL, NULL);
+    for (int k = 0; k < k1; ++k) proto.Add1D(n1d[k]);
+    for (int k = 0; k < k2; ++k) proto.Add2D(n2d[k]);
+    Sample* samples = proto.Duplicate((int)count);
+    RNG rng(task);
+    int64_t got = 0;
+    while (got < count) {
+        int n = sampler.GetMoreSamples(&samples[got], rng);
+        if (n == 0) break;
+        got += n;
+    }
+    int t1 = 0, t2 = 0;
+    for (int k = 0; k < k1; ++k) t1 += n1d[k];
+    for (int k = 0; k < k2; ++k) t2 += n2d[k];
+    for (int64_t i = 0; i < got; ++i) {
+        image_xy[2 * i] = samples[i].imageX;
+        image_xy[2 * i + 1] = samples[i].imageY;
+        float* o1 = oned + i * t1;
+        for (int k = 0; k < k1; ++k)
+            for (int j = 0; j < n1d[k]; ++j) *o1++ = samples[i].oneD[k][j];
+        float* o2 = twod + i * 2 * t2;
+        for (int k = 0; k < k2; ++k)
+            for (int j = 0; j < 2 * n2d[k]; ++j) *o2++ = samples[i].twoD[k][j];
+    }
+    for (int64_t k = 0; k < nrng; ++k) rng_out[k] = rng.RandomFloat();
+    delete[] samples;
+    return got;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- area light
+// pbrt's DiffuseAreaLight over a triangle mesh (lights/diffuse.cpp:61-79):
+// for each (p, eps, uPos[0], uPos[1], uComponent) row, Sample_L's radiance,
+// wi, pdf and shadow segment.  Pins the restatement of the light sampling.
+#include "lights/diffuse.h"
+
+extern "C" {
+
+// tris9: the emitter's triangles; q[n][5] = p.xyz... no: q rows are
+// (px, py, pz, eps, u0, u1, comp); out rows: L.rgb, wi.xyz, pdf, ray o.xyz,
+// d.xyz, mint, maxt (16 floats).
+void ref_area_light_sample(const float* tris9, int ntri, const float* L3, const float* q, int64_t n,
+                           float* out) {
+    Transform* identity = new Transform();
+    int nv = 3 * ntri;
+    std::vector<int> vi(nv);
+    std::vector<Point> P(nv);
+    for (int i = 0; i < nv; ++i) {
+        vi[i] = i;
+        P[i] = Point(tris9[3 * i], tris9[3 * i + 1], tris9[3 * i + 2]);
+    }
+    Reference<Shape> mesh = new TriangleMesh(identity, identity, false, ntri, nv, &vi[0], &P[0], NULL, NULL,
+                                             NULL, NULL);
+    float rgb[3] = {L3[0], L3[1], L3[2]};
+    DiffuseAreaLight light(Transform(), RGBSpectrum::FromRGB(rgb), 1, mesh);
+    for (int64_t i = 0; i < n; ++i) {
+        const float* r = q + 7 * i;
+        LightSample ls(r[4], r[5], r[6]);
+        Vector wi;
+        float pdf;
+        VisibilityTester vis;
+        Spectrum Ls = light.Sample_L(Point(r[0], r[1], r[2]), r[3], ls, 0.f, &wi, &pdf, &vis);
+        float c[3];
+        Ls.ToRGB(c);
+        float* o = out + 16 * i;
+        o[0] = c[0]; o[1] = c[1]; o[2] = c[2];
+        o[3] = wi.x; o[4] = wi.y; o[5] = wi.z;
+        o[6] = pdf;
+        o[7] = vis.r.o.x; o[8] = vis.r.o.y; o[9] = vis.r.o.z;
+        o[10] = vis.r.d.x; o[11] = vis.r.d.y; o[12] = vis.r.d.z;
+        o[13] = vis.r.mint; o[14] = vis.r.maxt; o[15] = 0.f;
+    }
+}
+
+}  // extern "C"

@@ -13,19 +13,33 @@
 //              spp consecutive samples (the breadth-first ray image);
 //   trace      the scene's accelerator (pbg_*_device) on the live queue;
 //   shade      Lambertian BSDF (core/reflection.cpp:165), light sampling
-//              (lights/point.cpp, a parallelogram area light), pbrt's
-//              EstimateDirect weights (core/integrator.cpp:212-298), one
-//              shadow slot per light sample and one bounce slot per path;
+//              (lights/point.cpp; lights/diffuse.cpp over scene triangles as
+//              ShapeSet samples them, core/light.cpp:137-165; a
+//              parallelogram emitter), the batch integrators' EstimateDirect
+//              (core/integrator.cpp:212-298 for path, :358-455 for
+//              directlighting, each with its own operation order), emission
+//              at camera hits on emitting triangles, one shadow slot per
+//              light sample and one bounce slot per path;
 //   compact    slots -> dense queues, order-preserving: per-warp ballots give
 //              ranks inside a block, a block scan gives block offsets;
 //   resolve    unoccluded shadow contributions added per sample in light
 //              sample order (deterministic, no float atomics);
 //   film       per pixel, samples in order, through XYZ as ImageFilm does
-//              (film/image.cpp AddSample / WriteImage), box filter.
+//              (film/image.cpp AddSample / WriteImage), box filter; samples
+//              whose radiance breadthFirst::Li would reject (NaN, negative or
+//              infinite luminance) count as black.
 //
-// Random numbers: a counter-based hash of (seed, sample, dimension) -- not
-// pbrt's MT19937 streams -- identical on every run and in the oracle's
-// restatement.
+// Random numbers: by default a counter-based hash of (seed, sample,
+// dimension), identical on every run and in the oracle's restatement.  With
+// a sample stream (pbg_render_stream) the values are the reference's own:
+// the caller passes one task's samples as pbrt's StratifiedSampler drew them
+// and the continuation of the task's RNG, which the renderer consumes in
+// the order the batch integrators do -- path tracing below bounce 3 reads
+// the sample arrays (integrators/path.cpp:31-38), from bounce 3 on
+// UniformSampleOneLight draws 7 values for every ray of the task, then each
+// ray that hit draws its BSDF sample (3) and, after bounce 3, its Russian
+// roulette value (1), in ray order (core/integrator.cpp:142-165,
+// integrators/path.cpp:104-124).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -54,8 +68,11 @@ __device__ __forceinline__ float rnd(uint64_t seed, uint64_t sample, uint32_t di
 }
 
 // Sample dimensions: 0-1 image, then 16 per bounce: light samples from 0,
-// Russian roulette at 13, BSDF sample at 14-15.
+// Russian roulette at 13, BSDF sample at 14-15.  The light-sample
+// components of triangle emitters and the light choice of the path
+// integrator use a second family from 512.
 __device__ __forceinline__ uint32_t dim_of(int bounce, int k) { return 2u + 16u * (uint32_t)bounce + (uint32_t)k; }
+__device__ __forceinline__ uint32_t dim_extra(int bounce, int k) { return 512u + 16u * (uint32_t)bounce + (uint32_t)k; }
 constexpr int kDimRR = 13, kDimBsdf = 14;
 
 // sin and cos in float from the Cephes single-precision polynomials
@@ -86,6 +103,8 @@ struct DevLight {
     int type, nsamples;
     float pos[3], I[3];
     float q0[3], e1[3], e3[3], n[3], area, L[3];
+    int first, ntri;  // triangle emitter: scene triangles [first, first + ntri)
+    int tab;          // ... its areas, CDF and total area in the light table
 };
 
 struct RenderConst {
@@ -95,21 +114,41 @@ struct RenderConst {
     float albedo[3];
     int nlights;
     DevLight lights[4];
+    int stream;           // 1: sample values from the caller's stream
+    const float* ltab;    // triangle emitters: areas[ntri], cdf[ntri + 1], sum
 };
 
-__global__ void raygen_kernel(RenderConst rc, int64_t n, float4* __restrict__ o4, float4* __restrict__ d4,
-                              int32_t* __restrict__ qidx, float* __restrict__ L, float* __restrict__ beta) {
+// The caller's sample stream on the device (see pbg_sample_stream).
+struct StreamArgs {
+    const float* img;        // [count][2] raster position
+    const float* dims;       // [count][ndims]
+    const float* rng;        // the task RNG's draws after the sampler's
+    int64_t count, nrng;
+    int ndims;
+    int64_t rng_base;        // path, bounces >= 3: this bounce's first draw
+    const int32_t* hit_rank; // ... and each queue entry's rank among its hits
+};
+
+__global__ void raygen_kernel(RenderConst rc, StreamArgs sa, int64_t n, float4* __restrict__ o4,
+                              float4* __restrict__ d4, int32_t* __restrict__ qidx, float* __restrict__ L,
+                              float* __restrict__ beta) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const int64_t pix = s / rc.spp;
-    const int k = (int)(s % rc.spp);
-    const int px = (int)(pix % rc.xres), py = (int)(pix / rc.xres);
-    const int sx = k % rc.spp_x, sy = k / rc.spp_x;
-    const float jx = rc.jitter ? rnd(rc.seed, (uint64_t)s, 0) : 0.5f;
-    const float jy = rc.jitter ? rnd(rc.seed, (uint64_t)s, 1) : 0.5f;
-    // (x + jx) * dx + xPos (samplers/stratified.cpp, StratifiedSample2D)
-    const float ix = __fadd_rn(__fmul_rn(__fadd_rn((float)sx, jx), __frcp_rn((float)rc.spp_x)), (float)px);
-    const float iy = __fadd_rn(__fmul_rn(__fadd_rn((float)sy, jy), __frcp_rn((float)rc.spp_y)), (float)py);
+    float ix, iy;
+    if (rc.stream) {
+        ix = sa.img[2 * s];
+        iy = sa.img[2 * s + 1];
+    } else {
+        const int64_t pix = s / rc.spp;
+        const int k = (int)(s % rc.spp);
+        const int px = (int)(pix % rc.xres), py = (int)(pix / rc.xres);
+        const int sx = k % rc.spp_x, sy = k / rc.spp_x;
+        const float jx = rc.jitter ? rnd(rc.seed, (uint64_t)s, 0) : 0.5f;
+        const float jy = rc.jitter ? rnd(rc.seed, (uint64_t)s, 1) : 0.5f;
+        // (x + jx) * dx + xPos (samplers/stratified.cpp, StratifiedSample2D)
+        ix = __fadd_rn(__fmul_rn(__fadd_rn((float)sx, jx), __frcp_rn((float)rc.spp_x)), (float)px);
+        iy = __fadd_rn(__fmul_rn(__fadd_rn((float)sy, jy), __frcp_rn((float)rc.spp_y)), (float)py);
+    }
     const V3 pc = xform_point(rc.r2c, v3(ix, iy, 0.f));
     const V3 dir = vnormalize(pc);
     const V3 o = xform_point(rc.c2w, v3(0.f, 0.f, 0.f));
@@ -132,8 +171,82 @@ struct Frame {
     }
 };
 
-// Light sample j of light l at p: wi, radiance, pdf, shadow segment.
-__device__ __forceinline__ bool sample_light(const DevLight& lt, V3 p, float eps, float u1, float u2,
+__device__ __forceinline__ V3 tri_vertex(const float* v9, int k) { return v3(v9[3 * k], v9[3 * k + 1], v9[3 * k + 2]); }
+
+// The scene triangle of an emitter's i-th ShapeSet shape: the ShapeSet
+// constructor refines the mesh through a stack (todo.back(),
+// core/light.cpp:106-118), so the mesh's triangles come out last first.
+__device__ __forceinline__ int64_t shape_tri(int first, int n, int i) { return (int64_t)first + n - 1 - i; }
+
+// Triangle::Intersect of one emitter triangle (shapes/trianglemesh.cpp:119-190):
+// pbrt's exact test, and the hit's geometric normal.
+__device__ bool emitter_hit(const float* v9, const float* uv6, V3 o, V3 d, float mint, float* t, V3* nn) {
+    const V3 p1 = tri_vertex(v9, 0), e1 = vsub(tri_vertex(v9, 1), p1), e2 = vsub(tri_vertex(v9, 2), p1);
+    float tt, b1, b2;
+    if (!pbg_exact(p1.x, p1.y, p1.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z, o.x, o.y, o.z, d.x, d.y, d.z, mint,
+                   INFINITY, &tt, &b1, &b2))
+        return false;
+    *t = tt;
+    *nn = hit_dg(v9, uv6, o, d, tt, b1, b2).nn;
+    return true;
+}
+
+// DiffuseAreaLight::Sample_L over scene triangles (lights/diffuse.cpp:61-73):
+// ShapeSet::Sample picks a triangle by its area CDF and a point on it
+// (Triangle::Sample, UniformSampleTriangle), re-intersects the ray from p
+// towards it with every triangle of the set (the last one hit gives the
+// point and its normal), ShapeSet::Pdf sums each triangle's solid-angle pdf
+// weighted by its area (core/light.cpp:137-165, core/shape.cpp:78-91).
+__device__ void sample_emitter(const DevLight& lt, const float* ltab, const float* tri9, const float* uv6, V3 p,
+                               float u0, float u1, float comp, V3* wi, V3* Li, float* pdf, V3* target) {
+    const int n = lt.ntri;
+    const float* areas = ltab + lt.tab;
+    const float* cdf = areas + n;
+    const float sum_area = cdf[n + 1];
+    int k = 0;  // upper_bound: first CDF entry above comp
+    while (k < n + 1 && !(cdf[k] > comp)) ++k;
+    const int sn = k > 0 ? k - 1 : 0;
+    const float* v = tri9 + 9 * shape_tri(lt.first, n, sn);
+    const float su1 = __fsqrt_rn(u0);
+    const float b1 = __fsub_rn(1.f, su1), b2 = __fmul_rn(u1, su1);
+    const float b0 = __fsub_rn(__fsub_rn(1.f, b1), b2);
+    const V3 p1 = tri_vertex(v, 0), p2 = tri_vertex(v, 1), p3 = tri_vertex(v, 2);
+    const V3 pt = vadd(vadd(vmul(p1, b1), vmul(p2, b2)), vmul(p3, b0));
+    V3 ns = vnormalize(vcross(vsub(p2, p1), vsub(p3, p1)));
+    const V3 dir = vsub(pt, p);
+    float thit = 1.f;
+    for (int i = 0; i < n; ++i) {
+        const int64_t tr = shape_tri(lt.first, n, i);
+        float t;
+        V3 nn;
+        if (emitter_hit(tri9 + 9 * tr, uv6 ? uv6 + 6 * tr : nullptr, p, dir, 1e-3f, &t, &nn)) {
+            thit = t;
+            ns = nn;
+        }
+    }
+    const V3 ps = vadd(p, vmul(dir, thit));
+    *target = ps;
+    *wi = vnormalize(vsub(ps, p));
+    float acc = 0.f;
+    for (int i = 0; i < n; ++i) {
+        const int64_t tr = shape_tri(lt.first, n, i);
+        float t, pi = 0.f;
+        V3 nn;
+        if (emitter_hit(tri9 + 9 * tr, uv6 ? uv6 + 6 * tr : nullptr, p, *wi, 1e-3f, &t, &nn)) {
+            const V3 dv = vsub(p, vadd(p, vmul(*wi, t)));
+            pi = __fdiv_rn(vdot(dv, dv), __fmul_rn(fabsf(vdot(nn, vneg(*wi))), areas[i]));
+            if (isinf(pi)) pi = 0.f;
+        }
+        acc = __fadd_rn(acc, __fmul_rn(areas[i], pi));
+    }
+    *pdf = __fdiv_rn(acc, sum_area);
+    *Li = vdot(ns, vneg(*wi)) > 0.f ? v3(lt.L[0], lt.L[1], lt.L[2]) : v3(0.f, 0.f, 0.f);
+}
+
+// Light sample (u0, u1, comp) of light lt at p: wi, radiance, pdf and the
+// shadow segment (VisibilityTester::SetSegment, core/light.h:79-84).
+__device__ __forceinline__ bool sample_light(const RenderConst& rc, const DevLight& lt, const float* tri9,
+                                             const float* uv6, V3 p, float eps, float u1, float u2, float comp,
                                              V3* wi, V3* Li, float* pdf, float4* so, float4* sd) {
     V3 target;
     float eps2;
@@ -145,6 +258,9 @@ __device__ __forceinline__ bool sample_light(const DevLight& lt, V3 p, float eps
         const float d2 = vdot(dv, dv);
         *Li = v3(__fdiv_rn(lt.I[0], d2), __fdiv_rn(lt.I[1], d2), __fdiv_rn(lt.I[2], d2));
         eps2 = 0.f;
+    } else if (lt.type == PBG_LIGHT_MESH) {
+        sample_emitter(lt, rc.ltab, tri9, uv6, p, u1, u2, comp, wi, Li, pdf, &target);
+        eps2 = 1e-3f;
     } else {
         const V3 q0 = v3(lt.q0[0], lt.q0[1], lt.q0[2]);
         target = vadd(vadd(q0, vmul(v3(lt.e1[0], lt.e1[1], lt.e1[2]), u1)),
@@ -158,7 +274,6 @@ __device__ __forceinline__ bool sample_light(const DevLight& lt, V3 p, float eps
         *Li = v3(lt.L[0], lt.L[1], lt.L[2]);
         eps2 = 1e-3f;
     }
-    // VisibilityTester::SetSegment (core/light.h:79-84)
     const float dist = vlen(vsub(p, target));
     const V3 dn = vmul(vsub(target, p), __frcp_rn(dist));
     *so = make_float4(p.x, p.y, p.z, eps);
@@ -166,8 +281,71 @@ __device__ __forceinline__ bool sample_light(const DevLight& lt, V3 p, float eps
     return true;
 }
 
-// One queue entry: shade the hit, fill its shadow slots and its bounce slot.
-__global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32_t* __restrict__ qidx,
+// Sample values of one vertex: the hash stream, or the caller's stream in
+// the layout of pbg_sample_stream.
+struct Draws {
+    const RenderConst& rc;
+    const StreamArgs& sa;
+    int64_t s, j;
+    int bounce;
+    // light sample m of a directlighting vertex (hash: light-local index q)
+    __device__ void direct_light(int m, int q, float* u0, float* u1, float* comp) const {
+        if (rc.stream) {
+            const float* v = sa.dims + s * sa.ndims + 6 * m;
+            *u0 = v[0];
+            *u1 = v[1];
+            *comp = v[2];
+        } else {
+            *u0 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, 2 * q));
+            *u1 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, 2 * q) + 1);
+            *comp = rnd(rc.seed, (uint64_t)s, dim_extra(bounce, m));
+        }
+    }
+    // the path integrator's light choice and light sample at this bounce
+    __device__ void path_light(float* lnum, float* u0, float* u1, float* comp) const {
+        if (!rc.stream) {
+            *lnum = rnd(rc.seed, (uint64_t)s, dim_extra(bounce, 15));
+            *u0 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, 0));
+            *u1 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, 1));
+            *comp = rnd(rc.seed, (uint64_t)s, dim_extra(bounce, 0));
+        } else if (bounce < 3) {
+            const float* v = sa.dims + s * sa.ndims + 10 * bounce;
+            *lnum = v[0];
+            *u0 = v[1];
+            *u1 = v[2];
+            *comp = v[3];
+        } else {
+            const float* v = sa.rng + sa.rng_base + 7 * s;
+            *lnum = v[0];
+            *u0 = v[1];
+            *u1 = v[2];
+            *comp = v[3];
+        }
+    }
+    // the path's BSDF sample (uDir) and Russian roulette value
+    __device__ void path_bsdf(float* u0, float* u1) const {
+        if (!rc.stream) {
+            *u0 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, kDimBsdf));
+            *u1 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, kDimBsdf + 1));
+        } else if (bounce < 3) {
+            const float* v = sa.dims + s * sa.ndims + 10 * bounce;
+            *u0 = v[7];
+            *u1 = v[8];
+        } else {
+            const float* v = sa.rng + sa.rng_base + 7 * sa.count + (int64_t)sa.hit_rank[j] * (bounce > 3 ? 4 : 3);
+            *u0 = v[0];
+            *u1 = v[1];
+        }
+    }
+    __device__ float path_rr() const {
+        if (!rc.stream) return rnd(rc.seed, (uint64_t)s, dim_of(bounce, kDimRR));
+        return sa.rng[sa.rng_base + 7 * sa.count + (int64_t)sa.hit_rank[j] * 4 + 3];
+    }
+};
+
+// One queue entry: shade the hit, fill its shadow slots, its bounce slot and
+// its emission (camera hits on emitting triangles).
+__global__ void shade_kernel(RenderConst rc, StreamArgs sa, int bounce, int64_t nq, const int32_t* __restrict__ qidx,
                              const float4* __restrict__ qo, const float4* __restrict__ qd,
                              const int32_t* __restrict__ prim, const float* __restrict__ th,
                              const float* __restrict__ b1v, const float* __restrict__ b2v,
@@ -175,14 +353,17 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
                              float* __restrict__ beta, int kslots, float4* __restrict__ so,
                              float4* __restrict__ sd, float* __restrict__ scontrib,
                              uint8_t* __restrict__ sflag, float4* __restrict__ no,
-                             float4* __restrict__ nd_, uint8_t* __restrict__ nflag) {
+                             float4* __restrict__ nd_, uint8_t* __restrict__ nflag, float* __restrict__ emit,
+                             int* __restrict__ rstat) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nq) return;
     for (int k = 0; k < kslots; ++k) sflag[j * kslots + k] = 0;
     nflag[j] = 0;
+    emit[3 * j] = emit[3 * j + 1] = emit[3 * j + 2] = 0.f;
     const int32_t pr = prim[j];
     if (pr < 0) return;  // miss: no environment light
     const int64_t s = qidx[j];
+    const Draws dr{rc, sa, s, j, bounce};
     const float4 o4 = qo[j], d4 = qd[j];
     const V3 ro = v3(o4.x, o4.y, o4.z), rdir = v3(d4.x, d4.y, d4.z);
     const float t = th[j];
@@ -195,6 +376,17 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
     fr.tn = vcross(fr.nn, fr.sn);
     const V3 ng = g.nn;
     const V3 wo = vneg(rdir);
+    // Intersection::Le at camera hits (DiffuseAreaLight::L, lights/diffuse.h:43-45)
+    if (bounce == 0) {
+        for (int l = 0; l < rc.nlights; ++l) {
+            const DevLight& lt = rc.lights[l];
+            if (lt.type == PBG_LIGHT_MESH && pr >= lt.first && pr < lt.first + lt.ntri && vdot(g.nn, wo) > 0.f) {
+                emit[3 * j] = lt.L[0];
+                emit[3 * j + 1] = lt.L[1];
+                emit[3 * j + 2] = lt.L[2];
+            }
+        }
+    }
     const V3 R = v3(rc.albedo[0], rc.albedo[1], rc.albedo[2]);
     const V3 fR = v3(__fmul_rn(R.x, kInvPi), __fmul_rn(R.y, kInvPi), __fmul_rn(R.z, kInvPi));
     const V3 bt = v3(beta[3 * s], beta[3 * s + 1], beta[3 * s + 2]);
@@ -202,30 +394,49 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
     const V3 wol = fr.to_local(wo);
 
     // Direct lighting: every light and sample (directlighting) or one light
-    // sample (path), core/integrator.cpp:73-176.
+    // sample (path).
     const bool all = rc.integrator == PBG_INTEGRATOR_DIRECT;
     int slot = 0;
-    for (int l = 0; l < rc.nlights; ++l) {
+    int first_light = 0, last_light = rc.nlights;
+    float pu0 = 0.f, pu1 = 0.f, pcomp = 0.f;
+    if (!all && rc.nlights > 0) {
+        // UniformSampleOneLight: lightNum = min(Floor2Int(u * nLights), nLights - 1)
+        float lnum;
+        dr.path_light(&lnum, &pu0, &pu1, &pcomp);
+        first_light = min((int)floorf(__fmul_rn(lnum, (float)rc.nlights)), rc.nlights - 1);
+        last_light = first_light + 1;
+    }
+    for (int l = first_light; l < last_light; ++l) {
         const DevLight& lt = rc.lights[l];
         const int ns = all ? (lt.type == PBG_LIGHT_POINT ? 1 : max(lt.nsamples, 1)) : 1;
-        if (!all && l > 0) break;  // UniformSampleOneLight: one light per vertex
         for (int q = 0; q < ns; ++q, ++slot) {
-            const float u1 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, 2 * q) + 0);
-            const float u2 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, 2 * q) + 1);
+            float u1, u2, comp;
+            if (all) {
+                dr.direct_light(slot, q, &u1, &u2, &comp);
+            } else {
+                u1 = pu0;
+                u2 = pu1;
+                comp = pcomp;
+            }
             V3 wi, Li;
             float pdf;
             float4 o_, d_;
             if (slot >= kslots) break;
-            if (!sample_light(lt, g.p, eps, u1, u2, &wi, &Li, &pdf, &o_, &d_)) continue;
+            if (!sample_light(rc, lt, tri9, uv6, g.p, eps, u1, u2, comp, &wi, &Li, &pdf, &o_, &d_)) continue;
             if (!(pdf > 0.f) || (Li.x == 0.f && Li.y == 0.f && Li.z == 0.f)) continue;
             const bool refl = __fmul_rn(vdot(wi, ng), won) > 0.f;
             if (!refl) continue;  // f = 0: Lambertian reflects only
             const float absdot = fabsf(vdot(wi, fr.nn));
+            const V3 fL = v3(__fmul_rn(fR.x, Li.x), __fmul_rn(fR.y, Li.y), __fmul_rn(fR.z, Li.z));
             V3 c;
             if (lt.type == PBG_LIGHT_POINT) {
-                const float w = __fdiv_rn(absdot, pdf);
-                c = v3(__fmul_rn(__fmul_rn(fR.x, Li.x), w), __fmul_rn(__fmul_rn(fR.y, Li.y), w),
-                       __fmul_rn(__fmul_rn(fR.z, Li.z), w));
+                if (all) {  // f * Li * AbsDot / lightPdf
+                    c = v3(__fdiv_rn(__fmul_rn(fL.x, absdot), pdf), __fdiv_rn(__fmul_rn(fL.y, absdot), pdf),
+                           __fdiv_rn(__fmul_rn(fL.z, absdot), pdf));
+                } else {    // f * Li * (AbsDot / lightPdf)
+                    const float w = __fdiv_rn(absdot, pdf);
+                    c = v3(__fmul_rn(fL.x, w), __fmul_rn(fL.y, w), __fmul_rn(fL.z, w));
+                }
             } else {
                 const V3 wil = fr.to_local(wi);
                 const bool same = __fmul_rn(wol.z, wil.z) > 0.f;
@@ -233,17 +444,20 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
                 // PowerHeuristic(1, pdf, 1, bpdf)
                 const float f2 = __fmul_rn(pdf, pdf), g2 = __fmul_rn(bpdf, bpdf);
                 const float weight = __fdiv_rn(f2, __fadd_rn(f2, g2));
-                const float w = __fdiv_rn(__fmul_rn(absdot, weight), pdf);
-                c = v3(__fmul_rn(__fmul_rn(fR.x, Li.x), w), __fmul_rn(__fmul_rn(fR.y, Li.y), w),
-                       __fmul_rn(__fmul_rn(fR.z, Li.z), w));
+                if (all) {  // f * Li * AbsDot * weight / lightPdf
+                    c = v3(__fdiv_rn(__fmul_rn(__fmul_rn(fL.x, absdot), weight), pdf),
+                           __fdiv_rn(__fmul_rn(__fmul_rn(fL.y, absdot), weight), pdf),
+                           __fdiv_rn(__fmul_rn(__fmul_rn(fL.z, absdot), weight), pdf));
+                } else {    // f * Li * (AbsDot * weight / lightPdf)
+                    const float w = __fdiv_rn(__fmul_rn(absdot, weight), pdf);
+                    c = v3(__fmul_rn(fL.x, w), __fmul_rn(fL.y, w), __fmul_rn(fL.z, w));
+                }
             }
-            if (!all) {  // UniformSampleOneLight: times nLights, then the throughput
+            if (!all) {  // Ld *= nLights, then L += pathThroughput * Ld
                 const float fl = (float)rc.nlights;
                 c = v3(__fmul_rn(c.x, fl), __fmul_rn(c.y, fl), __fmul_rn(c.z, fl));
                 c = v3(__fmul_rn(bt.x, c.x), __fmul_rn(bt.y, c.y), __fmul_rn(bt.z, c.z));
             }
-            // (directlighting divides each light's visible sum by nSamples
-            // when the shadow results are resolved)
             const int64_t si = j * kslots + slot;
             so[si] = o_;
             sd[si] = d_;
@@ -257,8 +471,8 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
 
     // BSDF sample for the next vertex (Lambertian::Sample_f, cosine-weighted
     // through ConcentricSampleDisk, core/montecarlo.cpp).
-    const float u1 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, kDimBsdf));
-    const float u2 = rnd(rc.seed, (uint64_t)s, dim_of(bounce, kDimBsdf + 1));
+    float u1, u2;
+    dr.path_bsdf(&u1, &u2);
     float sx = __fsub_rn(__fmul_rn(2.f, u1), 1.f), sy = __fsub_rn(__fmul_rn(2.f, u2), 1.f);
     float dx = 0.f, dy = 0.f;
     if (!(sx == 0.f && sy == 0.f)) {
@@ -280,9 +494,20 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
                 theta = __fadd_rn(6.f, __fdiv_rn(sx, r));
             }
         }
-        theta = __fmul_rn(theta, 0.785398163397448309616f);
         float st, ct;
-        own_sincos(theta, &st, &ct);
+        if (rc.stream) {
+            // theta *= M_PI / 4.f is a double product rounded to float; the
+            // reference's cosf/sinf come from the host's libm, here the
+            // correctly rounded value (one double evaluation, rounded once)
+            theta = __double2float_rn(__dmul_rn((double)theta, 0.78539816339744830962));
+            double ds, dc;
+            sincos((double)theta, &ds, &dc);
+            st = __double2float_rn(ds);
+            ct = __double2float_rn(dc);
+        } else {
+            theta = __fmul_rn(theta, 0.785398163397448309616f);
+            own_sincos(theta, &st, &ct);
+        }
         dx = __fmul_rn(r, ct);
         dy = __fmul_rn(r, st);
     }
@@ -292,7 +517,12 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
     const float pdf = same ? __fmul_rn(fabsf(wil.z), kInvPi) : 0.f;
     const V3 wi = fr.to_world(wil);
     const bool refl = __fmul_rn(vdot(wi, ng), won) > 0.f;
-    if (!refl || !(pdf > 0.f)) return;
+    if (!refl || !(pdf > 0.f)) {
+        // the reference keeps such a ray alive with its old direction
+        // (integrators/path.cpp:112-113); a stream render stops matching it
+        if (rc.stream) atomicAdd(&rstat[0], 1);
+        return;
+    }
     const float absdot = fabsf(vdot(wi, fr.nn));
     // pathThroughput *= f * AbsDot(wi, n) / pdf
     V3 nb = v3(__fmul_rn(bt.x, __fdiv_rn(__fmul_rn(fR.x, absdot), pdf)),
@@ -302,7 +532,7 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
         const float y = __fadd_rn(__fadd_rn(__fmul_rn(0.212671f, nb.x), __fmul_rn(0.715160f, nb.y)),
                                   __fmul_rn(0.072169f, nb.z));
         const float cont = fminf(0.5f, y);
-        if (rnd(rc.seed, (uint64_t)s, dim_of(bounce, kDimRR)) > cont) return;
+        if (dr.path_rr() > cont) return;
         nb = v3(__fdiv_rn(nb.x, cont), __fdiv_rn(nb.y, cont), __fdiv_rn(nb.z, cont));
     }
     if (bounce == rc.max_depth) return;
@@ -312,6 +542,29 @@ __global__ void shade_kernel(RenderConst rc, int bounce, int64_t nq, const int32
     no[j] = make_float4(g.p.x, g.p.y, g.p.z, eps);
     nd_[j] = make_float4(wi.x, wi.y, wi.z, INFINITY);
     nflag[j] = 1;
+}
+
+// Triangle-emitter tables: Triangle::Area (shapes/trianglemesh.cpp:276-282)
+// in ShapeSet order, the total area and the Distribution1D CDF
+// (core/montecarlo.h:48-70), in pbrt's float arithmetic.  One thread.
+__global__ void emitter_setup_kernel(const float* __restrict__ tri9, int first, int n, float* __restrict__ tab) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    float sum = 0.f;
+    for (int i = 0; i < n; ++i) {
+        const float* v = tri9 + 9 * shape_tri(first, n, i);
+        const V3 p1 = tri_vertex(v, 0);
+        const V3 c = vcross(vsub(tri_vertex(v, 1), p1), vsub(tri_vertex(v, 2), p1));
+        const float a = __fmul_rn(0.5f, vlen(c));
+        tab[i] = a;
+        sum = __fadd_rn(sum, a);
+    }
+    float* cdf = tab + n;
+    cdf[0] = 0.f;
+    for (int i = 1; i <= n; ++i) cdf[i] = __fadd_rn(cdf[i - 1], __fdiv_rn(tab[i - 1], (float)n));
+    const float integral = cdf[n];
+    for (int i = 1; i <= n; ++i)
+        cdf[i] = integral == 0.f ? __fdiv_rn((float)i, (float)n) : __fdiv_rn(cdf[i], integral);
+    cdf[n + 1] = sum;
 }
 
 // Order-preserving compaction, phase 1: per-block count of set flags.
@@ -374,36 +627,49 @@ __global__ void compact_bounce_kernel(const uint8_t* __restrict__ flag, int64_t 
     });
 }
 
-// Unoccluded shadow contributions, added per entry in slot order.
-// directlighting: per light, Ld = sum of its visible samples, L += Ld / ns
-// (UniformSampleAllLights, core/integrator.cpp:73-122); path: the single
-// slot already carries beta * nLights * Ld.
+// Stream renders, path bounces >= 3: each queue entry's rank among the
+// entries that hit (the order in which the reference's BSDF loop draws).
+__global__ void hit_flag_kernel(const int32_t* __restrict__ prim, int64_t n, uint8_t* __restrict__ flag) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flag[i] = prim[i] >= 0 ? 1 : 0;
+}
+
+__global__ void hit_rank_kernel(const uint8_t* __restrict__ flag, int64_t n, const uint32_t* __restrict__ offs,
+                                int32_t* __restrict__ rank) {
+    compact_rank(flag, n, offs, rank, [](int64_t, uint32_t) {});
+}
+
+// Unoccluded shadow contributions and emission, added per entry in slot
+// order.  directlighting: Ld = the sum over every light and sample
+// (UniformSampleAllLights' batch form, core/integrator.cpp:73-122, does not
+// divide by the sample count), L += Ld, then L += Le
+// (integrators/directlighting.cpp:112-133); path: L += Le at the camera
+// vertex, then the single slot, which already carries beta * nLights * Ld.
 __global__ void resolve_kernel(RenderConst rc, int64_t nq, int kslots, const int32_t* __restrict__ qidx,
                                const uint8_t* __restrict__ sflag, const int32_t* __restrict__ spos,
                                const uint8_t* __restrict__ occ, const float* __restrict__ scontrib,
-                               float* __restrict__ L) {
+                               const float* __restrict__ emit, float* __restrict__ L) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nq) return;
     const int64_t s = qidx[j];
     float lx = L[3 * s], ly = L[3 * s + 1], lz = L[3 * s + 2];
+    const float ex = emit[3 * j], ey = emit[3 * j + 1], ez = emit[3 * j + 2];
     if (rc.integrator == PBG_INTEGRATOR_DIRECT) {
-        int k = 0;
-        for (int l = 0; l < rc.nlights; ++l) {
-            const int ns = rc.lights[l].type == PBG_LIGHT_POINT ? 1 : max(rc.lights[l].nsamples, 1);
-            float ax = 0.f, ay = 0.f, az = 0.f;
-            for (int q = 0; q < ns && k < kslots; ++q, ++k) {
-                const int64_t si = j * kslots + k;
-                if (!sflag[si] || occ[spos[si]]) continue;
-                ax = __fadd_rn(ax, scontrib[3 * si]);
-                ay = __fadd_rn(ay, scontrib[3 * si + 1]);
-                az = __fadd_rn(az, scontrib[3 * si + 2]);
-            }
-            const float fn = (float)ns;
-            lx = __fadd_rn(lx, __fdiv_rn(ax, fn));
-            ly = __fadd_rn(ly, __fdiv_rn(ay, fn));
-            lz = __fadd_rn(lz, __fdiv_rn(az, fn));
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        for (int k = 0; k < kslots; ++k) {
+            const int64_t si = j * kslots + k;
+            if (!sflag[si] || occ[spos[si]]) continue;
+            ax = __fadd_rn(ax, scontrib[3 * si]);
+            ay = __fadd_rn(ay, scontrib[3 * si + 1]);
+            az = __fadd_rn(az, scontrib[3 * si + 2]);
         }
+        lx = __fadd_rn(__fadd_rn(lx, ax), ex);
+        ly = __fadd_rn(__fadd_rn(ly, ay), ey);
+        lz = __fadd_rn(__fadd_rn(lz, az), ez);
     } else {
+        lx = __fadd_rn(lx, ex);
+        ly = __fadd_rn(ly, ey);
+        lz = __fadd_rn(lz, ez);
         for (int k = 0; k < kslots; ++k) {
             const int64_t si = j * kslots + k;
             if (!sflag[si] || occ[spos[si]]) continue;
@@ -418,29 +684,46 @@ __global__ void resolve_kernel(RenderConst rc, int64_t nq, int kslots, const int
 }
 
 // ImageFilm: RGB -> XYZ per sample, summed in sample order, back to RGB,
-// divided by the weight sum, clamped at zero (film/image.cpp).
-__global__ void film_kernel(int64_t npix, int spp, const float* __restrict__ L, float* __restrict__ rgb) {
+// divided by the weight sum, clamped at zero (film/image.cpp).  A sample
+// whose radiance breadthFirst::Li rejects (NaN, luminance below -1e-5 or
+// infinite, renderers/breadth-first.cpp:196-213) adds black.  Samples of
+// pixel p: [off[p], off[p + 1]) of idx when a list is given (stream
+// renders), else the spp consecutive samples p * spp ...
+__device__ __forceinline__ void film_add(const float* L, int64_t s, float* X, float* Y, float* Z, float* w) {
+    float r = L[3 * s], g = L[3 * s + 1], b = L[3 * s + 2];
+    const float lum = __fadd_rn(__fadd_rn(__fmul_rn(0.212671f, r), __fmul_rn(0.715160f, g)), __fmul_rn(0.072169f, b));
+    if (isnan(r) || isnan(g) || isnan(b) || lum < -1e-5f || isinf(lum)) r = g = b = 0.f;
+    const float x = __fadd_rn(__fadd_rn(__fmul_rn(0.412453f, r), __fmul_rn(0.357580f, g)), __fmul_rn(0.180423f, b));
+    const float y = __fadd_rn(__fadd_rn(__fmul_rn(0.212671f, r), __fmul_rn(0.715160f, g)), __fmul_rn(0.072169f, b));
+    const float z = __fadd_rn(__fadd_rn(__fmul_rn(0.019334f, r), __fmul_rn(0.119193f, g)), __fmul_rn(0.950227f, b));
+    *X = __fadd_rn(*X, x);
+    *Y = __fadd_rn(*Y, y);
+    *Z = __fadd_rn(*Z, z);
+    *w = __fadd_rn(*w, 1.f);
+}
+
+__global__ void film_kernel(int64_t npix, int spp, const int32_t* __restrict__ off, const int32_t* __restrict__ idx,
+                            const float* __restrict__ L, float* __restrict__ rgb) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
     float X = 0.f, Y = 0.f, Z = 0.f, w = 0.f;
-    for (int k = 0; k < spp; ++k) {
-        const int64_t s = p * spp + k;
-        const float r = L[3 * s], g = L[3 * s + 1], b = L[3 * s + 2];
-        const float x = __fadd_rn(__fadd_rn(__fmul_rn(0.412453f, r), __fmul_rn(0.357580f, g)), __fmul_rn(0.180423f, b));
-        const float y = __fadd_rn(__fadd_rn(__fmul_rn(0.212671f, r), __fmul_rn(0.715160f, g)), __fmul_rn(0.072169f, b));
-        const float z = __fadd_rn(__fadd_rn(__fmul_rn(0.019334f, r), __fmul_rn(0.119193f, g)), __fmul_rn(0.950227f, b));
-        X = __fadd_rn(X, x);
-        Y = __fadd_rn(Y, y);
-        Z = __fadd_rn(Z, z);
-        w = __fadd_rn(w, 1.f);
+    if (off) {
+        for (int32_t k = off[p]; k < off[p + 1]; ++k) film_add(L, idx[k], &X, &Y, &Z, &w);
+    } else {
+        for (int k = 0; k < spp; ++k) film_add(L, p * spp + k, &X, &Y, &Z, &w);
     }
-    const float R = __fsub_rn(__fsub_rn(__fmul_rn(3.240479f, X), __fmul_rn(1.537150f, Y)), __fmul_rn(0.498535f, Z));
-    const float G = __fadd_rn(__fadd_rn(__fmul_rn(-0.969256f, X), __fmul_rn(1.875991f, Y)), __fmul_rn(0.041556f, Z));
-    const float B = __fadd_rn(__fsub_rn(__fmul_rn(0.055648f, X), __fmul_rn(0.204043f, Y)), __fmul_rn(1.057311f, Z));
-    const float inv = __frcp_rn(w);
-    rgb[3 * p] = fmaxf(0.f, __fmul_rn(R, inv));
-    rgb[3 * p + 1] = fmaxf(0.f, __fmul_rn(G, inv));
-    rgb[3 * p + 2] = fmaxf(0.f, __fmul_rn(B, inv));
+    float R = __fsub_rn(__fsub_rn(__fmul_rn(3.240479f, X), __fmul_rn(1.537150f, Y)), __fmul_rn(0.498535f, Z));
+    float G = __fadd_rn(__fadd_rn(__fmul_rn(-0.969256f, X), __fmul_rn(1.875991f, Y)), __fmul_rn(0.041556f, Z));
+    float B = __fadd_rn(__fsub_rn(__fmul_rn(0.055648f, X), __fmul_rn(0.204043f, Y)), __fmul_rn(1.057311f, Z));
+    if (w != 0.f) {
+        const float inv = __frcp_rn(w);
+        R = fmaxf(0.f, __fmul_rn(R, inv));
+        G = fmaxf(0.f, __fmul_rn(G, inv));
+        B = fmaxf(0.f, __fmul_rn(B, inv));
+    }
+    rgb[3 * p] = R;
+    rgb[3 * p + 1] = G;
+    rgb[3 * p + 2] = B;
 }
 
 // ------------------------------------------------------------------ host
@@ -449,11 +732,13 @@ int scan_counts(pbg_scene* s, uint32_t* a, int64_t m, cudaStream_t st);
 
 struct RenderBuffers {
     DeviceBuffer o4, d4, qidx, L, beta, prim, t, b1, b2, so, sd, scontrib, sflag, spos, sqo, sqd, occ,
-        no, nd, nflag, qidx2, o42, d42, counts, rgb;
+        no, nd, nflag, qidx2, o42, d42, counts, rgb, emit, rstat, ltab, simg, sdims, srng, hflag, hrank,
+        foff, fidx;
     ~RenderBuffers() {
-        DeviceBuffer* all[] = {&o4, &d4, &qidx, &L, &beta, &prim, &t, &b1, &b2, &so, &sd, &scontrib,
-                               &sflag, &spos, &sqo, &sqd, &occ, &no, &nd, &nflag, &qidx2, &o42, &d42,
-                               &counts, &rgb};
+        DeviceBuffer* all[] = {&o4,  &d4,  &qidx,  &L,   &beta,  &prim,  &t,     &b1,  &b2,    &so,   &sd,
+                               &scontrib, &sflag, &spos, &sqo, &sqd, &occ, &no, &nd, &nflag, &qidx2, &o42,
+                               &d42, &counts, &rgb, &emit, &rstat, &ltab, &simg, &sdims, &srng, &hflag, &hrank,
+                               &foff, &fidx};
         for (DeviceBuffer* b : all) release(*b);
     }
 };
@@ -480,10 +765,22 @@ static int compact_count(pbg_scene* s, const uint8_t* flag, int64_t n, uint32_t*
     return PBG_OK;
 }
 
+// The pixels a sample at (x, y) adds to: ImageFilm::AddSample's footprint of
+// the box filter of radius 0.5 (film/image.cpp), clipped to the image.
+static void film_footprint(float x, float y, int xres, int yres, int* x0, int* x1, int* y0, int* y1) {
+    const float dx = x - 0.5f, dy = y - 0.5f;
+    *x0 = std::max((int)std::ceil(dx - 0.5f), 0);
+    *x1 = std::min((int)std::floor(dx + 0.5f), xres - 1);
+    *y0 = std::max((int)std::ceil(dy - 0.5f), 0);
+    *y1 = std::min((int)std::floor(dy + 0.5f), yres - 1);
+}
+
 int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t nlights,
-           const pbg_render_params* prm, float* rgb_host, pbg_render_stats* stats) {
+           const pbg_render_params* prm, const pbg_sample_stream* stream, float* rgb_host,
+           pbg_render_stats* stats) {
     if (!cam || !prm || nlights < 0 || nlights > 4 || (nlights > 0 && !lights) || !rgb_host ||
-        cam->xres <= 0 || cam->yres <= 0 || prm->spp_x <= 0 || prm->spp_y <= 0) {
+        cam->xres <= 0 || cam->yres <= 0 || prm->spp_x <= 0 || prm->spp_y <= 0 ||
+        (prm->integrator != PBG_INTEGRATOR_DIRECT && prm->integrator != PBG_INTEGRATOR_PATH)) {
         set_last_error("pbg_render: bad arguments");
         return PBG_ERR_INVALID_ARGUMENT;
     }
@@ -499,9 +796,10 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     rc.max_depth = prm->max_depth > 0 ? prm->max_depth : 5;
     rc.integrator = prm->integrator;
     rc.seed = prm->seed;
+    rc.stream = stream != nullptr;
     for (int k = 0; k < 3; ++k) rc.albedo[k] = prm->albedo[k];
     rc.nlights = nlights;
-    int kslots = 0;
+    int kslots = 0, ltab_floats = 0;
     for (int l = 0; l < nlights; ++l) {
         const pbg_light& in = lights[l];
         DevLight& d = rc.lights[l];
@@ -514,6 +812,19 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
             d.e1[k] = in.quad[3 + k] - in.quad[k];
             d.e3[k] = in.quad[9 + k] - in.quad[k];
             d.L[k] = in.radiance[k];
+        }
+        if (in.type == PBG_LIGHT_MESH) {
+            if (in.ntri <= 0 || in.ntri > 64 || in.first_tri < 0 || (int64_t)in.first_tri + in.ntri > s->ntri) {
+                set_last_error("pbg_render: a triangle emitter needs 1..64 triangles of the scene");
+                return PBG_ERR_INVALID_ARGUMENT;
+            }
+            d.first = in.first_tri;
+            d.ntri = in.ntri;
+            d.tab = ltab_floats;
+            ltab_floats += 2 * in.ntri + 2;
+        } else if (in.type != PBG_LIGHT_POINT && in.type != PBG_LIGHT_QUAD) {
+            set_last_error("pbg_render: unknown light type");
+            return PBG_ERR_INVALID_ARGUMENT;
         }
         const double cx = (double)d.e1[1] * d.e3[2] - (double)d.e1[2] * d.e3[1];
         const double cy = (double)d.e1[2] * d.e3[0] - (double)d.e1[0] * d.e3[2];
@@ -530,10 +841,19 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     }
     if (kslots == 0) kslots = 1;
     const int64_t npix = (int64_t)cam->xres * cam->yres;
-    const int64_t n = npix * rc.spp;
-    if (n > (int64_t)INT32_MAX / std::max(kslots, 1)) {
-        set_last_error("pbg_render: image too large for one batch");
+    const int64_t n = stream ? stream->count : npix * rc.spp;
+    if (n <= 0 || n > (int64_t)INT32_MAX / std::max(kslots, 1)) {
+        set_last_error("pbg_render: image too large for one batch, or an empty sample stream");
         return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (stream) {
+        const int need = prm->integrator == PBG_INTEGRATOR_PATH ? 30 : 6 * kslots;
+        if (!stream->image_xy || !stream->dims || stream->ndims < need || stream->nrng < 0 ||
+            (stream->nrng > 0 && !stream->rng)) {
+            set_last_error("pbg_render_stream: the stream needs image positions, the sample values of its layout "
+                           "(30 per sample for path, 6 per light sample for directlighting) and its RNG draws");
+            return PBG_ERR_INVALID_ARGUMENT;
+        }
     }
     cudaStream_t st = s->stream;
     if (!s->render_bufs) s->render_bufs = new RenderBuffers();
@@ -547,21 +867,74 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
         (r = ensure(B.sflag, nk)) || (r = ensure(B.spos, nk * 4)) || (r = ensure(B.sqo, nk * 16)) ||
         (r = ensure(B.sqd, nk * 16)) || (r = ensure(B.occ, nk)) || (r = ensure(B.no, n * 16)) ||
         (r = ensure(B.nd, n * 16)) || (r = ensure(B.nflag, n)) || (r = ensure(B.qidx2, n * 4)) ||
-        (r = ensure(B.o42, n * 16)) || (r = ensure(B.d42, n * 16)) ||
-        (r = ensure(B.counts, ((nk + 255) / 256 + 64) * 4 + 4096)) || (r = ensure(B.rgb, npix * 12)))
+        (r = ensure(B.o42, n * 16)) || (r = ensure(B.d42, n * 16)) || (r = ensure(B.emit, n * 12)) ||
+        (r = ensure(B.counts, ((nk + 255) / 256 + 64) * 4 + 4096)) || (r = ensure(B.rgb, npix * 12)) ||
+        (r = ensure(B.rstat, 16)) || (r = ensure(B.ltab, (size_t)std::max(ltab_floats, 1) * 4)))
         return r;
+    PBG_CUDA(cudaMemsetAsync(B.rstat.ptr, 0, 16, st));
+    rc.ltab = (const float*)B.ltab.ptr;
+    for (int l = 0; l < nlights; ++l)
+        if (rc.lights[l].type == PBG_LIGHT_MESH) {
+            emitter_setup_kernel<<<1, 32, 0, st>>>((const float*)s->tri9.ptr, rc.lights[l].first, rc.lights[l].ntri,
+                                                   (float*)B.ltab.ptr + rc.lights[l].tab);
+            PBG_CUDA(cudaGetLastError());
+            s->counters.kernel_launches += 1;
+        }
+    StreamArgs sa{};
+    const int32_t* film_off = nullptr;
+    const int32_t* film_idx = nullptr;
+    if (stream) {
+        // the caller's sample values, and each pixel's samples in order
+        const size_t nd = (size_t)stream->ndims;
+        std::vector<int32_t> cnt(npix + 1, 0);
+        for (int64_t i = 0; i < n; ++i) {
+            int x0, x1, y0, y1;
+            film_footprint(stream->image_xy[2 * i], stream->image_xy[2 * i + 1], cam->xres, cam->yres, &x0, &x1, &y0, &y1);
+            for (int y = y0; y <= y1; ++y)
+                for (int x = x0; x <= x1; ++x) cnt[(int64_t)y * cam->xres + x + 1]++;
+        }
+        for (int64_t p = 0; p < npix; ++p) cnt[p + 1] += cnt[p];
+        std::vector<int32_t> idx(std::max<int32_t>(cnt[npix], 1)), fill(cnt.begin(), cnt.end() - 1);
+        for (int64_t i = 0; i < n; ++i) {
+            int x0, x1, y0, y1;
+            film_footprint(stream->image_xy[2 * i], stream->image_xy[2 * i + 1], cam->xres, cam->yres, &x0, &x1, &y0, &y1);
+            for (int y = y0; y <= y1; ++y)
+                for (int x = x0; x <= x1; ++x) idx[fill[(int64_t)y * cam->xres + x]++] = (int32_t)i;
+        }
+        if ((r = ensure(B.simg, n * 8)) || (r = ensure(B.sdims, n * nd * 4)) ||
+            (r = ensure(B.srng, (size_t)std::max<int64_t>(stream->nrng, 1) * 4)) || (r = ensure(B.hflag, n)) ||
+            (r = ensure(B.hrank, n * 4)) || (r = ensure(B.foff, (npix + 1) * 4)) ||
+            (r = ensure(B.fidx, idx.size() * 4)))
+            return r;
+        PBG_CUDA(cudaMemcpyAsync(B.simg.ptr, stream->image_xy, n * 8, cudaMemcpyHostToDevice, st));
+        PBG_CUDA(cudaMemcpyAsync(B.sdims.ptr, stream->dims, n * nd * 4, cudaMemcpyHostToDevice, st));
+        if (stream->nrng > 0)
+            PBG_CUDA(cudaMemcpyAsync(B.srng.ptr, stream->rng, stream->nrng * 4, cudaMemcpyHostToDevice, st));
+        PBG_CUDA(cudaMemcpyAsync(B.foff.ptr, cnt.data(), (npix + 1) * 4, cudaMemcpyHostToDevice, st));
+        PBG_CUDA(cudaMemcpyAsync(B.fidx.ptr, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, st));
+        PBG_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+        sa.img = (const float*)B.simg.ptr;
+        sa.dims = (const float*)B.sdims.ptr;
+        sa.rng = (const float*)B.srng.ptr;
+        sa.count = n;
+        sa.nrng = stream->nrng;
+        sa.ndims = stream->ndims;
+        film_off = (const int32_t*)B.foff.ptr;
+        film_idx = (const int32_t*)B.fidx.ptr;
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
     raygen_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        rc, n, (float4*)B.o4.ptr, (float4*)B.d4.ptr, (int32_t*)B.qidx.ptr, (float*)B.L.ptr,
+        rc, sa, n, (float4*)B.o4.ptr, (float4*)B.d4.ptr, (int32_t*)B.qidx.ptr, (float*)B.L.ptr,
         (float*)B.beta.ptr);
     PBG_CUDA(cudaGetLastError());
     s->counters.kernel_launches += 1;
     pbg_render_stats stt{};
     stt.camera_rays = (uint64_t)n;
     int64_t nq = n;
+    int64_t rng_base = 0;
     // queue arrays alternate between (qidx, o4, d4) and (qidx2, o42, d42)
     int32_t* qi = (int32_t*)B.qidx.ptr;
     float4* qo = (float4*)B.o4.ptr;
@@ -581,15 +954,35 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
                                       (float*)B.b2.ptr, st)))
             return r;
         stt.nearest_rays += (uint64_t)nq;
+        const bool draws = stream && rc.integrator == PBG_INTEGRATOR_PATH && bounce >= 3;
+        int64_t nhits = 0;
+        if (draws) {
+            hit_flag_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>((const int32_t*)B.prim.ptr, nq,
+                                                                           (uint8_t*)B.hflag.ptr);
+            PBG_CUDA(cudaGetLastError());
+            s->counters.kernel_launches += 1;
+            if ((r = compact_count(s, (const uint8_t*)B.hflag.ptr, nq, (uint32_t*)B.counts.ptr, &nhits, st))) return r;
+            hit_rank_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(
+                (const uint8_t*)B.hflag.ptr, nq, (const uint32_t*)B.counts.ptr, (int32_t*)B.hrank.ptr);
+            PBG_CUDA(cudaGetLastError());
+            s->counters.kernel_launches += 1;
+            if (rng_base + 7 * n + nhits * (bounce > 3 ? 4 : 3) > stream->nrng) {
+                set_last_error("pbg_render_stream: the stream's RNG draws ran out");
+                return PBG_ERR_INVALID_ARGUMENT;
+            }
+            sa.rng_base = rng_base;
+            sa.hit_rank = (const int32_t*)B.hrank.ptr;
+        }
         const int64_t nslots = nq * kslots;
         shade_kernel<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>(
-            rc, bounce, nq, qi, qo, qd, (const int32_t*)B.prim.ptr, (const float*)B.t.ptr,
+            rc, sa, bounce, nq, qi, qo, qd, (const int32_t*)B.prim.ptr, (const float*)B.t.ptr,
             (const float*)B.b1.ptr, (const float*)B.b2.ptr, (const float*)s->tri9.ptr,
             (const float*)s->uv6.ptr, (float*)B.beta.ptr, kslots, (float4*)B.so.ptr, (float4*)B.sd.ptr,
             (float*)B.scontrib.ptr, (uint8_t*)B.sflag.ptr, (float4*)B.no.ptr, (float4*)B.nd.ptr,
-            (uint8_t*)B.nflag.ptr);
+            (uint8_t*)B.nflag.ptr, (float*)B.emit.ptr, (int*)B.rstat.ptr);
         PBG_CUDA(cudaGetLastError());
         s->counters.kernel_launches += 1;
+        if (draws) rng_base += 7 * n + nhits * (bounce > 3 ? 4 : 3);
         // shadow queue
         int64_t nsh = 0;
         if ((r = compact_count(s, (const uint8_t*)B.sflag.ptr, nslots, (uint32_t*)B.counts.ptr, &nsh, st)))
@@ -605,7 +998,7 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
         stt.shadow_rays += (uint64_t)nsh;
         resolve_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(
             rc, nq, kslots, qi, (const uint8_t*)B.sflag.ptr, (const int32_t*)B.spos.ptr,
-            (const uint8_t*)B.occ.ptr, (const float*)B.scontrib.ptr, (float*)B.L.ptr);
+            (const uint8_t*)B.occ.ptr, (const float*)B.scontrib.ptr, (const float*)B.emit.ptr, (float*)B.L.ptr);
         PBG_CUDA(cudaGetLastError());
         s->counters.kernel_launches += 1;
         if (rc.integrator != PBG_INTEGRATOR_PATH) break;
@@ -626,12 +1019,14 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     }
     // online training of the learned ordering on this frame's records
     if (s->learn && s->learn->enabled && (r = learn_train(s, 0, st))) return r;
-    film_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(npix, rc.spp, (const float*)B.L.ptr,
-                                                                 (float*)B.rgb.ptr);
+    film_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(npix, rc.spp, film_off, film_idx,
+                                                                 (const float*)B.L.ptr, (float*)B.rgb.ptr);
     PBG_CUDA(cudaGetLastError());
     s->counters.kernel_launches += 1;
     cudaEventRecord(e1, st);
     PBG_CUDA(cudaMemcpyAsync(rgb_host, B.rgb.ptr, npix * 12, cudaMemcpyDeviceToHost, st));
+    int rstat[4] = {0, 0, 0, 0};
+    PBG_CUDA(cudaMemcpyAsync(rstat, B.rstat.ptr, 16, cudaMemcpyDeviceToHost, st));
     PBG_CUDA(cudaStreamSynchronize(st));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -639,6 +1034,15 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     cudaEventDestroy(e1);
     stt.ms_total = ms;
     if (stats) *stats = stt;
+    if (rstat[0] != 0) {
+        char buf[200];
+        snprintf(buf, sizeof(buf),
+                 "pbg_render_stream: %d path vertices sampled a direction the BSDF rejects; the reference traces "
+                 "such a ray again unchanged, so the stream no longer matches it",
+                 rstat[0]);
+        set_last_error(buf);
+        return PBG_ERR_UNSUPPORTED;
+    }
     return check_device_status(s, st);
 }
 
@@ -652,5 +1056,16 @@ extern "C" int pbg_render(pbg_scene* scene, const pbg_camera* camera, const pbg_
         return PBG_ERR_INVALID_ARGUMENT;
     }
     cudaSetDevice(scene->device);
-    return pbg::render(scene, camera, lights, nlights, params, rgb, stats);
+    return pbg::render(scene, camera, lights, nlights, params, nullptr, rgb, stats);
+}
+
+extern "C" int pbg_render_stream(pbg_scene* scene, const pbg_camera* camera, const pbg_light* lights,
+                                 int32_t nlights, const pbg_render_params* params,
+                                 const pbg_sample_stream* stream, float* rgb, pbg_render_stats* stats) {
+    if (!scene || !stream) {
+        pbg::set_last_error("pbg_render_stream: scene or stream is NULL");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(scene->device);
+    return pbg::render(scene, camera, lights, nlights, params, stream, rgb, stats);
 }

@@ -1,10 +1,12 @@
 """The breadth-first renderer on the device (pbg_render) from Python.
 
 Mirrors the reference's scene-file vocabulary: Camera "perspective",
-LightSource "point" / an area light on a parallelogram, Material "matte",
-SurfaceIntegrator "directlighting" | "path", Sampler "stratified"
-(renderers/breadth-first.cpp, integrators/directlighting.cpp,
-integrators/path.cpp).
+LightSource "point", AreaLightSource "diffuse" on scene triangles (or an
+emitter on a parallelogram), Material "matte", SurfaceIntegrator
+"directlighting" | "path", Sampler "stratified" (renderers/breadth-first.cpp,
+integrators/directlighting.cpp, integrators/path.cpp).  render_stream()
+takes the reference's own sample values (one breadth-first task's sampler
+output and RNG continuation) in place of the counter-based hash.
 """
 from __future__ import annotations
 
@@ -23,13 +25,20 @@ class Camera(C.Structure):
 
 class Light(C.Structure):
     _fields_ = [("type", C.c_int32), ("nsamples", C.c_int32), ("pos", C.c_float * 3),
-                ("intensity", C.c_float * 3), ("quad", C.c_float * 12), ("radiance", C.c_float * 3)]
+                ("intensity", C.c_float * 3), ("quad", C.c_float * 12), ("radiance", C.c_float * 3),
+                ("first_tri", C.c_int32), ("ntri", C.c_int32)]
 
 
 class RenderParams(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("spp_x", C.c_int32), ("spp_y", C.c_int32),
                 ("jitter", C.c_int32), ("max_depth", C.c_int32), ("reserved0", C.c_int32),
                 ("seed", C.c_uint64), ("albedo", C.c_float * 3), ("reserved", C.c_int32 * 8)]
+
+
+class SampleStream(C.Structure):
+    _fields_ = [("count", C.c_int64), ("image_xy", C.POINTER(C.c_float)), ("dims", C.POINTER(C.c_float)),
+                ("ndims", C.c_int32), ("reserved", C.c_int32), ("rng", C.POINTER(C.c_float)),
+                ("nrng", C.c_int64)]
 
 
 class RenderStats(C.Structure):
@@ -45,6 +54,9 @@ def _bind():
     if not getattr(lib, "_render_bound", False):
         lib.pbg_render.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
                                    C.POINTER(RenderParams), C.c_void_p, C.POINTER(RenderStats)]
+        lib.pbg_render_stream.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
+                                          C.POINTER(RenderParams), C.POINTER(SampleStream), C.c_void_p,
+                                          C.POINTER(RenderStats)]
         lib._render_bound = True
     return lib
 
@@ -125,6 +137,18 @@ def quad_light(quad, radiance, nsamples: int = 4) -> Light:
     return lt
 
 
+def mesh_light(first_tri: int, ntri: int, radiance, nsamples: int = 1) -> Light:
+    """AreaLightSource "diffuse" on the scene's triangles [first_tri,
+    first_tri + ntri): pbrt's DiffuseAreaLight over their ShapeSet
+    (lights/diffuse.cpp), emitting on the side of each triangle's normal."""
+    lt = Light()
+    lt.type = 2
+    lt.nsamples = int(nsamples)
+    lt.first_tri, lt.ntri = int(first_tri), int(ntri)
+    lt.radiance[:] = [float(x) for x in radiance]
+    return lt
+
+
 def render_params(integrator="directlighting", spp=(1, 1), jitter=False, max_depth=5, seed=1,
                   albedo=(0.7, 0.7, 0.7)) -> RenderParams:
     p = RenderParams()
@@ -137,6 +161,54 @@ def render_params(integrator="directlighting", spp=(1, 1), jitter=False, max_dep
     return p
 
 
+PATH_SAMPLE_DEPTH = 3  # integrators/path.h SAMPLE_DEPTH
+
+
+def sample_arrays(integrator: str, light_nsamples):
+    """The 1-D and 2-D sample array sizes the reference's integrators request,
+    in request order (Sample::Add1D / Add2D): directlighting's LightSample
+    and BSDFSample offsets per light (integrators/directlighting.cpp:45-62),
+    the path integrator's four per bounce below SAMPLE_DEPTH
+    (integrators/path.cpp:31-38), then the default volume integrator's two
+    (integrators/emission.cpp:31-35)."""
+    n1d, n2d = [], []
+    if integrator == "directlighting":
+        for ns in light_nsamples:
+            n1d += [ns, ns]
+            n2d += [ns, ns]
+    else:
+        for _ in range(PATH_SAMPLE_DEPTH):
+            n1d += [1, 1, 1, 1]
+            n2d += [1, 1, 1]
+    return n1d + [1, 1], n2d
+
+
+def stream_dims(integrator: str, light_nsamples, oned, twod):
+    """pbg_sample_stream's per-sample values from the reference's sample
+    arrays (oned [n, sum n1d], twod [n, sum n2d, 2] in the order of
+    sample_arrays)."""
+    oned = np.asarray(oned, np.float32)
+    twod = np.asarray(twod, np.float32)
+    n = oned.shape[0]
+    if integrator == "directlighting":
+        cols, o1, o2 = [], 0, 0
+        for ns in light_nsamples:
+            lcomp, bcomp = oned[:, o1:o1 + ns], oned[:, o1 + ns:o1 + 2 * ns]
+            lpos, bdir = twod[:, o2:o2 + ns], twod[:, o2 + ns:o2 + 2 * ns]
+            for j in range(ns):
+                cols += [lpos[:, j, 0], lpos[:, j, 1], lcomp[:, j], bdir[:, j, 0], bdir[:, j, 1], bcomp[:, j]]
+            o1 += 2 * ns
+            o2 += 2 * ns
+    else:
+        cols = []
+        for b in range(PATH_SAMPLE_DEPTH):
+            lcomp, lnum, bcomp, pcomp = (oned[:, 4 * b + k] for k in range(4))
+            lpos, bdir, pdir = (twod[:, 3 * b + k] for k in range(3))
+            cols += [lnum, lpos[:, 0], lpos[:, 1], lcomp, bdir[:, 0], bdir[:, 1], bcomp, pdir[:, 0], pdir[:, 1],
+                     pcomp]
+    return np.ascontiguousarray(np.stack(cols, 1) if cols else np.zeros((n, 1)), np.float32)
+
+
 def render(acc, camera: Camera, lights, params: RenderParams):
     """Renders through the accelerator's scene; returns (rgb [yres, xres, 3],
     stats dict)."""
@@ -147,5 +219,26 @@ def render(acc, camera: Camera, lights, params: RenderParams):
     st = RenderStats()
     L.check(lib.pbg_render(acc.handle, C.byref(camera), arr, len(lights), C.byref(params),
                            img.ctypes.data, C.byref(st)), "pbg_render")
+    return img, {"camera_rays": st.camera_rays, "nearest_rays": st.nearest_rays,
+                 "shadow_rays": st.shadow_rays, "bounces": st.bounces, "ms_total": st.ms_total}
+
+
+def render_stream(acc, camera: Camera, lights, params: RenderParams, image_xy, dims, rng):
+    """pbg_render_stream: one task's sample values (image_xy [n, 2], dims
+    [n, ndims] as stream_dims lays them out, rng = the task RNG's later
+    draws).  Returns (rgb [yres, xres, 3], stats dict)."""
+    lib = _bind()
+    lights = list(lights)
+    arr = (Light * max(1, len(lights)))(*lights)
+    image_xy = np.ascontiguousarray(image_xy, np.float32)
+    dims = np.ascontiguousarray(dims, np.float32)
+    rng = np.ascontiguousarray(rng, np.float32)
+    fp = C.POINTER(C.c_float)
+    ss = SampleStream(image_xy.shape[0], image_xy.ctypes.data_as(fp), dims.ctypes.data_as(fp), dims.shape[1], 0,
+                      rng.ctypes.data_as(fp), rng.shape[0])
+    img = np.empty((camera.yres, camera.xres, 3), np.float32)
+    st = RenderStats()
+    L.check(lib.pbg_render_stream(acc.handle, C.byref(camera), arr, len(lights), C.byref(params), C.byref(ss),
+                                  img.ctypes.data, C.byref(st)), "pbg_render_stream")
     return img, {"camera_rays": st.camera_rays, "nearest_rays": st.nearest_rays,
                  "shadow_rays": st.shadow_rays, "bounces": st.bounces, "ms_total": st.ms_total}

@@ -194,6 +194,74 @@ def case_render_small():
                 albedo=np.array([0.7, 0.7, 0.7], np.float32))
 
 
+# The breadth-first renders (Renderer "breadth-first", Accelerator "naive"
+# through the CPU batch backend of oracle/ref): the small sphere workload
+# plus a 2-triangle area light that the camera sees.
+BF = dict(xres=48, yres=40, spp=(2, 2), eye=(0.0, 0.3, -4.5), look=(0.0, 1.3, 0.0), up=(0.0, 1.0, 0.0),
+          fov=55.0, L=(5.0, 5.0, 5.0), nsamples=4, max_depth=5)
+BF_QUAD = np.array([[-1, 3, -1], [1, 3, -1], [1, 3, 1], [-1, 3, 1]], F32)
+
+
+def bf_scene_text(tris, integrator, light_text, out_name="out.pfm"):
+    n = len(tris)
+    P = " ".join(repr(float(x)) for x in tris.reshape(-1))
+    idx = " ".join(str(i) for i in range(3 * n))
+    c = BF
+    extra = f' "integer maxdepth" [{c["max_depth"]}]' if integrator == "path" else ""
+    return f'''LookAt {c["eye"][0]} {c["eye"][1]} {c["eye"][2]}  {c["look"][0]} {c["look"][1]} {c["look"][2]}  {c["up"][0]} {c["up"][1]} {c["up"][2]}
+Camera "perspective" "float fov" [{c["fov"]}]
+Sampler "stratified" "integer xsamples" [{c["spp"][0]}] "integer ysamples" [{c["spp"][1]}] "bool jitter" ["true"]
+PixelFilter "box"
+Film "image" "integer xresolution" [{c["xres"]}] "integer yresolution" [{c["yres"]}] "string filename" ["{out_name}"]
+Renderer "breadth-first"
+SurfaceIntegrator "{integrator}"{extra}
+Accelerator "naive"
+WorldBegin
+Material "matte" "rgb Kd" [0.7 0.7 0.7]
+Shape "trianglemesh" "integer indices" [{idx}] "point P" [{P}]
+{light_text}WorldEnd
+'''
+
+
+def case_render_bf():
+    import tempfile
+    from pbrt_gb300 import render as R
+    base = S.config_small_naive()["tris"]
+    c = BF
+    Q = " ".join(repr(float(x)) for x in BF_QUAD.reshape(-1))
+    area = (f'AttributeBegin\nAreaLightSource "diffuse" "rgb L" [{c["L"][0]} {c["L"][1]} {c["L"][2]}] '
+            f'"integer nsamples" [{{ns}}]\nShape "trianglemesh" "integer indices" [0 1 2 0 2 3] "point P" [{Q}]\n'
+            'AttributeEnd\n')
+    point = 'LightSource "point" "point from" [0 3 0] "rgb I" [8 8 8]\n'
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        out["image_direct"] = O.ref_render(bf_scene_text(base, "directlighting", area.format(ns=c["nsamples"])), td)
+        out["image_path"] = O.ref_render(bf_scene_text(base, "path", area.format(ns=1)), td)
+        out["image_point"] = O.ref_render(bf_scene_text(base, "directlighting", point), td)
+    r2c, c2w, _ = O.ref_camera(c["xres"], c["yres"], c["eye"], c["look"], c["up"], c["fov"],
+                               np.zeros((1, 2), F32))
+    out.update(r2c=r2c, c2w=c2w, quad=BF_QUAD)
+    # pins of the restated sampler: pbrt's own first samples and RNG draws
+    ext = (0, c["xres"] + 1, 0, c["yres"] + 1)
+    for tag, integ, nsl in (("path", "path", [1]), ("direct", "directlighting", [c["nsamples"]])):
+        n1d, n2d = R.sample_arrays(integ, nsl)
+        img, o1, o2, rng = O.pbrt_task_samples(ext, c["spp"], n1d, n2d, 64, 2048, reference=True)
+        out.update({f"samp_{tag}_img": img, f"samp_{tag}_oned": o1, f"samp_{tag}_twod": o2, f"samp_{tag}_rng": rng})
+    # pins of the restated area light: pbrt's DiffuseAreaLight::Sample_L
+    g = np.random.default_rng(11)
+    quad_tris = np.array([np.r_[BF_QUAD[0], BF_QUAD[1], BF_QUAD[2]], np.r_[BF_QUAD[0], BF_QUAD[2], BF_QUAD[3]]], F32)
+    uneven = g.uniform(-1, 1, (7, 9)).astype(F32)
+    uneven[:, 1::3] += 3.0
+    for tag, lt in (("quad", quad_tris), ("uneven", uneven)):
+        q = np.zeros((256, 7), F32)
+        q[:, 0:3] = g.uniform([-3, -1, -3], [3, 2.9, 3], (256, 3))
+        q[:, 3] = 1e-3
+        q[:, 4:7] = g.random((256, 3))
+        out.update({f"light_{tag}_tris": lt, f"light_{tag}_q": q,
+                    f"light_{tag}_out": O.area_light_sample(lt, c["L"], q, reference=True)})
+    return out
+
+
 def main():
     if not O.ref_available():
         if not O.build_ref():
@@ -239,6 +307,9 @@ def main():
 
     # the reference's own render of the small naive workload
     np.savez_compressed(os.path.join(HERE, "render_small.npz"), **case_render_small())
+
+    # the reference's breadth-first renders with an area light
+    np.savez_compressed(os.path.join(HERE, "render_bf.npz"), **case_render_bf())
 
     # empty scene
     tris = np.zeros((0, 9), F32)
