@@ -354,8 +354,9 @@ int pbg_sceneset_autotune(pbg_sceneset* set, const float* o4n, const float* d4n,
  * 256 top clusters of the BVH holds a ray's first hit; the traversal visits
  * that cluster first and then runs the full exact walk, so hits and
  * occlusion are identical with the ordering on or off.  Training is online,
- * on first-hit records the accelerator collects from its own nearest-hit
- * batches.
+ * on the records the accelerator collects from its own batches: first-hit
+ * clusters of nearest-hit rays, and the clusters of the occluders any-hit
+ * walks find (a shadow ray whose guess holds an occluder stops there).
  * ------------------------------------------------------------------- */
 typedef struct pbg_learn_params {
     int32_t batch;            /* records per SGD step (multiple of 128; 0 = 8192) */
@@ -367,7 +368,10 @@ typedef struct pbg_learn_params {
                                * top logit leads the second by at least this (0 = 1.0;
                                * < 0 = always) */
     uint64_t seed;            /* weight initialisation */
-    int32_t reserved[8];
+    int32_t queries;          /* batches the ordering serves and learns from:
+                               * 1 nearest-hit (first-hit clusters), 2 any-hit
+                               * (occluder clusters), 3 both (0 = 3) */
+    int32_t reserved[7];
 } pbg_learn_params;
 
 typedef struct pbg_learn_stats {
@@ -393,6 +397,28 @@ int pbg_learn_params_io(pbg_scene* scene, float* params, int32_t get);
  * pass against a CPU reference. */
 int pbg_learn_gradients(pbg_scene* scene, const float* x, const int32_t* labels, int32_t B,
                         float* grads, float* loss);
+
+/* Cluster hints (Accelerator "ray-bvh").  No counterpart in the reference.
+ * The learned ordering's clusters are the 256 subtrees of the BVH's top cut;
+ * a caller that knows a likely cluster per ray (the previous frame's hit of
+ * the same pixel, the occluder of a neighbouring shadow ray, its own model)
+ * passes it and the walk visits that subtree first.  Results are identical
+ * with or without hints.  All arrays are device memory on `stream`.
+ *   pbg_clusters_of_device     cluster[i] of triangle prim[i] (0..255, or
+ *                              0xffff for -1 and triangles outside the cut)
+ *   pbg_intersect_hinted_device / pbg_occluded_hinted_device
+ *                              hint[i] = the cluster to walk first, 0xffff =
+ *                              none (hint NULL: the learned ordering, if on);
+ *                              occluders (may be NULL) receives the triangle
+ *                              that blocked each any-hit ray, or -1 */
+int pbg_clusters_of_device(pbg_scene* scene, const int32_t* prim, int64_t n, uint16_t* cluster,
+                           void* stream);
+int pbg_intersect_hinted_device(pbg_scene* scene, const float* o4, const float* d4,
+                                const uint8_t* valid, int64_t n, const uint16_t* hint, int32_t* prim,
+                                float* t, float* b1, float* b2, void* stream);
+int pbg_occluded_hinted_device(pbg_scene* scene, const float* o4, const float* d4,
+                               const uint8_t* valid, int64_t n, const uint16_t* hint, uint8_t* occ,
+                               int32_t* occluders, void* stream);
 
 /* Tensor-core GEMM used by the learned traversal ordering, exposed for
  * checking: C[M x N] (+)= A[M x K] * B[N x K]^T with A, B row-major BF16

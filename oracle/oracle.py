@@ -34,10 +34,17 @@ def build() -> None:
     subprocess.check_call(["make", "-s", "-C", HERE])
 
 
+def reference_tree() -> str:
+    """The reference's source tree: $PBRT_REFERENCE, else a directory named
+    "reference" beside the repository checkout."""
+    return os.environ.get("PBRT_REFERENCE",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
+
+
 def build_ref() -> bool:
     """Build oracle/_ref/libpbrtref.so from the reference sources; returns
     False when the reference tree is not on this machine."""
-    ref = os.environ.get("PBRT_REFERENCE", "/root/reference")
+    ref = reference_tree()
     if not os.path.isdir(os.path.join(ref, "src", "shapes")):
         return False
     subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={ref}"])

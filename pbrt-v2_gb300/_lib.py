@@ -65,7 +65,7 @@ STAGES = ("sort", "build", "traverse", "other")
 class LearnParams(C.Structure):
     _fields_ = [("batch", C.c_int32), ("steps_per_train", C.c_int32), ("lr", C.c_float),
                 ("momentum", C.c_float), ("records", C.c_int32), ("margin", C.c_float),
-                ("seed", C.c_uint64), ("reserved", C.c_int32 * 8)]
+                ("seed", C.c_uint64), ("queries", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class LearnStats(C.Structure):
@@ -108,6 +108,9 @@ def lib():
     L.pbg_occluded.argtypes = [vp, C.POINTER(Rays), C.c_int64, vp]
     L.pbg_intersect_device.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp, vp]
     L.pbg_occluded_device.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp]
+    L.pbg_clusters_of_device.argtypes = [vp, vp, C.c_int64, vp, vp]
+    L.pbg_intersect_hinted_device.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp]
+    L.pbg_occluded_hinted_device.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp]
     L.pbg_hit_geometry.argtypes = [vp, C.POINTER(Rays), C.POINTER(Hits), C.c_int64, vp]
     L.pbg_hit_geometry_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64, vp, vp]
     L.pbg_stats.argtypes = [vp, C.POINTER(Counters)]

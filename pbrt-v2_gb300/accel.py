@@ -147,6 +147,28 @@ class Aggregate:
             n, occ.data_ptr(), None if stream is None else stream.cuda_stream),
             "pbg_occluded_device")
 
+    # -- cluster hints (ray-bvh) ----------------------------------------
+
+    def clusters_of_device(self, prim, cluster, stream=None):
+        """cluster[i] (uint16 tensor) = the BVH top-cut cluster of triangle
+        prim[i] (0xffff for -1)."""
+        L.check(L.lib().pbg_clusters_of_device(self.handle, prim.data_ptr(), prim.shape[0], cluster.data_ptr(),
+                                               None if stream is None else stream.cuda_stream),
+                "pbg_clusters_of_device")
+
+    def intersect_hinted_device(self, o4, d4, hint, prim, t, b1, b2, valid=None, stream=None):
+        L.check(L.lib().pbg_intersect_hinted_device(
+            self.handle, o4.data_ptr(), d4.data_ptr(), None if valid is None else valid.data_ptr(), o4.shape[0],
+            None if hint is None else hint.data_ptr(), prim.data_ptr(), t.data_ptr(), b1.data_ptr(),
+            b2.data_ptr(), None if stream is None else stream.cuda_stream), "pbg_intersect_hinted_device")
+
+    def occluded_hinted_device(self, o4, d4, hint, occ, occluders=None, valid=None, stream=None):
+        L.check(L.lib().pbg_occluded_hinted_device(
+            self.handle, o4.data_ptr(), d4.data_ptr(), None if valid is None else valid.data_ptr(), o4.shape[0],
+            None if hint is None else hint.data_ptr(), occ.data_ptr(),
+            None if occluders is None else occluders.data_ptr(), None if stream is None else stream.cuda_stream),
+            "pbg_occluded_hinted_device")
+
     def stats(self) -> dict:
         c = L.Counters()
         L.check(L.lib().pbg_stats(self.handle, C.byref(c)), "pbg_stats")
@@ -162,15 +184,16 @@ class Aggregate:
 
     def learn_enable(self, on: bool = True, batch: int = 0, steps_per_train: int = 0, lr: float = 0.0,
                      momentum: float = 0.0, records: int = 0, seed: int = 0,
-                     margin: float = 0.0) -> None:
+                     margin: float = 0.0, queries: int = 0) -> None:
         """Builds the BVH clusters and the MLP (pbg_learn_enable); the
-        accelerator then collects first-hit records from its nearest-hit
-        batches, and ordered walks start once the network has trained."""
+        accelerator then collects records from its batches (queries: 1
+        nearest-hit first hits, 2 any-hit occluders, 3 / 0 both) and ordered
+        walks start once the network has trained."""
         lib = L.lib()
         lib.pbg_learn_enable.argtypes = [C.c_void_p, C.c_int32, C.POINTER(L.LearnParams)]
         p = L.LearnParams()
         p.batch, p.steps_per_train, p.lr, p.momentum = batch, steps_per_train, lr, momentum
-        p.records, p.seed, p.margin = records, seed, margin
+        p.records, p.seed, p.margin, p.queries = records, seed, margin, queries
         L.check(lib.pbg_learn_enable(self.handle, int(on), C.byref(p)), "pbg_learn_enable")
 
     def learn_train(self, steps: int = 0) -> None:

@@ -6,8 +6,8 @@
 // declarations (accelerators/naive.h, rayhierarchy.h, rayBVH.h) over the C
 // ABI in include/pbrt_gb300.h, so core/scene.h's dynamic_cast dispatch,
 // core/api.cpp's factories and the breadth-first renderer keep working
-// unmodified.  Build it with the rest of pbrt and link -lpbrtgb300 (see
-// INTEGRATION.md).
+// unmodified.  Build it with the rest of pbrt and link -lpbrtgb300 (the
+// "adapter" target of oracle/ref/Makefile does exactly that).
 //
 // Per object state (the device scene, the refined primitives, host staging
 // buffers) lives in a side table keyed by the object, because the class

@@ -1031,6 +1031,56 @@ int pbg_occluded_device(pbg_scene* s, const float* o4, const float* d4, const ui
     return rc;
 }
 
+int pbg_clusters_of_device(pbg_scene* s, const int32_t* prim, int64_t n, uint16_t* cluster, void* stream) {
+    if (!s || n < 0 || (n > 0 && (!prim || !cluster))) {
+        set_last_error("pbg_clusters_of_device: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(s->device);
+    return clusters_of(s, prim, n, cluster, stream ? (cudaStream_t)stream : s->stream);
+}
+
+int pbg_intersect_hinted_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid, int64_t n,
+                                const uint16_t* hint, int32_t* prim, float* t, float* b1, float* b2,
+                                void* stream) {
+    if (!s || n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2))) {
+        set_last_error("pbg_intersect_hinted_device: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (s->accel != PBG_ACCEL_RAYBVH) {
+        set_last_error("pbg_intersect_hinted_device: cluster hints need Accelerator \"ray-bvh\"");
+        return PBG_ERR_UNSUPPORTED;
+    }
+    cudaSetDevice(s->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    int rc = bvh_nearest_hinted(s, (const float4*)o4, (const float4*)d4, valid, n, hint, prim, t, b1, b2, st);
+    if (rc == PBG_OK) {
+        s->counters.rays_nearest += (uint64_t)n;
+        s->counters.calls++;
+    }
+    return rc;
+}
+
+int pbg_occluded_hinted_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid, int64_t n,
+                               const uint16_t* hint, uint8_t* occ, int32_t* occluders, void* stream) {
+    if (!s || n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!o4 || !d4 || !occ))) {
+        set_last_error("pbg_occluded_hinted_device: bad arguments");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (s->accel != PBG_ACCEL_RAYBVH) {
+        set_last_error("pbg_occluded_hinted_device: cluster hints need Accelerator \"ray-bvh\"");
+        return PBG_ERR_UNSUPPORTED;
+    }
+    cudaSetDevice(s->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    int rc = bvh_occluded_hinted(s, (const float4*)o4, (const float4*)d4, valid, n, hint, occ, occluders, st);
+    if (rc == PBG_OK) {
+        s->counters.rays_occluded += (uint64_t)n;
+        s->counters.calls++;
+    }
+    return rc;
+}
+
 int pbg_intersect(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_hits* out) {
     if (!s || n < 0 || (n > 0 && (!rays_ok(r) || !out || !out->prim || !out->t || !out->b1 ||
                                   !out->b2))) {

@@ -8,8 +8,10 @@
 // first.  Rays run in the caller's order (camera and shadow batches from the
 // breadth-first renderer are already coherent) or, when the scene asks for
 // it, in the 6-D Morton order of the per-batch ray hierarchy
-// (pbg_rayorder.cu).  With the learned ordering on (pbg_learn.cu) each ray
-// first walks the cluster its model predicts.
+// (pbg_rayorder.cu).  With the learned ordering on (pbg_learn.cu), or with
+// cluster hints from the caller, each ray first walks the predicted cluster
+// of the BVH's top cut; an any-hit ray whose guess holds an occluder stops
+// there.
 #include <algorithm>
 
 #include "pbg_internal.h"
@@ -38,6 +40,7 @@ __global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
     if (!active) {
         if (ANY) {
             occ[ray] = 0;
+            if (prim_out) prim_out[ray] = -1;
         } else {
             prim_out[ray] = -1;
             t_out[ray] = 0.f;
@@ -52,7 +55,7 @@ __global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
     int32_t fref = INT32_MIN, fcnt = 0;
     if (ORDERED) {
         const int c = pred[ray];
-        if (c != kNoCluster) {
+        if (c < kClusters) {  // anything else (kNoCluster included): no hint
             fref = cref[2 * c];
             fcnt = cref[2 * c + 1];
         }
@@ -62,6 +65,7 @@ __global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
     if (STATS) wc.flush(wcount);
     if (ANY) {
         occ[ray] = h.prim >= 0 ? 1 : 0;
+        if (prim_out) prim_out[ray] = h.prim;  // the occluder found (labels, hints)
         return;
     }
     prim_out[ray] = h.prim;
@@ -116,6 +120,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
     auto finish = [&]() {
         if (ANY) {
             occ[ray] = h.prim >= 0 ? 1 : 0;
+            if (prim_out) prim_out[ray] = h.prim;
         } else {
             const bool hit = h.prim >= 0;
             prim_out[ray] = h.prim;
@@ -188,7 +193,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
                         skip = INT32_MIN;
                         if (ORDERED) {
                             const int c = pred[ray];
-                            if (c != kNoCluster) {
+                            if (c < kClusters) {
                                 // the root after the predicted cluster
                                 skip = cref[2 * c];
                                 stack_ref[0] = 0;
@@ -275,10 +280,14 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
 int ray_order(pbg_scene* s, const float4* o, const float4* d, int64_t n, const int32_t** perm,
               cudaStream_t st);
 
+// cluster_hint: a caller's cluster per ray (kNoCluster or any value outside
+// 0..kClusters-1 = none), walked first; else
+// the learned ordering's prediction when it is on for this kind of query.
+// occluders (any-hit): receives the triangle each walk found, or -1.
 template <bool ANY>
 static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,
                       int64_t n, int32_t* prim, float* t, float* b1, float* b2, uint8_t* occ,
-                      cudaStream_t st) {
+                      const uint16_t* cluster_hint, int32_t* occluders, cudaStream_t st) {
     if (n <= 0) return PBG_OK;
     const int32_t* perm = nullptr;
     if (s->params.ray_sort > 0) {
@@ -287,9 +296,23 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     }
     const uint16_t* pred = nullptr;
     const int32_t* cref = nullptr;
-    // the model predicts first-hit clusters: nearest-hit batches only
-    int rc = ANY ? PBG_OK : learn_predict(s, o, d, n, &pred, &cref, st);
+    Learner* lrn = s->learn;
+    const bool learning = lrn && lrn->enabled && (lrn->queries & (ANY ? 2 : 1));
+    int rc = PBG_OK;
+    if (cluster_hint) {
+        if ((rc = ensure_clusters(s))) return rc;
+        pred = cluster_hint;
+        cref = (const int32_t*)s->learn->cluster_ref.ptr;
+    } else if (learning) {
+        rc = learn_predict(s, o, d, n, &pred, &cref, st);
+    }
     if (rc) return rc;
+    // any-hit batches of a learning scene record their occluders as labels
+    if (ANY && learning && !occluders) {
+        if ((rc = ensure(lrn->occ_prim, (size_t)n * sizeof(int32_t)))) return rc;
+        occluders = (int32_t*)lrn->occ_prim.ptr;
+    }
+    if (ANY) prim = occluders;
     const unsigned grid = (unsigned)((n + kBvhThreads - 1) / kBvhThreads);
     const BvhNode* nodes = (const BvhNode*)s->bvh.ptr;
     const TriRec* tris = (const TriRec*)s->tris.ptr;
@@ -340,19 +363,29 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     }
     prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
-    // first-hit records for the learned ordering
-    if (!ANY && s->learn && s->learn->enabled) return learn_collect(s, o, d, prim, n, st);
+    // records for the learned ordering: first hits, occluders
+    if (learning) return learn_collect(s, o, d, prim, n, st);
     return PBG_OK;
 }
 
 int bvh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                 int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
-    return bvh_launch<false>(s, o, d, valid, n, prim, t, b1, b2, nullptr, st);
+    return bvh_launch<false>(s, o, d, valid, n, prim, t, b1, b2, nullptr, nullptr, nullptr, st);
 }
 
 int bvh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                  uint8_t* occ, cudaStream_t st) {
-    return bvh_launch<true>(s, o, d, valid, n, nullptr, nullptr, nullptr, nullptr, occ, st);
+    return bvh_launch<true>(s, o, d, valid, n, nullptr, nullptr, nullptr, nullptr, occ, nullptr, nullptr, st);
+}
+
+int bvh_nearest_hinted(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                       const uint16_t* hint, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
+    return bvh_launch<false>(s, o, d, valid, n, prim, t, b1, b2, nullptr, hint, nullptr, st);
+}
+
+int bvh_occluded_hinted(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                        const uint16_t* hint, uint8_t* occ, int32_t* occluders, cudaStream_t st) {
+    return bvh_launch<true>(s, o, d, valid, n, nullptr, nullptr, nullptr, nullptr, occ, hint, occluders, st);
 }
 
 }  // namespace pbg

@@ -139,6 +139,10 @@ int bvh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
                 int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
 int bvh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                  uint8_t* occ, cudaStream_t st);
+int bvh_nearest_hinted(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                       const uint16_t* hint, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
+int bvh_occluded_hinted(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                        const uint16_t* hint, uint8_t* occ, int32_t* occluders, cudaStream_t st);
 int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
 int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,

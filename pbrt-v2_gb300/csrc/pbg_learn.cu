@@ -444,9 +444,53 @@ void learn_free(Learner* L) {
                            &L->Z2, &L->Z3, &L->H1, &L->H2, &L->H1T, &L->H2T, &L->dZ3, &L->dZ3b,
                            &L->dZ3T, &L->dH2, &L->dZ2b, &L->dZ2T, &L->dH1, &L->dZ1b, &L->dZ1T, &L->G1,
                            &L->G2, &L->G3, &L->gb1, &L->gb2, &L->gb3, &L->acc, &L->feat, &L->pred,
-                           &L->gemm_work};
+                           &L->gemm_work, &L->occ_prim};
     for (DeviceBuffer* b : all) release(*b);
     delete L;
+}
+
+int ensure_clusters(pbg_scene* s) {
+    if (s->accel != PBG_ACCEL_RAYBVH) {
+        set_last_error("cluster hints need Accelerator \"ray-bvh\"");
+        return PBG_ERR_UNSUPPORTED;
+    }
+    if (!s->learn) s->learn = new Learner();
+    Learner* L = s->learn;
+    if (L->clusters_built) return PBG_OK;
+    std::vector<int32_t> refs;
+    std::vector<uint16_t> rc16;
+    build_clusters(s->host_nodes, s->ntri, &refs, &rc16);
+    L->nclusters = (int)(refs.size() / 2);
+    while (refs.size() < 2 * (size_t)kClusters) {
+        refs.push_back(INT32_MIN);
+        refs.push_back(0);
+    }
+    int rc;
+    if ((rc = ensure(L->cluster_ref, refs.size() * 4 + 8)) || (rc = ensure(L->record_cluster, rc16.size() * 2 + 8)))
+        return rc;
+    if (!refs.empty()) PBG_CUDA(cudaMemcpy(L->cluster_ref.ptr, refs.data(), refs.size() * 4, cudaMemcpyHostToDevice));
+    if (!rc16.empty()) PBG_CUDA(cudaMemcpy(L->record_cluster.ptr, rc16.data(), rc16.size() * 2, cudaMemcpyHostToDevice));
+    L->clusters_built = true;
+    return PBG_OK;
+}
+
+__global__ void clusters_of_kernel(const int32_t* __restrict__ prim, int64_t n, const int32_t* __restrict__ pos,
+                                   const uint16_t* __restrict__ rec_cluster, uint16_t* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t p = prim[i];
+    const uint16_t c = p >= 0 ? rec_cluster[pos[p]] : (uint16_t)kNoCluster;
+    out[i] = c < kClusters ? c : kNoCluster;
+}
+
+int clusters_of(pbg_scene* s, const int32_t* prim, int64_t n, uint16_t* out, cudaStream_t st) {
+    int rc = ensure_clusters(s);
+    if (rc || n <= 0) return rc;
+    clusters_of_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        prim, n, (const int32_t*)s->tri_pos.ptr, (const uint16_t*)s->learn->record_cluster.ptr, out);
+    PBG_CUDA(cudaGetLastError());
+    s->counters.kernel_launches += 1;
+    return PBG_OK;
 }
 
 int learn_init(pbg_scene* s, const pbg_learn_params* p) {
@@ -465,6 +509,7 @@ int learn_init(pbg_scene* s, const pbg_learn_params* p) {
         if (p->records > 0) L->capacity = p->records;
         if (p->seed) L->seed = p->seed;
     }
+    if (p && p->queries > 0) L->queries = p->queries & 3;
     if (L->capacity < L->batch) L->capacity = L->batch;
     for (int a = 0; a < 3; ++a) {
         L->box.lo[a] = s->scene_lo[a];
@@ -473,18 +518,7 @@ int learn_init(pbg_scene* s, const pbg_learn_params* p) {
     }
     cudaStream_t st = s->stream;
     int rc;
-    std::vector<int32_t> refs;
-    std::vector<uint16_t> rc16;
-    build_clusters(s->host_nodes, s->ntri, &refs, &rc16);
-    L->nclusters = (int)(refs.size() / 2);
-    while (refs.size() < 2 * (size_t)kClusters) {
-        refs.push_back(INT32_MIN);
-        refs.push_back(0);
-    }
-    if ((rc = ensure(L->cluster_ref, refs.size() * 4 + 8)) || (rc = ensure(L->record_cluster, rc16.size() * 2 + 8)))
-        return rc;
-    if (!refs.empty()) PBG_CUDA(cudaMemcpy(L->cluster_ref.ptr, refs.data(), refs.size() * 4, cudaMemcpyHostToDevice));
-    if (!rc16.empty()) PBG_CUDA(cudaMemcpy(L->record_cluster.ptr, rc16.data(), rc16.size() * 2, cudaMemcpyHostToDevice));
+    if ((rc = ensure_clusters(s))) return rc;
     // He-style initialisation from a seeded generator
     uint64_t z = L->seed * 0x9E3779B97F4A7C15ull + 12345;
     auto u01 = [&]() {

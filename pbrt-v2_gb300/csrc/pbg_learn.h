@@ -29,9 +29,13 @@ struct Learner {
     uint64_t trained_steps = 0;
     uint64_t seed = 1;
     LearnBox box{};
-    // clusters of the BVH: child references and per-record cluster ids
+    int queries = 3;  // 1: nearest-hit batches, 2: any-hit batches, 3: both
+    // clusters of the BVH: child references and per-record cluster ids (built
+    // once, also for caller-supplied hints without a trained network)
     DeviceBuffer cluster_ref, record_cluster;
     int nclusters = 0;
+    bool clusters_built = false;
+    DeviceBuffer occ_prim;  // any-hit batches: the occluder each walk found
     // parameters
     DeviceBuffer W1, W2, W3, V1, V2, V3, b1, b2, b3, vb1, vb2, vb3, W1b, W2b, W3b, W2Tb, W3Tb;
     // training scratch
@@ -44,6 +48,11 @@ struct Learner {
 };
 
 int learn_init(pbg_scene* s, const pbg_learn_params* p);
+// The cluster tables (kClusters subtrees of the BVH) without a network.
+int ensure_clusters(pbg_scene* s);
+// out[i] = the cluster of triangle prim[i] (kNoCluster for -1 or a triangle
+// outside the clusters).  Device arrays.
+int clusters_of(pbg_scene* s, const int32_t* prim, int64_t n, uint16_t* out, cudaStream_t st);
 void learn_free(Learner* L);
 // Predicted cluster per ray for the batch (NULL when the learner is off or
 // untrained; kNoCluster for a ray whose prediction is not confident);
@@ -51,8 +60,8 @@ void learn_free(Learner* L);
 constexpr uint16_t kNoCluster = 0xffffu;
 int learn_predict(pbg_scene* s, const float4* o, const float4* d, int64_t n, const uint16_t** pred,
                   const int32_t** cluster_ref, cudaStream_t st);
-// Appends training records (features + first-hit cluster) from a finished
-// nearest-hit batch.
+// Appends training records (features + the cluster of prim[i]) from a
+// finished batch: first hits of nearest-hit rays, occluders of any-hit rays.
 int learn_collect(pbg_scene* s, const float4* o, const float4* d, const int32_t* prim, int64_t n,
                   cudaStream_t st);
 int learn_train(pbg_scene* s, int steps, cudaStream_t st);

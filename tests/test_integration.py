@@ -1,8 +1,8 @@
 """The pbrt-side binding (pbrt-v2_gb300/adapters/pbrt_gpu_accels.cpp)
 compiles against the reference's unchanged headers, links into pbrt's own
 renderer, and a breadth-first scene reaches the library through pbrt's
-scene API.  Needs the reference tree next to the repository; skipped where
-it is absent (the GPU host)."""
+scene API.  Needs the reference tree ($PBRT_REFERENCE, or "reference" beside
+the repository checkout); skipped where it is absent."""
 import os
 import subprocess
 import tempfile
@@ -12,7 +12,7 @@ import pytest
 
 from conftest import ROOT
 
-REF = os.environ.get("PBRT_REFERENCE", "/root/reference")
+REF = os.environ.get("PBRT_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 HAVE_REF = os.path.isdir(os.path.join(REF, "src", "shapes"))
 
 
