@@ -403,6 +403,84 @@ def timed_cpu_sample(rc, threads, target_s, seed):
     return n + s, time.perf_counter() - t0, stride
 
 
+def ordering_study(acc, reps=5):
+    """What a cluster ordering can gain on the path scene.  Any-hit: shadow
+    segments from the camera hits of a 1024x1024 image (1 spp) to random
+    points on the area light; nearest-hit: those camera rays.  Times (CUDA
+    events on the launch stream) and counted work per ray of the plain walk,
+    of the walk with perfect hints (each ray's own occluder or first-hit
+    cluster: the ceiling of any ordering), and of the learned ordering when
+    the scene has a trained network (its inference and record collection
+    included)."""
+    import torch
+    from pbrt_gb300 import scenes as S
+    rays = S.pinhole_rays(PATH_RES, PATH_RES, PATH_CAMERA["eye"], PATH_CAMERA["look"], PATH_CAMERA["fov"], spp=1,
+                          jitter_seed=21)
+    n = rays.shape[1]
+    o4, d4 = to_dev(rays)
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    tt, b1, b2 = (torch.empty(n, device="cuda") for _ in range(3))
+    acc.intersect_device(o4, d4, prim, tt, b1, b2)
+    torch.cuda.synchronize()
+    hp, ht = prim.cpu().numpy(), tt.cpu().numpy()
+    shadows, hit = shadow_batches(rays, hp, ht, PATH_LIGHT, nsamples=1, seed=23)
+    so, sd = to_dev(shadows[0])
+    valid = torch.from_numpy(hit).cuda()
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    occluder = torch.empty(n, dtype=torch.int32, device="cuda")
+    hint = torch.empty(n, dtype=torch.int16, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def timed(fn, nrays):
+        with torch.cuda.stream(stream):
+            fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+        e1.synchronize()
+        acc.profile(2)
+        with torch.cuda.stream(stream):
+            fn()
+        stream.synchronize()
+        w = acc.stats()["work"]
+        acc.profile(False)
+        nv = max(int(nrays), 1)
+        return {"ms": round(e0.elapsed_time(e1) / reps, 4),
+                "node_tests_per_ray": round(w["node_tests"] / nv, 3),
+                "triangle_tests_per_ray": round(w["filter_tests"] / nv, 3)}
+
+    learner_on = acc.learn_stats()["trained_steps"] > 0
+    if learner_on:
+        acc.learn_enable(True, queries=2)
+        learned = timed(lambda: acc.occluded_device(so, sd, occ, valid=valid, stream=stream), hit.sum())
+        occ_l = occ.clone()
+        acc.learn_enable(False)
+    plain = timed(lambda: acc.occluded_hinted_device(so, sd, None, occ, occluder, valid=valid, stream=stream),
+                  hit.sum())
+    occ_p = occ.clone()
+    acc.clusters_of_device(occluder, hint, stream=stream)
+    perfect = timed(lambda: acc.occluded_hinted_device(so, sd, hint, occ, valid=valid, stream=stream), hit.sum())
+    same = bool(torch.equal(occ, occ_p)) and (not learner_on or bool(torch.equal(occ_l, occ_p)))
+    out = {"shadow_rays": int(hit.sum()), "occluded_fraction": round(float(occ_p.float().sum()) / max(int(hit.sum()), 1), 4),
+           "plain": plain, "perfect_hints": perfect,
+           "perfect_over_plain_time": round(plain["ms"] / perfect["ms"], 3), "results_identical": same}
+    if learner_on:
+        out["learned"] = learned
+        out["learned_over_plain_time"] = round(plain["ms"] / learned["ms"], 3)
+    # nearest hit: the camera rays themselves, hinted with their own first hit
+    nhint = torch.empty(n, dtype=torch.int16, device="cuda")
+    p2, t2, c1, c2 = (torch.empty_like(x) for x in (prim, tt, b1, b2))
+    nplain = timed(lambda: acc.intersect_hinted_device(o4, d4, None, p2, t2, c1, c2, stream=stream), n)
+    acc.clusters_of_device(prim, nhint, stream=stream)
+    nperfect = timed(lambda: acc.intersect_hinted_device(o4, d4, nhint, p2, t2, c1, c2, stream=stream), n)
+    out["nearest"] = {"camera_rays": n, "plain": nplain, "perfect_hints": nperfect,
+                      "perfect_over_plain_time": round(nplain["ms"] / nperfect["ms"], 3),
+                      "results_identical": bool(torch.equal(p2, prim) and torch.equal(t2, tt))}
+    return out
+
+
 def run_gpu_path(args, rank, world, dev):
     """The ray-bvh path-tracing frame: 1024x1024 x 8 spp (2x4 jittered) on
     800 displaced icospheres (1,024,000 triangles), path integrator to depth
@@ -465,7 +543,7 @@ def run_gpu_path(args, rank, world, dev):
     learned_line = None
     if args.learned:
         acc.learn_enable(True, seed=5, steps_per_train=args.learn_steps, lr=args.learn_lr,
-                         margin=args.learn_margin)
+                         margin=args.learn_margin, queries=args.learn_queries)
         lf, lw, lstt, lclocks, llaunch, img_learned = measure()
         lwork, _ = count_work(1000)
         ls = acc.learn_stats()
@@ -484,6 +562,7 @@ def run_gpu_path(args, rank, world, dev):
                     "last_loss": round(ls["last_loss"], 4), "top1_accuracy": round(ls["last_accuracy"], 4),
                     "train_ms_total": round(ls["train_ms"], 2), "infer_ms_total": round(ls["infer_ms"], 2)},
         }
+        learned_line["ordering_ceiling"] = ordering_study(acc)
         if args.learned == 1:  # the learned-ordered form as the value
             frames, walls, stt, clocks, launches = lf, lw, lstt, lclocks, llaunch
             rays, frame_ms = l_rays, l_ms
@@ -989,6 +1068,8 @@ def main():
     ap.add_argument("--learn-lr", type=float, default=0.0, help="learning rate (0 = 0.05)")
     ap.add_argument("--learn-margin", type=float, default=0.0,
                     help="logit lead needed to walk the predicted cluster first (0 = 1.0)")
+    ap.add_argument("--learn-queries", type=int, default=0,
+                    help="batches the learned ordering serves: 1 nearest-hit, 2 any-hit, 3 / 0 both")
     ap.add_argument("--learned", type=int, default=2,
                     help="path workload: 0 plain ordering, 1 learned ordering as the value, "
                          "2 plain as the value with the learned comparison attached")

@@ -76,7 +76,10 @@ typedef struct pbg_params {
                            * batches: nearest hit with a validity mask, and the
                            * renderer's bounces >= 1), 1 = one thread per ray,
                            * 2 = persistent warps refilled from a ray counter */
-    int32_t reserved[7];
+    int32_t bvh_build;    /* ray-bvh: 0 = build the SAH tree on the device,
+                           * 1 = on the host (the same splits; numbered depth
+                           * first instead of breadth first) */
+    int32_t reserved[6];
 } pbg_params;
 
 typedef struct pbg_rays {
@@ -111,6 +114,9 @@ typedef struct pbg_counters {
      * comparison's answer is read). */
     uint64_t origin_reuses;
     uint64_t origin_reruns;
+    /* rayhierarchy batches traced again with more triangle groups because a
+     * pair queue overflowed (the scene keeps the larger grouping) */
+    uint64_t queue_reruns;
     /* Device time per stage in ms while profiling is on (CUDA events around
      * each launch on its stream): [0] ray sort, [1] hierarchy build,
      * [2] traversal (the intersection kernels), [3] finalize / other. */
@@ -134,6 +140,18 @@ int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t 
                      const pbg_params* params, pbg_scene** out);
 /* Replaces the accelerators' destructors (naive.cpp:112-121). */
 void pbg_scene_destroy(pbg_scene* scene);
+
+/* The scene from pbrt's mesh arrays instead of packed triangles: P
+ * [nverts][3] positions (world space), indices [ntri][3] (TriangleMesh
+ * vertexIndex), uv [nverts][2] or NULL (TriangleMesh uvs).  Host arrays; the
+ * triangles are gathered on the device (the packing of
+ * accelerators/naive.cpp:59-101 without the host loop), and naive and
+ * ray-bvh scenes are then built there too; a rayhierarchy scene orders its
+ * records on the host, so it is gathered there.  Same triangle indices and
+ * results as pbg_scene_create on the packed triangles.  An index outside
+ * [0, nverts) is PBG_ERR_INVALID_ARGUMENT.  No counterpart in the reference. */
+int pbg_scene_create_mesh(const float* P, int64_t nverts, const int32_t* indices, int64_t ntri,
+                          const float* uv, int32_t accel, const pbg_params* params, pbg_scene** out);
 
 /* Batch size cap.  Replaces NaiveAccel::MaxRaysPerCall (naive.cpp:127-142),
  * RayHieararchy::MaxRaysPerCall (rayhierarchy.cpp:267-310) and
@@ -380,8 +398,11 @@ typedef struct pbg_learn_stats {
     double infer_ms, train_ms;      /* device time spent so far */
 } pbg_learn_stats;
 
-/* on = 1 builds the clusters and the network (params may be NULL);
- * on = 0 switches the ordering off (the plain kernels run). */
+/* on = 1 builds the clusters and the network (params may be NULL); a later
+ * call with on = 1 switches the ordering back on and updates the given
+ * (non-zero) batch, steps, learning rate, momentum, margin and queries,
+ * keeping the trained weights and the records.  on = 0 switches the
+ * ordering off (the plain kernels run). */
 int pbg_learn_enable(pbg_scene* scene, int32_t on, const pbg_learn_params* params);
 /* Runs SGD steps on the collected records (steps <= 0: steps_per_train). */
 int pbg_learn_train(pbg_scene* scene, int32_t steps);

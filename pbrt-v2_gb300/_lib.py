@@ -36,7 +36,7 @@ class Params(C.Structure):
     _fields_ = [("chunk_x", C.c_int32), ("chunk_y", C.c_int32), ("height", C.c_int32),
                 ("bvh_height", C.c_int32), ("max_bvh_prim", C.c_int32), ("device", C.c_int32),
                 ("ray_sort", C.c_int32), ("rh_cluster_levels", C.c_int32),
-                ("walk", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("walk", C.c_int32), ("bvh_build", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 _fp = C.POINTER(C.c_float)
@@ -55,7 +55,7 @@ class Counters(C.Structure):
     _fields_ = [("rays_nearest", C.c_uint64), ("rays_occluded", C.c_uint64),
                 ("calls", C.c_uint64), ("bvh_nodes", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("timed_launches", C.c_uint64 * 4), ("work", C.c_uint64 * 6),
-                ("origin_reuses", C.c_uint64), ("origin_reruns", C.c_uint64),
+                ("origin_reuses", C.c_uint64), ("origin_reruns", C.c_uint64), ("queue_reruns", C.c_uint64),
                 ("stage_ms", C.c_double * 4)]
 
 
@@ -101,6 +101,8 @@ def lib():
     L.pbg_last_error.restype = C.c_char_p
     L.pbg_device_count.restype = C.c_int
     L.pbg_scene_create.argtypes = [vp, vp, C.c_int64, C.c_int32, C.POINTER(Params), C.POINTER(vp)]
+    L.pbg_scene_create_mesh.argtypes = [vp, C.c_int64, vp, C.c_int64, vp, C.c_int32, C.POINTER(Params),
+                                        C.POINTER(vp)]
     L.pbg_scene_destroy.argtypes = [vp]
     L.pbg_scene_destroy.restype = None
     L.pbg_max_rays_per_call.argtypes = [vp, C.POINTER(C.c_int64)]

@@ -52,6 +52,26 @@ class Aggregate:
                                      C.byref(self.handle)), "pbg_scene_create")
         self.tile = None
 
+    @classmethod
+    def from_mesh(cls, P, indices, uv=None, params: L.Params | None = None):
+        """The scene from pbrt's TriangleMesh arrays (pbg_scene_create_mesh):
+        positions [nverts, 3], vertex indices [ntri, 3], per-vertex uvs
+        [nverts, 2] or None; the triangles are gathered on the device."""
+        self = cls.__new__(cls)
+        P = np.ascontiguousarray(np.asarray(P, np.float32).reshape(-1, 3))
+        vi = np.ascontiguousarray(np.asarray(indices, np.int32).reshape(-1, 3))
+        uvv = None if uv is None else np.ascontiguousarray(np.asarray(uv, np.float32).reshape(-1, 2))
+        self.tris = np.ascontiguousarray(P[vi].reshape(-1, 9)) if len(vi) else np.zeros((0, 9), np.float32)
+        self.uvs = None if uvv is None else np.ascontiguousarray(uvv[vi].reshape(-1, 6))
+        self.params = params or L.Params()
+        self.handle = C.c_void_p()
+        self.tile = None
+        L.check(L.lib().pbg_scene_create_mesh(P.ctypes.data if len(P) else None, len(P),
+                                              vi.ctypes.data if len(vi) else None, len(vi),
+                                              None if uvv is None else uvv.ctypes.data, L.ACCEL[cls.kind],
+                                              C.byref(self.params), C.byref(self.handle)), "pbg_scene_create_mesh")
+        return self
+
     def close(self):
         if getattr(self, "handle", None) and self.handle.value:
             L.lib().pbg_scene_destroy(self.handle)
@@ -178,6 +198,7 @@ class Aggregate:
                 "work": dict(zip(("node_tests", "leaves", "filter_tests", "exact_tests",
                                   "exact_hits", "filter_stage2"), list(c.work))),
                 "origin_reuses": c.origin_reuses, "origin_reruns": c.origin_reruns,
+                "queue_reruns": c.queue_reruns,
                 "stage_ms": dict(zip(L.STAGES, list(c.stage_ms)))}
 
     # -- learned traversal ordering (ray-bvh) ------------------------------
@@ -240,6 +261,7 @@ def _params_from(ps: dict | None) -> L.Params:
     p.ray_sort = int(ps.get("raySort", 0))
     p.rh_cluster_levels = int(ps.get("clusterLevels", 0))
     p.walk = int(ps.get("walk", 0))
+    p.bvh_build = int(ps.get("bvhBuild", 0))
     return p
 
 
@@ -257,6 +279,14 @@ def CreateRayHieararchy(tris, ps: dict | None = None, uvs=None) -> RayHieararchy
 def CreateRayBVH(tris, ps: dict | None = None, uvs=None) -> RayBVH:
     """rayBVH.cpp:1326-1344 (BVHheight, maxBVHPrim, ...)."""
     return RayBVH(tris, uvs, _params_from(ps))
+
+
+def MakeAcceleratorFromMesh(name: str, P, indices, uv=None, ps: dict | None = None) -> Aggregate:
+    """MakeAccelerator for a mesh given as pbrt's TriangleMesh arrays."""
+    cls = {"naive": NaiveAccel, "rayhierarchy": RayHieararchy, "ray-bvh": RayBVH}.get(name)
+    if cls is None:
+        raise ValueError(f'Accelerator "{name}" has no batch path')
+    return cls.from_mesh(P, indices, uv, _params_from(ps))
 
 
 def MakeAccelerator(name: str, tris, ps: dict | None = None, uvs=None) -> Aggregate:

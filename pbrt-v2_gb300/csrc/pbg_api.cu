@@ -388,17 +388,17 @@ int upload_triangles(pbg_scene* s, const float* tri9_host, const int32_t* order)
     const size_t nt = (size_t)(ntri > 0 ? ntri : 1);
     int rc;
     if ((rc = ensure(s->tri9, nt * 9 * sizeof(float))) || (rc = ensure(s->tris, nt * sizeof(TriRec))) ||
-        (rc = ensure(s->tri_pos, nt * sizeof(int32_t))) || (rc = ensure(s->spheres, nt * sizeof(float4))))
+        (rc = ensure(s->tri_pos, nt * sizeof(int32_t))))
         return rc;
     if (ntri == 0) return PBG_OK;
     PBG_CUDA(cudaMemcpyAsync(s->tri9.ptr, tri9_host, (size_t)ntri * 9 * sizeof(float),
                              cudaMemcpyHostToDevice, s->stream));
-    std::vector<float4> sph;
-    triangle_spheres(tri9_host, order, ntri, &sph);
-    PBG_CUDA(cudaMemcpyAsync(s->spheres.ptr, sph.data(), (size_t)ntri * sizeof(float4),
-                             cudaMemcpyHostToDevice, s->stream));
-    std::vector<float4> csph;
+    std::vector<float4> sph, csph;  // bounding spheres: the ray hierarchy's node tests only
     if (s->accel == PBG_ACCEL_RAYHIERARCHY) {
+        if ((rc = ensure(s->spheres, nt * sizeof(float4)))) return rc;
+        triangle_spheres(tri9_host, order, ntri, &sph);
+        PBG_CUDA(cudaMemcpyAsync(s->spheres.ptr, sph.data(), (size_t)ntri * sizeof(float4),
+                                 cudaMemcpyHostToDevice, s->stream));
         cluster_spheres(sph, &csph);
         if ((rc = ensure(s->clusters, csph.size() * sizeof(float4)))) return rc;
         PBG_CUDA(cudaMemcpyAsync(s->clusters.ptr, csph.data(), csph.size() * sizeof(float4),
@@ -871,24 +871,198 @@ int pbg_device_count(void) {
     return n;
 }
 
-int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t accel,
-                     const pbg_params* params, pbg_scene** out) {
+}  // extern "C"
+
+namespace pbg {
+
+int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf, int32_t* order_dev,
+                     cudaStream_t st);
+
+// pbrt's TriangleMesh arrays -> the 9 floats (and 6 uvs) of each triangle.
+__global__ void gather_mesh_kernel(const float* __restrict__ P, const int32_t* __restrict__ vi,
+                                   const float* __restrict__ uv, int64_t ntri, int64_t nverts,
+                                   float* __restrict__ tri9, float* __restrict__ uv6, int* __restrict__ bad) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntri) return;
+    for (int k = 0; k < 3; ++k) {
+        int32_t v = vi[3 * i + k];
+        if (v < 0 || v >= nverts) {  // an index outside the vertex array: reported, read as vertex 0
+            atomicAdd(bad, 1);
+            v = 0;
+        }
+        for (int a = 0; a < 3; ++a) tri9[9 * i + 3 * k + a] = P[3 * (int64_t)v + a];
+        if (uv6) {
+            uv6[6 * i + 2 * k] = uv[2 * (int64_t)v];
+            uv6[6 * i + 2 * k + 1] = uv[2 * (int64_t)v + 1];
+        }
+    }
+}
+
+// The scene's accelerator structures from triangles already in s->tri9 on
+// the device: naive needs only the records; ray-bvh builds its tree on the
+// device.  (rayhierarchy orders its records on the host; see scene_build.)
+static int scene_build_device(pbg_scene* s) {
+    const int64_t ntri = s->ntri;
+    const size_t nt = (size_t)(ntri > 0 ? ntri : 1);
+    int rc;
+    if ((rc = ensure(s->tris, nt * sizeof(TriRec))) || (rc = ensure(s->tri_pos, nt * sizeof(int32_t)))) return rc;
+    DeviceBuffer order;
+    if (s->accel == PBG_ACCEL_RAYBVH) {
+        if ((rc = ensure(order, nt * sizeof(int32_t)))) return rc;
+        rc = build_bvh_device(s, (const float*)s->tri9.ptr, ntri, s->params.max_bvh_prim > 0 ? s->params.max_bvh_prim : 4,
+                              (int32_t*)order.ptr, s->stream);
+        if (rc) {
+            release(order);
+            return rc;
+        }
+    } else {
+        // scene bounds for the naive scene (the device builder computes them for ray-bvh)
+        std::vector<float> h((size_t)ntri * 9);
+        if (ntri > 0) PBG_CUDA(cudaMemcpy(h.data(), s->tri9.ptr, h.size() * 4, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < ntri; ++i)
+            for (int k = 0; k < 9; ++k) {
+                const float v = h[9 * i + k];
+                const int a = k % 3;
+                if (i == 0 && k < 3) s->scene_lo[a] = s->scene_hi[a] = v;
+                s->scene_lo[a] = v < s->scene_lo[a] ? v : s->scene_lo[a];
+                s->scene_hi[a] = v > s->scene_hi[a] ? v : s->scene_hi[a];
+            }
+    }
+    if (ntri > 0) {
+        build_tris_kernel<<<(unsigned)((ntri + 255) / 256), 256, 0, s->stream>>>(
+            (const float*)s->tri9.ptr, (const int32_t*)order.ptr, ntri, (TriRec*)s->tris.ptr, (int32_t*)s->tri_pos.ptr);
+        s->counters.kernel_launches += 1;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    release(order);
+    if (e != cudaSuccess) return cuda_status(e, "build_tris_kernel");
+    return PBG_OK;
+}
+
+// The stream, status words and mailbox of a new scene.
+static int scene_init(pbg_scene* s) {
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamCreate");
+    int rc;
+    if ((rc = ensure(s->err, 4 * sizeof(int)))) return rc;
+    e = cudaHostAlloc((void**)&s->mbox_host, kMailboxWords * sizeof(int), cudaHostAllocMapped);
+    if (e == cudaSuccess) memset(s->mbox_host, 0, kMailboxWords * sizeof(int));
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&s->mbox_dev, s->mbox_host, 0);
+    if (e != cudaSuccess) return cuda_status(e, "cudaHostAlloc(status words)");
+    if (cudaMemset(s->err.ptr, 0, 4 * sizeof(int)) != cudaSuccess)
+        return cuda_status(cudaGetLastError(), "cudaMemset");
+    return PBG_OK;
+}
+
+static int scene_args(const char* what, int64_t ntri, int32_t accel, pbg_scene** out) {
     if (!out) {
-        set_last_error("pbg_scene_create: out is NULL");
+        set_last_error(std::string(what) + ": out is NULL");
         return PBG_ERR_INVALID_ARGUMENT;
     }
     *out = nullptr;
-    if (ntri < 0 || (ntri > 0 && !tri9) || ntri > (int64_t)INT32_MAX / 2) {
-        set_last_error("pbg_scene_create: bad triangle array");
+    if (ntri < 0 || ntri > (int64_t)INT32_MAX / 2) {
+        set_last_error(std::string(what) + ": bad triangle count");
         return PBG_ERR_INVALID_ARGUMENT;
     }
     if (accel != PBG_ACCEL_NAIVE && accel != PBG_ACCEL_RAYHIERARCHY && accel != PBG_ACCEL_RAYBVH) {
-        set_last_error("pbg_scene_create: unknown accelerator kind");
+        set_last_error(std::string(what) + ": unknown accelerator kind");
         return PBG_ERR_INVALID_ARGUMENT;
     }
     if (pbg_device_count() == 0) {
-        set_last_error("pbg_scene_create: no CUDA device");
+        set_last_error(std::string(what) + ": no CUDA device");
         return PBG_ERR_NO_DEVICE;
+    }
+    return PBG_OK;
+}
+
+}  // namespace pbg
+
+extern "C" {
+
+int pbg_scene_create_mesh(const float* P, int64_t nverts, const int32_t* indices, int64_t ntri, const float* uv,
+                          int32_t accel, const pbg_params* params, pbg_scene** out) {
+    int rc = scene_args("pbg_scene_create_mesh", ntri, accel, out);
+    if (rc) return rc;
+    if (nverts < 0 || (ntri > 0 && (!P || !indices || nverts == 0))) {
+        set_last_error("pbg_scene_create_mesh: bad vertex or index array");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if (accel == PBG_ACCEL_RAYHIERARCHY) {  // its record order and spheres are built on the host
+        std::vector<float> tri9((size_t)ntri * 9), uv6(uv ? (size_t)ntri * 6 : 0);
+        for (int64_t i = 0; i < ntri; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const int32_t v = indices[3 * i + k];
+                if (v < 0 || v >= nverts) {
+                    set_last_error("pbg_scene_create_mesh: vertex index out of range");
+                    return PBG_ERR_INVALID_ARGUMENT;
+                }
+                for (int a = 0; a < 3; ++a) tri9[9 * i + 3 * k + a] = P[3 * (int64_t)v + a];
+                if (uv) {
+                    uv6[6 * i + 2 * k] = uv[2 * (int64_t)v];
+                    uv6[6 * i + 2 * k + 1] = uv[2 * (int64_t)v + 1];
+                }
+            }
+        return pbg_scene_create(tri9.data(), uv ? uv6.data() : nullptr, ntri, accel, params, out);
+    }
+    pbg_scene* s = new (std::nothrow) pbg_scene();
+    if (!s) return PBG_ERR_OUT_OF_MEMORY;
+    if (params) s->params = *params;
+    s->device = s->params.device;
+    s->accel = accel;
+    s->ntri = ntri;
+    auto fail = [&](int code) {
+        pbg_scene_destroy(s);
+        return code;
+    };
+    if ((rc = scene_init(s))) return fail(rc);
+    const size_t nt = (size_t)(ntri > 0 ? ntri : 1);
+    if ((rc = ensure(s->tri9, nt * 9 * sizeof(float)))) return fail(rc);
+    if (uv && (rc = ensure(s->uv6, nt * 6 * sizeof(float)))) return fail(rc);
+    if (ntri > 0) {
+        DeviceBuffer dp, di, du;
+        struct G {
+            DeviceBuffer *a, *b, *c;
+            ~G() { release(*a); release(*b); release(*c); }
+        } g{&dp, &di, &du};
+        if ((rc = ensure(dp, (size_t)nverts * 12)) || (rc = ensure(di, (size_t)ntri * 12)) ||
+            (uv && (rc = ensure(du, (size_t)nverts * 8))))
+            return fail(rc);
+        cudaStream_t st = s->stream;
+        cudaError_t e = cudaMemcpyAsync(dp.ptr, P, (size_t)nverts * 12, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(di.ptr, indices, (size_t)ntri * 12, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && uv) e = cudaMemcpyAsync(du.ptr, uv, (size_t)nverts * 8, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->err.ptr, 0, sizeof(int), st);
+        if (e != cudaSuccess) return fail(cuda_status(e, "pbg_scene_create_mesh upload"));
+        gather_mesh_kernel<<<(unsigned)((ntri + 255) / 256), 256, 0, st>>>(
+            (const float*)dp.ptr, (const int32_t*)di.ptr, uv ? (const float*)du.ptr : nullptr, ntri, nverts,
+            (float*)s->tri9.ptr, uv ? (float*)s->uv6.ptr : nullptr, (int*)s->err.ptr);
+        s->counters.kernel_launches += 1;
+        int bad = 0;
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, s->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail(cuda_status(e, "gather_mesh_kernel"));
+        if (bad) {
+            PBG_CUDA(cudaMemset(s->err.ptr, 0, sizeof(int)));
+            set_last_error("pbg_scene_create_mesh: vertex index out of range");
+            return fail(PBG_ERR_INVALID_ARGUMENT);
+        }
+    }
+    if ((rc = scene_build_device(s))) return fail(rc);
+    *out = s;
+    return PBG_OK;
+}
+
+int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t accel,
+                     const pbg_params* params, pbg_scene** out) {
+    int rc0 = scene_args("pbg_scene_create", ntri, accel, out);
+    if (rc0) return rc0;
+    if (ntri > 0 && !tri9) {
+        set_last_error("pbg_scene_create: bad triangle array");
+        return PBG_ERR_INVALID_ARGUMENT;
     }
     pbg_scene* s = new (std::nothrow) pbg_scene();
     if (!s) return PBG_ERR_OUT_OF_MEMORY;
@@ -901,21 +1075,26 @@ int pbg_scene_create(const float* tri9, const float* uv6, int64_t ntri, int32_t 
         pbg_scene_destroy(s);
         return code;
     };
-    {
-        cudaError_t e = cudaSetDevice(s->device);
-        if (e != cudaSuccess) return fail(cuda_status(e, "cudaSetDevice"));
-        e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-        if (e != cudaSuccess) return fail(cuda_status(e, "cudaStreamCreate"));
+    if (accel != PBG_ACCEL_RAYHIERARCHY && !(accel == PBG_ACCEL_RAYBVH && s->params.bvh_build == 1)) {
+        // the triangles go to the device as they are; the rest is built there
+        if ((rc = scene_init(s))) return fail(rc);
+        const size_t nt = (size_t)(ntri > 0 ? ntri : 1);
+        if ((rc = ensure(s->tri9, nt * 9 * sizeof(float)))) return fail(rc);
+        if (ntri > 0) {
+            cudaError_t e = cudaMemcpy(s->tri9.ptr, tri9, (size_t)ntri * 9 * sizeof(float), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return fail(cuda_status(e, "cudaMemcpy(triangles)"));
+        }
+        if ((rc = scene_build_device(s))) return fail(rc);
+        if (uv6 && ntri > 0) {
+            if ((rc = ensure(s->uv6, (size_t)ntri * 6 * sizeof(float)))) return fail(rc);
+            cudaError_t e = cudaMemcpy(s->uv6.ptr, uv6, (size_t)ntri * 6 * sizeof(float), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return fail(cuda_status(e, "cudaMemcpy(uv)"));
+        }
+        *out = s;
+        return PBG_OK;
     }
-    if ((rc = ensure(s->err, 4 * sizeof(int)))) return fail(rc);
-    {
-        cudaError_t e = cudaHostAlloc((void**)&s->mbox_host, kMailboxWords * sizeof(int), cudaHostAllocMapped);
-        if (e == cudaSuccess) memset(s->mbox_host, 0, kMailboxWords * sizeof(int));
-        if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&s->mbox_dev, s->mbox_host, 0);
-        if (e != cudaSuccess) return fail(cuda_status(e, "cudaHostAlloc(status words)"));
-    }
-    if (cudaMemset(s->err.ptr, 0, 4 * sizeof(int)) != cudaSuccess)
-        return fail(cuda_status(cudaGetLastError(), "cudaMemset"));
+    // rayhierarchy (and ray-bvh with bvh_build = 1): record order built on the host
+    if ((rc = scene_init(s))) return fail(rc);
     for (int64_t i = 0; i < ntri; ++i)
         for (int k = 0; k < 9; ++k) {
             float v = tri9[9 * i + k];
@@ -997,9 +1176,15 @@ int pbg_max_rays_per_call(const pbg_scene* s, int64_t* out) {
     return PBG_OK;
 }
 
+// Device rays are read as float4: views that are not 16-byte aligned (a
+// sliced tensor, an odd offset) are refused instead of faulting the GPU.
+static bool rays_aligned(const float* o4, const float* d4) {
+    return (((uintptr_t)o4 | (uintptr_t)d4) & 15u) == 0;
+}
+
 int pbg_intersect_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid,
                          int64_t n, int32_t* prim, float* t, float* b1, float* b2, void* stream) {
-    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2))) {
+    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2)) || !rays_aligned(o4, d4)) {
         set_last_error("pbg_intersect_device: bad arguments");
         return PBG_ERR_INVALID_ARGUMENT;
     }
@@ -1016,7 +1201,7 @@ int pbg_intersect_device(pbg_scene* s, const float* o4, const float* d4, const u
 
 int pbg_occluded_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid,
                         int64_t n, uint8_t* occ, void* stream) {
-    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !occ))) {
+    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !occ)) || !rays_aligned(o4, d4)) {
         set_last_error("pbg_occluded_device: bad arguments");
         return PBG_ERR_INVALID_ARGUMENT;
     }
@@ -1043,7 +1228,8 @@ int pbg_clusters_of_device(pbg_scene* s, const int32_t* prim, int64_t n, uint16_
 int pbg_intersect_hinted_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid, int64_t n,
                                 const uint16_t* hint, int32_t* prim, float* t, float* b1, float* b2,
                                 void* stream) {
-    if (!s || n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2))) {
+    if (!s || n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2)) ||
+        !rays_aligned(o4, d4)) {
         set_last_error("pbg_intersect_hinted_device: bad arguments");
         return PBG_ERR_INVALID_ARGUMENT;
     }
@@ -1063,7 +1249,7 @@ int pbg_intersect_hinted_device(pbg_scene* s, const float* o4, const float* d4, 
 
 int pbg_occluded_hinted_device(pbg_scene* s, const float* o4, const float* d4, const uint8_t* valid, int64_t n,
                                const uint16_t* hint, uint8_t* occ, int32_t* occluders, void* stream) {
-    if (!s || n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!o4 || !d4 || !occ))) {
+    if (!s || n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!o4 || !d4 || !occ)) || !rays_aligned(o4, d4)) {
         set_last_error("pbg_occluded_hinted_device: bad arguments");
         return PBG_ERR_INVALID_ARGUMENT;
     }
@@ -1169,7 +1355,7 @@ int pbg_occluded(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t* occ) {
 int pbg_hit_geometry_device(pbg_scene* s, const float* o4, const float* d4, const int32_t* prim,
                             const float* t, const float* b1, const float* b2, int64_t n,
                             float* out14, void* stream) {
-    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2 || !out14)))
+    if (!s || n < 0 || (n > 0 && (!o4 || !d4 || !prim || !t || !b1 || !b2 || !out14)) || !rays_aligned(o4, d4))
         return PBG_ERR_INVALID_ARGUMENT;
     cudaSetDevice(s->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;

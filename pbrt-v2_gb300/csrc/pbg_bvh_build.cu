@@ -1,0 +1,574 @@
+// pbg_bvh_build.cu -- the ray-bvh tree built on the device.
+//
+// The reference builds pbrt's BVHAccel on the CPU for every triangle part
+// (accelerators/bvh.cpp:209-283, rayBVH.cpp:204-276).  This builder makes
+// the tree of bvh_build.cpp -- binned SAH over all three axes with 32 bins,
+// leaves of at most max_leaf triangles, degenerate triangles in front of the
+// tree, every box padded outward the same way -- with the same split
+// decisions, level by level on the GPU:
+//
+//   prep      per triangle: degenerate or not (the host test, in double),
+//             its box and centroid; degenerate triangles first in the record
+//             order, the others become build items in index order; the scene
+//             bounds and the largest coordinate (the global pad)
+//   split     one CTA per segment of the current level: node and centroid
+//             bounds (block reduction), the leaf decision, 3 x 32 bins in
+//             shared memory, the SAH sweep of each axis by one thread in the
+//             host builder's float order, and a stable partition of the
+//             segment's items into the other buffer; leaves write their
+//             triangles' record order
+//   link      a scan over the level's inner segments numbers their nodes
+//             (breadth first), every segment writes its box (padded) and
+//             reference into its parent's slot, and inner segments emit the
+//             next level's two children
+//
+// The host reads one count per level.  Segments whose centroids fall into
+// one bin split at the middle of their current order (the host builder
+// takes a median by centroid there); the tree is otherwise the host tree,
+// numbered breadth first instead of depth first.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "pbg_internal.h"
+
+namespace pbg {
+
+int scan_counts(pbg_scene* s, uint32_t* a, int64_t m, cudaStream_t st);
+
+namespace {
+
+constexpr int kBins = 32;
+constexpr int kBT = 256;  // threads per CTA
+constexpr int kDepthLimit = 48;
+
+struct BItem {
+    float lo[3], hi[3], c[3];
+    int32_t idx;
+};
+
+struct BSeg {
+    int32_t begin, end, node, slot, depth;
+};
+
+struct BRes {
+    int32_t leaf, mid;
+    float lo[3], hi[3];
+};
+
+// Floats as unsigned keys whose order is the floats' order (for atomics).
+__device__ __forceinline__ uint32_t fenc(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fdec(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// triangle_degenerate of bvh_build.cpp, in the same double arithmetic.
+__device__ bool degenerate(const float* v) {
+    for (int k = 0; k < 9; ++k)
+        if (!isfinite(v[k])) return true;
+    double e1[3], e2[3];
+    for (int k = 0; k < 3; ++k) {
+        e1[k] = __dsub_rn((double)v[3 + k], (double)v[k]);
+        e2[k] = __dsub_rn((double)v[6 + k], (double)v[k]);
+    }
+    const double cx = __dsub_rn(__dmul_rn(e1[1], e2[2]), __dmul_rn(e1[2], e2[1]));
+    const double cy = __dsub_rn(__dmul_rn(e1[2], e2[0]), __dmul_rn(e1[0], e2[2]));
+    const double cz = __dsub_rn(__dmul_rn(e1[0], e2[1]), __dmul_rn(e1[1], e2[0]));
+    const double a2 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(cx, cx), __dmul_rn(cy, cy)), __dmul_rn(cz, cz)));
+    const double l1 = __dmul_rn(__dadd_rn(__dadd_rn(fabs(e1[0]), fabs(e1[1])), fabs(e1[2])),
+                                __dadd_rn(__dadd_rn(fabs(e2[0]), fabs(e2[1])), fabs(e2[2])));
+    return !(a2 > __dmul_rn(0x1p-16, l1));
+}
+
+// Box::area of bvh_build.cpp.
+__device__ __forceinline__ float box_area(const float* lo, const float* hi) {
+    const float dx = __fsub_rn(hi[0], lo[0]), dy = __fsub_rn(hi[1], lo[1]), dz = __fsub_rn(hi[2], lo[2]);
+    if (!(dx >= 0.f) || !(dy >= 0.f) || !(dz >= 0.f)) return 0.f;
+    return __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(dx, dy), __fmul_rn(dx, dz)), __fmul_rn(dy, dz)));
+}
+
+__device__ __forceinline__ int bin_of(float c, float lo, float scale) {
+    int b = (int)__fmul_rn(__fsub_rn(c, lo), scale);
+    return b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+}
+
+// Degenerate flags per triangle, counted per block; scene bounds.
+__global__ void prep_count_kernel(const float* __restrict__ tri9, int64_t n, uint32_t* __restrict__ counts,
+                                  uint32_t* __restrict__ bounds) {
+    const int64_t i = (int64_t)blockIdx.x * kBT + threadIdx.x;
+    bool deg = false;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (i < n) {
+        const float* v = tri9 + 9 * i;
+        deg = degenerate(v);
+        for (int k = 0; k < 9; ++k) {
+            const float x = v[k];
+            if (x == x) {
+                lo[k % 3] = fminf(lo[k % 3], x);
+                hi[k % 3] = fmaxf(hi[k % 3], x);
+            }
+        }
+    }
+    const int c = __syncthreads_count(deg);
+    if (threadIdx.x == 0) counts[blockIdx.x] = (uint32_t)c;
+    for (int a = 0; a < 3; ++a) {
+        for (int off = 16; off; off >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], off));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&bounds[a], fenc(lo[a]));
+            atomicMax(&bounds[3 + a], fenc(hi[a]));
+        }
+    }
+}
+
+// Degenerate triangles to the front of the record order, the others to
+// build items, both in index order; the largest item coordinate.
+__global__ void prep_scatter_kernel(const float* __restrict__ tri9, int64_t n, const uint32_t* __restrict__ offs,
+                                    int32_t* __restrict__ order, BItem* __restrict__ items,
+                                    uint32_t* __restrict__ gmax) {
+    __shared__ uint32_t wdeg[kBT / 32];
+    const int64_t i = (int64_t)blockIdx.x * kBT + threadIdx.x;
+    const bool valid = i < n;
+    const float* v = tri9 + 9 * (valid ? i : 0);
+    const bool deg = valid && degenerate(v);
+    const unsigned bd = __ballot_sync(0xffffffffu, deg), bv = __ballot_sync(0xffffffffu, valid);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wdeg[warp] = __popc(bd);
+    __syncthreads();
+    uint32_t before = 0;  // degenerate triangles of this block before this warp
+    for (int w = 0; w < warp; ++w) before += wdeg[w];
+    if (!valid) return;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t deg_rank = before + __popc(bd & lt);
+    const int64_t block0 = (int64_t)blockIdx.x * kBT;
+    if (deg) {
+        order[offs[blockIdx.x] + deg_rank] = (int32_t)i;
+        return;
+    }
+    // non-degenerate: position = non-degenerate triangles before this one
+    const int64_t nd_before = block0 - offs[blockIdx.x] + (warp * 32 - before) + __popc(bv & ~bd & lt);
+    BItem it;
+    float m = 0.f;
+    for (int a = 0; a < 3; ++a) {
+        const float x0 = v[a], x1 = v[3 + a], x2 = v[6 + a];
+        it.lo[a] = fminf(fminf(x0, x1), x2);
+        it.hi[a] = fmaxf(fmaxf(x0, x1), x2);
+        it.c[a] = __fmul_rn(0.5f, __fadd_rn(it.lo[a], it.hi[a]));
+        m = fmaxf(m, fmaxf(fabsf(it.lo[a]), fabsf(it.hi[a])));
+    }
+    it.idx = (int32_t)i;
+    items[nd_before] = it;
+    atomicMax(gmax, __float_as_uint(m));  // non-negative floats order as their bits
+}
+
+// One CTA per segment: bounds, leaf decision, binned SAH, stable partition.
+__global__ void __launch_bounds__(kBT) split_kernel(const BItem* __restrict__ in, BItem* __restrict__ out,
+                                                    const BSeg* __restrict__ segs, BRes* __restrict__ res,
+                                                    int32_t* __restrict__ order, int32_t unculled, int max_leaf,
+                                                    int* __restrict__ max_depth) {
+    __shared__ float red[kBT / 32][12];
+    __shared__ float nb[6], cb[6];
+    __shared__ uint32_t bcnt[3][kBins], blo[3][kBins][3], bhi[3][kBins][3];
+    __shared__ float acost[3];
+    __shared__ int asplit[3];
+    __shared__ int s_leaf, s_axis, s_split, s_median;
+    __shared__ uint32_t wl[kBT / 32], wr[kBT / 32];
+    __shared__ int32_t run_l, run_r;
+    const BSeg sg = segs[blockIdx.x];
+    const int32_t np = sg.end - sg.begin;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) atomicMax(max_depth, sg.depth);
+    // node box and centroid box
+    float v[12];
+    for (int a = 0; a < 3; ++a) {
+        v[a] = INFINITY;
+        v[3 + a] = -INFINITY;
+        v[6 + a] = INFINITY;
+        v[9 + a] = -INFINITY;
+    }
+    for (int32_t i = sg.begin + threadIdx.x; i < sg.end; i += kBT) {
+        const BItem it = in[i];
+        for (int a = 0; a < 3; ++a) {
+            v[a] = fminf(v[a], it.lo[a]);
+            v[3 + a] = fmaxf(v[3 + a], it.hi[a]);
+            v[6 + a] = fminf(v[6 + a], it.c[a]);
+            v[9 + a] = fmaxf(v[9 + a], it.c[a]);
+        }
+    }
+    for (int k = 0; k < 12; ++k) {
+        const bool is_min = (k % 6) < 3;
+        for (int off = 16; off; off >>= 1) {
+            const float o = __shfl_xor_sync(0xffffffffu, v[k], off);
+            v[k] = is_min ? fminf(v[k], o) : fmaxf(v[k], o);
+        }
+        if (lane == 0) red[warp][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        const int k = threadIdx.x;
+        const bool is_min = (k % 6) < 3;
+        float r = red[0][k];
+        for (int w = 1; w < kBT / 32; ++w) r = is_min ? fminf(r, red[w][k]) : fmaxf(r, red[w][k]);
+        if (k < 6) nb[k] = r;
+        else cb[k - 6] = r;
+    }
+    for (int k = threadIdx.x; k < 3 * kBins; k += kBT) {
+        (&bcnt[0][0])[k] = 0u;
+        for (int q = 0; q < 3; ++q) {
+            (&blo[0][0][0])[3 * k + q] = 0xffffffffu;  // fenc(+inf) < this: empty bins decode to NaN-free +inf below
+            (&bhi[0][0][0])[3 * k + q] = 0u;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int axis = 0;
+        float ext = __fsub_rn(cb[3], cb[0]);
+        for (int a = 1; a < 3; ++a)
+            if (__fsub_rn(cb[3 + a], cb[a]) > ext) {
+                axis = a;
+                ext = __fsub_rn(cb[3 + a], cb[a]);
+            }
+        s_axis = axis;
+        s_leaf = np <= max_leaf || !(ext > 0.f) || sg.depth >= kDepthLimit;
+        s_median = 0;
+        s_split = -1;
+    }
+    __syncthreads();
+    if (!s_leaf) {
+        for (int32_t i = sg.begin + threadIdx.x; i < sg.end; i += kBT) {
+            const BItem it = in[i];
+            for (int a = 0; a < 3; ++a) {
+                const float ea = __fsub_rn(cb[3 + a], cb[a]);
+                if (!(ea > 0.f)) continue;
+                const int b = bin_of(it.c[a], cb[a], __fdiv_rn((float)kBins, ea));
+                atomicAdd(&bcnt[a][b], 1u);
+                for (int q = 0; q < 3; ++q) {
+                    atomicMin(&blo[a][b][q], fenc(it.lo[q]));
+                    atomicMax(&bhi[a][b][q], fenc(it.hi[q]));
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {  // the SAH sweep of one axis, in the host builder's order
+            const int a = threadIdx.x;
+            float best = INFINITY;
+            int bk = -1;
+            if (__fsub_rn(cb[3 + a], cb[a]) > 0.f) {
+                float rarea[kBins];
+                int rcnt[kBins];
+                float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+                int c = 0;
+                for (int k = kBins - 1; k > 0; --k) {
+                    if (bcnt[a][k]) {
+                        for (int q = 0; q < 3; ++q) {
+                            lo[q] = fminf(lo[q], fdec(blo[a][k][q]));
+                            hi[q] = fmaxf(hi[q], fdec(bhi[a][k][q]));
+                        }
+                    }
+                    c += (int)bcnt[a][k];
+                    rarea[k] = box_area(lo, hi);
+                    rcnt[k] = c;
+                }
+                for (int q = 0; q < 3; ++q) {
+                    lo[q] = INFINITY;
+                    hi[q] = -INFINITY;
+                }
+                c = 0;
+                for (int k = 0; k < kBins - 1; ++k) {
+                    if (bcnt[a][k]) {
+                        for (int q = 0; q < 3; ++q) {
+                            lo[q] = fminf(lo[q], fdec(blo[a][k][q]));
+                            hi[q] = fmaxf(hi[q], fdec(bhi[a][k][q]));
+                        }
+                    }
+                    c += (int)bcnt[a][k];
+                    if (c == 0 || rcnt[k + 1] == 0) continue;
+                    const float cost = __fadd_rn(__fmul_rn(box_area(lo, hi), (float)c),
+                                                 __fmul_rn(rarea[k + 1], (float)rcnt[k + 1]));
+                    if (cost < best) {
+                        best = cost;
+                        bk = k;
+                    }
+                }
+            }
+            acost[a] = best;
+            asplit[a] = bk;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float best = INFINITY;
+            int ba = -1, bs = -1;
+            for (int a = 0; a < 3; ++a)
+                if (asplit[a] >= 0 && acost[a] < best) {
+                    best = acost[a];
+                    ba = a;
+                    bs = asplit[a];
+                }
+            if (bs < 0) {
+                s_leaf = np <= 4 * max_leaf || sg.depth >= kDepthLimit;
+                s_median = !s_leaf;
+            } else {
+                s_axis = ba;
+                s_split = bs;
+            }
+        }
+        __syncthreads();
+    }
+    if (s_leaf) {
+        for (int32_t i = sg.begin + threadIdx.x; i < sg.end; i += kBT) order[unculled + i] = in[i].idx;
+        if (threadIdx.x == 0) {
+            BRes r;
+            r.leaf = 1;
+            r.mid = -1;
+            for (int q = 0; q < 6; ++q) (q < 3 ? r.lo[q] : r.hi[q - 3]) = nb[q];
+            res[blockIdx.x] = r;
+        }
+        return;
+    }
+    int32_t nleft;
+    if (s_median) {  // centroids in one bin on every axis: split the current order in the middle
+        for (int32_t i = sg.begin + threadIdx.x; i < sg.end; i += kBT) out[i] = in[i];
+        nleft = np / 2;
+    } else {
+        const int a = s_axis, bs = s_split;
+        nleft = 0;
+        for (int k = 0; k <= bs; ++k) nleft += (int32_t)bcnt[a][k];
+        const float scale = __fdiv_rn((float)kBins, __fsub_rn(cb[3 + a], cb[a]));
+        const float lo = cb[a];
+        if (threadIdx.x == 0) {
+            run_l = 0;
+            run_r = 0;
+        }
+        __syncthreads();
+        for (int32_t base = sg.begin; base < sg.end; base += kBT) {
+            const int32_t i = base + threadIdx.x;
+            const bool valid = i < sg.end;
+            BItem it;
+            bool left = false;
+            if (valid) {
+                it = in[i];
+                left = bin_of(it.c[a], lo, scale) <= bs;
+            }
+            const unsigned bl = __ballot_sync(0xffffffffu, valid && left);
+            const unsigned br = __ballot_sync(0xffffffffu, valid && !left);
+            if (lane == 0) {
+                wl[warp] = __popc(bl);
+                wr[warp] = __popc(br);
+            }
+            __syncthreads();
+            uint32_t pl = 0, pr = 0, tl = 0, tr = 0;
+            for (int w = 0; w < kBT / 32; ++w) {
+                if (w < warp) {
+                    pl += wl[w];
+                    pr += wr[w];
+                }
+                tl += wl[w];
+                tr += wr[w];
+            }
+            const unsigned lt = (1u << lane) - 1u;
+            if (valid) {
+                const int32_t dst = left ? sg.begin + run_l + (int32_t)(pl + __popc(bl & lt))
+                                         : sg.begin + nleft + run_r + (int32_t)(pr + __popc(br & lt));
+                out[dst] = it;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                run_l += (int32_t)tl;
+                run_r += (int32_t)tr;
+            }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        BRes r;
+        r.leaf = 0;
+        r.mid = sg.begin + nleft;
+        for (int q = 0; q < 6; ++q) (q < 3 ? r.lo[q] : r.hi[q - 3]) = nb[q];
+        res[blockIdx.x] = r;
+    }
+}
+
+__global__ void inner_count_kernel(const BRes* __restrict__ res, int64_t nseg, uint32_t* __restrict__ counts) {
+    const int64_t i = (int64_t)blockIdx.x * kBT + threadIdx.x;
+    const int c = __syncthreads_count(i < nseg && !res[i].leaf);
+    if (threadIdx.x == 0) counts[blockIdx.x] = (uint32_t)c;
+}
+
+// pad_of / write_child of bvh_build.cpp, one scalar store per field (the
+// two children of a node are written by different threads).
+__device__ void write_slot(BvhNode* nd, int slot, const float* lo_in, const float* hi_in, int32_t child,
+                           int32_t count, float gpad) {
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        if (count == 0 && child < 0) {
+            lo[a] = INFINITY;
+            hi[a] = -INFINITY;
+            continue;
+        }
+        const float mag = fmaxf(fabsf(lo_in[a]), fabsf(hi_in[a]));
+        float ext = __fsub_rn(hi_in[a], lo_in[a]);
+        if (!(ext >= 0.f)) ext = 0.f;
+        const float p = __fadd_rn(__fmul_rn(__fadd_rn(mag, ext), 0x1p-13f), gpad);
+        lo[a] = nextafterf(__fsub_rn(lo_in[a], p), -INFINITY);
+        hi[a] = nextafterf(__fadd_rn(hi_in[a], p), INFINITY);
+    }
+    if (slot == 0) {
+        nd->n0.x = lo[0]; nd->n0.y = hi[0]; nd->n0.z = lo[1]; nd->n0.w = hi[1];
+        nd->n2.x = lo[2]; nd->n2.y = hi[2];
+        nd->n3.x = child; nd->n3.z = count;
+    } else {
+        nd->n1.x = lo[0]; nd->n1.y = hi[0]; nd->n1.z = lo[1]; nd->n1.w = hi[1];
+        nd->n2.z = lo[2]; nd->n2.w = hi[2];
+        nd->n3.y = child; nd->n3.w = count;
+    }
+}
+
+__global__ void link_kernel(const BSeg* __restrict__ segs, const BRes* __restrict__ res, int64_t nseg,
+                            const uint32_t* __restrict__ offs, int32_t node_base, BvhNode* __restrict__ nodes,
+                            BSeg* __restrict__ next, int32_t unculled, const uint32_t* __restrict__ gmax) {
+    __shared__ uint32_t wbase[kBT / 32];
+    const int64_t i = (int64_t)blockIdx.x * kBT + threadIdx.x;
+    const bool valid = i < nseg;
+    const bool inner = valid && !res[i].leaf;
+    const unsigned b = __ballot_sync(0xffffffffu, inner);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wbase[warp] = __popc(b);
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; ++w) before += wbase[w];
+    if (!valid) return;
+    const float m = __uint_as_float(*gmax);
+    const float gpad = isfinite(m) ? __fmul_rn(m, 0x1p-18f) : 0.f;
+    const BSeg sg = segs[i];
+    const BRes r = res[i];
+    const float empty_lo[3] = {INFINITY, INFINITY, INFINITY}, empty_hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (r.leaf) {
+        const int32_t start = unculled + sg.begin, cnt = sg.end - sg.begin;
+        if (sg.node < 0) {  // the whole scene in one leaf
+            write_slot(&nodes[0], 0, r.lo, r.hi, ~start, cnt, gpad);
+            write_slot(&nodes[0], 1, empty_lo, empty_hi, -1, 0, gpad);
+        } else {
+            write_slot(&nodes[sg.node], sg.slot, r.lo, r.hi, ~start, cnt, gpad);
+        }
+        return;
+    }
+    const uint32_t rank = offs[blockIdx.x] + before + __popc(b & ((1u << lane) - 1u));
+    const int32_t self = node_base + (int32_t)rank;
+    if (sg.node >= 0) write_slot(&nodes[sg.node], sg.slot, r.lo, r.hi, self, 0, gpad);
+    next[2 * rank] = BSeg{sg.begin, r.mid, self, 0, sg.depth + 1};
+    next[2 * rank + 1] = BSeg{r.mid, sg.end, self, 1, sg.depth + 1};
+}
+
+__global__ void empty_root_kernel(BvhNode* nodes) {
+    const float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    write_slot(&nodes[0], 0, lo, hi, -1, 0, 0.f);
+    write_slot(&nodes[0], 1, lo, hi, -1, 0, 0.f);
+}
+
+}  // namespace
+
+// Builds s->bvh from the scene's device triangles (original order, tri9)
+// and writes the record order (degenerate triangles first) into order_dev
+// [ntri]; fills bvh_nodes, bvh_depth, unculled, scene_lo / scene_hi.
+int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf, int32_t* order_dev,
+                     cudaStream_t st) {
+    if (max_leaf < 1) max_leaf = 4;
+    const int64_t nb = (ntri + kBT - 1) / kBT;
+    DeviceBuffer counts, small, items_a, items_b, segs_a, segs_b, res;
+    struct Guard {
+        DeviceBuffer* b[7];
+        ~Guard() {
+            for (DeviceBuffer* x : b) release(*x);
+        }
+    } guard{{&counts, &small, &items_a, &items_b, &segs_a, &segs_b, &res}};
+    const size_t ni = (size_t)std::max<int64_t>(ntri, 1);
+    int rc;
+    if ((rc = ensure(counts, (size_t)(std::max<int64_t>(nb, ni / kBT + 1) + 8) * 4)) || (rc = ensure(small, 64)) ||
+        (rc = ensure(items_a, ni * sizeof(BItem))) || (rc = ensure(items_b, ni * sizeof(BItem))) ||
+        (rc = ensure(segs_a, ni * sizeof(BSeg))) || (rc = ensure(segs_b, ni * sizeof(BSeg))) ||
+        (rc = ensure(res, ni * sizeof(BRes))) || (rc = ensure(s->bvh, ni * sizeof(BvhNode))))
+        return rc;
+    uint32_t* sm = (uint32_t*)small.ptr;  // [0..5] scene bounds, [6] gmax, [7] max depth
+    std::vector<uint32_t> init = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u, 0u, 0u};
+    PBG_CUDA(cudaMemcpyAsync(sm, init.data(), init.size() * 4, cudaMemcpyHostToDevice, st));
+    int32_t ndeg = 0;
+    if (ntri > 0) {
+        uint32_t* cnt = (uint32_t*)counts.ptr;
+        prep_count_kernel<<<(unsigned)nb, kBT, 0, st>>>(tri9, ntri, cnt, sm);
+        PBG_CUDA(cudaGetLastError());
+        uint32_t last = 0, off = 0;
+        PBG_CUDA(cudaMemcpyAsync(&last, cnt + nb - 1, 4, cudaMemcpyDeviceToHost, st));
+        if ((rc = scan_counts(s, cnt, nb, st))) return rc;
+        PBG_CUDA(cudaMemcpyAsync(&off, cnt + nb - 1, 4, cudaMemcpyDeviceToHost, st));
+        prep_scatter_kernel<<<(unsigned)nb, kBT, 0, st>>>(tri9, ntri, cnt, order_dev, (BItem*)items_a.ptr, sm + 6);
+        PBG_CUDA(cudaGetLastError());
+        PBG_CUDA(cudaStreamSynchronize(st));
+        ndeg = (int32_t)(off + last);
+        s->counters.kernel_launches += 2;
+    }
+    const int64_t nitems = ntri - ndeg;
+    BvhNode* nodes = (BvhNode*)s->bvh.ptr;
+    int32_t node_base = 0;
+    if (nitems == 0) {
+        empty_root_kernel<<<1, 1, 0, st>>>(nodes);
+        PBG_CUDA(cudaGetLastError());
+        node_base = 1;
+    } else {
+        BSeg root{0, (int32_t)nitems, -1, 0, 0};
+        PBG_CUDA(cudaMemcpyAsync(segs_a.ptr, &root, sizeof(root), cudaMemcpyHostToDevice, st));
+        BItem* in = (BItem*)items_a.ptr;
+        BItem* out = (BItem*)items_b.ptr;
+        BSeg* cur = (BSeg*)segs_a.ptr;
+        BSeg* nxt = (BSeg*)segs_b.ptr;
+        int64_t nseg = 1;
+        while (nseg > 0) {
+            split_kernel<<<(unsigned)nseg, kBT, 0, st>>>(in, out, cur, (BRes*)res.ptr, order_dev, ndeg, max_leaf,
+                                                        (int*)(sm + 7));
+            PBG_CUDA(cudaGetLastError());
+            const int64_t lb = (nseg + kBT - 1) / kBT;
+            uint32_t* cnt = (uint32_t*)counts.ptr;
+            inner_count_kernel<<<(unsigned)lb, kBT, 0, st>>>((const BRes*)res.ptr, nseg, cnt);
+            PBG_CUDA(cudaGetLastError());
+            uint32_t last = 0, off = 0;
+            PBG_CUDA(cudaMemcpyAsync(&last, cnt + lb - 1, 4, cudaMemcpyDeviceToHost, st));
+            if ((rc = scan_counts(s, cnt, lb, st))) return rc;
+            PBG_CUDA(cudaMemcpyAsync(&off, cnt + lb - 1, 4, cudaMemcpyDeviceToHost, st));
+            link_kernel<<<(unsigned)lb, kBT, 0, st>>>(cur, (const BRes*)res.ptr, nseg, cnt, node_base, nodes, nxt,
+                                                      ndeg, sm + 6);
+            PBG_CUDA(cudaGetLastError());
+            PBG_CUDA(cudaStreamSynchronize(st));
+            s->counters.kernel_launches += 3;
+            const int64_t inner = (int64_t)off + last;
+            node_base += (int32_t)inner;
+            if (node_base == 0) node_base = 1;  // the root was a leaf
+            nseg = 2 * inner;
+            std::swap(in, out);
+            std::swap(cur, nxt);
+        }
+    }
+    uint32_t h[8];
+    PBG_CUDA(cudaMemcpyAsync(h, sm, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PBG_CUDA(cudaStreamSynchronize(st));
+    auto dec = [](uint32_t u) {
+        const uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+        float f;
+        memcpy(&f, &b, 4);
+        return f;
+    };
+    for (int a = 0; a < 3; ++a) {
+        s->scene_lo[a] = ntri > 0 ? dec(h[a]) : 0.f;
+        s->scene_hi[a] = ntri > 0 ? dec(h[3 + a]) : 0.f;
+    }
+    s->bvh_nodes = node_base;
+    s->bvh_depth = (int)h[7];
+    s->unculled = ndeg;
+    s->counters.bvh_nodes = (uint64_t)node_base;
+    return PBG_OK;
+}
+
+}  // namespace pbg

@@ -457,6 +457,11 @@ int ensure_clusters(pbg_scene* s) {
     if (!s->learn) s->learn = new Learner();
     Learner* L = s->learn;
     if (L->clusters_built) return PBG_OK;
+    if (s->host_nodes.empty() && s->bvh_nodes > 0) {  // a tree built on the device: the cut is made on the host
+        s->host_nodes.resize((size_t)s->bvh_nodes);
+        PBG_CUDA(cudaMemcpy(s->host_nodes.data(), s->bvh.ptr, s->host_nodes.size() * sizeof(BvhNode),
+                            cudaMemcpyDeviceToHost));
+    }
     std::vector<int32_t> refs;
     std::vector<uint16_t> rc16;
     build_clusters(s->host_nodes, s->ntri, &refs, &rc16);
@@ -506,10 +511,14 @@ int learn_init(pbg_scene* s, const pbg_learn_params* p) {
         if (p->lr > 0.f) L->lr = p->lr;
         if (p->margin != 0.f) L->margin = p->margin;
         if (p->momentum > 0.f) L->momentum = p->momentum;
-        if (p->records > 0) L->capacity = p->records;
+        if (p->records > 0 && !L->W1.ptr) L->capacity = p->records;  // the ring is sized once
         if (p->seed) L->seed = p->seed;
     }
     if (p && p->queries > 0) L->queries = p->queries & 3;
+    if (L->W1.ptr) {  // initialised before: keep the weights and records
+        L->enabled = true;
+        return PBG_OK;
+    }
     if (L->capacity < L->batch) L->capacity = L->batch;
     for (int a = 0; a < 3; ++a) {
         L->box.lo[a] = s->scene_lo[a];
@@ -535,6 +544,8 @@ int learn_init(pbg_scene* s, const pbg_learn_params* p) {
     if ((rc = upload_params(L, w1, b1, w2, b2, w3, b3, st))) return rc;
     L->enabled = true;
     L->count = L->head = 0;
+    if ((rc = ensure(L->acc, 64))) return rc;
+    PBG_CUDA(cudaMemset(L->acc.ptr, 0, 64));  // loss, accuracy, batch count, running record total
     L->trained_steps = 0;
     return PBG_OK;
 }
@@ -613,7 +624,8 @@ __global__ void collect_kernel(const float4* __restrict__ ro, const float4* __re
                                const int32_t* __restrict__ prim, const int32_t* __restrict__ pos,
                                const uint16_t* __restrict__ rec_cluster, int64_t n, int64_t stride,
                                LearnBox box, uint16_t* __restrict__ recX, int32_t* __restrict__ recY,
-                               int64_t cap, int64_t head, unsigned int* __restrict__ taken, int64_t take) {
+                               int64_t cap, const unsigned long long* __restrict__ total,
+                               unsigned int* __restrict__ taken, int64_t take) {
     const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * stride;
     if (i >= n) return;
     const int32_t p = prim[i];
@@ -622,7 +634,7 @@ __global__ void collect_kernel(const float4* __restrict__ ro, const float4* __re
     if (c >= kClusters) return;
     const unsigned int k = atomicAdd(taken, 1u);
     if ((int64_t)k >= take) return;
-    const int64_t slot = (head + k) % cap;
+    const int64_t slot = (int64_t)((*total + k) % (unsigned long long)cap);
     float f[kFeat];
     ray_features(ro[i], rd[i], box.lo, box.inv_ext, f);
     uint16_t* row = recX + slot * kFeat;
@@ -630,6 +642,14 @@ __global__ void collect_kernel(const float4* __restrict__ ro, const float4* __re
     recY[slot] = c;
 }
 
+// The ring's running total advances by this batch's records (stream order:
+// the next batch's collect_kernel sees the new total).
+__global__ void collect_advance_kernel(unsigned long long* total, const unsigned int* taken, int64_t take) {
+    *total += (unsigned long long)min((int64_t)*taken, take);
+}
+
+// Records are written and counted on the device; the host reads the count
+// only when it trains (learn_train), so collecting never stalls the stream.
 int learn_collect(pbg_scene* s, const float4* o, const float4* d, const int32_t* prim, int64_t n,
                   cudaStream_t st) {
     Learner* L = s->learn;
@@ -644,20 +664,39 @@ int learn_collect(pbg_scene* s, const float4* o, const float4* d, const int32_t*
     const int64_t threads = (n + stride - 1) / stride;
     collect_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
         o, d, prim, (const int32_t*)s->tri_pos.ptr, (const uint16_t*)L->record_cluster.ptr, n, stride, L->box,
-        (uint16_t*)L->recX.ptr, (int32_t*)L->recY.ptr, L->capacity, L->head,
-        (unsigned int*)((uint8_t*)L->acc.ptr + 32), take);
+        (uint16_t*)L->recX.ptr, (int32_t*)L->recY.ptr, L->capacity,
+        (const unsigned long long*)((uint8_t*)L->acc.ptr + 40), (unsigned int*)((uint8_t*)L->acc.ptr + 32), take);
     PBG_CUDA(cudaGetLastError());
-    unsigned int got = 0;
-    PBG_CUDA(cudaMemcpyAsync(&got, (uint8_t*)L->acc.ptr + 32, 4, cudaMemcpyDeviceToHost, st));
-    PBG_CUDA(cudaStreamSynchronize(st));
-    const int64_t added = std::min<int64_t>((int64_t)got, take);
-    L->head = (L->head + added) % L->capacity;
-    L->count = std::min<int64_t>(L->capacity, L->count + added);
+    collect_advance_kernel<<<1, 1, 0, st>>>((unsigned long long*)((uint8_t*)L->acc.ptr + 40),
+                                            (const unsigned int*)((uint8_t*)L->acc.ptr + 32), take);
+    PBG_CUDA(cudaGetLastError());
+    s->counters.kernel_launches += 2;
+    return PBG_OK;
+}
+
+// Records collected so far (a synchronising read of the device total).
+static int records_available(Learner* L, cudaStream_t st) {
+    unsigned long long total = 0;
+    if (L->acc.ptr) {
+        PBG_CUDA(cudaMemcpyAsync(&total, (uint8_t*)L->acc.ptr + 40, 8, cudaMemcpyDeviceToHost, st));
+        PBG_CUDA(cudaStreamSynchronize(st));
+    }
+    L->count = (int64_t)std::min<unsigned long long>((unsigned long long)L->capacity, total);
     return PBG_OK;
 }
 
 // One forward + backward pass on B rows of X (bf16 [B x 112]) with labels
 // Y; gradients into G1/G2/G3, gb1/gb2/gb3 (FP32); loss / correct in acc.
+// tc_gemm with its launches counted: the GEMM, and the split-K reduction
+// when a work buffer spreads K over slices.
+static int gemm(pbg_scene* s, const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K, int acc,
+                int* status, cudaStream_t st, float* work) {
+    const int rc = tc_gemm(A, B, C, M, N, K, acc, status, st, work);
+    if (rc == PBG_OK)
+        s->counters.kernel_launches += 1 + (work && tc_gemm_work_floats(M, N, K) > (size_t)M * (size_t)N ? 1 : 0);
+    return rc;
+}
+
 static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const int32_t* Y, int B,
                             cudaStream_t st) {
     int* status = (int*)s->err.ptr;
@@ -683,14 +722,14 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
     }
     auto blocks = [](size_t n) { return (unsigned)((n + 255) / 256); };
     // forward
-    if ((rc = tc_gemm(X, (const uint16_t*)L->W1b.ptr, (float*)L->Z1.ptr, B, kHidden, kFeat, 0, status, st, nullptr))) return rc;
+    if ((rc = gemm(s, X, (const uint16_t*)L->W1b.ptr, (float*)L->Z1.ptr, B, kHidden, kFeat, 0, status, st, nullptr))) return rc;
     bias_relu_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->Z1.ptr, (const float*)L->b1.ptr, B, kHidden, 1,
                                                            (uint16_t*)L->H1.ptr);
-    if ((rc = tc_gemm((const uint16_t*)L->H1.ptr, (const uint16_t*)L->W2b.ptr, (float*)L->Z2.ptr, B, kHidden,
+    if ((rc = gemm(s, (const uint16_t*)L->H1.ptr, (const uint16_t*)L->W2b.ptr, (float*)L->Z2.ptr, B, kHidden,
                       kHidden, 0, status, st, nullptr))) return rc;
     bias_relu_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->Z2.ptr, (const float*)L->b2.ptr, B, kHidden, 1,
                                                            (uint16_t*)L->H2.ptr);
-    if ((rc = tc_gemm((const uint16_t*)L->H2.ptr, (const uint16_t*)L->W3b.ptr, (float*)L->Z3.ptr, B, kClusters,
+    if ((rc = gemm(s, (const uint16_t*)L->H2.ptr, (const uint16_t*)L->W3b.ptr, (float*)L->Z3.ptr, B, kClusters,
                       kHidden, 0, status, st, nullptr))) return rc;
     bias_relu_kernel<<<blocks(b * kClusters), 256, 0, st>>>((float*)L->Z3.ptr, (const float*)L->b3.ptr, B,
                                                              kClusters, 0, nullptr);
@@ -703,11 +742,11 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
                                                                   kClusters, (uint16_t*)L->dZ3T.ptr);
     transpose_bf16_kernel<<<blocks(b * kHidden), 256, 0, st>>>((const uint16_t*)L->H2.ptr, B, kHidden, kHidden,
                                                                 (uint16_t*)L->H2T.ptr);
-    if ((rc = tc_gemm((const uint16_t*)L->dZ3T.ptr, (const uint16_t*)L->H2T.ptr, (float*)L->G3.ptr, kClusters,
+    if ((rc = gemm(s, (const uint16_t*)L->dZ3T.ptr, (const uint16_t*)L->H2T.ptr, (float*)L->G3.ptr, kClusters,
                       kHidden, B, 0, status, st, (float*)L->gemm_work.ptr))) return rc;
     colsum_kernel<<<kClusters, 256, 0, st>>>((const float*)L->dZ3.ptr, B, kClusters, (float*)L->gb3.ptr);
     // dH2 = dZ3 W3 ; dZ2 = dH2 * relu'
-    if ((rc = tc_gemm((const uint16_t*)L->dZ3b.ptr, (const uint16_t*)L->W3Tb.ptr, (float*)L->dH2.ptr, B, kHidden,
+    if ((rc = gemm(s, (const uint16_t*)L->dZ3b.ptr, (const uint16_t*)L->W3Tb.ptr, (float*)L->dH2.ptr, B, kHidden,
                       kClusters, 0, status, st, nullptr))) return rc;
     relu_grad_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->dH2.ptr, (const float*)L->Z2.ptr, b * kHidden,
                                                            (uint16_t*)L->dZ2b.ptr);
@@ -717,10 +756,10 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
                                                             (uint16_t*)L->dZ2T.ptr);
     transpose_bf16_kernel<<<blocks(b * kHidden), 256, 0, st>>>((const uint16_t*)L->H1.ptr, B, kHidden, kHidden,
                                                                 (uint16_t*)L->H1T.ptr);
-    if ((rc = tc_gemm((const uint16_t*)L->dZ2T.ptr, (const uint16_t*)L->H1T.ptr, (float*)L->G2.ptr, 128, kHidden,
+    if ((rc = gemm(s, (const uint16_t*)L->dZ2T.ptr, (const uint16_t*)L->H1T.ptr, (float*)L->G2.ptr, 128, kHidden,
                       B, 0, status, st, (float*)L->gemm_work.ptr))) return rc;
     // dH1 = dZ2 W2 ; dZ1 = dH1 * relu'
-    if ((rc = tc_gemm((const uint16_t*)L->dZ2b.ptr, (const uint16_t*)L->W2Tb.ptr, (float*)L->dH1.ptr, B, kHidden,
+    if ((rc = gemm(s, (const uint16_t*)L->dZ2b.ptr, (const uint16_t*)L->W2Tb.ptr, (float*)L->dH1.ptr, B, kHidden,
                       kHidden, 0, status, st, nullptr))) return rc;
     relu_grad_kernel<<<blocks(b * kHidden), 256, 0, st>>>((float*)L->dH1.ptr, (const float*)L->Z1.ptr, b * kHidden,
                                                            (uint16_t*)L->dZ1b.ptr);
@@ -729,9 +768,10 @@ static int forward_backward(pbg_scene* s, Learner* L, const uint16_t* X, const i
     transpose_bf16_kernel<<<blocks(b * 128), 256, 0, st>>>((const uint16_t*)L->dZ1b.ptr, B, kHidden, 128,
                                                             (uint16_t*)L->dZ1T.ptr);
     transpose_bf16_kernel<<<blocks(b * kFeat), 256, 0, st>>>(X, B, kFeat, kFeat, (uint16_t*)L->XT.ptr);
-    if ((rc = tc_gemm((const uint16_t*)L->dZ1T.ptr, (const uint16_t*)L->XT.ptr, (float*)L->G1.ptr, 128, kFeat, B,
+    if ((rc = gemm(s, (const uint16_t*)L->dZ1T.ptr, (const uint16_t*)L->XT.ptr, (float*)L->G1.ptr, 128, kFeat, B,
                       0, status, st, (float*)L->gemm_work.ptr))) return rc;
     PBG_CUDA(cudaGetLastError());
+    s->counters.kernel_launches += 15;  // bias/ReLU 3, softmax 1, transposes 6, column sums 3, ReLU grads 2
     return PBG_OK;
 }
 
@@ -758,6 +798,8 @@ int learn_train(pbg_scene* s, int steps, cudaStream_t st) {
     Learner* L = s->learn;
     if (!L || !L->enabled) return PBG_OK;
     if (steps <= 0) steps = L->steps_per_train;
+    int rc0 = records_available(L, st);
+    if (rc0) return rc0;
     if (L->count < L->batch) return PBG_OK;  // not enough records yet
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -771,6 +813,7 @@ int learn_train(pbg_scene* s, int steps, cudaStream_t st) {
         const int32_t* Y = (const int32_t*)L->recY.ptr + start;
         rc = forward_backward(s, L, X, Y, L->batch, st);
         if (rc == PBG_OK) rc = sgd_update(L, st);
+        if (rc == PBG_OK) s->counters.kernel_launches += 6;
         ++L->trained_steps;
     }
     cudaEventRecord(e1, st);
@@ -815,6 +858,9 @@ int pbg_learn_get_stats(pbg_scene* s, pbg_learn_stats* out) {
     Learner* L = s->learn;
     memset(out, 0, sizeof(*out));
     if (!L) return PBG_OK;
+    cudaSetDevice(s->device);
+    int rc = records_available(L, s->stream);
+    if (rc) return rc;
     out->trained_steps = L->trained_steps;
     out->records = (uint64_t)L->count;
     out->last_loss = L->last_loss;

@@ -17,10 +17,15 @@
 //   - every call shares the one array, so calls that overlap on the GPU
 //     (different streams, or different host threads on one device) race;
 //     serialise them;
-//   - the first call on each device looks up the array's device address with
-//     cudaGetSymbolAddress while that device is current; make that first
-//     call before any stream capture.
-#include <mutex>
+//   - every call looks up the array's device address with
+//     cudaGetSymbolAddress in the calling thread's current context (after
+//     the first call in a context that is a host-side table lookup), so a
+//     device reset, or a caller on its own driver-API context, gets the
+//     address that is valid there; the first call in each context loads the
+//     library's device code and should come before any stream capture;
+//   - the rays (o4, d4) must be 16-byte aligned and the other arrays 4-byte
+//     aligned (misaligned views are rejected, not faulted on).
+#include <cstdint>
 
 #include "pbg_internal.h"
 #include "pbg_tma.cuh"
@@ -52,6 +57,7 @@ __global__ void __launch_bounds__(kNaThreads)
                          const float4* __restrict__ ro, const float4* __restrict__ rd, int64_t n,
                          unsigned long long* __restrict__ keys) {
     __shared__ TriRec tile[kNaTile];
+    __shared__ float raw[kNaTile * 9];
     const int64_t ray = (int64_t)blockIdx.x * kNaThreads + threadIdx.x;
     const int64_t t0 = (int64_t)blockIdx.y * per_split;
     const int64_t t1 = min(ntri, t0 + per_split);
@@ -67,8 +73,11 @@ __global__ void __launch_bounds__(kNaThreads)
     for (int64_t base = t0; base < t1; base += kNaTile) {
         const int cnt = (int)min((int64_t)kNaTile, t1 - base);
         __syncthreads();
-        for (int k = threadIdx.x; k < cnt; k += kNaThreads)
-            tile[k] = rec_from_tri9(tri9 + 9 * (base + k), (int32_t)(base + k));
+        // the tile's vertices in one coalesced sweep, then the records
+        const float* src = tri9 + 9 * base;
+        for (int k = threadIdx.x; k < 9 * cnt; k += kNaThreads) raw[k] = src[k];
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += kNaThreads) tile[k] = rec_from_tri9(raw + 9 * k, (int32_t)(base + k));
         __syncthreads();
         if (!active) continue;
         for (int j = 0; j < cnt; ++j) {
@@ -110,26 +119,18 @@ __global__ void noalloc_finalize_kernel(const float* __restrict__ tri9, const fl
     b2[i] = u2;
 }
 
-// Device address of the scratch array, looked up once per device.
-static unsigned char* noalloc_scratch(int device, int* status) {
-    static std::mutex mu;
-    static unsigned char* addr[128] = {nullptr};
-    if (device < 0 || device >= 128) {
-        *status = PBG_ERR_INVALID_ARGUMENT;
+// Device address of the scratch array in the current context.  Looked up on
+// every call: a cached address would outlive a device reset, and would be
+// wrong for a caller that runs on another context of the same device.
+static unsigned char* noalloc_scratch(int* status) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        *status = cuda_status(e, "cudaGetSymbolAddress(noalloc scratch)");
         return nullptr;
     }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            *status = cuda_status(e, "cudaGetSymbolAddress(noalloc scratch)");
-            return nullptr;
-        }
-        addr[device] = (unsigned char*)p;
-    }
     *status = PBG_OK;
-    return addr[device];
+    return (unsigned char*)p;
 }
 
 }  // namespace pbg
@@ -149,12 +150,19 @@ extern "C" int pbg_intersect_naive_noalloc(const float* tri9, int64_t ntri, cons
                        "(the fixed scratch holds one merge key per ray)");
         return PBG_ERR_INVALID_ARGUMENT;
     }
+    const uintptr_t a16 = (uintptr_t)o4 | (uintptr_t)d4;
+    const uintptr_t a4 = (uintptr_t)tri9 | (uintptr_t)prim | (uintptr_t)t | (uintptr_t)b1 | (uintptr_t)b2;
+    if ((a16 & 15u) || (a4 & 3u)) {
+        set_last_error("pbg_intersect_naive_noalloc: o4/d4 must be 16-byte aligned, the other arrays 4-byte "
+                       "aligned");
+        return PBG_ERR_INVALID_ARGUMENT;
+    }
     if (n == 0) return PBG_OK;
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
     int rc = PBG_OK;
-    unsigned char* scratch = noalloc_scratch(device, &rc);
+    unsigned char* scratch = noalloc_scratch(&rc);
     if (!scratch) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned long long* keys = (unsigned long long*)scratch;

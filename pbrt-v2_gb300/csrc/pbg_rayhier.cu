@@ -1027,6 +1027,7 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
         if (h[0] == 0) return PBG_OK;
         groups *= 4;  // rerun: atomicMax / atomicOr merges make a rerun idempotent
         s->rh_groups = groups;
+        s->counters.queue_reruns++;
     }
     set_last_error("rayhierarchy: pair queues overflowed at every triangle grouping");
     return PBG_ERR_INTERNAL;

@@ -78,3 +78,19 @@ def test_struct_mirrors_match_the_header(tmp_path):
         assert got[(cname, ":size")] == ctypes.sizeof(cls), cname
         for name, *_ in cls._fields_:
             assert got[(cname, name)] == getattr(cls, name).offset, (cname, name)
+
+
+def test_noalloc_rejects_misaligned_views():
+    """The allocation-free entry point reads rays as float4 and the rest as
+    4-byte words: a misaligned view is refused with a status before any
+    device work (the pointers here are never dereferenced)."""
+    lib = L.lib()
+    fn = lib.pbg_intersect_naive_noalloc
+    vp = ctypes.c_void_p
+    fn.argtypes = [vp, ctypes.c_int64, vp, vp, ctypes.c_int64, vp, vp, vp, vp, vp]
+    a, odd8, odd2 = vp(1 << 16), vp((1 << 16) + 8), vp((1 << 16) + 2)
+    assert fn(a, 1, odd8, a, 1, a, a, a, a, None) == L.PBG_ERR_INVALID_ARGUMENT
+    assert "16-byte" in L.last_error()
+    assert fn(a, 1, a, odd8, 1, a, a, a, a, None) == L.PBG_ERR_INVALID_ARGUMENT
+    assert fn(odd2, 1, a, a, 1, a, a, a, a, None) == L.PBG_ERR_INVALID_ARGUMENT
+    assert fn(a, 1, a, a, 1, a, odd2, a, a, None) == L.PBG_ERR_INVALID_ARGUMENT

@@ -358,3 +358,59 @@ def test_randomised_scenes_against_oracle(gpu_lib, oracle, seed):
             np.testing.assert_array_equal((occ == ord("1"))[hitm], want_occ[hitm], err_msg=f"{kind} shadow {seed}/{q}")
         assert_same(acc.Intersect(inc.copy()), B.nearest(inc), f"{kind} incoherent {seed}")
         np.testing.assert_array_equal(acc.IntersectP(inc) == ord("1"), B.anyhit(inc) == 1)
+
+
+def test_device_entry_reruns_on_a_caller_stream(gpu_lib, oracle):
+    """The device entry points on a caller's stream, through the two paths
+    that trace a batch again after its first attempt already wrote the
+    caller's arrays: a pair-queue overflow (a million incoherent rays of
+    unbounded length against the 181,250-triangle scene, the scene's first
+    call) and a shadow batch whose origins moved from the kept order.  The
+    final results equal the oracle's."""
+    import torch
+    sc = S.terrain_icospheres(seed=2)
+    tris = sc["tris"]
+    acc = A.MakeAccelerator("rayhierarchy", tris)
+    B = oracle.BVH(tris)
+    stream = torch.cuda.Stream()
+    rays = S.random_rays(1 << 20, [-8, -1, -8], [8, 4, 8], seed=41)
+
+    def dev(r):
+        o = torch.from_numpy(np.ascontiguousarray(np.stack([r[0], r[1], r[2], r[6]], 1))).cuda()
+        d = torch.from_numpy(np.ascontiguousarray(np.stack([r[3], r[4], r[5], r[7]], 1))).cuda()
+        return o, d
+
+    n = rays.shape[1]
+    o4, d4 = dev(rays)
+    prim = torch.full((n,), 7, dtype=torch.int32, device="cuda")
+    t, b1, b2 = (torch.full((n,), 7.0, device="cuda") for _ in range(3))
+    before = acc.stats()
+    with torch.cuda.stream(stream):
+        acc.intersect_device(o4, d4, prim, t, b1, b2, stream=stream)
+    stream.synchronize()
+    assert acc.stats()["queue_reruns"] > before["queue_reruns"]
+    want = B.nearest(rays)
+    assert_same([x.cpu().numpy() for x in (prim, t, b1, b2)], want, "overflow rerun")
+    # shadow batches: the same origins twice (kept order), then one moved
+    base = rays[:, :200000].copy()
+    g = np.random.default_rng(5)
+    cases = []
+    for k in range(2):
+        r = base.copy()
+        r[3:6] = g.normal(size=(3, r.shape[1])).astype(np.float32)
+        r[7] = g.uniform(0.5, 6.0, r.shape[1]).astype(np.float32)
+        cases.append(r)
+    moved = cases[-1].copy()
+    moved[0, 1000] += 0.5
+    cases.append(moved)
+    occ = torch.full((base.shape[1],), 9, dtype=torch.uint8, device="cuda")
+    for i, r in enumerate(cases):
+        so, sd = dev(r)
+        before = acc.stats()
+        with torch.cuda.stream(stream):
+            acc.occluded_device(so, sd, occ, stream=stream)
+        stream.synchronize()
+        after = acc.stats()
+        if i == 2:
+            assert after["origin_reruns"] == before["origin_reruns"] + 1
+        np.testing.assert_array_equal(occ.cpu().numpy(), B.anyhit(r), err_msg=f"shadow batch {i}")
