@@ -24,6 +24,7 @@
 #include "paramset.h"
 #include "pbrt_gb300.h"
 
+#include <cmath>
 #include <map>
 
 namespace {
@@ -54,10 +55,38 @@ void check(int rc, const char* what) {
     if (rc != PBG_OK) Severe("%s failed: %s (%s)", what, pbg_status_string(rc), pbg_last_error());
 }
 
-// Creates the device scene from packed triangles.
-void create_scene(GpuAccel* g, const vector<float>& tri9, const vector<float>& uv6, int kind,
-                  const pbg_params& prm) {
-    const int64_t n = (int64_t)(tri9.size() / 9);
+// The refined triangles as pbrt holds them: every TriangleMesh's points once
+// (world space), one index triple per triangle in refinement order, and the
+// meshes' per-vertex uvs.
+struct MeshArrays {
+    vector<float> P, uv;
+    vector<int32_t> idx;
+    int with_uv, without_uv;  // meshes that have / lack uvs
+    MeshArrays() : with_uv(0), without_uv(0) {}
+};
+
+// Creates the device scene: straight from the mesh arrays (gathered on the
+// device) unless the meshes mix explicit uvs with pbrt's per-corner default
+// ((0,0), (1,0), (1,1)), which no per-vertex array can hold -- then the
+// triangles are packed here as float[9n] + float[6n].
+void create_scene(GpuAccel* g, const MeshArrays& m, int kind, const pbg_params& prm) {
+    const int64_t n = (int64_t)(m.idx.size() / 3), nv = (int64_t)(m.P.size() / 3);
+    if (m.with_uv == 0 || m.without_uv == 0) {
+        check(pbg_scene_create_mesh(nv ? &m.P[0] : NULL, nv, n ? &m.idx[0] : NULL, n,
+                                    m.with_uv && nv ? &m.uv[0] : NULL, kind, &prm, &g->scene),
+              "pbg_scene_create_mesh");
+        return;
+    }
+    vector<float> tri9((size_t)n * 9), uv6((size_t)n * 6);
+    static const float d[6] = {0.f, 0.f, 1.f, 0.f, 1.f, 1.f};
+    for (int64_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const int32_t v = m.idx[3 * i + k];
+            for (int a = 0; a < 3; ++a) tri9[9 * i + 3 * k + a] = m.P[3 * v + a];
+            const bool has = m.uv[2 * v] == m.uv[2 * v];  // NaN marks a vertex of a mesh without uvs
+            uv6[6 * i + 2 * k] = has ? m.uv[2 * v] : d[2 * k];
+            uv6[6 * i + 2 * k + 1] = has ? m.uv[2 * v + 1] : d[2 * k + 1];
+        }
     check(pbg_scene_create(n ? &tri9[0] : NULL, n ? &uv6[0] : NULL, n, kind, &prm, &g->scene),
           "pbg_scene_create");
 }
@@ -186,38 +215,41 @@ void destroy(const void* self) {
 
 }  // namespace
 
-// Packs refined triangles in order; runs inside a member function of each
-// accelerator class, which the fork made friends of Triangle
-// (shapes/trianglemesh.h:51-53, :102-104) for exactly this access.
-#define PBG_PACK_TRIANGLES(G, P, TRI9, UV6, BOUND)                                      \
+// Collects the refined triangles in order as mesh arrays; runs inside a
+// member function of each accelerator class, which the fork made friends of
+// Triangle (shapes/trianglemesh.h:51-53, :102-104) for exactly this access.
+#define PBG_COLLECT_TRIANGLES(ACC, PRIMS, ARR, BOX)                                           \
     do {                                                                                \
-        for (uint32_t i_ = 0; i_ < (P).size(); ++i_) (P)[i_]->FullyRefine((G)->prims);   \
+        for (uint32_t i_ = 0; i_ < (PRIMS).size(); ++i_) (PRIMS)[i_]->FullyRefine((ACC)->prims);   \
         vector<Reference<Primitive> > kept_;                                            \
-        for (size_t i_ = 0; i_ < (G)->prims.size(); ++i_) {                             \
+        std::map<const TriangleMesh*, int32_t> base_;                                   \
+        for (size_t i_ = 0; i_ < (ACC)->prims.size(); ++i_) {                             \
             const GeometricPrimitive* gp_ =                                             \
-                dynamic_cast<const GeometricPrimitive*>((G)->prims[i_].GetPtr());       \
+                dynamic_cast<const GeometricPrimitive*>((ACC)->prims[i_].GetPtr());       \
             const Triangle* sh_ = gp_ ? dynamic_cast<const Triangle*>(gp_->GetShapePtr()) : NULL; \
             if (!sh_) continue; /* non-triangles are dropped, as naive.cpp:66-69 */     \
             const TriangleMesh* m_ = sh_->GetMeshPtr();                                 \
-            for (int v_ = 0; v_ < 3; ++v_) {                                            \
-                const Point& pt_ = m_->p[sh_->v[v_]];                                   \
-                (TRI9).push_back(pt_.x);                                                \
-                (TRI9).push_back(pt_.y);                                                \
-                (TRI9).push_back(pt_.z);                                                \
-                (BOUND) = Union((BOUND), pt_);                                          \
-                if (m_->uvs) {                                                          \
-                    (UV6).push_back(m_->uvs[2 * sh_->v[v_]]);                           \
-                    (UV6).push_back(m_->uvs[2 * sh_->v[v_] + 1]);                       \
-                } else {                                                                \
-                    static const float d_[6] = {0.f, 0.f, 1.f, 0.f, 1.f, 1.f};          \
-                    (UV6).push_back(d_[2 * v_]);                                        \
-                    (UV6).push_back(d_[2 * v_ + 1]);                                    \
+            std::map<const TriangleMesh*, int32_t>::iterator b_ = base_.find(m_);       \
+            if (b_ == base_.end()) { /* a new mesh: its points (and uvs) once */        \
+                b_ = base_.insert(std::make_pair(m_, (int32_t)((ARR).P.size() / 3))).first; \
+                for (int v_ = 0; v_ < m_->nverts; ++v_) {                               \
+                    (ARR).P.push_back(m_->p[v_].x);                                       \
+                    (ARR).P.push_back(m_->p[v_].y);                                       \
+                    (ARR).P.push_back(m_->p[v_].z);                                       \
+                    (ARR).uv.push_back(m_->uvs ? m_->uvs[2 * v_] : NAN);                  \
+                    (ARR).uv.push_back(m_->uvs ? m_->uvs[2 * v_ + 1] : NAN);              \
                 }                                                                       \
+                if (m_->uvs) ++(ARR).with_uv;                                             \
+                else ++(ARR).without_uv;                                                  \
             }                                                                           \
-            kept_.push_back((G)->prims[i_]);                                            \
-            (G)->alpha.push_back(m_->alphaTexture.GetPtr());                            \
+            for (int v_ = 0; v_ < 3; ++v_) {                                            \
+                (ARR).idx.push_back(b_->second + sh_->v[v_]);                             \
+                (BOX) = Union((BOX), m_->p[sh_->v[v_]]);                            \
+            }                                                                           \
+            kept_.push_back((ACC)->prims[i_]);                                            \
+            (ACC)->alpha.push_back(m_->alphaTexture.GetPtr());                            \
         }                                                                               \
-        (G)->prims.swap(kept_);                                                         \
+        (ACC)->prims.swap(kept_);                                                         \
     } while (0)
 
 // ----------------------------------------------------------------- naive
@@ -226,12 +258,12 @@ NaiveAccel::NaiveAccel(const vector<Reference<Primitive> >& p, bool onG, const s
     onGPU = onG;
     method = m;
     GpuAccel* g = new GpuAccel();
-    vector<float> tri9, uv6;
-    PBG_PACK_TRIANGLES(g, p, tri9, uv6, bbox);
+    MeshArrays mesh;
+    PBG_COLLECT_TRIANGLES(g, p, mesh, bbox);
     triangleCount = g->prims.size();
     pbg_params prm;
     memset(&prm, 0, sizeof(prm));
-    create_scene(g, tri9, uv6, PBG_ACCEL_NAIVE, prm);
+    create_scene(g, mesh, PBG_ACCEL_NAIVE, prm);
     g->bound = bbox;
     table()[this] = g;
 }
@@ -265,15 +297,15 @@ RayHieararchy::RayHieararchy(const vector<Reference<Primitive> >& p, bool onG, i
 #endif
 ) {
     GpuAccel* g = new GpuAccel();
-    vector<float> tri9, uv6;
-    PBG_PACK_TRIANGLES(g, p, tri9, uv6, bbox);
+    MeshArrays mesh;
+    PBG_COLLECT_TRIANGLES(g, p, mesh, bbox);
     triangleCount = g->prims.size();
     pbg_params prm;
     memset(&prm, 0, sizeof(prm));
     prm.chunk_x = chunkX;
     prm.chunk_y = chunkY;
     prm.height = height;
-    create_scene(g, tri9, uv6, PBG_ACCEL_RAYHIERARCHY, prm);
+    create_scene(g, mesh, PBG_ACCEL_RAYHIERARCHY, prm);
     g->bound = bbox;
     table()[this] = g;
 }
@@ -333,8 +365,8 @@ RayBVH::RayBVH(const vector<Reference<Primitive> >& p, bool onG, int chunkX, int
 #endif
 ) {
     GpuAccel* g = new GpuAccel();
-    vector<float> tri9, uv6;
-    PBG_PACK_TRIANGLES(g, p, tri9, uv6, bbox);
+    MeshArrays mesh;
+    PBG_COLLECT_TRIANGLES(g, p, mesh, bbox);
     triangleCount = g->prims.size();
     pbg_params prm;
     memset(&prm, 0, sizeof(prm));
@@ -345,7 +377,7 @@ RayBVH::RayBVH(const vector<Reference<Primitive> >& p, bool onG, int chunkX, int
     // the scene-file default of 1 triangle per leaf served the OpenCL
     // kernels; below 2 the library's tuned leaf size is used
     prm.max_bvh_prim = MaxBVHPrim > 1 ? MaxBVHPrim : 0;
-    create_scene(g, tri9, uv6, PBG_ACCEL_RAYBVH, prm);
+    create_scene(g, mesh, PBG_ACCEL_RAYBVH, prm);
     g->bound = bbox;
     table()[this] = g;
 }
