@@ -500,6 +500,16 @@ void* orc_bvh_build(const float* tris, int64_t ntri, int maxprims) {
     free(pos);
     free(info2);
     free(info);
+    /* the traversal tests the padded boxes: pad each node once here */
+    for (int64_t k = 0; k < b->nnodes; ++k) {
+        bvh_node_t* nd = &b->nodes[k];
+        for (int a = 0; a < 3; ++a) {
+            float pad = (fabsf(nd->lo[a]) + fabsf(nd->hi[a]) + (nd->hi[a] - nd->lo[a])) * 0x1p-10f + 1e-30f;
+            float lo = nd->lo[a] - pad, hi = nd->hi[a] + pad;
+            nd->lo[a] = lo;
+            nd->hi[a] = hi;
+        }
+    }
     return b;
 }
 
@@ -515,17 +525,18 @@ void orc_bvh_free(void* p) {
 int64_t orc_bvh_node_count(void* p) { return ((bvh_t*)p)->nnodes; }
 
 /* Slab test (accelerators/bvh.cpp:430-460 form) on a box padded by a relative
- * 2^-10 of its extent and magnitude, with the far distance widened by 2^-10,
- * so that float rounding never culls a triangle that the exact test accepts. */
+ * 2^-10 of its extent and magnitude (done once, after the build), with the far
+ * distance widened by 2^-10, so that float rounding never culls a triangle
+ * that the exact test accepts. */
 static inline int box_hit(const bvh_node_t* nd, const float o[3], const float inv[3],
-                          float mint, float maxt) {
+                          const int dirneg[3], float mint, float maxt) {
     float t0 = mint, t1 = maxt;
     for (int a = 0; a < 3; ++a) {
-        float pad = (fabsf(nd->lo[a]) + fabsf(nd->hi[a]) + (nd->hi[a] - nd->lo[a])) * 0x1p-10f + 1e-30f;
-        float lo = nd->lo[a] - pad, hi = nd->hi[a] + pad;
-        float tn = (lo - o[a]) * inv[a];
-        float tf = (hi - o[a]) * inv[a];
-        if (tn > tf) { float s = tn; tn = tf; tf = s; }
+        const float lo = nd->lo[a], hi = nd->hi[a];
+        /* near and far planes by the direction's sign (a padded box has
+         * lo < hi, so this equals ordering the two distances) */
+        float tn = ((dirneg[a] ? hi : lo) - o[a]) * inv[a];
+        float tf = ((dirneg[a] ? lo : hi) - o[a]) * inv[a];
         tf *= 1.f + 0x1p-10f;
         if (!(tn <= tf)) { /* NaN from 0*inf: the ray lies in the slab plane */
             if (o[a] >= lo && o[a] <= hi) continue;
@@ -576,7 +587,7 @@ static void bvh_trace_one(bvh_t* b, const float o[3], const float d[3], float mi
     }
     while (1) {
         const bvh_node_t* nd = &b->nodes[node];
-        if (box_hit(nd, o, inv, mint, curmax)) {
+        if (box_hit(nd, o, inv, dirneg, mint, curmax)) {
             if (nd->count > 0) {
                 for (int32_t k = 0; k < nd->count; ++k) {
                     int32_t tri = b->order[nd->offset + k];
