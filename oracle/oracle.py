@@ -64,6 +64,8 @@ def lib():
         L.orc_hits_geometry.argtypes = [_fp, _fp, _fp, C.c_int64, _ip, _fp, _fp, _fp, _fp]
         L.orc_bvh_build.restype = C.c_void_p
         L.orc_bvh_build.argtypes = [_fp, C.c_int64, C.c_int]
+        L.orc_bvh_build_mode.restype = C.c_void_p
+        L.orc_bvh_build_mode.argtypes = [_fp, C.c_int64, C.c_int, C.c_int]
         L.orc_bvh_free.argtypes = [C.c_void_p]
         L.orc_bvh_node_count.restype = C.c_int64
         L.orc_bvh_node_count.argtypes = [C.c_void_p]
@@ -159,9 +161,12 @@ class BVH:
     """The timed CPU baseline: SAH BVH in the manner of pbrt's BVHAccel with
     a conservative box test, so answers equal the brute-force loop."""
 
-    def __init__(self, tris, maxprims: int = 4):
+    def __init__(self, tris, maxprims: int = 4, box_degenerate: bool = False):
+        """box_degenerate: degenerate triangles go into the tree with their
+        own boxes, as pbrt's BVHAccel puts them (answers then equal
+        BVHAccel's rather than the all-pairs loop's)."""
         self.tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
-        self.h = lib().orc_bvh_build(_f(self.tris), self.tris.shape[0], maxprims)
+        self.h = lib().orc_bvh_build_mode(_f(self.tris), self.tris.shape[0], maxprims, int(box_degenerate))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -470,7 +470,19 @@ static int64_t bvh_build_rec(bvh_t* b, const prim_info_t* info, int32_t* idx, in
     return node;
 }
 
+/* box_degenerate = 0: degenerate triangles stay out of the tree and every
+ * ray tests them (answers equal the all-pairs loop).  1: they go into the
+ * tree with their own boxes, as pbrt's BVHAccel puts every primitive
+ * (accelerators/bvh.cpp:220-229); a rounding-noise hit of such a triangle
+ * far from its box is then missed, as BVHAccel misses it.  The timed CPU
+ * samples use 1, the parity checks 0. */
+void* orc_bvh_build_mode(const float* tris, int64_t ntri, int maxprims, int box_degenerate);
+
 void* orc_bvh_build(const float* tris, int64_t ntri, int maxprims) {
+    return orc_bvh_build_mode(tris, ntri, maxprims, 0);
+}
+
+void* orc_bvh_build_mode(const float* tris, int64_t ntri, int maxprims, int box_degenerate) {
     bvh_t* b = (bvh_t*)calloc(1, sizeof(bvh_t));
     b->tris = tris;
     b->ntri = ntri;
@@ -480,7 +492,13 @@ void* orc_bvh_build(const float* tris, int64_t ntri, int maxprims) {
     int64_t ncull = 0;
     for (int64_t i = 0; i < ntri; ++i) {
         const float* v = tris + 9 * i;
-        if (orc_tri_degenerate(v)) { b->unculled[b->nunculled++] = (int32_t)i; continue; }
+        int finite = 1;
+        for (int k = 0; k < 9; ++k) finite &= isfinite(v[k]) ? 1 : 0;
+        /* a non-finite vertex has no box: always tested */
+        if ((!box_degenerate || !finite) && orc_tri_degenerate(v)) {
+            b->unculled[b->nunculled++] = (int32_t)i;
+            continue;
+        }
         for (int k = 0; k < 3; ++k) {
             float a = v[k], c = v[3 + k], e = v[6 + k];
             info[ncull].lo[k] = fminf(a, fminf(c, e));

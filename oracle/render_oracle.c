@@ -45,6 +45,7 @@
 #include <string.h>
 
 void* orc_bvh_build(const float* tris, int64_t ntri, int maxprims);
+void* orc_bvh_build_mode(const float* tris, int64_t ntri, int maxprims, int box_degenerate);
 void orc_bvh_free(void* p);
 int32_t orc_bvh_trace(void* bvh, const float o[3], const float d[3], float mint, float maxt,
                       int anyhit, float* t, float* b1, float* b2);
@@ -723,9 +724,10 @@ int orc_render_stream(const float* tris, int64_t ntri, const orc_camera* cam, co
 }
 
 /* The CPU baseline's bounded sample of a frame: the BVH is built once
- * (orc_render_bvh), then orc_render_count traces the samples first,
- * first + stride, ... of the image and returns only the ray counts. */
-void* orc_render_bvh(const float* tris, int64_t ntri) { return orc_bvh_build(tris, ntri, 4); }
+ * (orc_render_bvh, degenerate triangles boxed as pbrt's BVHAccel boxes
+ * them), then orc_render_count traces the samples first, first + stride,
+ * ... of the image and returns only the ray counts. */
+void* orc_render_bvh(const float* tris, int64_t ntri) { return orc_bvh_build_mode(tris, ntri, 4, 1); }
 void orc_render_bvh_free(void* bvh) { orc_bvh_free(bvh); }
 void orc_render_count(const float* tris, void* bvh, const orc_camera* cam, const orc_light* lights,
                       int nlights, const orc_params* prm, int64_t first, int64_t stride, int nthreads,

@@ -51,6 +51,27 @@ def test_bvh_baseline_equals_brute_force(oracle, case):
     np.testing.assert_array_equal(B.anyhit(g["rays"], threads=4), g["occ"])
 
 
+def test_timed_bvh_mode_answers_like_bvhaccel(oracle):
+    """The CPU baseline's timed samples build the tree with degenerate
+    triangles boxed (as pbrt's BVHAccel boxes them): on the small naive
+    workload, whose UV sphere has 64 pole triangles with two equal
+    vertices, its answers equal BVHAccel's own (the reference build) and
+    the exact mode's."""
+    if not oracle.ref_available():
+        pytest.skip("reference build not present")
+    from pbrt_gb300 import scenes as S
+    cfg = S.config_small_naive()
+    tris = cfg["tris"]
+    ref = oracle.RefScene(tris)
+    for rays in (np.ascontiguousarray(cfg["rays"][:, ::4]), S.random_rays(20000, -3.0, 3.0, seed=3)):
+        boxed = oracle.BVH(tris, box_degenerate=True)
+        a = boxed.nearest(rays, threads=4)
+        b = ref.nearest(rays, use_bvh=True)
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[0], oracle.BVH(tris).nearest(rays, threads=4)[0])
+        np.testing.assert_array_equal(boxed.anyhit(rays, threads=4), ref.anyhit(rays, use_bvh=True))
+
+
 def test_valid_mask(oracle):
     g = load_golden("soup")
     valid = (np.arange(g["rays"].shape[1]) % 3 != 0).astype(np.uint8)
