@@ -658,6 +658,172 @@ def run_gpu_path(args, rank, world, dev):
     print(json.dumps(line), flush=True)
 
 
+NAIVE_WORKLOAD = ("naive direct lighting 256x256x1spp at pixel centres, UV sphere + ground quad "
+                  "(4,034 triangles), point light, whole frame on device")
+
+
+def flush_l2(buf):
+    """Overwrites a buffer larger than L2 (129 MB) so the next frame starts
+    with a cold cache."""
+    buf.add_(1.0)
+
+
+def run_gpu_naive(args, rank, world, dev):
+    """Accelerator "naive" on its small workload: 256x256 at pixel centres,
+    one camera ray and one point-light shadow ray per pixel, every ray
+    against all 4,034 triangles; the whole frame runs on the device
+    (pbg_render).  The inputs fit in L2, so L2 is flushed before every
+    frame.  The camera matrices and the light come from the reference's own
+    render of this scene (tests/golden/render_small.npz), and the image is
+    compared with that render."""
+    import torch
+    from pbrt_gb300 import accel as A
+    from pbrt_gb300 import render as R
+    from pbrt_gb300 import scenes as S
+    torch.cuda.set_device(dev)
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "render_small.npz")))
+    tris = S.config_small_naive()["tris"]
+    acc = A.MakeAccelerator("naive", tris, {"device": dev})
+    acc.Preprocess(None, 1, 1, 1, xres=256, yres=256)
+    cam = R.camera_struct(g["r2c"], g["c2w"], 256, 256)
+    light = R.point_light(g["light_pos"], g["light_I"])
+    prm = R.render_params("directlighting")
+    flush = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
+    for _ in range(args.warmup):
+        flush_l2(flush)
+        R.render(acc, cam, [light], prm)
+    torch.cuda.synchronize()
+    l0 = acc.stats()["kernel_launches"]
+    acc.profile(True)
+    frames, walls = [], []
+    rank_barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            img, st = R.render(acc, cam, [light], prm)
+            walls.append(time.perf_counter() - w0)
+            frames.append(st)
+    torch.cuda.synchronize()
+    rank_barrier(world)
+    stt = acc.stats()
+    acc.profile(False)
+    launches = stt["kernel_launches"] - l0
+    clocks = clk.summary()
+    acc.profile(2)
+    flush_l2(flush)
+    _, wst = R.render(acc, cam, [light], prm)
+    work = acc.stats()["work"]
+    acc.profile(False)
+    rays = sum(f["nearest_rays"] + f["shadow_rays"] for f in frames) / len(frames)
+    near_rays = sum(f["nearest_rays"] for f in frames) / len(frames)
+    sh_rays = sum(f["shadow_rays"] for f in frames) / len(frames)
+    frame_ms = max_over_ranks(sum(f["ms_total"] for f in frames) / len(frames), world)
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    n_launch = max(stt["timed_launches"]["traverse"], 1)
+    launches_per_frame = n_launch / args.steps
+    avg_launch_ms = stt["stage_ms"]["traverse"] / n_launch
+    per_launch_bytes = (near_rays * 48 + sh_rays * 33) / launches_per_frame + len(tris) * 48
+    achieved = per_launch_bytes / (avg_launch_ms * 1e-3) / 1e9
+    flops_frame = (work["filter_tests"] * FLOP_STAGE1 + work["filter_stage2"] * FLOP_STAGE23
+                   + work["exact_tests"] * FLOP_EXACT)
+    flops_per_launch = flops_frame / launches_per_frame
+    fp32_achieved = flops_per_launch / (avg_launch_ms * 1e-3) / 1e12
+    fp32_peak, sms = fp32_peak_tflops(clocks.get("sm_max_mhz") or 2070.0)
+    cpu = None
+    lights = [{"type": "point", "pos": g["light_pos"], "I": g["light_I"]}]
+    if not args.no_cpu and world == 1:
+        from oracle import oracle as O
+        rc = O.RenderCounter(tris, g["r2c"], g["c2w"], 256, 256, lights, "directlighting", (1, 1), False, 5, 1)
+        threads = os.cpu_count() or 1
+        r_all, s_all, stride_all = timed_cpu_sample(rc, threads, 5.0, 1)
+        r_one, s_one, stride_one = timed_cpu_sample(rc, 1, 3.0, 1)
+        cpu = {"value": round(r_all / s_all / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "seconds": round(s_all, 2), "cpu_model": cpu_model(),
+               "sample": ("the whole frame" if stride_all == 1 else f"every {stride_all}th pixel of the frame")
+                         + f" ({r_all} camera + shadow rays), SAH BVH + pbrt's triangle test "
+                           "(oracle/render_oracle.c)",
+               "single_core": {"value": round(r_one / s_one / 1e6, 3), "cores": 1, "seconds": round(s_one, 2),
+                               "sample": f"every {stride_one}th pixel ({r_one} rays)"}}
+        del rc
+    parity = None
+    if not args.no_parity and world == 1:
+        diff = img.astype(np.float64) - g["image"].astype(np.float64)
+        parity = {"image": "256x256 frame against the reference's own render of it",
+                  "rmse_vs_reference": float(np.sqrt(np.mean(diff ** 2))),
+                  "pixels_differing": int(np.count_nonzero(np.any(diff != 0, axis=2))),
+                  "tolerance": "bit-exact"}
+    line = {
+        "metric": METRIC, "value": round(job_rate(rays, world, frame_ms), 2), "unit": "Mrays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(frame_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (UV sphere + ground quad; the reference's camera and light)",
+        "config": {"workload": NAIVE_WORKLOAD, "accelerator": "naive", "rays_per_step": int(rays),
+                   "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays), "triangles": int(len(tris)),
+                   "parallelism": f"replicas x{world}", "l2": "flushed before every frame (256 MB write)"},
+        "e2e": {"value": round(rays / (sum(walls) / len(walls)) / 1e6, 2), "unit": "Mrays/s",
+                "ms_per_step": round(sum(walls) / len(walls) * 1e3, 4),
+                "h2d_bytes_per_step": 256 + 112, "d2h_bytes_per_step": 256 * 256 * 12,
+                "api": "pbg_render (camera, light and parameters in, RGB image out; wall time of the host call)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 5), "traffic": None,
+                     "kernel": "naive_kernel (one nearest-hit and one any-hit launch per frame)",
+                     "launches_per_step": round(launches_per_frame, 2),
+                     "algorithmic_bytes_per_launch": int(per_launch_bytes),
+                     "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind + " (of measured copy)",
+                     "fp32": {"achieved_tflops": round(fp32_achieved, 3), "peak_tflops": round(fp32_peak, 1),
+                              "frac": round(fp32_achieved / fp32_peak, 5),
+                              "flops_per_launch": int(flops_per_launch),
+                              "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 x max SM clock",
+                              "counted": {k: int(v) for k, v in work.items()},
+                              "flop_per_unit": {"tri_stage1": FLOP_STAGE1, "tri_stage2_3": FLOP_STAGE23,
+                                                "exact_test": FLOP_EXACT}}},
+        "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stt["stage_ms"].items()},
+        "gpu_launches": int(launches),
+        "cpu_baseline": cpu,
+        "parity": parity,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_naive(args):
+    """The reference's CPU path for the naive workload's frame on all host
+    cores: the oracle's restatement of the breadth-first direct-lighting
+    render (camera ray and point-light shadow ray per pixel) over its SAH
+    BVH and pbrt's triangle test; each step renders the whole frame."""
+    from oracle import oracle as O
+    from pbrt_gb300 import scenes as S
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "render_small.npz")))
+    tris = S.config_small_naive()["tris"]
+    lights = [{"type": "point", "pos": g["light_pos"], "I": g["light_I"]}]
+    rc = O.RenderCounter(tris, g["r2c"], g["c2w"], 256, 256, lights, "directlighting", (1, 1), False, 5, 1)
+    threads = os.cpu_count() or 1
+    times, nrays = [], 0
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        a, b = rc.count(0, 1, threads, 1)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            nrays += a + b
+    value = nrays / sum(times) / 1e6
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sum(times) / len(times) * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (UV sphere + ground quad; the reference's camera and light)", "impl": "reference",
+            "config": {"workload": NAIVE_WORKLOAD, "accelerator": "naive", "sample": "the whole frame per step"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(), "sample": "the whole frame per step (oracle/render_oracle.c)"},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def _o4d4(rays):
     o4 = np.ascontiguousarray(np.stack([rays[0], rays[1], rays[2], rays[6]], 1).astype(np.float32))
     d4 = np.ascontiguousarray(np.stack([rays[3], rays[4], rays[5], rays[7]], 1).astype(np.float32))
@@ -1058,7 +1224,9 @@ def main():
     ap.add_argument("--accel", default="rayhierarchy", choices=["naive", "rayhierarchy", "ray-bvh"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
-    ap.add_argument("--workload", default="path", choices=["path", "frame", "batch"])
+    ap.add_argument("--workload", default="path", choices=["path", "frame", "batch", "naive"])
+    ap.add_argument("--path-res", type=int, default=PATH_RES,
+                    help="path workload: image width and height (profiler captures use a smaller frame)")
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--rh-cluster-levels", type=int, default=0,
                     help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")
@@ -1074,6 +1242,10 @@ def main():
                     help="path workload: 0 plain ordering, 1 learned ordering as the value, "
                          "2 plain as the value with the learned comparison attached")
     args = ap.parse_args()
+    if args.path_res != PATH_RES:  # a smaller frame of the same scene, for profiler captures
+        global PATH_WORKLOAD
+        PATH_WORKLOAD = PATH_WORKLOAD.replace(f"{PATH_RES}x{PATH_RES}", f"{args.path_res}x{args.path_res}")
+        globals()["PATH_RES"] = args.path_res
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -1083,6 +1255,8 @@ def main():
                 run_reference_path(args)
             elif args.workload == "frame":
                 run_reference_frame(args)
+            elif args.workload == "naive":
+                run_reference_naive(args)
             else:
                 print(json.dumps({"impl": "reference", "unavailable": "the 64-scene batch has no reference arm; "
                                   "its CPU baseline is in the GPU line"}), flush=True)
@@ -1095,6 +1269,8 @@ def main():
         run_gpu_path(args, rank, world, local)
     elif args.workload == "batch":
         run_gpu_batch(args, rank, world, local)
+    elif args.workload == "naive":
+        run_gpu_naive(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

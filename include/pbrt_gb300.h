@@ -79,7 +79,12 @@ typedef struct pbg_params {
     int32_t bvh_build;    /* ray-bvh: 0 = build the SAH tree on the device,
                            * 1 = on the host (the same splits; numbered depth
                            * first instead of breadth first) */
-    int32_t reserved[6];
+    int32_t rh_queue_pairs; /* rayhierarchy: capacity of each ray/node pair queue
+                             * in pairs (0 = 2^25; at least 4096).  Three such
+                             * buffers of 8, 8 and 4 bytes a pair are held; a
+                             * batch whose pairs overflow them is traced again
+                             * with the triangles split into more groups. */
+    int32_t reserved[5];
 } pbg_params;
 
 typedef struct pbg_rays {
@@ -200,8 +205,11 @@ int pbg_occluded_device(pbg_scene* scene, const float* o4, const float* d4,
  * fixed 8 MB __device__ array inside the library, so at most 1048576 rays
  * per call (more is rejected with PBG_ERR_INVALID_ARGUMENT); every call
  * shares that array, so calls that overlap on the GPU race and must be
- * serialised; the first call on a device looks the array up and should come
- * before any stream capture.  stream = NULL is the legacy default stream. */
+ * serialised.  Each call looks the array up in the calling thread's current
+ * context; the first call in a context loads the library's device code and
+ * should come before any stream capture.  o4 and d4 must be 16-byte aligned
+ * and the other arrays 4-byte aligned (misaligned views are rejected with
+ * PBG_ERR_INVALID_ARGUMENT).  stream = NULL is the legacy default stream. */
 int pbg_intersect_naive_noalloc(const float* tri9, int64_t ntri, const float* o4,
                                 const float* d4, int64_t n, int32_t* prim, float* t, float* b1,
                                 float* b2, void* stream);

@@ -36,7 +36,8 @@ class Params(C.Structure):
     _fields_ = [("chunk_x", C.c_int32), ("chunk_y", C.c_int32), ("height", C.c_int32),
                 ("bvh_height", C.c_int32), ("max_bvh_prim", C.c_int32), ("device", C.c_int32),
                 ("ray_sort", C.c_int32), ("rh_cluster_levels", C.c_int32),
-                ("walk", C.c_int32), ("bvh_build", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("walk", C.c_int32), ("bvh_build", C.c_int32), ("rh_queue_pairs", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 _fp = C.POINTER(C.c_float)

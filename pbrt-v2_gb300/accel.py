@@ -61,15 +61,16 @@ class Aggregate:
         P = np.ascontiguousarray(np.asarray(P, np.float32).reshape(-1, 3))
         vi = np.ascontiguousarray(np.asarray(indices, np.int32).reshape(-1, 3))
         uvv = None if uv is None else np.ascontiguousarray(np.asarray(uv, np.float32).reshape(-1, 2))
-        self.tris = np.ascontiguousarray(P[vi].reshape(-1, 9)) if len(vi) else np.zeros((0, 9), np.float32)
-        self.uvs = None if uvv is None else np.ascontiguousarray(uvv[vi].reshape(-1, 6))
         self.params = params or L.Params()
         self.handle = C.c_void_p()
         self.tile = None
+        # the library checks the indices; the host copies below come after
         L.check(L.lib().pbg_scene_create_mesh(P.ctypes.data if len(P) else None, len(P),
                                               vi.ctypes.data if len(vi) else None, len(vi),
                                               None if uvv is None else uvv.ctypes.data, L.ACCEL[cls.kind],
                                               C.byref(self.params), C.byref(self.handle)), "pbg_scene_create_mesh")
+        self.tris = np.ascontiguousarray(P[vi].reshape(-1, 9)) if len(vi) else np.zeros((0, 9), np.float32)
+        self.uvs = None if uvv is None else np.ascontiguousarray(uvv[vi].reshape(-1, 6))
         return self
 
     def close(self):
@@ -262,6 +263,7 @@ def _params_from(ps: dict | None) -> L.Params:
     p.rh_cluster_levels = int(ps.get("clusterLevels", 0))
     p.walk = int(ps.get("walk", 0))
     p.bvh_build = int(ps.get("bvhBuild", 0))
+    p.rh_queue_pairs = int(ps.get("queuePairs", 0))
     return p
 
 

@@ -14,6 +14,7 @@
 // through a 64-bit atomicMax on (t, index) keys and a finalize pass recomputes
 // b1/b2 of the winner with the exact test.  Any-hit leaves a tile loop as
 // soon as every ray of the CTA is occluded.
+#include "pbg_count.cuh"
 #include "pbg_internal.h"
 #include "pbg_tma.cuh"
 
@@ -23,14 +24,16 @@ constexpr int kNaiveThreads = 256;
 constexpr int kNaiveTile = 128;
 constexpr int kNaiveStages = 2;
 
-template <bool ANY>
+// STATS: the counting variant (profiling level 2) adds each thread's filter
+// tests, second-stage filter passes, exact tests and exact hits to wcount.
+template <bool ANY, bool STATS>
 __global__ void __launch_bounds__(kNaiveThreads)
     naive_kernel(const TriRec* __restrict__ tris, int64_t ntri, int64_t per_split,
                  const float4* __restrict__ ro, const float4* __restrict__ rd,
                  const uint8_t* __restrict__ valid, int64_t n, int32_t* __restrict__ prim_out,
                  float* __restrict__ t_out, float* __restrict__ b1_out,
                  float* __restrict__ b2_out, unsigned long long* __restrict__ keys,
-                 uint8_t* __restrict__ occ, int* status) {
+                 uint8_t* __restrict__ occ, int* status, unsigned long long* wcount) {
     __shared__ __align__(128) TriRec tile[kNaiveStages][kNaiveTile];
     __shared__ __align__(8) uint64_t bar[kNaiveStages];
 
@@ -50,6 +53,7 @@ __global__ void __launch_bounds__(kNaiveThreads)
     float best_t = d.w, bb1 = 0.f, bb2 = 0.f;
     int32_t best = -1;
     bool done = !active;
+    WorkCount wc;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kNaiveStages; ++s) mbar_init(&bar[s], 1);
@@ -78,9 +82,12 @@ __global__ void __launch_bounds__(kNaiveThreads)
         if (!done) {
             for (int j = 0; j < cnt; ++j) {
                 const TriRec tr = tile[s][j];
-                if (!pbg_filter(tr, o, d, nd, best_t)) continue;
+                if (STATS) wc.filt++;
+                if (!pbg_filter(tr, o, d, nd, best_t, STATS ? &wc.filt2 : nullptr)) continue;
                 float tt, u1, u2;
+                if (STATS) wc.exact++;
                 if (!pbg_exact_rec(tr, o, d, best_t, &tt, &u1, &u2)) continue;
+                if (STATS) wc.hit++;
                 const int32_t id = __float_as_int(tr.c.w);
                 if (ANY) {
                     best = id;
@@ -110,6 +117,7 @@ __global__ void __launch_bounds__(kNaiveThreads)
             issue(k + kNaiveStages, s);
         }
     }
+    if (STATS) wc.flush(wcount);
     if (failed || ray >= n) return;
 
     if (ANY) {
@@ -203,9 +211,14 @@ int naive_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t*
         PBG_CUDA(cudaMemsetAsync(keys, 0, (size_t)n * sizeof(unsigned long long), st));
     }
     prof_begin(s, st);
-    naive_kernel<false><<<grid, kNaiveThreads, 0, st>>>((const TriRec*)s->tris.ptr, s->ntri, per, o,
-                                                        d, valid, n, prim, t, b1, b2, keys, nullptr,
-                                                        (int*)s->err.ptr);
+    if (s->prof.level >= 2)
+        naive_kernel<false, true><<<grid, kNaiveThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, s->ntri, per, o, d, valid, n, prim, t, b1, b2, keys, nullptr,
+            (int*)s->err.ptr, (unsigned long long*)s->workc.ptr);
+    else
+        naive_kernel<false, false><<<grid, kNaiveThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, s->ntri, per, o, d, valid, n, prim, t, b1, b2, keys, nullptr,
+            (int*)s->err.ptr, nullptr);
     prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
     if (splits > 1) return finalize_keys(s, nullptr, o, d, keys, n, prim, t, b1, b2, st);
@@ -221,9 +234,14 @@ int naive_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t
     dim3 grid((unsigned)((n + kNaiveThreads - 1) / kNaiveThreads), splits);
     if (splits > 1) PBG_CUDA(cudaMemsetAsync(occ, 0, (size_t)n, st));
     prof_begin(s, st);
-    naive_kernel<true><<<grid, kNaiveThreads, 0, st>>>((const TriRec*)s->tris.ptr, s->ntri, per, o,
-                                                       d, valid, n, nullptr, nullptr, nullptr,
-                                                       nullptr, nullptr, occ, (int*)s->err.ptr);
+    if (s->prof.level >= 2)
+        naive_kernel<true, true><<<grid, kNaiveThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, s->ntri, per, o, d, valid, n, nullptr, nullptr, nullptr,
+            nullptr, nullptr, occ, (int*)s->err.ptr, (unsigned long long*)s->workc.ptr);
+    else
+        naive_kernel<true, false><<<grid, kNaiveThreads, 0, st>>>(
+            (const TriRec*)s->tris.ptr, s->ntri, per, o, d, valid, n, nullptr, nullptr, nullptr,
+            nullptr, nullptr, occ, (int*)s->err.ptr, nullptr);
     prof_end(s, st, kStageTraverse, 1);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;

@@ -850,9 +850,16 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     return PBG_OK;
 }
 
-// Pairs per queue buffer: 2^25 (256 MB); a batch that overflows it reruns
-// with the triangles split into more groups.
+// Pairs per queue buffer: 2^25 (256 MB) unless the scene's parameters set
+// another capacity; a batch that overflows it reruns with the triangles split
+// into more groups.
 constexpr uint32_t kQueueCap = 1u << 25;
+constexpr uint32_t kQueueCapMin = 4096;
+
+static uint32_t queue_capacity(const pbg_scene* s) {
+    const int32_t q = s->params.rh_queue_pairs;
+    return q > 0 ? std::max<uint32_t>((uint32_t)q, kQueueCapMin) : kQueueCap;
+}
 
 template <bool ANY>
 static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const float4* sd,
@@ -861,9 +868,10 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
     Work& w = s->work;
     int rc;
     const int64_t nleaf = lv.cnt[0];
-    if ((rc = ensure(w.queue_a, (size_t)kQueueCap * sizeof(Pair))) ||
-        (rc = ensure(w.queue_b, (size_t)kQueueCap * sizeof(Pair))) ||
-        (rc = ensure(w.pair_rank, (size_t)kQueueCap * sizeof(uint32_t))) ||
+    const uint32_t cap = queue_capacity(s);
+    if ((rc = ensure(w.queue_a, (size_t)cap * sizeof(Pair))) ||
+        (rc = ensure(w.queue_b, (size_t)cap * sizeof(Pair))) ||
+        (rc = ensure(w.pair_rank, (size_t)cap * sizeof(uint32_t))) ||
         (rc = ensure(w.leafcnt, (size_t)nleaf * sizeof(uint32_t))) ||
         (rc = ensure(w.qcount, 64 * sizeof(uint32_t))))
         return rc;
@@ -919,10 +927,10 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                 grid, ((int64_t)(s1 - s0) * lv.cnt[ls] + 255) / 256);
             if (stats)
                 rh_seed_kernel<true><<<(unsigned)seed_grid, 256, 0, st>>>(
-                    seed_sph, s0, s1, nodes + lv.off[ls], lv.cnt[ls], qa, cnt_of[ls], kQueueCap, status, wc);
+                    seed_sph, s0, s1, nodes + lv.off[ls], lv.cnt[ls], qa, cnt_of[ls], cap, status, wc);
             else
                 rh_seed_kernel<false><<<(unsigned)seed_grid, 256, 0, st>>>(
-                    seed_sph, s0, s1, nodes + lv.off[ls], lv.cnt[ls], qa, cnt_of[ls], kQueueCap, status,
+                    seed_sph, s0, s1, nodes + lv.off[ls], lv.cnt[ls], qa, cnt_of[ls], cap, status,
                     nullptr);
             uint32_t* leafcnt = (uint32_t*)w.leafcnt.ptr;
             uint32_t* rank = (uint32_t*)w.pair_rank.ptr;
@@ -935,10 +943,10 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                     if (order_hist) {  // nearest: front-to-back pairs, taken in order
                         PBG_CUDA(cudaMemsetAsync(order_hist, 0, kOrderBuckets * sizeof(uint32_t), st));
                         rh_order_count_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[1], qa, cnt_of[1],
-                                                                    kQueueCap, order_hist, status);
+                                                                    cap, order_hist, status);
                         if ((rc = scan_counts(s, order_hist, kOrderBuckets, st))) return rc;
                         rh_order_scatter_kernel<<<grid, 256, 0, st>>>(csph, nodes + lv.off[1], qa,
-                                                                      cnt_of[1], kQueueCap, order_hist, qb,
+                                                                      cnt_of[1], cap, order_hist, qb,
                                                                       status);
                         Pair* tq = qa;
                         qa = qb;
@@ -949,12 +957,12 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                     if (stats)
                         rh_split_test_kernel<ANY, true><<<tgrid, 256, 0, st>>>(
                             tsph, (const TriRec*)s->tris.ptr, t0, t1, nodes + lv.off[1], nodes + lv.off[0],
-                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, leaf_reach,
+                            lv.cnt[0], qa, cnt_of[1], cap, so, sd, keys, mask, leaf_reach,
                             parent_reach, status, wc);
                     else
                         rh_split_test_kernel<ANY, false><<<tgrid, 256, 0, st>>>(
                             tsph, (const TriRec*)s->tris.ptr, t0, t1, nodes + lv.off[1], nodes + lv.off[0],
-                            lv.cnt[0], qa, cnt_of[1], kQueueCap, so, sd, keys, mask, leaf_reach,
+                            lv.cnt[0], qa, cnt_of[1], cap, so, sd, keys, mask, leaf_reach,
                             parent_reach, status, nullptr);
                     fused = true;
                     ++nl;
@@ -963,11 +971,11 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                 if (cl && l == split) {  // clusters -> triangles, same level
                     if (stats)
                         rh_split_kernel<true><<<grid * 2, 256, 0, st>>>(
-                            tsph, t0, t1, nodes + lv.off[l], qa, cnt_of[l], qb, &counts[l], kQueueCap,
+                            tsph, t0, t1, nodes + lv.off[l], qa, cnt_of[l], qb, &counts[l], cap,
                             status, wc);
                     else
                         rh_split_kernel<false><<<grid * 2, 256, 0, st>>>(
-                            tsph, t0, t1, nodes + lv.off[l], qa, cnt_of[l], qb, &counts[l], kQueueCap,
+                            tsph, t0, t1, nodes + lv.off[l], qa, cnt_of[l], qb, &counts[l], cap,
                             status, nullptr);
                     Pair* tq = qa;
                     qa = qb;
@@ -980,11 +988,11 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
                 if (stats)
                     rh_expand_kernel<true><<<grid, 256, 0, st>>>(
                         sph, nodes + lv.off[l - 1], lv.cnt[l - 1], qa, cnt_of[l], qb, cnt_of[l - 1],
-                        kQueueCap, status, wc);
+                        cap, status, wc);
                 else
                     rh_expand_kernel<false><<<grid, 256, 0, st>>>(
                         sph, nodes + lv.off[l - 1], lv.cnt[l - 1], qa, cnt_of[l], qb, cnt_of[l - 1],
-                        kQueueCap, status, nullptr);
+                        cap, status, nullptr);
                 Pair* tq = qa;
                 qa = qb;
                 qb = tq;
@@ -992,17 +1000,17 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
             }
             // group the leaf pairs by leaf (qa -> qb), then the leaf tests
             if (!fused) {
-                rh_leaf_count_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank);
+                rh_leaf_count_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], cap, leafcnt, rank);
                 if ((rc = scan_counts(s, leafcnt, nleaf, st))) return rc;
-                rh_leaf_scatter_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], kQueueCap, leafcnt, rank, qb,
+                rh_leaf_scatter_kernel<<<grid, 256, 0, st>>>(qa, &counts[0], cap, leafcnt, rank, qb,
                                                              status);
                 if (stats)
                     rh_leaf_sorted_kernel<ANY, true><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
-                        (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask,
+                        (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], cap, so, sd, keys, mask,
                         status, wc);
                 else
                     rh_leaf_sorted_kernel<ANY, false><<<grid * 2, 32 * kLeafWarps, 0, st>>>(
-                        (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], kQueueCap, so, sd, keys, mask,
+                        (const TriRec*)s->tris.ptr, nodes, qb, &counts[0], cap, so, sd, keys, mask,
                         status, nullptr);
                 nl += 3;
             }

@@ -364,13 +364,14 @@ def test_device_entry_reruns_on_a_caller_stream(gpu_lib, oracle):
     """The device entry points on a caller's stream, through the two paths
     that trace a batch again after its first attempt already wrote the
     caller's arrays: a pair-queue overflow (a million incoherent rays of
-    unbounded length against the 181,250-triangle scene, the scene's first
-    call) and a shadow batch whose origins moved from the kept order.  The
-    final results equal the oracle's."""
+    unbounded length against the 181,250-triangle scene with its pair
+    queues held to 2^18 pairs, the scene's first call) and a shadow batch
+    whose origins moved from the kept order.  The final results equal the
+    oracle's."""
     import torch
     sc = S.terrain_icospheres(seed=2)
     tris = sc["tris"]
-    acc = A.MakeAccelerator("rayhierarchy", tris)
+    acc = A.MakeAccelerator("rayhierarchy", tris, {"queuePairs": 1 << 18})
     B = oracle.BVH(tris)
     stream = torch.cuda.Stream()
     rays = S.random_rays(1 << 20, [-8, -1, -8], [8, 4, 8], seed=41)
