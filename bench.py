@@ -232,6 +232,12 @@ def run_gpu(args, rank, world, dev):
     nhit = int(hitmask.sum())
     rays_per_step = n + len(shadows) * nhit
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    tuned = None
+    if not args.no_tune:  # launch shapes for the camera batch and the shadow batches
+        tuned = {"camera (nearest)": acc.autotune(o4, d4, stream=stream),
+                 "shadow (any-hit)": acc.autotune(sdev[0][0], sdev[0][1], anyhit=True, valid=valid,
+                                                  stream=stream)}
+        stream.synchronize()
 
     def step():
         acc.intersect_device(o4, d4, prim, tt, b1, b2, stream=stream)
@@ -315,7 +321,9 @@ def run_gpu(args, rank, world, dev):
                        "accelerator": args.accel, "rays_per_step": rays_per_step,
                        "primary_rays": n, "shadow_rays": len(shadows) * nhit,
                        "triangles": int(len(tris)), "parallelism": f"replicas x{world}",
-                       "l2": "flushed between steps (256 MB write), outside the timed region"},
+                       "l2": "flushed between steps (256 MB write), outside the timed region",
+                       "autotune": {k: v["best"] for k, v in tuned.items()} if tuned else None},
+            "autotune": tuned,
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
                          "unit": "GB/s", "frac": round(achieved / hbm, 5),
@@ -392,7 +400,9 @@ def path_cpu_counter(tris, r2c, c2w, seed):
 def timed_cpu_sample(rc, threads, target_s, seed):
     """Traces a strided subset of the frame's samples sized to about target_s
     seconds on `threads` host threads; returns (rays, seconds, stride)."""
-    probe = 8192
+    # the probe traces about 65,536 samples: enough that thread start-up
+    # does not dominate its time
+    probe = max(1, rc.samples // 65536)
     t0 = time.perf_counter()
     n0, s0 = rc.count(0, probe, threads, seed)
     dt = max(time.perf_counter() - t0, 1e-4)
@@ -499,6 +509,20 @@ def run_gpu_path(args, rank, world, dev):
     cam = R.camera_struct(r2c, c2w, PATH_RES, PATH_RES)
     light = R.quad_light(PATH_LIGHT, PATH_LIGHT_L, 1)
     prm = R.render_params("path", spp=PATH_SPP, jitter=True, max_depth=PATH_DEPTH, seed=17)
+    tuned = None
+    if not args.no_tune:
+        # the walk per batch class: camera rays (coherent) and rays with
+        # uniform origins and directions in the scene's box (incoherent,
+        # like the bounces), nearest hit and any hit
+        from pbrt_gb300 import scenes as S
+        co4, cd4 = to_dev(S.pinhole_rays(PATH_RES, PATH_RES, PATH_CAMERA["eye"], PATH_CAMERA["look"],
+                                        PATH_CAMERA["fov"], spp=1))
+        io4, id4 = to_dev(S.random_rays(1 << 20, -20.0, 20.0, seed=77))
+        tuned = {"coherent nearest": acc.autotune(co4, cd4), "coherent any-hit": acc.autotune(co4, cd4, anyhit=True),
+                 "incoherent nearest": acc.autotune(io4, id4, incoherent=True),
+                 "incoherent any-hit": acc.autotune(io4, id4, anyhit=True, incoherent=True)}
+        del co4, cd4, io4, id4
+        torch.cuda.synchronize()
 
     def measure():
         for k in range(args.warmup):
@@ -628,7 +652,9 @@ def run_gpu_path(args, rank, world, dev):
                    "rays_per_step": int(rays), "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays),
                    "triangles": int(len(tris)), "bvh_build_s": round(build_s, 2),
                    "ray_sort": bool(args.ray_sort), "parallelism": f"replicas x{world}",
-                   "l2": "inputs > L2 (8.4M paths x 32 B rays per bounce)"},
+                   "l2": "inputs > L2 (8.4M paths x 32 B rays per bounce)",
+                   "autotune": {k: v["best"] for k, v in tuned.items()} if tuned else None},
+        "autotune": tuned,
         "traversal_mrays_s": round(rays / (trav_ms * 1e-3) / 1e6, 2),
         "e2e": {"value": round(rays / (sum(walls) / len(walls)) / 1e6, 2), "unit": "Mrays/s",
                 "ms_per_step": round(sum(walls) / len(walls) * 1e3, 3),
@@ -689,6 +715,12 @@ def run_gpu_naive(args, rank, world, dev):
     light = R.point_light(g["light_pos"], g["light_I"])
     prm = R.render_params("directlighting")
     flush = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
+    tuned = None
+    if not args.no_tune:  # the splits' launch shape, on the frame's camera rays
+        cr = S.config_small_naive()["rays"]
+        o4, d4 = to_dev(cr)
+        tuned = {"camera (nearest)": acc.autotune(o4, d4), "camera rays as any-hit": acc.autotune(o4, d4, anyhit=True)}
+        torch.cuda.synchronize()
     for _ in range(args.warmup):
         flush_l2(flush)
         R.render(acc, cam, [light], prm)
@@ -764,7 +796,9 @@ def run_gpu_naive(args, rank, world, dev):
         "data": "synthetic (UV sphere + ground quad; the reference's camera and light)",
         "config": {"workload": NAIVE_WORKLOAD, "accelerator": "naive", "rays_per_step": int(rays),
                    "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays), "triangles": int(len(tris)),
-                   "parallelism": f"replicas x{world}", "l2": "flushed before every frame (256 MB write)"},
+                   "parallelism": f"replicas x{world}", "l2": "flushed before every frame (256 MB write)",
+                   "autotune": {k: v["best"] for k, v in tuned.items()} if tuned else None},
+        "autotune": tuned,
         "e2e": {"value": round(rays / (sum(walls) / len(walls)) / 1e6, 2), "unit": "Mrays/s",
                 "ms_per_step": round(sum(walls) / len(walls) * 1e3, 4),
                 "h2d_bytes_per_step": 256 + 112, "d2h_bytes_per_step": 256 * 256 * 12,
@@ -1224,6 +1258,7 @@ def main():
     ap.add_argument("--accel", default="rayhierarchy", choices=["naive", "rayhierarchy", "ray-bvh"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no pbg_autotune)")
     ap.add_argument("--workload", default="path", choices=["path", "frame", "batch", "naive"])
     ap.add_argument("--path-res", type=int, default=PATH_RES,
                     help="path workload: image width and height (profiler captures use a smaller frame)")

@@ -458,6 +458,29 @@ int pbg_occluded_hinted_device(pbg_scene* scene, const float* o4, const float* d
 int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t M, int32_t N,
                      int32_t K, int32_t accumulate, void* stream);
 
+/* Launch-shape autotuner (replaces picking chunkXSize / chunkYSize /
+ * height by hand, rayhierarchy.cpp:1329-1348).  Traces the device batch
+ * o4/d4 (16-byte ray records, valid may be NULL) with every candidate shape
+ * of the scene's accelerator -- naive: CTAs per SM of the triangle splits
+ * (2, 4, 8, 16); rayhierarchy: nodes of the seed level (64, 256, 1024) x
+ * CTAs per SM of the grid-stride kernels (16, 32); ray-bvh: one thread per
+ * ray or persistent warps for this batch class -- times each on `stream`
+ * (best of `reps` after a warm-up run), checks that every candidate's
+ * results equal the first one's bit for bit (else PBG_ERR_INTERNAL and the
+ * scene keeps its shapes), and keeps the fastest for later calls.
+ * query: bit 0 = any-hit (else nearest hit), bit 1 = an incoherent batch
+ * (bounce rays; ray-bvh keeps a walk per any-hit/incoherent class).
+ * Allocates scratch for two result sets while it runs; synchronises. */
+typedef struct pbg_tune_result {
+    int32_t ncandidates;
+    int32_t best;            /* index of the candidate kept */
+    int32_t setting[16][3];  /* naive {ctas}, rayhierarchy {seed nodes, grid}, ray-bvh {walk} */
+    float ms[16];            /* device time of the batch with each candidate */
+    uint64_t mismatches;     /* results that differed from the first candidate's (0) */
+} pbg_tune_result;
+int pbg_autotune(pbg_scene* scene, const float* o4, const float* d4, const uint8_t* valid, int64_t n,
+                 int32_t query, int32_t reps, pbg_tune_result* out, void* stream);
+
 /* Counters and per-stage device times (replaces the GPU_TIMES / STAT_*
  * printouts, core/GPUparallel.h:532-538 and rayhierarchy.cpp:229-239).
  * Reading them synchronises the scene's pending timing events. */

@@ -32,6 +32,11 @@ class PbgError(RuntimeError):
         super().__init__(f"{what}: status {status} ({status_string(status)}): {last_error()}")
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("ncandidates", C.c_int32), ("best", C.c_int32), ("setting", (C.c_int32 * 3) * 16),
+                ("ms", C.c_float * 16), ("mismatches", C.c_uint64)]
+
+
 class Params(C.Structure):
     _fields_ = [("chunk_x", C.c_int32), ("chunk_y", C.c_int32), ("height", C.c_int32),
                 ("bvh_height", C.c_int32), ("max_bvh_prim", C.c_int32), ("device", C.c_int32),
@@ -116,6 +121,7 @@ def lib():
     L.pbg_occluded_hinted_device.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp]
     L.pbg_hit_geometry.argtypes = [vp, C.POINTER(Rays), C.POINTER(Hits), C.c_int64, vp]
     L.pbg_hit_geometry_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64, vp, vp]
+    L.pbg_autotune.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_int32, C.c_int32, C.POINTER(TuneResult), vp]
     L.pbg_stats.argtypes = [vp, C.POINTER(Counters)]
     L.pbg_profile.argtypes = [vp, C.c_int]
     L.pbg_preprocess.argtypes = [vp, C.c_int64, C.c_int64]

@@ -161,6 +161,22 @@ class Aggregate:
             n, prim.data_ptr(), t.data_ptr(), b1.data_ptr(), b2.data_ptr(),
             None if stream is None else stream.cuda_stream), "pbg_intersect_device")
 
+    def autotune(self, o4, d4, anyhit=False, incoherent=False, valid=None, reps=3, stream=None) -> dict:
+        """pbg_autotune on a device batch: times every launch shape of this
+        accelerator on it, checks that they all give the same results, and
+        keeps the fastest.  Returns the candidates' settings and times."""
+        r = L.TuneResult()
+        query = (1 if anyhit else 0) | (2 if incoherent else 0)
+        L.check(L.lib().pbg_autotune(self.handle, o4.data_ptr(), d4.data_ptr(),
+                                     None if valid is None else valid.data_ptr(), o4.shape[0], query, reps,
+                                     C.byref(r), None if stream is None else stream.cuda_stream),
+                "pbg_autotune")
+        names = {"naive": ("ctas_per_sm",), "rayhierarchy": ("seed_nodes", "grid_ctas_per_sm"),
+                 "ray-bvh": ("walk",)}[self.kind]
+        cands = [{"setting": {k: int(r.setting[i][j]) for j, k in enumerate(names)}, "ms": round(float(r.ms[i]), 4)}
+                 for i in range(r.ncandidates)]
+        return {"candidates": cands, "best": cands[r.best]["setting"], "mismatches": int(r.mismatches)}
+
     def occluded_device(self, o4, d4, occ, valid=None, stream=None):
         n = o4.shape[0]
         L.check(L.lib().pbg_occluded_device(

@@ -432,7 +432,7 @@ int launch_build_tris(const float* tri9_dev, const int32_t* order_dev, int64_t n
 
 // ------------------------------------------------------------- dispatch
 
-static int run_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,
+int run_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,
                        int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
     switch (s->accel) {
         case PBG_ACCEL_NAIVE: return naive_nearest(s, o, d, valid, n, prim, t, b1, b2, st);
@@ -443,7 +443,7 @@ static int run_nearest(pbg_scene* s, const float4* o, const float4* d, const uin
     return PBG_ERR_INVALID_ARGUMENT;
 }
 
-static int run_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,
+int run_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid,
                         int64_t n, uint8_t* occ, cudaStream_t st) {
     switch (s->accel) {
         case PBG_ACCEL_NAIVE: return naive_occluded(s, o, d, valid, n, occ, st);

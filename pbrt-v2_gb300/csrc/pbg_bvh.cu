@@ -322,7 +322,9 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // bounce batches are incoherent: the reference's bounce form of Intersect
     // is the one with a validity mask (rayhierarchy.cpp:602-813)
     const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
-    const bool persistent = s->params.walk == 2 || (s->params.walk == 0 && hint == 1);
+    const int tuned = s->tune.bvh_walk[ANY ? 1 : 0][hint == 1 ? 1 : 0];
+    const bool persistent =
+        s->params.walk == 2 || (s->params.walk == 0 && (tuned != 0 ? tuned == 2 : hint == 1));
     if (persistent) {
         // persistent while-while walk: one counter word, zeroed per launch
         Work& w = s->work;

@@ -73,6 +73,17 @@ enum { kOrderDefault = 0, kOrderOrigin = 1 };
 // Records per rayhierarchy triangle cluster (one warp splits a cluster).
 constexpr int kClusterTris = 32;
 
+// Launch-shape settings that change no result, chosen by pbg_autotune (the
+// defaults are the shapes measured best on the benchmark scenes).
+struct Tunables {
+    int naive_ctas = 4;      // naive: CTAs per SM the triangle splits aim for
+    // rayhierarchy [any-hit]: nodes of the level the descent starts at (at
+    // most), CTAs per SM of the grid-stride kernels
+    int rh_seed[2] = {256, 256};
+    int rh_grid[2] = {32, 32};
+    int bvh_walk[2][2] = {{0, 0}, {0, 0}};  // ray-bvh [any-hit][incoherent]: 0 automatic, 1 per ray, 2 persistent
+};
+
 // Per-batch device scratch owned by a scene.
 struct Work {
     DeviceBuffer ray_o, ray_d, ray_o2, ray_d2, valid, prim, t, b1, b2, occ, keys, stage, perm,
@@ -109,6 +120,7 @@ struct pbg_scene {
     int32_t unculled = 0;      // records [0, unculled) are tested by every ray
     int rh_groups = 1;         // triangle groups per rayhierarchy traversal (grows on overflow)
     int walk_hint = -1;        // ray-bvh: 1 = incoherent batch, 0 = coherent, -1 = infer
+    pbg::Tunables tune;        // launch shapes (pbg_autotune)
     std::vector<pbg::BvhNode> host_nodes;  // ray-bvh tree, kept for the learned clusters
     std::vector<int32_t> host_order;
     struct pbg::Learner* learn = nullptr;
@@ -147,6 +159,11 @@ int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* va
                int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
 int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                 uint8_t* occ, cudaStream_t st);
+// The accelerator's batch query (device rays and results on st).
+int run_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
+int run_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
+                 uint8_t* occ, cudaStream_t st);
 int hit_geometry(pbg_scene* s, const float4* o, const float4* d, const int32_t* prim,
                  const float* t, const float* b1, const float* b2, int64_t n, float* out14,
                  cudaStream_t st);

@@ -12,8 +12,9 @@
 // stages deep, and every thread reads each record as a broadcast.  With one
 // split the thread writes its hit directly; with several, the splits merge
 // through a 64-bit atomicMax on (t, index) keys and a finalize pass recomputes
-// b1/b2 of the winner with the exact test.  Any-hit leaves a tile loop as
-// soon as every ray of the CTA is occluded.
+// b1/b2 of the winner with the exact test.  Any-hit: a warp leaves a tile
+// once all its rays are occluded, the CTA leaves the tile loop once every
+// ray of the CTA is.
 #include "pbg_count.cuh"
 #include "pbg_internal.h"
 #include "pbg_tma.cuh"
@@ -74,12 +75,38 @@ __global__ void __launch_bounds__(kNaiveThreads)
     for (int k = 0; k < ntiles; ++k) {
         const int s = k % kNaiveStages;
         const uint32_t parity = (uint32_t)(k / kNaiveStages) & 1u;
-        if (!mbar_wait_bounded(&bar[s], parity, status)) {
+        // a wait that gave up ends the loop for the whole CTA at once, so
+        // that no thread is left at a barrier or warp vote below
+        const bool ok = mbar_wait_bounded(&bar[s], parity, status);
+        if (__syncthreads_or(ok ? 0 : 1)) {
             failed = true;
             break;
         }
         const int cnt = (int)min((int64_t)kNaiveTile, t1 - (t0 + (int64_t)k * kNaiveTile));
-        if (!done) {
+        if (ANY) {
+            // Every lane runs every iteration (a finished lane skips the
+            // test) so that the warp stays converged: a per-lane break out
+            // of this loop left lanes running it one small group at a time.
+            // The warp leaves once all its rays are occluded.
+            if (!__all_sync(0xffffffffu, done)) {
+                for (int j = 0; j < cnt; ++j) {
+                    if (!done) {
+                        const TriRec tr = tile[s][j];
+                        if (STATS) wc.filt++;
+                        if (pbg_filter(tr, o, d, nd, best_t, STATS ? &wc.filt2 : nullptr)) {
+                            float tt, u1, u2;
+                            if (STATS) wc.exact++;
+                            if (pbg_exact_rec(tr, o, d, best_t, &tt, &u1, &u2)) {
+                                if (STATS) wc.hit++;
+                                best = __float_as_int(tr.c.w);
+                                done = true;
+                            }
+                        }
+                    }
+                    if ((j & 7) == 7 && __all_sync(0xffffffffu, done)) break;
+                }
+            }
+        } else if (!done) {
             for (int j = 0; j < cnt; ++j) {
                 const TriRec tr = tile[s][j];
                 if (STATS) wc.filt++;
@@ -89,11 +116,6 @@ __global__ void __launch_bounds__(kNaiveThreads)
                 if (!pbg_exact_rec(tr, o, d, best_t, &tt, &u1, &u2)) continue;
                 if (STATS) wc.hit++;
                 const int32_t id = __float_as_int(tr.c.w);
-                if (ANY) {
-                    best = id;
-                    done = true;
-                    break;
-                }
                 if (tt < best_t || id > best) {
                     best_t = tt;
                     best = id;
@@ -182,8 +204,10 @@ static int naive_launch_shape(pbg_scene* s, int64_t n, int64_t* per_split, unsig
     const int64_t ray_ctas = (n + kNaiveThreads - 1) / kNaiveThreads;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-    // Aim for about four CTAs per SM; never split below one tile per split.
-    int64_t want = (4 * (int64_t)sms + ray_ctas - 1) / ray_ctas;
+    // Aim for tune.naive_ctas CTAs per SM (4 unless tuned); never split
+    // below one tile per split.
+    const int64_t per_sm = s->tune.naive_ctas > 0 ? s->tune.naive_ctas : 4;
+    int64_t want = (per_sm * (int64_t)sms + ray_ctas - 1) / ray_ctas;
     int64_t max_splits = (s->ntri + kNaiveTile - 1) / kNaiveTile;
     if (want > max_splits) want = max_splits;
     if (want < 1) want = 1;

@@ -779,12 +779,12 @@ __global__ void rh_finalize_occluded(const int32_t* __restrict__ perm,
 
 // The levels the traversal reads: clusters split into triangles at level
 // `split`, and the descent is seeded at `seed`, the lowest level of at most
-// kSeedNodes nodes not below max(split, 1).  No level above the seed is
+// kSeedNodes (tune.rh_seed) nodes not below max(split, 1).  No level above the seed is
 // read, so the build stops there.
 struct Descent {
     int split, seed;
 };
-static Descent descent_levels(const pbg_scene* s, const Levels& lv) {
+static Descent descent_levels(const pbg_scene* s, const Levels& lv, bool any) {
     const int top = lv.nlev - 1;
     // levels walked by 32-triangle clusters before they split into triangles
     // (default: down to the leaves' parents, the fastest split on the
@@ -795,7 +795,8 @@ static Descent descent_levels(const pbg_scene* s, const Levels& lv) {
     Descent d;
     d.split = std::max(0, top - kcl);
     d.seed = top;
-    while (d.seed > std::max(d.split, 1) && lv.cnt[d.seed - 1] <= kSeedNodes) --d.seed;
+    const int64_t seed_nodes = s->tune.rh_seed[any] > 0 ? s->tune.rh_seed[any] : kSeedNodes;
+    while (d.seed > std::max(d.split, 1) && lv.cnt[d.seed - 1] <= seed_nodes) --d.seed;
     return d;
 }
 
@@ -836,7 +837,8 @@ static int rh_build(pbg_scene* s, const float4* o, const float4* d, const uint8_
     leaf_build_kernel<<<(unsigned)((nleaf * 32 + 255) / 256), 256, 0, st>>>(o, d, *perm, *so, *sd, skeys,
                                                                             n, nleaf, nodes, keep_o);
     prof_end(s, st, kStageBuild, 1);
-    const int built = descent_levels(s, *lv).seed;  // the levels above are never read
+    // the levels above are never read (any-hit batches are the origin-ordered ones)
+    const int built = descent_levels(s, *lv, order == kOrderOrigin).seed;
     for (int l0 = 0; l0 < built; l0 += kLevelsPerLaunch) {
         const int l1 = std::min(l0 + kLevelsPerLaunch, built);
         const int64_t group = 1ll << (2 * (l1 - l0));
@@ -877,7 +879,9 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
         return rc;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-    const unsigned grid = (unsigned)(sms * 32);  // grid-stride kernels: measured best of 4, 8, 16, 32
+    // grid-stride kernels: 32 CTAs per SM measured best of 4, 8, 16, 32 on
+    // the terrain frame (tune.rh_grid)
+    const unsigned grid = (unsigned)(sms * (s->tune.rh_grid[ANY] > 0 ? s->tune.rh_grid[ANY] : 32));
     const bool stats = s->prof.level >= 2;
     unsigned long long* wc = (unsigned long long*)s->workc.ptr;
     int* status = (int*)s->err.ptr;
@@ -886,7 +890,7 @@ static int rh_traverse(pbg_scene* s, const Levels& lv, const float4* so, const f
     static_assert(2 * kMaxLevels <= 64, "pair counters");
     int groups = s->rh_groups > 0 ? s->rh_groups : 1;
     const int top = lv.nlev - 1;
-    const Descent dsc = descent_levels(s, lv);
+    const Descent dsc = descent_levels(s, lv, ANY);
     const int split = dsc.split;
     const int kcl = top - split;  // levels walked by clusters (0: none)
     const float4* tsph = (const float4*)s->spheres.ptr;
