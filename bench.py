@@ -66,8 +66,9 @@ FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 148_000_000, "ray-bvh": 116_000_00
 # fraction of the dominant kernel (smsp__issue_active, --set full capture of
 # the frame's camera and first shadow batch)
 # dram__bytes_read.sum + dram__bytes_write.sum per traversal launch of the
-# path frame (None until captured)
-PATH_LAUNCH_DRAM_BYTES = None
+# path frame: the average over the 12 traversal launches of one full-size
+# frame (ncu, the automatic walk, first frame of the run)
+PATH_LAUNCH_DRAM_BYTES = 294_658_368
 # smsp__issue_active of the persistent walk on the path frame's bounces
 # (ncu --set full, bounce 2 of the warm-up frame: nearest, any-hit)
 PATH_ISSUE_ACTIVE = {"bvh_persistent_kernel (nearest)": 0.67, "bvh_persistent_kernel (any-hit)": 0.66}
@@ -504,7 +505,7 @@ def run_gpu_path(args, rank, world, dev):
     sc, r2c, c2w = path_setup()
     tris = sc["tris"]
     t0 = time.perf_counter()
-    acc = A.MakeAccelerator("ray-bvh", tris, {"device": dev, "raySort": int(args.ray_sort)})
+    acc = A.MakeAccelerator("ray-bvh", tris, {"device": dev, "raySort": int(args.ray_sort), "walk": args.walk})
     build_s = time.perf_counter() - t0
     cam = R.camera_struct(r2c, c2w, PATH_RES, PATH_RES)
     light = R.quad_light(PATH_LIGHT, PATH_LIGHT_L, 1)
@@ -651,7 +652,7 @@ def run_gpu_path(args, rank, world, dev):
                    "ordering": "learned" if args.learned == 1 else "plain",
                    "rays_per_step": int(rays), "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays),
                    "triangles": int(len(tris)), "bvh_build_s": round(build_s, 2),
-                   "ray_sort": bool(args.ray_sort), "parallelism": f"replicas x{world}",
+                   "ray_sort": bool(args.ray_sort), "walk": args.walk, "parallelism": f"replicas x{world}",
                    "l2": "inputs > L2 (8.4M paths x 32 B rays per bounce)",
                    "autotune": {k: v["best"] for k, v in tuned.items()} if tuned else None},
         "autotune": tuned,
@@ -1266,7 +1267,8 @@ def main():
     ap.add_argument("--rh-cluster-levels", type=int, default=0,
                     help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")
     ap.add_argument("--walk", type=int, default=0,
-                    help="ray-bvh: 0 automatic, 1 one thread per ray, 2 persistent warps")
+                    help="ray-bvh: 0 automatic (or tuned), 1 one thread per ray, 2 persistent warps, "
+                         "3 warp packets over the ray hierarchy's leaves")
     ap.add_argument("--learn-steps", type=int, default=0, help="SGD steps per frame (0 = 8)")
     ap.add_argument("--learn-lr", type=float, default=0.0, help="learning rate (0 = 0.05)")
     ap.add_argument("--learn-margin", type=float, default=0.0,

@@ -74,6 +74,115 @@ __global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
     b2_out[ray] = h.prim >= 0 ? h.b2 : 0.f;
 }
 
+// Co-traversal of the ray hierarchy with the BVH (walk = 3): the batch is
+// put in the ray hierarchy's leaf order (6-D Morton keys of origin and
+// direction, or the declared ray image's Morton order), and each warp takes
+// one leaf of 32 rays and walks the BVH with them as one packet: a node is
+// visited when any of the warp's rays hits it, every lane tests its own ray
+// against both children's boxes, leaves are tested by the lanes whose rays
+// reach them, and the stack is the warp's, in shared memory.  The nearer
+// child by the lanes' majority vote goes first.  The replaced reference
+// kernels pair ray-hierarchy nodes with BVH nodes level by level
+// (rayBVH.cpp:615-836, intersection6DB_BVH.cl); the warp packet makes the
+// same pairing one leaf at a time.  Warps take leaves from a global counter.
+constexpr int kPacketThreads = 128;
+constexpr int kPacketStack = 64;
+
+template <bool ANY, bool STATS>
+__global__ void __launch_bounds__(kPacketThreads)
+    bvh_packet_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris, int32_t unculled,
+                      const float4* __restrict__ ro, const float4* __restrict__ rd,
+                      const uint8_t* __restrict__ valid, const int32_t* __restrict__ perm, int64_t n,
+                      int32_t* __restrict__ prim_out, float* __restrict__ t_out, float* __restrict__ b1_out,
+                      float* __restrict__ b2_out, uint8_t* __restrict__ occ, int* status,
+                      unsigned long long* next, unsigned long long* wcount) {
+    __shared__ int32_t stk[kPacketThreads / 32][kPacketStack];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    const int64_t npk = (n + 31) / 32;
+    WorkCount wc;
+    bool overflow = false;
+    for (;;) {
+        unsigned long long pk = 0;
+        if (lane == 0) pk = atomicAdd(next, 1ull);
+        pk = __shfl_sync(full, pk, 0);
+        if ((int64_t)pk >= npk) break;
+        const int64_t slot = (int64_t)pk * 32 + lane;
+        const int64_t ray = slot < n ? (perm ? (int64_t)perm[slot] : slot) : -1;
+        const bool active = ray >= 0 && (valid == nullptr || valid[ray] != 0);
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, 0.f);
+        if (active) {
+            o = ro[ray];
+            d = rd[ray];
+        }
+        const float ndd = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+        const RayInv ri{o.x, o.y, o.z, safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+        WalkHit h{d.w, 0.f, 0.f, -1};
+        bool done = !active;
+        if (!done && unculled > 0) done = test_run<ANY, STATS>(tris, 0, unculled, o, d, ndd, h, wc);
+        int sp = 0;  // warp-uniform
+        int32_t node = 0;
+        for (;;) {
+            if (__all_sync(full, done)) break;
+            const BvhNode nd_ = nodes[node];
+            float tn0 = 0.f, tn1 = 0.f;
+            bool h0 = false, h1 = false;
+            if (!done) {
+                if (STATS) wc.node += 2;
+                h0 = slab(ri, nd_.n0.x, nd_.n0.y, nd_.n0.z, nd_.n0.w, nd_.n2.x, nd_.n2.y, o.w, h.t, &tn0);
+                h1 = slab(ri, nd_.n1.x, nd_.n1.y, nd_.n1.z, nd_.n1.w, nd_.n2.z, nd_.n2.w, o.w, h.t, &tn1);
+            }
+            const int32_t c0 = nd_.n3.x, c1 = nd_.n3.y;
+            const unsigned both = __ballot_sync(full, h0 && h1);
+            const unsigned near1 = __ballot_sync(full, h0 && h1 && tn1 < tn0);
+            const bool first1 = 2 * __popc(near1) > __popc(both);
+            // leaf children at once, the nearer one first
+            for (int q = 0; q < 2; ++q) {
+                const int side = first1 ? 1 - q : q;
+                const int32_t c = side ? c1 : c0;
+                const bool hh = side ? h1 : h0;
+                if (c < 0 && __any_sync(full, hh && !done)) {
+                    if (hh && !done) {
+                        if (STATS) wc.leaf++;
+                        done = test_run<ANY, STATS>(tris, ~c, side ? nd_.n3.w : nd_.n3.z, o, d, ndd, h, wc);
+                    }
+                }
+            }
+            const bool g0 = c0 >= 0 && __any_sync(full, h0 && !done);
+            const bool g1 = c1 >= 0 && __any_sync(full, h1 && !done);
+            if (g0 && g1) {
+                const int32_t nearc = first1 ? c1 : c0, farc = first1 ? c0 : c1;
+                if (sp < kPacketStack) {
+                    if (lane == 0) stk[warp][sp] = farc;
+                    ++sp;
+                } else {
+                    overflow = true;
+                }
+                node = nearc;
+            } else if (g0 || g1) {
+                node = g0 ? c0 : c1;
+            } else {
+                if (sp == 0) break;
+                __syncwarp();
+                node = stk[warp][--sp];
+                __syncwarp();
+            }
+        }
+        if (ray < 0) continue;
+        if (ANY) {
+            occ[ray] = h.prim >= 0 ? 1 : 0;
+            if (prim_out) prim_out[ray] = h.prim;
+        } else {
+            prim_out[ray] = h.prim;
+            t_out[ray] = h.prim >= 0 ? h.t : 0.f;
+            b1_out[ray] = h.prim >= 0 ? h.b1 : 0.f;
+            b2_out[ray] = h.prim >= 0 ? h.b2 : 0.f;
+        }
+    }
+    if (overflow && lane == 0) atomicAdd(&status[kStatusOverflow], 1);
+    if (STATS) wc.flush(wcount);
+}
+
 // Persistent "while-while" form for incoherent batches (one thread per ray
 // leaves most lanes of a warp idle: rays finish at different times and leaf
 // tests run for a few lanes at a time).  Each lane takes a new ray from a
@@ -323,9 +432,30 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // is the one with a validity mask (rayhierarchy.cpp:602-813)
     const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
     const int tuned = s->tune.bvh_walk[ANY ? 1 : 0][hint == 1 ? 1 : 0];
-    const bool persistent =
-        s->params.walk == 2 || (s->params.walk == 0 && (tuned != 0 ? tuned == 2 : hint == 1));
-    if (persistent) {
+    const int walk = s->params.walk != 0 ? s->params.walk : (tuned != 0 ? tuned : (hint == 1 ? 2 : 1));
+    // the packet walk has no ordered form: with cluster hints or the learned
+    // ordering it gives way to the persistent walk
+    const bool packet = walk == 3 && !pred;
+    const bool persistent = walk == 2 || (walk == 3 && pred);
+    if (packet) {
+        const int32_t* order = perm;  // the ray hierarchy's leaf order
+        int rc3 = order ? PBG_OK : ray_order(s, o, d, n, &order, st);
+        if (rc3) return rc3;
+        Work& w = s->work;
+        if ((rc3 = ensure(w.counters, 64))) return rc3;
+        unsigned long long* next = (unsigned long long*)w.counters.ptr;
+        PBG_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_packet_kernel<ANY, false>, kPacketThreads, 0);
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+        int64_t blocks = (int64_t)std::max(per_sm, 1) * sms;
+        blocks = std::min<int64_t>(blocks, (n + kPacketThreads - 1) / kPacketThreads);
+        const bool stats = s->prof.level >= 2;
+        auto kern = stats ? bvh_packet_kernel<ANY, true> : bvh_packet_kernel<ANY, false>;
+        kern<<<(unsigned)blocks, kPacketThreads, 0, st>>>(nodes, tris, s->unculled, o, d, valid, order, n, prim, t,
+                                                          b1, b2, occ, status, next, stats ? wc : nullptr);
+    } else if (persistent) {
         // persistent while-while walk: one counter word, zeroed per launch
         Work& w = s->work;
         int rc2 = ensure(w.counters, 64);

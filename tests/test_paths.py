@@ -1,12 +1,14 @@
 """Every internal path choice gives the same answers: rayhierarchy with and
 without triangle clusters (and splitting at any level), ray-bvh with one
-thread per ray or persistent warps, the ray image ordered by the direct
+thread per ray, persistent warps or warp packets over the ray hierarchy's
+leaves, the ray image ordered by the direct
 Morton permutation (power-of-two sides) or by sorting (other sides), and
 host buffers read in place (pageable or pinned) or staged through copies.
 All compared bit for bit against the oracle's SAH BVH on the same rays."""
 import numpy as np
 import pytest
 
+from conftest import GOLDEN_CASES, load_golden
 from pbrt_gb300 import accel as A
 from pbrt_gb300 import scenes as S
 
@@ -44,7 +46,7 @@ def test_rayhierarchy_cluster_levels(gpu_lib, terrain, levels):
     np.testing.assert_array_equal(occ == ord("1"), terrain["occ_inc"] == 1)
 
 
-@pytest.mark.parametrize("walk", [1, 2])
+@pytest.mark.parametrize("walk", [1, 2, 3])
 def test_raybvh_walks(gpu_lib, terrain, walk):
     acc = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": walk})
     assert_same(acc.Intersect(terrain["cam"].copy()), terrain["want_cam"], f"cam, walk {walk}")
@@ -56,6 +58,43 @@ def test_raybvh_walks(gpu_lib, terrain, walk):
     got = acc.Intersect(terrain["inc"].copy(), hit=hit.copy(), bounce=1)
     assert (got[0][~hit] == -1).all()
     np.testing.assert_array_equal(got[0][hit], terrain["want_inc"][0][hit])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_packet_walk_golden(gpu_lib, case):
+    """walk 3 (warp packets over the ray hierarchy's leaves) on the
+    reference's own answers: ties, degenerate triangles, limits, empty."""
+    g = load_golden(case)
+    acc = A.MakeAccelerator("ray-bvh", g["tris"], {"walk": 3})
+    got = acc.Intersect(g["rays"].copy())
+    np.testing.assert_array_equal(got[0], g["prim"])
+    h = g["prim"] >= 0
+    np.testing.assert_array_equal(got[1][h], g["t"][h])
+    np.testing.assert_array_equal(acc.IntersectP(g["rays"]) == ord("1"), g["occ"] == 1)
+
+
+def test_packet_walk_sorted_batches(gpu_lib, oracle):
+    """walk 3 on batches large enough to be put in the ray hierarchy's
+    order (6-D Morton keys; a declared ray image's Morton order), with and
+    without a validity mask, nearest and any hit."""
+    sc = S.terrain_icospheres(seed=2, grid=96, n_spheres=12)
+    tris = sc["tris"]
+    B = oracle.BVH(tris)
+    acc = A.MakeAccelerator("ray-bvh", tris, {"walk": 3})
+    inc = S.random_rays(50000, [-8, -1, -8], [8, 4, 8], seed=31)
+    inc[7, ::2] = 2.5
+    assert_same(acc.Intersect(inc.copy()), B.nearest(inc), "incoherent")
+    np.testing.assert_array_equal(acc.IntersectP(inc) == ord("1"), B.anyhit(inc) == 1)
+    hit = (np.arange(inc.shape[1]) % 4) != 1
+    got = acc.Intersect(inc.copy(), hit=hit.copy(), bounce=1)
+    assert (got[0][~hit] == -1).all()
+    np.testing.assert_array_equal(got[0][hit], B.nearest(inc)[0][hit])
+    occ = acc.IntersectP(inc, hit=hit.copy())
+    np.testing.assert_array_equal(occ[hit] == ord("1"), B.anyhit(inc)[hit] == 1)
+    assert (occ[~hit] == ord("0")).all()
+    cam = S.pinhole_rays(128, 128, (0.0, 9.0, -14.0), (0.0, 0.0, 0.0), 50.0, spp=1, jitter_seed=5)
+    acc.Preprocess(None, 1, 1, 1, xres=128, yres=128)
+    assert_same(acc.Intersect(cam.copy()), B.nearest(cam), "camera, image order")
 
 
 @pytest.mark.parametrize("width,height", [(128, 64), (96, 80)])
