@@ -505,19 +505,21 @@ def run_gpu_path(args, rank, world, dev):
     sc, r2c, c2w = path_setup()
     tris = sc["tris"]
     t0 = time.perf_counter()
-    acc = A.MakeAccelerator("ray-bvh", tris, {"device": dev, "raySort": int(args.ray_sort), "walk": args.walk})
+    acc = A.MakeAccelerator("ray-bvh", tris, {"device": dev, "raySort": int(args.ray_sort), "walk": args.walk,
+                                              "bvhBuild": args.bvh_build})
     build_s = time.perf_counter() - t0
     cam = R.camera_struct(r2c, c2w, PATH_RES, PATH_RES)
     light = R.quad_light(PATH_LIGHT, PATH_LIGHT_L, 1)
     prm = R.render_params("path", spp=PATH_SPP, jitter=True, max_depth=PATH_DEPTH, seed=17)
     tuned = None
     if not args.no_tune:
-        # the walk per batch class: camera rays (coherent) and rays with
-        # uniform origins and directions in the scene's box (incoherent,
-        # like the bounces), nearest hit and any hit
+        # the walk per batch class: camera rays as the frame traces them
+        # (8 jittered samples per pixel, consecutive) for the coherent class,
+        # and rays with uniform origins and directions in the scene's box for
+        # the incoherent one (like the bounces), nearest hit and any hit
         from pbrt_gb300 import scenes as S
         co4, cd4 = to_dev(S.pinhole_rays(PATH_RES, PATH_RES, PATH_CAMERA["eye"], PATH_CAMERA["look"],
-                                        PATH_CAMERA["fov"], spp=1))
+                                        PATH_CAMERA["fov"], spp=PATH_SPP[0] * PATH_SPP[1], jitter_seed=5))
         io4, id4 = to_dev(S.random_rays(1 << 20, -20.0, 20.0, seed=77))
         tuned = {"coherent nearest": acc.autotune(co4, cd4), "coherent any-hit": acc.autotune(co4, cd4, anyhit=True),
                  "incoherent nearest": acc.autotune(io4, id4, incoherent=True),
@@ -652,7 +654,8 @@ def run_gpu_path(args, rank, world, dev):
                    "ordering": "learned" if args.learned == 1 else "plain",
                    "rays_per_step": int(rays), "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays),
                    "triangles": int(len(tris)), "bvh_build_s": round(build_s, 2),
-                   "ray_sort": bool(args.ray_sort), "walk": args.walk, "parallelism": f"replicas x{world}",
+                   "ray_sort": bool(args.ray_sort), "walk": args.walk,
+                   "bvh_build": "host" if args.bvh_build == 1 else "device", "parallelism": f"replicas x{world}",
                    "l2": "inputs > L2 (8.4M paths x 32 B rays per bounce)",
                    "autotune": {k: v["best"] for k, v in tuned.items()} if tuned else None},
         "autotune": tuned,
@@ -1263,6 +1266,8 @@ def main():
     ap.add_argument("--workload", default="path", choices=["path", "frame", "batch", "naive"])
     ap.add_argument("--path-res", type=int, default=PATH_RES,
                     help="path workload: image width and height (profiler captures use a smaller frame)")
+    ap.add_argument("--bvh-build", type=int, default=0,
+                    help="path workload: 0 build the BVH on the device, 1 on the host cores")
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--rh-cluster-levels", type=int, default=0,
                     help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")

@@ -427,7 +427,6 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     const TriRec* tris = (const TriRec*)s->tris.ptr;
     int* status = (int*)s->err.ptr;
     unsigned long long* wc = (unsigned long long*)s->workc.ptr;
-    prof_begin(s, st);
     // bounce batches are incoherent: the reference's bounce form of Intersect
     // is the one with a validity mask (rayhierarchy.cpp:602-813)
     const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
@@ -437,10 +436,14 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // ordering it gives way to the persistent walk
     const bool packet = walk == 3 && !pred;
     const bool persistent = walk == 2 || (walk == 3 && pred);
-    if (packet) {
-        const int32_t* order = perm;  // the ray hierarchy's leaf order
-        int rc3 = order ? PBG_OK : ray_order(s, o, d, n, &order, st);
+    const int32_t* order = perm;  // packet walk: the ray hierarchy's leaf order (timed as the sort stage)
+    if (packet && !order) {
+        int rc3 = ray_order(s, o, d, n, &order, st);
         if (rc3) return rc3;
+    }
+    prof_begin(s, st);
+    if (packet) {
+        int rc3 = PBG_OK;
         Work& w = s->work;
         if ((rc3 = ensure(w.counters, 64))) return rc3;
         unsigned long long* next = (unsigned long long*)w.counters.ptr;
