@@ -194,11 +194,56 @@ __global__ void __launch_bounds__(kPacketThreads)
 constexpr int kPersistThreads = 128;
 constexpr int kPersistMinBlocks = 10;  // CTAs per SM: measured best of 6, 8, 9, 10, 12, 16
 
+// The walk's stack.  PACK: one 8-byte entry (one local load per pop) when
+// the scene allows it: a child reference, with a leaf's record start (below
+// 2^24) and triangle count (below 128) packed into one negative word, and
+// the entry distance.  Otherwise reference, count and distance in three
+// arrays.
+template <bool PACK>
+struct WalkStack;
+
+template <>
+struct WalkStack<true> {
+    int2 e[kStackDepth];
+    __device__ __forceinline__ void put(int i, int32_t ref, int32_t cnt, float t) {
+        const int32_t v = ref >= 0 ? ref : (int32_t)(0x80000000u | ((uint32_t)cnt << 24) | (uint32_t)(~ref));
+        e[i] = make_int2(v, __float_as_int(t));
+    }
+    // entry i: its distance, and (reference, count) when it is taken
+    __device__ __forceinline__ float get(int i, int32_t* ref, int32_t* cnt) const {
+        const int2 v = e[i];
+        if (v.x >= 0) {
+            *ref = v.x;
+            *cnt = 0;
+        } else {
+            *ref = ~(int32_t)((uint32_t)v.x & 0xffffffu);
+            *cnt = (int32_t)(((uint32_t)v.x >> 24) & 0x7fu);
+        }
+        return __int_as_float(v.y);
+    }
+};
+
+template <>
+struct WalkStack<false> {
+    int32_t r[kStackDepth], c[kStackDepth];
+    float tt[kStackDepth];
+    __device__ __forceinline__ void put(int i, int32_t ref, int32_t cnt, float t) {
+        r[i] = ref;
+        c[i] = cnt;
+        tt[i] = t;
+    }
+    __device__ __forceinline__ float get(int i, int32_t* ref, int32_t* cnt) const {
+        *ref = r[i];
+        *cnt = c[i];
+        return tt[i];
+    }
+};
+
 // ORDERED: the learned ordering's predicted cluster (pred, cref as in
 // bvh_kernel) is walked first, then the whole tree skipping it.  STATS: the
 // counting variant (profiling level 2) tallies node tests, leaves and
 // triangle tests into wcount.
-template <bool ANY, bool ORDERED, bool STATS>
+template <bool ANY, bool ORDERED, bool STATS, bool PACK>
 __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
     bvh_persistent_kernel(const BvhNode* __restrict__ nodes, const TriRec* __restrict__ tris,
                           int32_t unculled, const float4* __restrict__ ro, const float4* __restrict__ rd,
@@ -211,9 +256,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    int32_t stack_ref[kStackDepth];
-    int32_t stack_cnt[kStackDepth];
-    float stack_t[kStackDepth];
+    WalkStack<PACK> stk;
     int sp = 0;
     int64_t ray = 0;
     bool has = false, exhausted = false, ok = true;
@@ -255,12 +298,14 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
     auto pop = [&]() -> bool {
         while (sp > 0) {
             --sp;
-            if (stack_t[sp] <= h.t) {
-                if (stack_cnt[sp] == 0) {
-                    node = stack_ref[sp];
+            int32_t ref, cnt;
+            const float te = stk.get(sp, &ref, &cnt);
+            if (te <= h.t) {
+                if (cnt == 0) {
+                    node = ref;
                 } else {
                     node = -1;
-                    take_leaf(~stack_ref[sp], stack_cnt[sp], stack_t[sp]);
+                    take_leaf(~ref, cnt, te);
                 }
                 return true;
             }
@@ -305,16 +350,12 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
                             if (c < kClusters) {
                                 // the root after the predicted cluster
                                 skip = cref[2 * c];
-                                stack_ref[0] = 0;
-                                stack_cnt[0] = 0;
-                                stack_t[0] = -INFINITY;
+                                stk.put(0, 0, 0, -INFINITY);
                                 sp = 1;
                                 if (skip >= 0) {
                                     node = skip;
                                 } else {
-                                    stack_ref[1] = skip;
-                                    stack_cnt[1] = cref[2 * c + 1];
-                                    stack_t[1] = -INFINITY;
+                                    stk.put(1, skip, cref[2 * c + 1], -INFINITY);
                                     sp = 2;
                                     node = -1;
                                 }
@@ -355,9 +396,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
                 if (h0 && h1) {
                     const int32_t cf = near0 ? nn.n3.y : nn.n3.x, kf = near0 ? nn.n3.w : nn.n3.z;
                     if (sp < kStackDepth) {
-                        stack_ref[sp] = cf;
-                        stack_cnt[sp] = cf >= 0 ? 0 : kf;
-                        stack_t[sp] = near0 ? tn1 : tn0;
+                        stk.put(sp, cf, cf >= 0 ? 0 : kf, near0 ? tn1 : tn0);
                         ++sp;
                     } else {
                         ok = false;
@@ -466,15 +505,23 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
         unsigned long long* next = (unsigned long long*)w.counters.ptr;
         PBG_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_persistent_kernel<ANY, false, false>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh_persistent_kernel<ANY, false, false, true>,
                                                       kPersistThreads, 0);
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
         int64_t blocks = (int64_t)std::max(per_sm, 1) * sms;
         blocks = std::min<int64_t>(blocks, (n + kPersistThreads - 1) / kPersistThreads);
         const bool stats = s->prof.level >= 2;
-        auto kern = pred ? (stats ? bvh_persistent_kernel<ANY, true, true> : bvh_persistent_kernel<ANY, true, false>)
-                         : (stats ? bvh_persistent_kernel<ANY, false, true> : bvh_persistent_kernel<ANY, false, false>);
+        // packed stack entries: record starts below 2^24, leaves below 128 triangles
+        const bool pack = s->ntri < (1 << 24) && (s->params.max_bvh_prim > 0 ? s->params.max_bvh_prim : 4) < 128;
+        auto kern = pack ? (pred ? (stats ? bvh_persistent_kernel<ANY, true, true, true>
+                                          : bvh_persistent_kernel<ANY, true, false, true>)
+                                 : (stats ? bvh_persistent_kernel<ANY, false, true, true>
+                                          : bvh_persistent_kernel<ANY, false, false, true>))
+                         : (pred ? (stats ? bvh_persistent_kernel<ANY, true, true, false>
+                                          : bvh_persistent_kernel<ANY, true, false, false>)
+                                 : (stats ? bvh_persistent_kernel<ANY, false, true, false>
+                                          : bvh_persistent_kernel<ANY, false, false, false>));
         kern<<<(unsigned)blocks, kPersistThreads, 0, st>>>(nodes, tris, s->unculled, o, d, valid, perm, n,
                                                            prim, t, b1, b2, occ, status, next, pred, cref,
                                                            stats ? wc : nullptr);
