@@ -730,16 +730,35 @@ __global__ void film_kernel(int64_t npix, int spp, const int32_t* __restrict__ o
 
 int scan_counts(pbg_scene* s, uint32_t* a, int64_t m, cudaStream_t st);
 
-struct RenderBuffers {
-    DeviceBuffer o4, d4, qidx, L, beta, prim, t, b1, b2, so, sd, scontrib, sflag, spos, sqo, sqd, occ,
-        no, nd, nflag, qidx2, o42, d42, counts, rgb, emit, rstat, ltab, simg, sdims, srng, hflag, hrank,
-        foff, fidx;
-    ~RenderBuffers() {
-        DeviceBuffer* all[] = {&o4,  &d4,  &qidx,  &L,   &beta,  &prim,  &t,     &b1,  &b2,    &so,   &sd,
-                               &scontrib, &sflag, &spos, &sqo, &sqd, &occ, &no, &nd, &nflag, &qidx2, &o42,
-                               &d42, &counts, &rgb, &emit, &rstat, &ltab, &simg, &sdims, &srng, &hflag, &hrank,
-                               &foff, &fidx};
+// One bounce's shadow queue: its slots (shade), the compacted rays, their
+// occlusion and the bounce's emission (resolve).  Path frames on ray-bvh
+// and naive scenes keep two, so that a bounce's shadow traversal and resolve
+// run on a second stream beside the next bounce's nearest-hit traversal.
+struct ShadowSet {
+    DeviceBuffer so, sd, scontrib, sflag, spos, sqo, sqd, occ, emit;
+    void release_all() {
+        DeviceBuffer* all[] = {&so, &sd, &scontrib, &sflag, &spos, &sqo, &sqd, &occ, &emit};
         for (DeviceBuffer* b : all) release(*b);
+    }
+};
+
+struct RenderBuffers {
+    DeviceBuffer o4, d4, qidx, L, beta, prim, t, b1, b2, no, nd, nflag, qidx2, o42, d42, counts, rgb, rstat,
+        ltab, simg, sdims, srng, hflag, hrank, foff, fidx;
+    ShadowSet sh[2];
+    cudaStream_t side = nullptr;           // the shadow stream of overlapped frames
+    cudaEvent_t ready[2] = {}, resolved[2] = {};
+    ~RenderBuffers() {
+        DeviceBuffer* all[] = {&o4,    &d4,     &qidx,  &L,     &beta, &prim,  &t,     &b1,   &b2,
+                               &no,    &nd,     &nflag, &qidx2, &o42,  &d42,   &counts, &rgb, &rstat,
+                               &ltab,  &simg,   &sdims, &srng,  &hflag, &hrank, &foff,  &fidx};
+        for (DeviceBuffer* b : all) release(*b);
+        for (ShadowSet& x : sh) x.release_all();
+        for (int k = 0; k < 2; ++k) {
+            if (ready[k]) cudaEventDestroy(ready[k]);
+            if (resolved[k]) cudaEventDestroy(resolved[k]);
+        }
+        if (side) cudaStreamDestroy(side);
     }
 };
 
@@ -860,17 +879,36 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     RenderBuffers& B = *s->render_bufs;  // grown on demand, kept for the next frame
     int r;
     const size_t nk = (size_t)n * kslots;
+    // Overlapped bounces (path frames on ray-bvh and naive scenes, learned
+    // ordering off): each bounce's shadow traversal and resolve go to a
+    // second stream, beside the next bounce's nearest-hit traversal and
+    // shading.  rayhierarchy batches share the scene's status words and the
+    // learned ordering one prediction buffer, so those frames stay serial.
+    const bool overlap = prm->integrator == PBG_INTEGRATOR_PATH &&
+                         (s->accel == PBG_ACCEL_RAYBVH || s->accel == PBG_ACCEL_NAIVE) &&
+                         !(s->learn && s->learn->enabled);
     if ((r = ensure(B.o4, n * 16)) || (r = ensure(B.d4, n * 16)) || (r = ensure(B.qidx, n * 4)) ||
         (r = ensure(B.L, n * 12)) || (r = ensure(B.beta, n * 12)) || (r = ensure(B.prim, n * 4)) ||
         (r = ensure(B.t, n * 4)) || (r = ensure(B.b1, n * 4)) || (r = ensure(B.b2, n * 4)) ||
-        (r = ensure(B.so, nk * 16)) || (r = ensure(B.sd, nk * 16)) || (r = ensure(B.scontrib, nk * 12)) ||
-        (r = ensure(B.sflag, nk)) || (r = ensure(B.spos, nk * 4)) || (r = ensure(B.sqo, nk * 16)) ||
-        (r = ensure(B.sqd, nk * 16)) || (r = ensure(B.occ, nk)) || (r = ensure(B.no, n * 16)) ||
-        (r = ensure(B.nd, n * 16)) || (r = ensure(B.nflag, n)) || (r = ensure(B.qidx2, n * 4)) ||
-        (r = ensure(B.o42, n * 16)) || (r = ensure(B.d42, n * 16)) || (r = ensure(B.emit, n * 12)) ||
+        (r = ensure(B.no, n * 16)) || (r = ensure(B.nd, n * 16)) || (r = ensure(B.nflag, n)) ||
+        (r = ensure(B.qidx2, n * 4)) || (r = ensure(B.o42, n * 16)) || (r = ensure(B.d42, n * 16)) ||
         (r = ensure(B.counts, ((nk + 255) / 256 + 64) * 4 + 4096)) || (r = ensure(B.rgb, npix * 12)) ||
         (r = ensure(B.rstat, 16)) || (r = ensure(B.ltab, (size_t)std::max(ltab_floats, 1) * 4)))
         return r;
+    for (int k = 0; k < (overlap ? 2 : 1); ++k) {
+        ShadowSet& X = B.sh[k];
+        if ((r = ensure(X.so, nk * 16)) || (r = ensure(X.sd, nk * 16)) || (r = ensure(X.scontrib, nk * 12)) ||
+            (r = ensure(X.sflag, nk)) || (r = ensure(X.spos, nk * 4)) || (r = ensure(X.sqo, nk * 16)) ||
+            (r = ensure(X.sqd, nk * 16)) || (r = ensure(X.occ, nk)) || (r = ensure(X.emit, n * 12)))
+            return r;
+    }
+    if (overlap && !B.side) {
+        PBG_CUDA(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            PBG_CUDA(cudaEventCreateWithFlags(&B.ready[k], cudaEventDisableTiming));
+            PBG_CUDA(cudaEventCreateWithFlags(&B.resolved[k], cudaEventDisableTiming));
+        }
+    }
     PBG_CUDA(cudaMemsetAsync(B.rstat.ptr, 0, 16, st));
     rc.ltab = (const float*)B.ltab.ptr;
     for (int l = 0; l < nlights; ++l)
@@ -947,8 +985,12 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
         pbg_scene* s;
         ~HintGuard() { s->walk_hint = -1; }
     } hint_guard{s};
+    cudaStream_t side = overlap ? B.side : st;
+    bool pending[2] = {false, false};  // a resolve on the side stream still reads set k
     for (int bounce = 0; nq > 0; ++bounce) {
         s->walk_hint = bounce > 0 ? 1 : 0;
+        const int k = overlap ? (bounce & 1) : 0;
+        ShadowSet& X = B.sh[k];
         if ((r = pbg_intersect_device(s, (const float*)qo, (const float*)qd, nullptr, nq,
                                       (int32_t*)B.prim.ptr, (float*)B.t.ptr, (float*)B.b1.ptr,
                                       (float*)B.b2.ptr, st)))
@@ -974,38 +1016,59 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
             sa.hit_rank = (const int32_t*)B.hrank.ptr;
         }
         const int64_t nslots = nq * kslots;
+        // set k was last read by the resolve of two bounces ago
+        if (pending[k]) PBG_CUDA(cudaStreamWaitEvent(st, B.resolved[k], 0));
+        pending[k] = false;
         shade_kernel<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>(
             rc, sa, bounce, nq, qi, qo, qd, (const int32_t*)B.prim.ptr, (const float*)B.t.ptr,
             (const float*)B.b1.ptr, (const float*)B.b2.ptr, (const float*)s->tri9.ptr,
-            (const float*)s->uv6.ptr, (float*)B.beta.ptr, kslots, (float4*)B.so.ptr, (float4*)B.sd.ptr,
-            (float*)B.scontrib.ptr, (uint8_t*)B.sflag.ptr, (float4*)B.no.ptr, (float4*)B.nd.ptr,
-            (uint8_t*)B.nflag.ptr, (float*)B.emit.ptr, (int*)B.rstat.ptr);
+            (const float*)s->uv6.ptr, (float*)B.beta.ptr, kslots, (float4*)X.so.ptr, (float4*)X.sd.ptr,
+            (float*)X.scontrib.ptr, (uint8_t*)X.sflag.ptr, (float4*)B.no.ptr, (float4*)B.nd.ptr,
+            (uint8_t*)B.nflag.ptr, (float*)X.emit.ptr, (int*)B.rstat.ptr);
         PBG_CUDA(cudaGetLastError());
         s->counters.kernel_launches += 1;
         if (draws) rng_base += 7 * n + nhits * (bounce > 3 ? 4 : 3);
         // shadow queue
         int64_t nsh = 0;
-        if ((r = compact_count(s, (const uint8_t*)B.sflag.ptr, nslots, (uint32_t*)B.counts.ptr, &nsh, st)))
+        if ((r = compact_count(s, (const uint8_t*)X.sflag.ptr, nslots, (uint32_t*)B.counts.ptr, &nsh, st)))
             return r;
         compact_shadow_kernel<<<(unsigned)((nslots + 255) / 256), 256, 0, st>>>(
-            (const uint8_t*)B.sflag.ptr, nslots, (const uint32_t*)B.counts.ptr, (const float4*)B.so.ptr,
-            (const float4*)B.sd.ptr, (float4*)B.sqo.ptr, (float4*)B.sqd.ptr, (int32_t*)B.spos.ptr);
+            (const uint8_t*)X.sflag.ptr, nslots, (const uint32_t*)B.counts.ptr, (const float4*)X.so.ptr,
+            (const float4*)X.sd.ptr, (float4*)X.sqo.ptr, (float4*)X.sqd.ptr, (int32_t*)X.spos.ptr);
         PBG_CUDA(cudaGetLastError());
         s->counters.kernel_launches += 1;
-        if (nsh > 0 && (r = pbg_occluded_device(s, (const float*)B.sqo.ptr, (const float*)B.sqd.ptr,
-                                                nullptr, nsh, (uint8_t*)B.occ.ptr, st)))
-            return r;
+        if (overlap) {  // the shadow rays and this bounce's resolve on the side stream
+            PBG_CUDA(cudaEventRecord(B.ready[k], st));
+            PBG_CUDA(cudaStreamWaitEvent(side, B.ready[k], 0));
+        }
+        if (nsh > 0) {
+            if (overlap) std::swap(s->work, s->alt);  // its own walk counter, beside the nearest-hit walk
+            r = pbg_occluded_device(s, (const float*)X.sqo.ptr, (const float*)X.sqd.ptr, nullptr, nsh,
+                                    (uint8_t*)X.occ.ptr, side);
+            if (overlap) std::swap(s->work, s->alt);
+            if (r) return r;
+        }
         stt.shadow_rays += (uint64_t)nsh;
-        resolve_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(
-            rc, nq, kslots, qi, (const uint8_t*)B.sflag.ptr, (const int32_t*)B.spos.ptr,
-            (const uint8_t*)B.occ.ptr, (const float*)B.scontrib.ptr, (const float*)B.emit.ptr, (float*)B.L.ptr);
+        resolve_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, side>>>(
+            rc, nq, kslots, qi, (const uint8_t*)X.sflag.ptr, (const int32_t*)X.spos.ptr,
+            (const uint8_t*)X.occ.ptr, (const float*)X.scontrib.ptr, (const float*)X.emit.ptr, (float*)B.L.ptr);
         PBG_CUDA(cudaGetLastError());
         s->counters.kernel_launches += 1;
+        if (overlap) {
+            PBG_CUDA(cudaEventRecord(B.resolved[k], side));
+            pending[k] = true;
+        }
         if (rc.integrator != PBG_INTEGRATOR_PATH) break;
         // bounce queue
         int64_t nn = 0;
         if ((r = compact_count(s, (const uint8_t*)B.nflag.ptr, nq, (uint32_t*)B.counts.ptr, &nn, st)))
             return r;
+        // the resolve above reads this bounce's queue indices, which the
+        // compaction after the next bounce overwrites: it waits there (below)
+        if (overlap && pending[k ^ 1]) {
+            PBG_CUDA(cudaStreamWaitEvent(st, B.resolved[k ^ 1], 0));
+            pending[k ^ 1] = false;
+        }
         compact_bounce_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(
             (const uint8_t*)B.nflag.ptr, nq, (const uint32_t*)B.counts.ptr, qi, (const float4*)B.no.ptr,
             (const float4*)B.nd.ptr, qi2, qo2, qd2);
@@ -1017,6 +1080,8 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
         nq = nn;
         stt.bounces = (uint64_t)bounce + 1;
     }
+    for (int k = 0; k < 2; ++k)  // the last resolves add to L before the film reads it
+        if (pending[k]) PBG_CUDA(cudaStreamWaitEvent(st, B.resolved[k], 0));
     // online training of the learned ordering on this frame's records
     if (s->learn && s->learn->enabled && (r = learn_train(s, 0, st))) return r;
     film_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(npix, rc.spp, film_off, film_idx,
