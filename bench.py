@@ -468,7 +468,10 @@ def ordering_study(acc, reps=5):
         learned = timed(lambda: acc.occluded_device(so, sd, occ, valid=valid, stream=stream), hit.sum())
         occ_l = occ.clone()
         acc.learn_enable(False)
-    plain = timed(lambda: acc.occluded_hinted_device(so, sd, None, occ, occluder, valid=valid, stream=stream),
+    # the plain legs pass "no cluster" for every ray, so that plain and
+    # hinted walks run the same kernel
+    none = torch.full((n,), -1, dtype=torch.int16, device="cuda")
+    plain = timed(lambda: acc.occluded_hinted_device(so, sd, none, occ, occluder, valid=valid, stream=stream),
                   hit.sum())
     occ_p = occ.clone()
     acc.clusters_of_device(occluder, hint, stream=stream)
@@ -483,13 +486,63 @@ def ordering_study(acc, reps=5):
     # nearest hit: the camera rays themselves, hinted with their own first hit
     nhint = torch.empty(n, dtype=torch.int16, device="cuda")
     p2, t2, c1, c2 = (torch.empty_like(x) for x in (prim, tt, b1, b2))
-    nplain = timed(lambda: acc.intersect_hinted_device(o4, d4, None, p2, t2, c1, c2, stream=stream), n)
+    nplain = timed(lambda: acc.intersect_hinted_device(o4, d4, none, p2, t2, c1, c2, stream=stream), n)
     acc.clusters_of_device(prim, nhint, stream=stream)
     nperfect = timed(lambda: acc.intersect_hinted_device(o4, d4, nhint, p2, t2, c1, c2, stream=stream), n)
     out["nearest"] = {"camera_rays": n, "plain": nplain, "perfect_hints": nperfect,
                       "perfect_over_plain_time": round(nplain["ms"] / nperfect["ms"], 3),
                       "results_identical": bool(torch.equal(p2, prim) and torch.equal(t2, tt))}
     return out
+
+
+def path_tuning(acc, tris):
+    """pbg_autotune on batches shaped like the path frame's own, one per
+    batch class: the camera rays (8 jittered samples per pixel, consecutive)
+    and the shadow rays from their hits to the light (coherent), and bounce
+    rays (cosine-weighted directions from 2 M of the camera hits) with the
+    shadow rays from their hits (incoherent).  Queues are compacted as the
+    renderer compacts them (no validity masks)."""
+    import torch
+    from pbrt_gb300 import scenes as S
+
+    def nearest(o4, d4):
+        n = o4.shape[0]
+        prim = torch.empty(n, dtype=torch.int32, device="cuda")
+        t, b1, b2 = (torch.empty(n, device="cuda") for _ in range(3))
+        acc.intersect_device(o4, d4, prim, t, b1, b2)
+        torch.cuda.synchronize()
+        return prim.cpu().numpy(), t.cpu().numpy()
+
+    def shadow_queue(rays, prim, t, seed):
+        sh, hit = shadow_batches(rays, prim, t, PATH_LIGHT, nsamples=1, seed=seed)
+        return to_dev(np.ascontiguousarray(sh[0][:, hit == 1]))
+
+    cam = S.pinhole_rays(PATH_RES, PATH_RES, PATH_CAMERA["eye"], PATH_CAMERA["look"], PATH_CAMERA["fov"],
+                         spp=PATH_SPP[0] * PATH_SPP[1], jitter_seed=5)
+    co4, cd4 = to_dev(cam)
+    hp, ht = nearest(co4, cd4)
+    so4, sd4 = shadow_queue(cam, hp, ht, 29)
+    tuned = {"coherent nearest": acc.autotune(co4, cd4), "coherent any-hit": acc.autotune(so4, sd4, anyhit=True)}
+    del co4, cd4, so4, sd4
+    g = np.random.default_rng(31)
+    idx = np.flatnonzero(hp >= 0)
+    idx = idx[:: max(1, len(idx) // (1 << 21))][: 1 << 21]
+    v = tris[hp[idx]].reshape(-1, 3, 3).astype(np.float64)
+    nrm = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
+    nrm *= np.where((nrm * cam[3:6, idx].T).sum(1, keepdims=True) > 0, -1.0, 1.0)
+    b = np.empty((8, len(idx)), np.float32)
+    b[0:3] = cam[0:3, idx] + cam[3:6, idx] * ht[idx][None]
+    b[3:6] = S._cosine_dirs(nrm, g).T
+    b[6] = 1e-3 * ht[idx]
+    b[7] = np.inf
+    bo4, bd4 = to_dev(b)
+    bp, bt = nearest(bo4, bd4)
+    bso4, bsd4 = shadow_queue(b, bp, bt, 37)
+    tuned["incoherent nearest"] = acc.autotune(bo4, bd4, incoherent=True)
+    tuned["incoherent any-hit"] = acc.autotune(bso4, bsd4, anyhit=True, incoherent=True)
+    torch.cuda.synchronize()
+    return tuned
 
 
 def run_gpu_path(args, rank, world, dev):
@@ -511,21 +564,7 @@ def run_gpu_path(args, rank, world, dev):
     cam = R.camera_struct(r2c, c2w, PATH_RES, PATH_RES)
     light = R.quad_light(PATH_LIGHT, PATH_LIGHT_L, 1)
     prm = R.render_params("path", spp=PATH_SPP, jitter=True, max_depth=PATH_DEPTH, seed=17)
-    tuned = None
-    if not args.no_tune:
-        # the walk per batch class: camera rays as the frame traces them
-        # (8 jittered samples per pixel, consecutive) for the coherent class,
-        # and rays with uniform origins and directions in the scene's box for
-        # the incoherent one (like the bounces), nearest hit and any hit
-        from pbrt_gb300 import scenes as S
-        co4, cd4 = to_dev(S.pinhole_rays(PATH_RES, PATH_RES, PATH_CAMERA["eye"], PATH_CAMERA["look"],
-                                        PATH_CAMERA["fov"], spp=PATH_SPP[0] * PATH_SPP[1], jitter_seed=5))
-        io4, id4 = to_dev(S.random_rays(1 << 20, -20.0, 20.0, seed=77))
-        tuned = {"coherent nearest": acc.autotune(co4, cd4), "coherent any-hit": acc.autotune(co4, cd4, anyhit=True),
-                 "incoherent nearest": acc.autotune(io4, id4, incoherent=True),
-                 "incoherent any-hit": acc.autotune(io4, id4, anyhit=True, incoherent=True)}
-        del co4, cd4, io4, id4
-        torch.cuda.synchronize()
+    tuned = path_tuning(acc, tris) if not args.no_tune else None
 
     def measure():
         for k in range(args.warmup):
@@ -654,6 +693,7 @@ def run_gpu_path(args, rank, world, dev):
                    "ordering": "learned" if args.learned == 1 else "plain",
                    "rays_per_step": int(rays), "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays),
                    "triangles": int(len(tris)), "bvh_build_s": round(build_s, 2),
+                   "bvh_nodes": int(acc.stats()["bvh_nodes"]),
                    "ray_sort": bool(args.ray_sort), "walk": args.walk,
                    "bvh_build": "host" if args.bvh_build == 1 else "device", "parallelism": f"replicas x{world}",
                    "l2": "inputs > L2 (8.4M paths x 32 B rays per bounce)",

@@ -1267,6 +1267,14 @@ int pbg_occluded_hinted_device(pbg_scene* s, const float* o4, const float* d4, c
     return rc;
 }
 
+// Marks a host-buffer call for its duration (ray-bvh runs its packet walk
+// in the caller's order there, see bvh_launch).
+struct HostCall {
+    pbg_scene* s;
+    explicit HostCall(pbg_scene* sc) : s(sc) { s->host_call = true; }
+    ~HostCall() { s->host_call = false; }
+};
+
 int pbg_intersect(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_hits* out) {
     if (!s || n < 0 || (n > 0 && (!rays_ok(r) || !out || !out->prim || !out->t || !out->b1 ||
                                   !out->b2))) {
@@ -1275,6 +1283,7 @@ int pbg_intersect(pbg_scene* s, const pbg_rays* r, int64_t n, pbg_hits* out) {
     }
     if (n == 0) return PBG_OK;
     cudaSetDevice(s->device);
+    HostCall host_call(s);
     bool done = false;
     int rc = intersect_two_halves(s, r, n, out, &done);
     if (rc) return rc;
@@ -1323,6 +1332,7 @@ int pbg_occluded(pbg_scene* s, const pbg_rays* r, int64_t n, uint8_t* occ) {
     }
     if (n == 0) return PBG_OK;
     cudaSetDevice(s->device);
+    HostCall host_call(s);
     bool done = false;
     int rc = occluded_in_parts(s, r, n, occ, &done);
     if (rc) return rc;

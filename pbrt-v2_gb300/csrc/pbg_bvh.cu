@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(kBvhThreads, kBvhMinBlocks)
 
 // Co-traversal of the ray hierarchy with the BVH (walk = 3): the batch is
 // put in the ray hierarchy's leaf order (6-D Morton keys of origin and
-// direction, or the declared ray image's Morton order), and each warp takes
+// direction, or the declared ray image's Morton order; walk = 4 keeps the
+// caller's order, already coherent for image-ordered batches), and each warp takes
 // one leaf of 32 rays and walks the BVH with them as one packet: a node is
 // visited when any of the warp's rays hits it, every lane tests its own ray
 // against both children's boxes, leaves are tested by the lanes whose rays
@@ -470,13 +471,22 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // is the one with a validity mask (rayhierarchy.cpp:602-813)
     const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
     const int tuned = s->tune.bvh_walk[ANY ? 1 : 0][hint == 1 ? 1 : 0];
-    const int walk = s->params.walk != 0 ? s->params.walk : (tuned != 0 ? tuned : (hint == 1 ? 2 : 1));
+    int walk = s->params.walk != 0 ? s->params.walk : (tuned != 0 ? tuned : (hint == 1 ? 2 : 1));
+    // Host-buffer calls run the packets in the caller's order: there the
+    // batch arrives in parts whose copies overlap the traversal, and sorting
+    // each part cost more than its packets gained (terrain frame end to end:
+    // 1,888 Mrays/s sorted, 2,639 in the caller's order).
+    if (walk == 3 && s->host_call && s->params.walk == 0) walk = 4;
     // the packet walk has no ordered form: with cluster hints or the learned
     // ordering it gives way to the persistent walk
-    const bool packet = walk == 3 && !pred;
-    const bool persistent = walk == 2 || (walk == 3 && pred);
-    const int32_t* order = perm;  // packet walk: the ray hierarchy's leaf order (timed as the sort stage)
-    if (packet && !order) {
+    // walk 3: packets over the ray hierarchy's leaves (the batch sorted into
+    // its leaf order); walk 4: packets over the batch in the caller's order
+    // (camera rays in image order and the shadow rays that follow them are
+    // already coherent)
+    const bool packet = (walk == 3 || walk == 4) && !pred;
+    const bool persistent = walk == 2 || ((walk == 3 || walk == 4) && pred);
+    const int32_t* order = perm;  // packet walk 3: the ray hierarchy's leaf order (timed as the sort stage)
+    if (packet && walk == 3 && !order) {
         int rc3 = ray_order(s, o, d, n, &order, st);
         if (rc3) return rc3;
     }

@@ -121,6 +121,7 @@ struct pbg_scene {
     int rh_groups = 1;         // triangle groups per rayhierarchy traversal (grows on overflow)
     int walk_hint = -1;        // ray-bvh: 1 = incoherent batch, 0 = coherent, -1 = infer
     pbg::Tunables tune;        // launch shapes (pbg_autotune)
+    bool host_call = false;    // inside pbg_intersect / pbg_occluded (host buffers)
     std::vector<pbg::BvhNode> host_nodes;  // ray-bvh tree, kept for the learned clusters
     std::vector<int32_t> host_order;
     struct pbg::Learner* learn = nullptr;

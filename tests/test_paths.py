@@ -46,7 +46,7 @@ def test_rayhierarchy_cluster_levels(gpu_lib, terrain, levels):
     np.testing.assert_array_equal(occ == ord("1"), terrain["occ_inc"] == 1)
 
 
-@pytest.mark.parametrize("walk", [1, 2, 3])
+@pytest.mark.parametrize("walk", [1, 2, 3, 4])
 def test_raybvh_walks(gpu_lib, terrain, walk):
     acc = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": walk})
     assert_same(acc.Intersect(terrain["cam"].copy()), terrain["want_cam"], f"cam, walk {walk}")
@@ -60,12 +60,14 @@ def test_raybvh_walks(gpu_lib, terrain, walk):
     np.testing.assert_array_equal(got[0][hit], terrain["want_inc"][0][hit])
 
 
+@pytest.mark.parametrize("walk", [3, 4])
 @pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_packet_walk_golden(gpu_lib, case):
-    """walk 3 (warp packets over the ray hierarchy's leaves) on the
-    reference's own answers: ties, degenerate triangles, limits, empty."""
+def test_packet_walk_golden(gpu_lib, case, walk):
+    """walks 3 and 4 (warp packets over the ray hierarchy's leaves, or over
+    the batch in its own order) on the reference's own answers: ties,
+    degenerate triangles, limits, empty."""
     g = load_golden(case)
-    acc = A.MakeAccelerator("ray-bvh", g["tris"], {"walk": 3})
+    acc = A.MakeAccelerator("ray-bvh", g["tris"], {"walk": walk})
     got = acc.Intersect(g["rays"].copy())
     np.testing.assert_array_equal(got[0], g["prim"])
     h = g["prim"] >= 0
