@@ -34,32 +34,44 @@ size_t tc_gemm_work_floats(int M, int N, int K);
 
 // ------------------------------------------------------------ features
 
-__device__ __forceinline__ void ray_features(float4 o, float4 d, const float* lo, const float* inv_ext,
-                                             float* f /* kFeat */) {
-    f[0] = o.x; f[1] = o.y; f[2] = o.z;
+// The features of one ray in order, passed to emit(value) one at a time
+// (fully unrolled, so a caller can pack them as they come).
+template <class Emit>
+__device__ __forceinline__ void for_each_feature(float4 o, float4 d, const float* lo, const float* inv_ext,
+                                                 Emit&& emit) {
     const float len = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
     const float il = len > 0.f ? 1.f / len : 0.f;
     const float dx = d.x * il, dy = d.y * il, dz = d.z * il;
-    f[3] = dx; f[4] = dy; f[5] = dz;
-    f[6] = fminf(fmaxf(dx != 0.f ? 1.f / dx : 16.f, -16.f), 16.f) * 0.0625f;
-    f[7] = fminf(fmaxf(dy != 0.f ? 1.f / dy : 16.f, -16.f), 16.f) * 0.0625f;
-    f[8] = fminf(fmaxf(dz != 0.f ? 1.f / dz : 16.f, -16.f), 16.f) * 0.0625f;
     const float u[3] = {(o.x - lo[0]) * inv_ext[0], (o.y - lo[1]) * inv_ext[1], (o.z - lo[2]) * inv_ext[2]};
-    // normalise raw coordinates too
-    f[0] = u[0] * 2.f - 1.f; f[1] = u[1] * 2.f - 1.f; f[2] = u[2] * 2.f - 1.f;
-    int k = 9;
-#pragma unroll 4
+    // normalised origin, direction, clamped reciprocal direction
+    emit(u[0] * 2.f - 1.f);
+    emit(u[1] * 2.f - 1.f);
+    emit(u[2] * 2.f - 1.f);
+    emit(dx);
+    emit(dy);
+    emit(dz);
+    emit(fminf(fmaxf(dx != 0.f ? 1.f / dx : 16.f, -16.f), 16.f) * 0.0625f);
+    emit(fminf(fmaxf(dy != 0.f ? 1.f / dy : 16.f, -16.f), 16.f) * 0.0625f);
+    emit(fminf(fmaxf(dz != 0.f ? 1.f / dz : 16.f, -16.f), 16.f) * 0.0625f);
+#pragma unroll
     for (int b = 0; b < 16; ++b) {
         const float w = 3.14159265358979f * exp2f(0.5f * (float)b);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            float s, c;
-            __sincosf(w * u[a], &s, &c);
-            f[k++] = s;
-            f[k++] = c;
+            float sn, cs;
+            __sincosf(w * u[a], &sn, &cs);
+            emit(sn);
+            emit(cs);
         }
     }
-    for (; k < kFeat; ++k) f[k] = 0.f;
+#pragma unroll
+    for (int k = 9 + 96; k < kFeat; ++k) emit(0.f);
+}
+
+__device__ __forceinline__ void ray_features(float4 o, float4 d, const float* lo, const float* inv_ext,
+                                             float* f /* kFeat */) {
+    int k = 0;
+    for_each_feature(o, d, lo, inv_ext, [&](float v) { f[k++] = v; });
 }
 
 // X [n_pad x 112] bf16 rows; rows >= n are zero.
@@ -234,15 +246,42 @@ __device__ __forceinline__ void stage_rows(uint8_t* dst, const uint16_t* src, in
     }
 }
 
-// One thread's row of `cols` bf16 values into a core-matrix tile.
-__device__ __forceinline__ void store_row(uint8_t* dst, int r, const float* v, int cols) {
-    for (int g = 0; g < cols; g += 8) {
-        uint4 w;
-        w.x = (uint32_t)f2bf(v[g]) | ((uint32_t)f2bf(v[g + 1]) << 16);
-        w.y = (uint32_t)f2bf(v[g + 2]) | ((uint32_t)f2bf(v[g + 3]) << 16);
-        w.z = (uint32_t)f2bf(v[g + 4]) | ((uint32_t)f2bf(v[g + 5]) << 16);
-        w.w = (uint32_t)f2bf(v[g + 6]) | ((uint32_t)f2bf(v[g + 7]) << 16);
-        *(uint4*)(dst + core_offset(r, g, cols)) = w;
+// Eight values as bf16 into a row's group of a core-matrix tile.
+__device__ __forceinline__ void store_group(uint8_t* dst, int r, int g, int cols, const float* v) {
+    uint4 w;
+    w.x = (uint32_t)f2bf(v[0]) | ((uint32_t)f2bf(v[1]) << 16);
+    w.y = (uint32_t)f2bf(v[2]) | ((uint32_t)f2bf(v[3]) << 16);
+    w.z = (uint32_t)f2bf(v[4]) | ((uint32_t)f2bf(v[5]) << 16);
+    w.w = (uint32_t)f2bf(v[6]) | ((uint32_t)f2bf(v[7]) << 16);
+    *(uint4*)(dst + core_offset(r, g, cols)) = w;
+}
+
+// A ray's features straight into its row of the X tile, eight at a time.
+__device__ __forceinline__ void store_features(uint8_t* dst, int r, float4 o, float4 d, const float* lo,
+                                               const float* inv_ext) {
+    float buf[8];
+    int n = 0, g = 0;
+    for_each_feature(o, d, lo, inv_ext, [&](float v) {
+        buf[n++] = v;
+        if (n == 8) {
+            store_group(dst, r, g, kFeat, buf);
+            g += 8;
+            n = 0;
+        }
+    });
+}
+
+// Bias + ReLU of 64 hidden values read 16 at a time from TMEM (columns
+// col..col+63 of this warp's lanes), packed into the row of a bf16 tile.
+__device__ __forceinline__ void store_hidden(uint8_t* dst, int r, uint32_t taddr, const float* bias) {
+#pragma unroll
+    for (int c = 0; c < kHidden; c += 16) {
+        float z[16];
+        tmem_ld16(taddr + (uint32_t)c, z);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) z[j] = fmaxf(z[j] + bias[c + j], 0.f);
+        store_group(dst, r, c, kHidden, z);
+        store_group(dst, r, c + 8, kHidden, z + 8);
     }
 }
 
@@ -299,12 +338,12 @@ __global__ void __launch_bounds__(kInferThreads)
     bool ok = true;
     for (int64_t tile = blockIdx.x; tile * 128 < n && ok; tile += gridDim.x) {
         const int64_t ray = tile * 128 + r;
-        float f[kFeat];
-        if (ray < n)
-            ray_features(ro[ray], rd[ray], box.lo, box.inv_ext, f);
-        else
-            for (int k = 0; k < kFeat; ++k) f[k] = 0.f;
-        store_row(sX, r, f, kFeat);
+        if (ray < n) {
+            store_features(sX, r, ro[ray], rd[ray], box.lo, box.inv_ext);
+        } else {
+            const float zero[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int g = 0; g < kFeat; g += 8) store_group(sX, r, g, kFeat, zero);
+        }
         fence_proxy_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -315,10 +354,7 @@ __global__ void __launch_bounds__(kInferThreads)
         phase ^= 1u;
         tc_fence_after();
         if (!ok) break;
-        float h[kHidden];
-        for (int c = 0; c < kHidden; c += 16) tmem_ld16(tbase + lane_addr + (uint32_t)c, h + c);
-        for (int c = 0; c < kHidden; ++c) h[c] = fmaxf(h[c] + sb1[c], 0.f);
-        store_row(sH1, r, h, kHidden);
+        store_hidden(sH1, r, tbase + lane_addr, sb1);
         fence_proxy_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -329,9 +365,7 @@ __global__ void __launch_bounds__(kInferThreads)
         phase ^= 1u;
         tc_fence_after();
         if (!ok) break;
-        for (int c = 0; c < kHidden; c += 16) tmem_ld16(tbase + lane_addr + 64u + (uint32_t)c, h + c);
-        for (int c = 0; c < kHidden; ++c) h[c] = fmaxf(h[c] + sb2[c], 0.f);
-        store_row(sH2, r, h, kHidden);
+        store_hidden(sH2, r, tbase + lane_addr + 64u, sb2);
         fence_proxy_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -446,6 +480,8 @@ void learn_free(Learner* L) {
                            &L->G2, &L->G3, &L->gb1, &L->gb2, &L->gb3, &L->acc, &L->feat, &L->pred,
                            &L->gemm_work, &L->occ_prim};
     for (DeviceBuffer* b : all) release(*b);
+    for (cudaEvent_t e : L->infer_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : L->infer_pool) cudaEventDestroy(e);
     delete L;
 }
 
@@ -592,6 +628,26 @@ static int upload_params(Learner* L, const std::vector<float>& w1, const std::ve
     return PBG_OK;
 }
 
+// Adds the inference launches' event-pair times to infer_ms and returns the
+// events to the pool: all of them (wait_all, when the statistics are read),
+// else only the pairs already complete.
+static void harvest_infer_events(Learner* L, bool wait_all) {
+    size_t k = 0;
+    for (; k + 1 < L->infer_ev.size(); k += 2) {
+        if (wait_all) {
+            if (cudaEventSynchronize(L->infer_ev[k + 1]) != cudaSuccess) break;
+        } else if (cudaEventQuery(L->infer_ev[k + 1]) != cudaSuccess) {
+            cudaGetLastError();  // cudaErrorNotReady is not an error here
+            break;
+        }
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, L->infer_ev[k], L->infer_ev[k + 1]) == cudaSuccess) L->infer_ms += ms;
+        L->infer_pool.push_back(L->infer_ev[k]);
+        L->infer_pool.push_back(L->infer_ev[k + 1]);
+    }
+    L->infer_ev.erase(L->infer_ev.begin(), L->infer_ev.begin() + (std::ptrdiff_t)k);
+}
+
 int learn_predict(pbg_scene* s, const float4* o, const float4* d, int64_t n, const uint16_t** pred,
                   const int32_t** cluster_ref, cudaStream_t st) {
     Learner* L = s->learn;
@@ -606,6 +662,17 @@ int learn_predict(pbg_scene* s, const float4* o, const float4* d, int64_t n, con
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     const int64_t tiles = (n + 127) / 128;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, 2 * (int64_t)sms);  // two CTAs per SM
+    if (L->infer_ev.size() >= 256) harvest_infer_events(L, false);  // keep the list short
+    cudaEvent_t ev[2];
+    for (cudaEvent_t& e : ev) {
+        if (!L->infer_pool.empty()) {
+            e = L->infer_pool.back();
+            L->infer_pool.pop_back();
+        } else {
+            PBG_CUDA(cudaEventCreate(&e));
+        }
+    }
+    PBG_CUDA(cudaEventRecord(ev[0], st));
     prof_begin(s, st);
     mlp_infer_kernel<<<grid, kInferThreads, kInferSmem, st>>>(
         o, d, n, L->box, (const uint16_t*)L->W1b.ptr, (const uint16_t*)L->W2b.ptr, (const uint16_t*)L->W3b.ptr,
@@ -613,6 +680,9 @@ int learn_predict(pbg_scene* s, const float4* o, const float4* d, int64_t n, con
         (uint16_t*)L->pred.ptr, (int*)s->err.ptr);
     prof_end(s, st, kStageOther, 1);
     PBG_CUDA(cudaGetLastError());
+    PBG_CUDA(cudaEventRecord(ev[1], st));
+    L->infer_ev.push_back(ev[0]);
+    L->infer_ev.push_back(ev[1]);
     *pred = (const uint16_t*)L->pred.ptr;
     *cluster_ref = (const int32_t*)L->cluster_ref.ptr;
     return PBG_OK;
@@ -865,6 +935,7 @@ int pbg_learn_get_stats(pbg_scene* s, pbg_learn_stats* out) {
     out->records = (uint64_t)L->count;
     out->last_loss = L->last_loss;
     out->last_accuracy = L->last_acc;
+    harvest_infer_events(L, true);
     out->infer_ms = L->infer_ms;
     out->train_ms = L->train_ms;
     return PBG_OK;

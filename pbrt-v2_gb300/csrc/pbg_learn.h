@@ -45,6 +45,9 @@ struct Learner {
     DeviceBuffer feat, pred;
     float last_loss = 0.f, last_acc = 0.f;
     double infer_ms = 0.0, train_ms = 0.0;
+    // event pairs around inference launches, summed into infer_ms when the
+    // statistics are read (no synchronisation on the launch path)
+    std::vector<cudaEvent_t> infer_ev, infer_pool;
 };
 
 int learn_init(pbg_scene* s, const pbg_learn_params* p);

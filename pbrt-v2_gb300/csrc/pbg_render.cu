@@ -879,14 +879,15 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
     RenderBuffers& B = *s->render_bufs;  // grown on demand, kept for the next frame
     int r;
     const size_t nk = (size_t)n * kslots;
-    // Overlapped bounces (path frames on ray-bvh and naive scenes, learned
-    // ordering off): each bounce's shadow traversal and resolve go to a
-    // second stream, beside the next bounce's nearest-hit traversal and
-    // shading.  rayhierarchy batches share the scene's status words and the
-    // learned ordering one prediction buffer, so those frames stay serial.
+    // Overlapped bounces (path frames on ray-bvh and naive scenes): each
+    // bounce's shadow traversal and resolve go to a second stream, beside
+    // the next bounce's nearest-hit traversal and shading.  rayhierarchy
+    // batches share the scene's status words, and a learned ordering that
+    // serves nearest-hit batches shares its prediction and record buffers
+    // with the any-hit ones, so those frames stay serial.
     const bool overlap = prm->integrator == PBG_INTEGRATOR_PATH &&
                          (s->accel == PBG_ACCEL_RAYBVH || s->accel == PBG_ACCEL_NAIVE) &&
-                         !(s->learn && s->learn->enabled);
+                         !(s->learn && s->learn->enabled && (s->learn->queries & 1));
     if ((r = ensure(B.o4, n * 16)) || (r = ensure(B.d4, n * 16)) || (r = ensure(B.qidx, n * 4)) ||
         (r = ensure(B.L, n * 12)) || (r = ensure(B.beta, n * 12)) || (r = ensure(B.prim, n * 4)) ||
         (r = ensure(B.t, n * 4)) || (r = ensure(B.b1, n * 4)) || (r = ensure(B.b2, n * 4)) ||
