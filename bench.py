@@ -760,10 +760,27 @@ def run_gpu_naive(args, rank, world, dev):
     prm = R.render_params("directlighting")
     flush = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
     tuned = None
-    if not args.no_tune:  # the splits' launch shape, on the frame's camera rays
+    if not args.no_tune:  # the splits' launch shape, on the frame's camera rays and its shadow rays
         cr = S.config_small_naive()["rays"]
         o4, d4 = to_dev(cr)
-        tuned = {"camera (nearest)": acc.autotune(o4, d4), "camera rays as any-hit": acc.autotune(o4, d4, anyhit=True)}
+        tuned = {"camera (nearest)": acc.autotune(o4, d4)}
+        n0 = cr.shape[1]
+        prim = torch.empty(n0, dtype=torch.int32, device="cuda")
+        tt, b1, b2 = (torch.empty(n0, device="cuda") for _ in range(3))
+        acc.intersect_device(o4, d4, prim, tt, b1, b2)
+        torch.cuda.synchronize()
+        hp, ht = prim.cpu().numpy(), tt.cpu().numpy()
+        hit = hp >= 0
+        p = cr[0:3, hit] + cr[3:6, hit] * ht[hit][None]
+        dl = g["light_pos"].astype(np.float32)[:, None] - p
+        dist = np.sqrt((dl ** 2).sum(0))
+        sh = np.empty((8, int(hit.sum())), np.float32)
+        sh[0:3] = p
+        sh[3:6] = dl / dist[None]
+        sh[6] = 1e-3 * ht[hit]
+        sh[7] = dist * (1 - 1e-3)
+        so4, sd4 = to_dev(sh)
+        tuned["shadow (any-hit)"] = acc.autotune(so4, sd4, anyhit=True)
         torch.cuda.synchronize()
     for _ in range(args.warmup):
         flush_l2(flush)
