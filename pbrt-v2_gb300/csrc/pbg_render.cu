@@ -903,6 +903,8 @@ int render(pbg_scene* s, const pbg_camera* cam, const pbg_light* lights, int32_t
             (r = ensure(X.sqd, nk * 16)) || (r = ensure(X.occ, nk)) || (r = ensure(X.emit, n * 12)))
             return r;
     }
+    // a frame that ended early on an error may have left work on the side stream
+    if (B.side) PBG_CUDA(cudaStreamSynchronize(B.side));
     if (overlap && !B.side) {
         PBG_CUDA(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
         for (int k = 0; k < 2; ++k) {
