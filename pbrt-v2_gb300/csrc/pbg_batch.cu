@@ -147,15 +147,16 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_trace_kernel(BatchArgs
 // persistent kernel, with the scene looked up per ray).  Completion stamps:
 // the lanes that finish a ray in an iteration raise their scene's stamp
 // with one atomicMax per scene per warp.
+// PACK: one 8-byte stack entry (WalkStack) when every scene has fewer than
+// 2^24 records.
+template <bool PACK>
 __global__ void __launch_bounds__(kBatchMaxThreads) batch_persistent_kernel(BatchArgs a) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nseg = 2 * a.nscenes;
     const int64_t total = a.rseg_off[nseg];
-    int32_t stack_ref[kStackDepth];
-    int32_t stack_cnt[kStackDepth];
-    float stack_t[kStackDepth];
+    WalkStack<PACK> stk;
     int sp = 0;
     int64_t r = 0;
     int k = 0;
@@ -185,13 +186,14 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_persistent_kernel(Batc
     auto pop = [&]() -> bool {
         while (sp > 0) {
             --sp;
-            if (stack_t[sp] <= h.t) {
-                if (stack_cnt[sp] == 0) {
-                    node = stack_ref[sp];
+            int32_t ref, cnt;
+            if (stk.get(sp, &ref, &cnt) <= h.t) {
+                if (cnt == 0) {
+                    node = ref;
                 } else {
                     node = -1;
-                    leaf_start = ~stack_ref[sp];
-                    leaf_cnt = stack_cnt[sp];
+                    leaf_start = ~ref;
+                    leaf_cnt = cnt;
                 }
                 return true;
             }
@@ -259,9 +261,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_persistent_kernel(Batc
                 if (h0 && h1) {
                     const int32_t cf = near0 ? nn.n3.y : nn.n3.x, kf = near0 ? nn.n3.w : nn.n3.z;
                     if (sp < kStackDepth) {
-                        stack_ref[sp] = cf;
-                        stack_cnt[sp] = cf >= 0 ? 0 : kf;
-                        stack_t[sp] = near0 ? tn1 : tn0;
+                        stk.put(sp, cf, cf >= 0 ? 0 : kf, near0 ? tn1 : tn0);
                         ++sp;
                     } else {
                         ok = false;
@@ -325,7 +325,7 @@ struct Shape {
 int max_ctas_per_sm(int threads, int walk) {
     int n = 0;
     const cudaError_t e =
-        walk == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_persistent_kernel, threads, 0)
+        walk == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_persistent_kernel<true>, threads, 0)
                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_trace_kernel, threads, 0);
     if (e != cudaSuccess) return 1;
     return n > 0 ? n : 1;
@@ -426,9 +426,15 @@ int launch_pair(pbg_sceneset* set, const BatchArgs& a, const Shape& s, cudaStrea
     batch_reset_kernel<<<(unsigned)((set->nscenes + 255) / 256), 256, 0, st>>>(a);
     PBG_CUDA(cudaGetLastError());
     const unsigned grid = (unsigned)(s.ctas_per_sm * set->sm_count);
-    if (s.walk == 2)
-        batch_persistent_kernel<<<grid, (unsigned)s.threads, 0, st>>>(a);
-    else
+    if (s.walk == 2) {
+        // scene-local record starts below 2^24 fit a packed stack entry
+        int64_t max_ntri = 0;
+        for (int64_t k : set->ntri) max_ntri = std::max(max_ntri, k);
+        if (max_ntri < (1 << 24))
+            batch_persistent_kernel<true><<<grid, (unsigned)s.threads, 0, st>>>(a);
+        else
+            batch_persistent_kernel<false><<<grid, (unsigned)s.threads, 0, st>>>(a);
+    } else
         batch_trace_kernel<<<grid, (unsigned)s.threads, 0, st>>>(a);
     PBG_CUDA(cudaGetLastError());
     return PBG_OK;

@@ -195,51 +195,6 @@ __global__ void __launch_bounds__(kPacketThreads)
 constexpr int kPersistThreads = 128;
 constexpr int kPersistMinBlocks = 10;  // CTAs per SM: measured best of 6, 8, 9, 10, 12, 16
 
-// The walk's stack.  PACK: one 8-byte entry (one local load per pop) when
-// the scene allows it: a child reference, with a leaf's record start (below
-// 2^24) and triangle count (below 128) packed into one negative word, and
-// the entry distance.  Otherwise reference, count and distance in three
-// arrays.
-template <bool PACK>
-struct WalkStack;
-
-template <>
-struct WalkStack<true> {
-    int2 e[kStackDepth];
-    __device__ __forceinline__ void put(int i, int32_t ref, int32_t cnt, float t) {
-        const int32_t v = ref >= 0 ? ref : (int32_t)(0x80000000u | ((uint32_t)cnt << 24) | (uint32_t)(~ref));
-        e[i] = make_int2(v, __float_as_int(t));
-    }
-    // entry i: its distance, and (reference, count) when it is taken
-    __device__ __forceinline__ float get(int i, int32_t* ref, int32_t* cnt) const {
-        const int2 v = e[i];
-        if (v.x >= 0) {
-            *ref = v.x;
-            *cnt = 0;
-        } else {
-            *ref = ~(int32_t)((uint32_t)v.x & 0xffffffu);
-            *cnt = (int32_t)(((uint32_t)v.x >> 24) & 0x7fu);
-        }
-        return __int_as_float(v.y);
-    }
-};
-
-template <>
-struct WalkStack<false> {
-    int32_t r[kStackDepth], c[kStackDepth];
-    float tt[kStackDepth];
-    __device__ __forceinline__ void put(int i, int32_t ref, int32_t cnt, float t) {
-        r[i] = ref;
-        c[i] = cnt;
-        tt[i] = t;
-    }
-    __device__ __forceinline__ float get(int i, int32_t* ref, int32_t* cnt) const {
-        *ref = r[i];
-        *cnt = c[i];
-        return tt[i];
-    }
-};
-
 // ORDERED: the learned ordering's predicted cluster (pred, cref as in
 // bvh_kernel) is walked first, then the whole tree skipping it.  STATS: the
 // counting variant (profiling level 2) tallies node tests, leaves and

@@ -38,6 +38,51 @@ __device__ __forceinline__ bool slab(const RayInv& r, float lx, float hx, float 
     return tn <= fmaf(fabsf(tf), 2.f * 3.f * 0x1p-24f / (1.f - 3.f * 0x1p-24f), tf);
 }
 
+// The walk's stack.  PACK: one 8-byte entry (one local load per pop) when
+// the scene allows it: a child reference, with a leaf's record start (below
+// 2^24) and triangle count (below 128) packed into one negative word, and
+// the entry distance.  Otherwise reference, count and distance in three
+// arrays.
+template <bool PACK>
+struct WalkStack;
+
+template <>
+struct WalkStack<true> {
+    int2 e[kStackDepth];
+    __device__ __forceinline__ void put(int i, int32_t ref, int32_t cnt, float t) {
+        const int32_t v = ref >= 0 ? ref : (int32_t)(0x80000000u | ((uint32_t)cnt << 24) | (uint32_t)(~ref));
+        e[i] = make_int2(v, __float_as_int(t));
+    }
+    // entry i: its distance, and (reference, count) when it is taken
+    __device__ __forceinline__ float get(int i, int32_t* ref, int32_t* cnt) const {
+        const int2 v = e[i];
+        if (v.x >= 0) {
+            *ref = v.x;
+            *cnt = 0;
+        } else {
+            *ref = ~(int32_t)((uint32_t)v.x & 0xffffffu);
+            *cnt = (int32_t)(((uint32_t)v.x >> 24) & 0x7fu);
+        }
+        return __int_as_float(v.y);
+    }
+};
+
+template <>
+struct WalkStack<false> {
+    int32_t r[kStackDepth], c[kStackDepth];
+    float tt[kStackDepth];
+    __device__ __forceinline__ void put(int i, int32_t ref, int32_t cnt, float t) {
+        r[i] = ref;
+        c[i] = cnt;
+        tt[i] = t;
+    }
+    __device__ __forceinline__ float get(int i, int32_t* ref, int32_t* cnt) const {
+        *ref = r[i];
+        *cnt = c[i];
+        return tt[i];
+    }
+};
+
 struct WalkHit {
     float t, b1, b2;
     int32_t prim;
@@ -82,8 +127,7 @@ __device__ __forceinline__ bool bvh_walk(const BvhNode* __restrict__ nodes, cons
     const float nd = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
     const RayInv ri{o.x, o.y, o.z, safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
     bool done = unculled > 0 && test_run<ANY, STATS>(tris, 0, unculled, o, d, nd, h, wc);
-    int32_t stack[kStackDepth];
-    float stack_t[kStackDepth];
+    int2 stack[kStackDepth];  // (inner node, entry distance bits): one 8-byte entry
     int sp = 0;
     int32_t node = 0;
     bool ok = true;
@@ -93,8 +137,7 @@ __device__ __forceinline__ bool bvh_walk(const BvhNode* __restrict__ nodes, cons
             if (STATS) wc.leaf++;
             done = test_run<ANY, STATS>(tris, ~first_ref, first_cnt, o, d, nd, h, wc);
         } else {
-            stack[sp] = 0;  // resume at the root afterwards
-            stack_t[sp] = -INFINITY;
+            stack[sp] = make_int2(0, __float_as_int(-INFINITY));  // resume at the root afterwards
             ++sp;
             node = first_ref;
         }
@@ -126,8 +169,7 @@ __device__ __forceinline__ bool bvh_walk(const BvhNode* __restrict__ nodes, cons
         if (h0 && h1) {
             const bool first0 = tn0 <= tn1;
             if (sp < kStackDepth) {
-                stack[sp] = first0 ? c1 : c0;
-                stack_t[sp] = first0 ? tn1 : tn0;
+                stack[sp] = make_int2(first0 ? c1 : c0, __float_as_int(first0 ? tn1 : tn0));
                 ++sp;
             } else {
                 ok = false;
@@ -142,8 +184,9 @@ __device__ __forceinline__ bool bvh_walk(const BvhNode* __restrict__ nodes, cons
         bool found = false;
         while (sp > 0) {
             --sp;
-            if (stack_t[sp] <= h.t) {
-                node = stack[sp];
+            const int2 e = stack[sp];
+            if (__int_as_float(e.y) <= h.t) {
+                node = e.x;
                 found = true;
                 break;
             }
