@@ -1278,14 +1278,15 @@ def run_reference_path(args):
     """The reference's CPU path for the path-tracing frame on all host cores:
     the oracle's restatement of the breadth-first path integrator over its
     SAH BVH and pbrt's triangle test, the same frame and samples as the GPU
-    arm; each step traces a strided 1/16 of the frame's paths (a different
-    subset each step), timed whole (camera rays, shading, bounce and shadow
-    rays)."""
+    arm; each step traces every fourth path of the frame (a different
+    quarter each step), timed whole (camera rays, shading, bounce and shadow
+    rays).  With smaller samples the last of each step's 409,600-sample
+    tasks (the reference's MaxRaysPerCall) left host threads idle."""
     from pbrt_gb300 import scenes  # noqa: F401  (package import for the scene generator)
     sc, r2c, c2w = path_setup()
     rc = path_cpu_counter(sc["tris"], r2c, c2w, 1000)
     threads = os.cpu_count() or 1
-    stride = 16
+    stride = 4
     times, nrays = [], 0
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
