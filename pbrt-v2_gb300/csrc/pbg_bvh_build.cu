@@ -95,6 +95,53 @@ __device__ __forceinline__ int bin_of(float c, float lo, float scale) {
     return b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
 }
 
+// The SAH sweep of one axis over its bins (counts, encoded lower and upper
+// bounds), in the host builder's float order: the best cost and the last bin
+// of the left side, or -1.
+__device__ void sah_sweep(const uint32_t* cnt, const uint32_t (*blo)[3], const uint32_t (*bhi)[3], float* best_out,
+                          int* bk_out) {
+    float best = INFINITY;
+    int bk = -1;
+    float rarea[kBins];
+    int rcnt[kBins];
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    int c = 0;
+    for (int k = kBins - 1; k > 0; --k) {
+        if (cnt[k]) {
+            for (int q = 0; q < 3; ++q) {
+                lo[q] = fminf(lo[q], fdec(blo[k][q]));
+                hi[q] = fmaxf(hi[q], fdec(bhi[k][q]));
+            }
+        }
+        c += (int)cnt[k];
+        rarea[k] = box_area(lo, hi);
+        rcnt[k] = c;
+    }
+    for (int q = 0; q < 3; ++q) {
+        lo[q] = INFINITY;
+        hi[q] = -INFINITY;
+    }
+    c = 0;
+    for (int k = 0; k < kBins - 1; ++k) {
+        if (cnt[k]) {
+            for (int q = 0; q < 3; ++q) {
+                lo[q] = fminf(lo[q], fdec(blo[k][q]));
+                hi[q] = fmaxf(hi[q], fdec(bhi[k][q]));
+            }
+        }
+        c += (int)cnt[k];
+        if (c == 0 || rcnt[k + 1] == 0) continue;
+        const float cost =
+            __fadd_rn(__fmul_rn(box_area(lo, hi), (float)c), __fmul_rn(rarea[k + 1], (float)rcnt[k + 1]));
+        if (cost < best) {
+            best = cost;
+            bk = k;
+        }
+    }
+    *best_out = best;
+    *bk_out = bk;
+}
+
 // Degenerate flags per triangle, counted per block; scene bounds.
 __global__ void prep_count_kernel(const float* __restrict__ tri9, int64_t n, uint32_t* __restrict__ counts,
                                   uint32_t* __restrict__ bounds) {
@@ -258,44 +305,7 @@ __global__ void __launch_bounds__(kBT) split_kernel(const BItem* __restrict__ in
             const int a = threadIdx.x;
             float best = INFINITY;
             int bk = -1;
-            if (__fsub_rn(cb[3 + a], cb[a]) > 0.f) {
-                float rarea[kBins];
-                int rcnt[kBins];
-                float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-                int c = 0;
-                for (int k = kBins - 1; k > 0; --k) {
-                    if (bcnt[a][k]) {
-                        for (int q = 0; q < 3; ++q) {
-                            lo[q] = fminf(lo[q], fdec(blo[a][k][q]));
-                            hi[q] = fmaxf(hi[q], fdec(bhi[a][k][q]));
-                        }
-                    }
-                    c += (int)bcnt[a][k];
-                    rarea[k] = box_area(lo, hi);
-                    rcnt[k] = c;
-                }
-                for (int q = 0; q < 3; ++q) {
-                    lo[q] = INFINITY;
-                    hi[q] = -INFINITY;
-                }
-                c = 0;
-                for (int k = 0; k < kBins - 1; ++k) {
-                    if (bcnt[a][k]) {
-                        for (int q = 0; q < 3; ++q) {
-                            lo[q] = fminf(lo[q], fdec(blo[a][k][q]));
-                            hi[q] = fmaxf(hi[q], fdec(bhi[a][k][q]));
-                        }
-                    }
-                    c += (int)bcnt[a][k];
-                    if (c == 0 || rcnt[k + 1] == 0) continue;
-                    const float cost = __fadd_rn(__fmul_rn(box_area(lo, hi), (float)c),
-                                                 __fmul_rn(rarea[k + 1], (float)rcnt[k + 1]));
-                    if (cost < best) {
-                        best = cost;
-                        bk = k;
-                    }
-                }
-            }
+            if (__fsub_rn(cb[3 + a], cb[a]) > 0.f) sah_sweep(bcnt[a], blo[a], bhi[a], &best, &bk);
             acost[a] = best;
             asplit[a] = bk;
         }
@@ -393,6 +403,303 @@ __global__ void __launch_bounds__(kBT) split_kernel(const BItem* __restrict__ in
     }
 }
 
+// ---------------------------------------------------------------------
+// The top levels (a few segments holding most of the items): several CTAs
+// per segment, each over a chunk of kChunk items, with the segment's bounds
+// and bins merged in global memory by atomics.  Every reduction is
+// order-independent and the partition stable (each chunk's left and right
+// items land after those of the chunks before it, in order), so the split
+// decisions and the item order equal those of split_kernel.
+constexpr int kChunk = 4096;             // items per CTA
+constexpr int kBigLevelSegs = 8;         // levels of at most this many segments ...
+constexpr int64_t kBigItems = 1 << 17;   // ... in scenes of at least this many items
+
+struct SegAcc {
+    uint32_t box[12];  // encoded: node lo (min), node hi (max), centroid lo (min), centroid hi (max)
+    uint32_t cnt[3][kBins];
+    uint32_t lo[3][kBins][3], hi[3][kBins][3];
+    int32_t leaf, median, axis, split, nleft;
+};
+
+__device__ __forceinline__ bool chunk_of(const BSeg& sg, int32_t* b0, int32_t* b1) {
+    *b0 = sg.begin + (int32_t)blockIdx.x * kChunk;
+    *b1 = min(sg.end, *b0 + kChunk);
+    return *b0 < sg.end;
+}
+
+// The leaf decision of split_kernel from the segment's centroid box.
+__device__ __forceinline__ bool seg_leaf(const BSeg& sg, const float* cb, int max_leaf, int* axis) {
+    int ax = 0;
+    float ext = __fsub_rn(cb[3], cb[0]);
+    for (int a = 1; a < 3; ++a)
+        if (__fsub_rn(cb[3 + a], cb[a]) > ext) {
+            ax = a;
+            ext = __fsub_rn(cb[3 + a], cb[a]);
+        }
+    *axis = ax;
+    return (sg.end - sg.begin) <= max_leaf || !(ext > 0.f) || sg.depth >= kDepthLimit;
+}
+
+__global__ void big_init_kernel(SegAcc* __restrict__ acc) {
+    SegAcc& A = acc[blockIdx.x];
+    for (int k = threadIdx.x; k < 12; k += blockDim.x) A.box[k] = (k % 6) < 3 ? 0xffffffffu : 0u;
+    for (int k = threadIdx.x; k < 3 * kBins; k += blockDim.x) {
+        (&A.cnt[0][0])[k] = 0u;
+        for (int q = 0; q < 3; ++q) {
+            (&A.lo[0][0][0])[3 * k + q] = 0xffffffffu;
+            (&A.hi[0][0][0])[3 * k + q] = 0u;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBT) big_bounds_kernel(const BItem* __restrict__ in, const BSeg* __restrict__ segs,
+                                                         SegAcc* __restrict__ acc, int* __restrict__ max_depth) {
+    __shared__ float red[kBT / 32][12];
+    const BSeg sg = segs[blockIdx.y];
+    int32_t b0, b1;
+    if (!chunk_of(sg, &b0, &b1)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(max_depth, sg.depth);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float v[12];
+    for (int a = 0; a < 3; ++a) {
+        v[a] = INFINITY;
+        v[3 + a] = -INFINITY;
+        v[6 + a] = INFINITY;
+        v[9 + a] = -INFINITY;
+    }
+    for (int32_t i = b0 + threadIdx.x; i < b1; i += kBT) {
+        const BItem it = in[i];
+        for (int a = 0; a < 3; ++a) {
+            v[a] = fminf(v[a], it.lo[a]);
+            v[3 + a] = fmaxf(v[3 + a], it.hi[a]);
+            v[6 + a] = fminf(v[6 + a], it.c[a]);
+            v[9 + a] = fmaxf(v[9 + a], it.c[a]);
+        }
+    }
+    for (int k = 0; k < 12; ++k) {
+        const bool is_min = (k % 6) < 3;
+        for (int off = 16; off; off >>= 1) {
+            const float o = __shfl_xor_sync(0xffffffffu, v[k], off);
+            v[k] = is_min ? fminf(v[k], o) : fmaxf(v[k], o);
+        }
+        if (lane == 0) red[warp][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        const int k = threadIdx.x;
+        const bool is_min = (k % 6) < 3;
+        float r = red[0][k];
+        for (int w = 1; w < kBT / 32; ++w) r = is_min ? fminf(r, red[w][k]) : fmaxf(r, red[w][k]);
+        if (is_min)
+            atomicMin(&acc[blockIdx.y].box[k], fenc(r));
+        else
+            atomicMax(&acc[blockIdx.y].box[k], fenc(r));
+    }
+}
+
+__global__ void __launch_bounds__(kBT) big_bins_kernel(const BItem* __restrict__ in, const BSeg* __restrict__ segs,
+                                                       SegAcc* __restrict__ acc, int max_leaf) {
+    __shared__ uint32_t bcnt[3][kBins], blo[3][kBins][3], bhi[3][kBins][3];
+    const BSeg sg = segs[blockIdx.y];
+    int32_t b0, b1;
+    if (!chunk_of(sg, &b0, &b1)) return;
+    SegAcc& A = acc[blockIdx.y];
+    float cb[6];
+    for (int k = 0; k < 6; ++k) cb[k] = fdec(A.box[6 + k]);
+    int axis;
+    if (seg_leaf(sg, cb, max_leaf, &axis)) return;  // the same for every CTA of the segment
+    for (int k = threadIdx.x; k < 3 * kBins; k += kBT) {
+        (&bcnt[0][0])[k] = 0u;
+        for (int q = 0; q < 3; ++q) {
+            (&blo[0][0][0])[3 * k + q] = 0xffffffffu;
+            (&bhi[0][0][0])[3 * k + q] = 0u;
+        }
+    }
+    __syncthreads();
+    for (int32_t i = b0 + threadIdx.x; i < b1; i += kBT) {
+        const BItem it = in[i];
+        for (int a = 0; a < 3; ++a) {
+            const float ea = __fsub_rn(cb[3 + a], cb[a]);
+            if (!(ea > 0.f)) continue;
+            const int b = bin_of(it.c[a], cb[a], __fdiv_rn((float)kBins, ea));
+            atomicAdd(&bcnt[a][b], 1u);
+            for (int q = 0; q < 3; ++q) {
+                atomicMin(&blo[a][b][q], fenc(it.lo[q]));
+                atomicMax(&bhi[a][b][q], fenc(it.hi[q]));
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * kBins; k += kBT) {
+        const int a = k / kBins, b = k % kBins;
+        if (bcnt[a][b] == 0u) continue;
+        atomicAdd(&A.cnt[a][b], bcnt[a][b]);
+        for (int q = 0; q < 3; ++q) {
+            atomicMin(&A.lo[a][b][q], blo[a][b][q]);
+            atomicMax(&A.hi[a][b][q], bhi[a][b][q]);
+        }
+    }
+}
+
+// One warp per segment: split_kernel's leaf decision and SAH choice from the
+// merged bins; the segment's result.
+__global__ void big_decide_kernel(const BSeg* __restrict__ segs, SegAcc* __restrict__ acc, BRes* __restrict__ res,
+                                  int max_leaf) {
+    __shared__ float acost[3];
+    __shared__ int asplit[3];
+    const BSeg sg = segs[blockIdx.x];
+    SegAcc& A = acc[blockIdx.x];
+    float nb[6], cb[6];
+    for (int k = 0; k < 6; ++k) {
+        nb[k] = fdec(A.box[k]);
+        cb[k] = fdec(A.box[6 + k]);
+    }
+    int axis;
+    const bool leaf0 = seg_leaf(sg, cb, max_leaf, &axis);
+    if (!leaf0 && threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        float best = INFINITY;
+        int bk = -1;
+        if (__fsub_rn(cb[3 + a], cb[a]) > 0.f) sah_sweep(A.cnt[a], A.lo[a], A.hi[a], &best, &bk);
+        acost[a] = best;
+        asplit[a] = bk;
+    }
+    __syncwarp();
+    if (threadIdx.x != 0) return;
+    const int32_t np = sg.end - sg.begin;
+    int leaf = leaf0, median = 0, split = -1;
+    if (!leaf) {
+        float best = INFINITY;
+        int ba = -1, bs = -1;
+        for (int a = 0; a < 3; ++a)
+            if (asplit[a] >= 0 && acost[a] < best) {
+                best = acost[a];
+                ba = a;
+                bs = asplit[a];
+            }
+        if (bs < 0) {
+            leaf = np <= 4 * max_leaf || sg.depth >= kDepthLimit;
+            median = !leaf;
+        } else {
+            axis = ba;
+            split = bs;
+        }
+    }
+    int32_t nleft = 0;
+    if (!leaf) {
+        if (median) {
+            nleft = np / 2;
+        } else {
+            for (int k = 0; k <= split; ++k) nleft += (int32_t)A.cnt[axis][k];
+        }
+    }
+    A.leaf = leaf;
+    A.median = median;
+    A.axis = axis;
+    A.split = split;
+    A.nleft = nleft;
+    BRes r;
+    r.leaf = leaf;
+    r.mid = leaf ? -1 : sg.begin + nleft;
+    for (int q = 0; q < 6; ++q) (q < 3 ? r.lo[q] : r.hi[q - 3]) = nb[q];
+    res[blockIdx.x] = r;
+}
+
+// Leaves write their record order, median splits copy their items; splits by
+// bin count each chunk's left items.
+__global__ void __launch_bounds__(kBT) big_count_kernel(const BItem* __restrict__ in, BItem* __restrict__ out,
+                                                        const BSeg* __restrict__ segs, const SegAcc* __restrict__ acc,
+                                                        int32_t* __restrict__ order, int32_t unculled,
+                                                        uint32_t* __restrict__ lcnt, int64_t chunks) {
+    const BSeg sg = segs[blockIdx.y];
+    int32_t b0, b1;
+    if (!chunk_of(sg, &b0, &b1)) return;
+    const SegAcc& A = acc[blockIdx.y];
+    if (A.leaf) {
+        for (int32_t i = b0 + threadIdx.x; i < b1; i += kBT) order[unculled + i] = in[i].idx;
+        return;
+    }
+    if (A.median) {
+        for (int32_t i = b0 + threadIdx.x; i < b1; i += kBT) out[i] = in[i];
+        return;
+    }
+    const int a = A.axis;
+    const float lo = fdec(A.box[6 + a]);
+    const float scale = __fdiv_rn((float)kBins, __fsub_rn(fdec(A.box[9 + a]), lo));
+    uint32_t c = 0;
+    for (int32_t base = b0; base < b1; base += kBT) {
+        const int32_t i = base + threadIdx.x;
+        const bool left = i < b1 && bin_of(in[i].c[a], lo, scale) <= A.split;
+        c += (uint32_t)__syncthreads_count(left);
+    }
+    if (threadIdx.x == 0) lcnt[(int64_t)blockIdx.y * chunks + blockIdx.x] = c;
+}
+
+// The stable partition of split segments: each chunk's left items after the
+// left items of the chunks before it, its right items likewise after nleft.
+__global__ void __launch_bounds__(kBT) big_scatter_kernel(const BItem* __restrict__ in, BItem* __restrict__ out,
+                                                          const BSeg* __restrict__ segs,
+                                                          const SegAcc* __restrict__ acc,
+                                                          const uint32_t* __restrict__ lcnt, int64_t chunks) {
+    __shared__ uint32_t wl[kBT / 32], wr[kBT / 32];
+    __shared__ int32_t run_l, run_r;
+    const BSeg sg = segs[blockIdx.y];
+    int32_t b0, b1;
+    if (!chunk_of(sg, &b0, &b1)) return;
+    const SegAcc& A = acc[blockIdx.y];
+    if (A.leaf || A.median) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        int32_t pl = 0;
+        for (unsigned k = 0; k < blockIdx.x; ++k) pl += (int32_t)lcnt[(int64_t)blockIdx.y * chunks + k];
+        run_l = pl;
+        run_r = (b0 - sg.begin) - pl;
+    }
+    __syncthreads();
+    const int a = A.axis;
+    const float lo = fdec(A.box[6 + a]);
+    const float scale = __fdiv_rn((float)kBins, __fsub_rn(fdec(A.box[9 + a]), lo));
+    const int32_t nleft = A.nleft;
+    for (int32_t base = b0; base < b1; base += kBT) {
+        const int32_t i = base + threadIdx.x;
+        const bool valid = i < b1;
+        BItem it;
+        bool left = false;
+        if (valid) {
+            it = in[i];
+            left = bin_of(it.c[a], lo, scale) <= A.split;
+        }
+        const unsigned bl = __ballot_sync(0xffffffffu, valid && left);
+        const unsigned br = __ballot_sync(0xffffffffu, valid && !left);
+        if (lane == 0) {
+            wl[warp] = __popc(bl);
+            wr[warp] = __popc(br);
+        }
+        __syncthreads();
+        uint32_t pl = 0, pr = 0, tl = 0, tr = 0;
+        for (int w = 0; w < kBT / 32; ++w) {
+            if (w < warp) {
+                pl += wl[w];
+                pr += wr[w];
+            }
+            tl += wl[w];
+            tr += wr[w];
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        if (valid) {
+            const int32_t dst = left ? sg.begin + run_l + (int32_t)(pl + __popc(bl & lt))
+                                     : sg.begin + nleft + run_r + (int32_t)(pr + __popc(br & lt));
+            out[dst] = it;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            run_l += (int32_t)tl;
+            run_r += (int32_t)tr;
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void inner_count_kernel(const BRes* __restrict__ res, int64_t nseg, uint32_t* __restrict__ counts) {
     const int64_t i = (int64_t)blockIdx.x * kBT + threadIdx.x;
     const int c = __syncthreads_count(i < nseg && !res[i].leaf);
@@ -479,13 +786,13 @@ int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf
                      cudaStream_t st) {
     if (max_leaf < 1) max_leaf = 4;
     const int64_t nb = (ntri + kBT - 1) / kBT;
-    DeviceBuffer counts, small, items_a, items_b, segs_a, segs_b, res;
+    DeviceBuffer counts, small, items_a, items_b, segs_a, segs_b, res, acc, lcnt;
     struct Guard {
-        DeviceBuffer* b[7];
+        DeviceBuffer* b[9];
         ~Guard() {
             for (DeviceBuffer* x : b) release(*x);
         }
-    } guard{{&counts, &small, &items_a, &items_b, &segs_a, &segs_b, &res}};
+    } guard{{&counts, &small, &items_a, &items_b, &segs_a, &segs_b, &res, &acc, &lcnt}};
     const size_t ni = (size_t)std::max<int64_t>(ntri, 1);
     int rc;
     if ((rc = ensure(counts, (size_t)(std::max<int64_t>(nb, ni / kBT + 1) + 8) * 4)) || (rc = ensure(small, 64)) ||
@@ -527,8 +834,24 @@ int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf
         BSeg* nxt = (BSeg*)segs_b.ptr;
         int64_t nseg = 1;
         while (nseg > 0) {
-            split_kernel<<<(unsigned)nseg, kBT, 0, st>>>(in, out, cur, (BRes*)res.ptr, order_dev, ndeg, max_leaf,
-                                                        (int*)(sm + 7));
+            if (nseg <= kBigLevelSegs && nitems >= kBigItems) {  // the top levels: several CTAs per segment
+                const int64_t chunks = (nitems + kChunk - 1) / kChunk;
+                if ((rc = ensure(acc, (size_t)nseg * sizeof(SegAcc))) ||
+                    (rc = ensure(lcnt, (size_t)(nseg * chunks) * sizeof(uint32_t))))
+                    return rc;
+                SegAcc* A = (SegAcc*)acc.ptr;
+                const dim3 g((unsigned)chunks, (unsigned)nseg);
+                big_init_kernel<<<(unsigned)nseg, kBT, 0, st>>>(A);
+                big_bounds_kernel<<<g, kBT, 0, st>>>(in, cur, A, (int*)(sm + 7));
+                big_bins_kernel<<<g, kBT, 0, st>>>(in, cur, A, max_leaf);
+                big_decide_kernel<<<(unsigned)nseg, 32, 0, st>>>(cur, A, (BRes*)res.ptr, max_leaf);
+                big_count_kernel<<<g, kBT, 0, st>>>(in, out, cur, A, order_dev, ndeg, (uint32_t*)lcnt.ptr, chunks);
+                big_scatter_kernel<<<g, kBT, 0, st>>>(in, out, cur, A, (const uint32_t*)lcnt.ptr, chunks);
+                s->counters.kernel_launches += 5;
+            } else {
+                split_kernel<<<(unsigned)nseg, kBT, 0, st>>>(in, out, cur, (BRes*)res.ptr, order_dev, ndeg,
+                                                            max_leaf, (int*)(sm + 7));
+            }
             PBG_CUDA(cudaGetLastError());
             const int64_t lb = (nseg + kBT - 1) / kBT;
             uint32_t* cnt = (uint32_t*)counts.ptr;
