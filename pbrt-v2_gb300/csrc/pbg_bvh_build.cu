@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(kBT) split_kernel(const BItem* __restrict__ in
 // items land after those of the chunks before it, in order), so the split
 // decisions and the item order equal those of split_kernel.
 constexpr int kChunk = 4096;             // items per CTA
-constexpr int kBigLevelSegs = 8;         // levels of at most this many segments ...
+constexpr int kBigLevelSegs = 32;        // levels of at most this many segments ...
 constexpr int64_t kBigItems = 1 << 17;   // ... in scenes of at least this many items
 
 struct SegAcc {
