@@ -403,6 +403,160 @@ __global__ void __launch_bounds__(kBT) split_kernel(const BItem* __restrict__ in
     }
 }
 
+// The deep levels (many small segments): one warp per segment, the same
+// steps as split_kernel (bounds, leaf decision, bins, SAH, stable partition)
+// at warp scale.  Order-independent reductions and an in-order partition
+// give split_kernel's decisions and item order.
+constexpr int kWarpSegs = 8;            // segments (warps) per CTA
+constexpr int64_t kWarpLevelSegs = 4096;  // levels of more segments than this
+
+__global__ void __launch_bounds__(32 * kWarpSegs)
+    split_warp_kernel(const BItem* __restrict__ in, BItem* __restrict__ out, const BSeg* __restrict__ segs,
+                      BRes* __restrict__ res, int32_t* __restrict__ order, int32_t unculled, int max_leaf,
+                      int* __restrict__ max_depth, int64_t nseg) {
+    __shared__ uint32_t bcnt[kWarpSegs][3][kBins], blo[kWarpSegs][3][kBins][3], bhi[kWarpSegs][3][kBins][3];
+    __shared__ float acost[kWarpSegs][3];
+    __shared__ int asplit[kWarpSegs][3];
+    const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t sidx = (int64_t)blockIdx.x * kWarpSegs + w;
+    if (sidx >= nseg) return;  // the whole warp: this kernel synchronises warps only
+    const BSeg sg = segs[sidx];
+    const int32_t np = sg.end - sg.begin;
+    if (lane == 0) atomicMax(max_depth, sg.depth);
+    float v[12];
+    for (int a = 0; a < 3; ++a) {
+        v[a] = INFINITY;
+        v[3 + a] = -INFINITY;
+        v[6 + a] = INFINITY;
+        v[9 + a] = -INFINITY;
+    }
+    for (int32_t i = sg.begin + lane; i < sg.end; i += 32) {
+        const BItem it = in[i];
+        for (int a = 0; a < 3; ++a) {
+            v[a] = fminf(v[a], it.lo[a]);
+            v[3 + a] = fmaxf(v[3 + a], it.hi[a]);
+            v[6 + a] = fminf(v[6 + a], it.c[a]);
+            v[9 + a] = fmaxf(v[9 + a], it.c[a]);
+        }
+    }
+    for (int k = 0; k < 12; ++k) {
+        const bool is_min = (k % 6) < 3;
+        for (int off = 16; off; off >>= 1) {
+            const float o = __shfl_xor_sync(full, v[k], off);
+            v[k] = is_min ? fminf(v[k], o) : fmaxf(v[k], o);
+        }
+    }
+    const float* nb = v;      // node box: lo[3], hi[3]
+    const float* cb = v + 6;  // centroid box: lo[3], hi[3]
+    int axis = 0;
+    float ext = __fsub_rn(cb[3], cb[0]);
+    for (int a = 1; a < 3; ++a)
+        if (__fsub_rn(cb[3 + a], cb[a]) > ext) {
+            axis = a;
+            ext = __fsub_rn(cb[3 + a], cb[a]);
+        }
+    bool leaf = np <= max_leaf || !(ext > 0.f) || sg.depth >= kDepthLimit;
+    bool median = false;
+    int split = -1;
+    if (!leaf) {
+        for (int k = lane; k < 3 * kBins; k += 32) {
+            (&bcnt[w][0][0])[k] = 0u;
+            for (int q = 0; q < 3; ++q) {
+                (&blo[w][0][0][0])[3 * k + q] = 0xffffffffu;
+                (&bhi[w][0][0][0])[3 * k + q] = 0u;
+            }
+        }
+        __syncwarp();
+        for (int32_t i = sg.begin + lane; i < sg.end; i += 32) {
+            const BItem it = in[i];
+            for (int a = 0; a < 3; ++a) {
+                const float ea = __fsub_rn(cb[3 + a], cb[a]);
+                if (!(ea > 0.f)) continue;
+                const int b = bin_of(it.c[a], cb[a], __fdiv_rn((float)kBins, ea));
+                atomicAdd(&bcnt[w][a][b], 1u);
+                for (int q = 0; q < 3; ++q) {
+                    atomicMin(&blo[w][a][b][q], fenc(it.lo[q]));
+                    atomicMax(&bhi[w][a][b][q], fenc(it.hi[q]));
+                }
+            }
+        }
+        __syncwarp();
+        if (lane < 3) {
+            const int a = lane;
+            float best = INFINITY;
+            int bk = -1;
+            if (__fsub_rn(cb[3 + a], cb[a]) > 0.f) sah_sweep(bcnt[w][a], blo[w][a], bhi[w][a], &best, &bk);
+            acost[w][a] = best;
+            asplit[w][a] = bk;
+        }
+        __syncwarp();
+        float best = INFINITY;
+        int ba = -1, bs = -1;
+        for (int a = 0; a < 3; ++a)
+            if (asplit[w][a] >= 0 && acost[w][a] < best) {
+                best = acost[w][a];
+                ba = a;
+                bs = asplit[w][a];
+            }
+        if (bs < 0) {
+            leaf = np <= 4 * max_leaf || sg.depth >= kDepthLimit;
+            median = !leaf;
+        } else {
+            axis = ba;
+            split = bs;
+        }
+    }
+    if (leaf) {
+        for (int32_t i = sg.begin + lane; i < sg.end; i += 32) order[unculled + i] = in[i].idx;
+        if (lane == 0) {
+            BRes r;
+            r.leaf = 1;
+            r.mid = -1;
+            for (int q = 0; q < 6; ++q) (q < 3 ? r.lo[q] : r.hi[q - 3]) = nb[q];
+            res[sidx] = r;
+        }
+        return;
+    }
+    int32_t nleft = 0;
+    if (median) {
+        for (int32_t i = sg.begin + lane; i < sg.end; i += 32) out[i] = in[i];
+        nleft = np / 2;
+    } else {
+        for (int k = 0; k <= split; ++k) nleft += (int32_t)bcnt[w][axis][k];
+        const float scale = __fdiv_rn((float)kBins, __fsub_rn(cb[3 + axis], cb[axis]));
+        const float lo = cb[axis];
+        int32_t run_l = 0, run_r = 0;
+        const unsigned lt = (1u << lane) - 1u;
+        for (int32_t base = sg.begin; base < sg.end; base += 32) {
+            const int32_t i = base + lane;
+            const bool valid = i < sg.end;
+            BItem it;
+            bool left = false;
+            if (valid) {
+                it = in[i];
+                left = bin_of(it.c[axis], lo, scale) <= split;
+            }
+            const unsigned bl = __ballot_sync(full, valid && left);
+            const unsigned br = __ballot_sync(full, valid && !left);
+            if (valid) {
+                const int32_t dst = left ? sg.begin + run_l + __popc(bl & lt)
+                                         : sg.begin + nleft + run_r + __popc(br & lt);
+                out[dst] = it;
+            }
+            run_l += __popc(bl);
+            run_r += __popc(br);
+        }
+    }
+    if (lane == 0) {
+        BRes r;
+        r.leaf = 0;
+        r.mid = sg.begin + nleft;
+        for (int q = 0; q < 6; ++q) (q < 3 ? r.lo[q] : r.hi[q - 3]) = nb[q];
+        res[sidx] = r;
+    }
+}
+
 // ---------------------------------------------------------------------
 // The top levels (a few segments holding most of the items): several CTAs
 // per segment, each over a chunk of kChunk items, with the segment's bounds
@@ -848,6 +1002,9 @@ int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf
                 big_count_kernel<<<g, kBT, 0, st>>>(in, out, cur, A, order_dev, ndeg, (uint32_t*)lcnt.ptr, chunks);
                 big_scatter_kernel<<<g, kBT, 0, st>>>(in, out, cur, A, (const uint32_t*)lcnt.ptr, chunks);
                 s->counters.kernel_launches += 5;
+            } else if (nseg > kWarpLevelSegs) {  // the deep levels: a warp per segment
+                split_warp_kernel<<<(unsigned)((nseg + kWarpSegs - 1) / kWarpSegs), 32 * kWarpSegs, 0, st>>>(
+                    in, out, cur, (BRes*)res.ptr, order_dev, ndeg, max_leaf, (int*)(sm + 7), nseg);
             } else {
                 split_kernel<<<(unsigned)nseg, kBT, 0, st>>>(in, out, cur, (BRes*)res.ptr, order_dev, ndeg,
                                                             max_leaf, (int*)(sm + 7));
