@@ -72,3 +72,25 @@ def test_autotune_rejects_bad_arguments(gpu_lib):
         rc = L.lib().pbg_autotune(acc.handle, o4.data_ptr(), d4.data_ptr(), None, n, query, 1, C.byref(r), None)
         assert rc == L.PBG_ERR_INVALID_ARGUMENT
     acc.close()
+
+
+@pytest.mark.parametrize("kind", ["naive", "rayhierarchy", "ray-bvh"])
+def test_autotune_tiny_batches_and_empty_scenes(gpu_lib, oracle, kind):
+    """One ray, and a scene without triangles: every shape still answers
+    identically (and a miss for the empty scene)."""
+    import torch
+    sc = S.terrain_icospheres(seed=2, grid=16, n_spheres=2)
+    for tris in (sc["tris"], np.zeros((0, 9), np.float32)):
+        acc = A.MakeAccelerator(kind, tris)
+        rays = S.random_rays(1, [-4, -1, -4], [4, 4, 4], seed=9)
+        o4, d4 = dev(rays)
+        for anyhit in (False, True):
+            r = acc.autotune(o4, d4, anyhit=anyhit, reps=1)
+            assert r["mismatches"] == 0 and len(r["candidates"]) == EXPECTED[kind]
+        prim = torch.empty(1, dtype=torch.int32, device="cuda")
+        t, b1, b2 = (torch.empty(1, device="cuda") for _ in range(3))
+        acc.intersect_device(o4, d4, prim, t, b1, b2)
+        torch.cuda.synchronize()
+        want = oracle.nearest(tris, rays)[0] if len(tris) else np.array([-1], np.int32)
+        np.testing.assert_array_equal(prim.cpu().numpy(), want)
+        acc.close()
