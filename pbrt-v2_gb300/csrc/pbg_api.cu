@@ -1146,6 +1146,8 @@ void pbg_scene_destroy(pbg_scene* s) {
     release(s->tri9);
     release(s->uv6);
     release(s->bvh);
+    release(s->wide);
+    release(s->tris_wide);
     release(s->spheres);
     release(s->clusters);
     release(s->tri_pos);

@@ -10,10 +10,10 @@
 //                 1024) x CTAs per SM of the grid-stride kernels (16, 32),
 //                 kept apart for nearest-hit and any-hit batches
 //   ray-bvh       the walk for this batch class (any-hit or not, coherent
-//                 or not): one thread per ray, persistent warps, or warp
+//                 or not): one thread per ray, persistent warps, warp
 //                 packets over the ray hierarchy's leaves (sorted) or over
-//                 the batch in its own order; skipped when pbg_params.walk
-//                 fixes the walk
+//                 the batch in its own order, or persistent warps over the
+//                 eight-wide tree; skipped when pbg_params.walk fixes the walk
 // Every candidate traces the same batch; its results must equal the first
 // candidate's bit for bit (prim, t, b1, b2 of hits, or occlusion), else the
 // call fails with PBG_ERR_INTERNAL and the scene keeps its previous shapes.
@@ -96,6 +96,7 @@ std::vector<Candidate> candidates(const pbg_scene* s) {
                 out.push_back({{2, 0, 0}});
                 out.push_back({{3, 0, 0}});
                 out.push_back({{4, 0, 0}});
+                out.push_back({{5, 0, 0}});
             }
             break;
     }

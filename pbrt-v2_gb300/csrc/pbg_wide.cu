@@ -1,0 +1,707 @@
+// pbg_wide.cu -- ray-bvh walk 5: the binary SAH tree collapsed into an
+// eight-wide tree, walked by persistent warps.
+//
+// The reference walks its two-wide GPU BVH (bvh.cpp:154-206 lays it out,
+// rayBVH.cpp:615-1323 walks it).  Walking one node per step, the two-wide
+// walk of incoherent bounce rays waits on a dependent node load at every
+// step and spends much of its issue on per-visit control (votes, stack
+// traffic, child ordering).  Eight children per node make the path from the
+// root about a third as long (68 -> 21 node visits per ray on the
+// 1,024,000-triangle path scene, every box the ray meets), and the eight box
+// tests of one node are independent work for the scheduler.  The collapse is
+// the SAH-optimal one (the dynamic programme of Ylitie, Karras and Laine,
+// "Efficient incoherent ray traversal on GPUs through compressed wide BVHs",
+// HPG 2017); the child boxes stay in 32-bit floats.
+//
+// Exactness.  The collapse keeps the binary tree's padded child boxes as
+// they are and only drops inner levels, so every triangle still sits inside
+// the boxes above it.  The slab test is the two-wide walk's, plane for plane
+// (t = (plane - o) * inv, far distance widened by 1 + 2 gamma(3)); the near
+// plane of each axis is picked by the sign of inv instead of a min/max of
+// the two planes' distances, which is the same value (the rounded
+// subtraction and product are monotone, and lo <= hi).  The leaf tests are
+// the same exact tests, so every walk returns the same prim, t, b1, b2 or
+// occlusion bit for bit.
+//
+// Layout (built lazily on the first walk-5 batch of a scene, 240 bytes per
+// node: per axis the eight low planes, then the eight high planes; the
+// references; the slots' triangle masks):
+//   * inner children of a node are contiguous from child_base, in slot
+//     order; a child's index is child_base + popc(imask below its slot);
+//   * the triangles of a node's leaf children are contiguous from tri_base
+//     (a second copy of the records in this order, after the degenerate
+//     records that every ray tests); a slot's 32-bit mask marks its leaf's
+//     triangles (zero for an inner or empty slot);
+//   * children sit in slots by the direction octant that meets them first
+//     (a greedy assignment of child centroids to the eight octant
+//     directions), so visiting slots in the order slot ^ octant walks the
+//     children roughly front to back without sorting distances.
+// A lane reads only the near and far planes its octant needs, by address.
+// Traversal state per lane: the current node group (child base, the hit
+// inner children in visiting order, the group's nearest entry distance), the
+// pending triangle mask of the last node, and a private stack of groups.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "pbg_internal.h"
+#include "pbg_tma.cuh"
+#include "pbg_walk.cuh"
+
+namespace pbg {
+
+struct __align__(16) WideNode {
+    float4 plane[12];  // per axis: lo[0-3], lo[4-7], hi[0-3], hi[4-7]
+    int4 refs;         // child_base | imask << 24, tri_base, 0, 0
+    uint4 tris[2];     // per slot: its leaf's triangles as bits of the node's triangle mask (0: inner or empty)
+};
+static_assert(sizeof(WideNode) == 240, "wide node is fifteen 16-byte words");
+
+namespace {
+
+constexpr int kWideWidth = 8;
+constexpr int kWideMaxLeaf = 7;    // triangles per leaf child (3 bits)
+constexpr int kWideMaxOffset = 31; // leaf offset within a node (5 bits)
+constexpr int kWideAbsorb = 4;     // subtrees of at most this many triangles may become one leaf
+constexpr float kWideTriCost = 0.3f;  // a triangle test against a wide node visit
+
+struct Item {
+    int32_t ref, cnt;  // binary child reference (>= 0 inner, else ~start) and leaf count
+    int32_t inner;     // an absorbed subtree's binary node (else -1)
+    float lo[3], hi[3];
+};
+
+float area(const Item& it) {
+    const float dx = it.hi[0] - it.lo[0], dy = it.hi[1] - it.lo[1], dz = it.hi[2] - it.lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// Record range [first, first + count) of each binary node's subtree (the
+// builder's leaf order keeps a subtree's records contiguous).
+struct Span {
+    int32_t first, count;
+};
+
+bool subtree_spans(const std::vector<BvhNode>& bin, std::vector<Span>* out) {
+    out->assign(bin.size(), Span{INT32_MAX, 0});
+    // children have larger indices than their parent in both builders
+    for (size_t i = bin.size(); i-- > 0;) {
+        const BvhNode& b = bin[i];
+        const int32_t ref[2] = {b.n3.x, b.n3.y}, cnt[2] = {b.n3.z, b.n3.w};
+        Span sp{INT32_MAX, 0};
+        for (int c = 0; c < 2; ++c) {
+            Span cs{INT32_MAX, 0};
+            if (ref[c] >= 0) {
+                if ((size_t)ref[c] <= i || (size_t)ref[c] >= bin.size()) return false;
+                cs = (*out)[(size_t)ref[c]];
+            } else if (cnt[c] > 0) {
+                cs = Span{~ref[c], cnt[c]};
+            }
+            if (cs.count == 0) continue;
+            if (sp.count > 0 && cs.first != sp.first + sp.count && sp.first != cs.first + cs.count) return false;
+            sp.first = std::min(sp.first, cs.first);
+            sp.count += cs.count;
+        }
+        (*out)[i] = sp;
+    }
+    return true;
+}
+
+// Child c of binary node n as an item (cnt 0 and ref < 0: an empty slot).
+Item child_item(const BvhNode& b, int c) {
+    Item it;
+    it.ref = c == 0 ? b.n3.x : b.n3.y;
+    it.cnt = it.ref >= 0 ? 0 : (c == 0 ? b.n3.z : b.n3.w);
+    it.inner = -1;
+    const float4 box = c == 0 ? b.n0 : b.n1;
+    it.lo[0] = box.x;
+    it.hi[0] = box.y;
+    it.lo[1] = box.z;
+    it.hi[1] = box.w;
+    it.lo[2] = c == 0 ? b.n2.x : b.n2.z;
+    it.hi[2] = c == 0 ? b.n2.y : b.n2.w;
+    return it;
+}
+
+bool empty_item(const Item& it) { return it.ref < 0 && it.cnt == 0; }
+
+// The SAH-optimal collapse (the dynamic programme of the compressed wide BVH
+// paper, with its node and triangle costs as parameters): cost[n][j] is the
+// least expected cost of binary node n's subtree when it may take j slots of
+// its wide parent -- as one wide node (a visit, then its children in eight
+// slots), as one leaf of all its triangles (at most `absorb`), or dissolved
+// into its two children's items with k and j - k slots.
+struct Plan {
+    float c_node, c_tri;
+    int absorb;
+    std::vector<float> cost;    // [n * 9 + j], j = 1..8
+    std::vector<int8_t> how;    // -1 wide node, -2 one leaf, -3 as with j - 1 slots, k >= 0: child 0 takes k
+    std::vector<int8_t> split;  // [n]: child 0's slots when n is a wide node
+    std::vector<float> area;    // [n]: surface area of n's box
+};
+
+float item_cost(const Plan& P, const std::vector<Span>& span, const Item& it, int k) {
+    if (empty_item(it)) return 0.f;
+    if (k < 1) return INFINITY;
+    if (it.ref < 0) return P.c_tri * (float)it.cnt * area(it);
+    (void)span;
+    return P.cost[(size_t)it.ref * 9 + (size_t)k];
+}
+
+// least cost of children a, b in j slots, and child 0's share
+float best_split(const Plan& P, const std::vector<Span>& span, const Item& a, const Item& b, int j, int* k_out) {
+    float best = INFINITY;
+    int bk = -1;
+    for (int k = 0; k <= j; ++k) {
+        const float c = item_cost(P, span, a, k) + item_cost(P, span, b, j - k);
+        if (c < best) {
+            best = c;
+            bk = k;
+        }
+    }
+    *k_out = bk;
+    return best;
+}
+
+void plan_collapse(const std::vector<BvhNode>& bin, const std::vector<Span>& span, Plan* P) {
+    const size_t nn = bin.size();
+    P->cost.assign(nn * 9, INFINITY);
+    P->how.assign(nn * 9, -1);
+    P->split.assign(nn, 4);
+    P->area.assign(nn, 0.f);
+    for (size_t i = nn; i-- > 0;) {  // children after parents: bottom up
+        const Item a = child_item(bin[i], 0), b = child_item(bin[i], 1);
+        Item u = a;
+        if (empty_item(a)) u = b;
+        for (int ax = 0; ax < 3; ++ax) {
+            if (!empty_item(a) && !empty_item(b)) {
+                u.lo[ax] = std::min(a.lo[ax], b.lo[ax]);
+                u.hi[ax] = std::max(a.hi[ax], b.hi[ax]);
+            }
+        }
+        const float ar = empty_item(a) && empty_item(b) ? 0.f : area(u);
+        P->area[i] = ar;
+        int k8 = 0;
+        const float as_node = P->c_node * ar + best_split(*P, span, a, b, kWideWidth, &k8);
+        P->split[i] = (int8_t)k8;
+        const float as_leaf = span[i].count <= P->absorb ? P->c_tri * (float)span[i].count * ar : INFINITY;
+        float* c = &P->cost[i * 9];
+        int8_t* h = &P->how[i * 9];
+        int k1 = 0;
+        const float s1 = best_split(*P, span, a, b, 1, &k1);
+        c[1] = as_node;
+        h[1] = -1;
+        if (as_leaf < c[1]) {
+            c[1] = as_leaf;
+            h[1] = -2;
+        }
+        if (s1 < c[1]) {
+            c[1] = s1;
+            h[1] = (int8_t)k1;
+        }
+        for (int j = 2; j <= kWideWidth; ++j) {
+            int kj = 0;
+            const float sj = best_split(*P, span, a, b, j, &kj);
+            if (sj < c[j - 1]) {
+                c[j] = sj;
+                h[j] = (int8_t)kj;
+            } else {
+                c[j] = c[j - 1];
+                h[j] = -3;
+            }
+        }
+    }
+}
+
+// The items of `it` in at most j slots, as the plan decided.
+void emit(const std::vector<BvhNode>& bin, const std::vector<Span>& span, const Plan& P, const Item& it, int j,
+          std::vector<Item>* out) {
+    if (empty_item(it) || j < 1) return;
+    if (it.ref < 0) {
+        out->push_back(it);
+        return;
+    }
+    const size_t n = (size_t)it.ref;
+    int h = P.how[n * 9 + (size_t)j];
+    while (h == -3) h = P.how[n * 9 + (size_t)(--j)];
+    if (h == -1) {
+        out->push_back(it);
+    } else if (h == -2) {
+        Item leaf = it;
+        leaf.ref = ~span[n].first;
+        leaf.cnt = span[n].count;
+        leaf.inner = it.ref;
+        out->push_back(leaf);
+    } else {
+        emit(bin, span, P, child_item(bin[n], 0), h, out);
+        emit(bin, span, P, child_item(bin[n], 1), j - h, out);
+    }
+}
+
+// A wide node's items for binary node n.
+void node_items(const std::vector<BvhNode>& bin, const std::vector<Span>& span, const Plan& P, int32_t n,
+                std::vector<Item>* out) {
+    const int k = P.split[(size_t)n];
+    emit(bin, span, P, child_item(bin[(size_t)n], 0), k, out);
+    emit(bin, span, P, child_item(bin[(size_t)n], 1), kWideWidth - k, out);
+}
+
+// Slots by octant: the child that a ray of octant s meets first goes to
+// slot s (greedy on dot(centroid - node centroid, octant direction)).
+void assign_slots(const std::vector<Item>& items, int slot_of[kWideWidth]) {
+    const int k = (int)items.size();
+    float cmin[3], cmax[3];
+    for (int a = 0; a < 3; ++a) {
+        cmin[a] = INFINITY;
+        cmax[a] = -INFINITY;
+        for (const Item& it : items) {
+            cmin[a] = std::min(cmin[a], it.lo[a]);
+            cmax[a] = std::max(cmax[a], it.hi[a]);
+        }
+    }
+    struct Cost {
+        float c;
+        int item, slot;
+    };
+    std::vector<Cost> cost;
+    for (int i = 0; i < k; ++i)
+        for (int s = 0; s < kWideWidth; ++s) {
+            float c = 0.f;
+            for (int a = 0; a < 3; ++a) {
+                const float rel = 0.5f * (items[i].lo[a] + items[i].hi[a]) - 0.5f * (cmin[a] + cmax[a]);
+                c += (s >> a & 1) ? -rel : rel;
+            }
+            cost.push_back({c, i, s});
+        }
+    std::stable_sort(cost.begin(), cost.end(), [](const Cost& x, const Cost& y) { return x.c < y.c; });
+    bool used_item[kWideWidth] = {}, used_slot[kWideWidth] = {};
+    for (int i = 0; i < kWideWidth; ++i) slot_of[i] = -1;
+    for (const Cost& c : cost) {
+        if (used_item[c.item] || used_slot[c.slot]) continue;
+        used_item[c.item] = used_slot[c.slot] = true;
+        slot_of[c.item] = c.slot;
+    }
+}
+
+}  // namespace
+
+// The collapse: wide nodes breadth first (root 0) and, per record position
+// of the wide copy, the position of that record in the binary tree's order.
+// False when the tree does not fit the format (a leaf of more than 7
+// triangles, a node's leaf triangles beyond offset 31, 2^24 nodes or more):
+// the scene then keeps the two-wide walks.
+bool collapse_wide(const std::vector<BvhNode>& bin, int32_t unculled, int64_t ntri, int absorb, float c_tri,
+                   std::vector<WideNode>* out, std::vector<int32_t>* src) {
+    out->clear();
+    src->clear();
+    if (bin.empty()) return false;
+    std::vector<Span> span;
+    if (!subtree_spans(bin, &span)) return false;
+    Plan plan;
+    plan.c_node = 1.f;
+    plan.c_tri = c_tri;
+    plan.absorb = std::min(absorb, kWideMaxLeaf);
+    plan_collapse(bin, span, &plan);
+    src->reserve((size_t)ntri);
+    for (int32_t i = 0; i < unculled; ++i) src->push_back(i);
+    struct Pending {
+        int32_t wide, bin;
+    };
+    std::vector<Pending> queue{{0, 0}};
+    out->resize(1);
+    std::vector<Item> items;
+    for (size_t head = 0; head < queue.size(); ++head) {
+        const Pending pd = queue[head];
+        items.clear();
+        node_items(bin, span, plan, pd.bin, &items);
+        if ((int)items.size() > kWideWidth) return false;
+        // a node's leaf triangles fit the 32-bit triangle mask: the largest
+        // absorbed subtrees go back to being inner children until they do
+        int32_t leaf_tris = 0;
+        for (const Item& it : items) leaf_tris += it.ref < 0 ? it.cnt : 0;
+        while (leaf_tris > 32) {
+            int big = -1;
+            for (int i = 0; i < (int)items.size(); ++i)
+                if (items[(size_t)i].inner >= 0 && (big < 0 || items[(size_t)i].cnt > items[(size_t)big].cnt)) big = i;
+            if (big < 0) return false;
+            leaf_tris -= items[(size_t)big].cnt;
+            items[(size_t)big].ref = items[(size_t)big].inner;
+            items[(size_t)big].cnt = 0;
+            items[(size_t)big].inner = -1;
+        }
+        int slot_of[kWideWidth];
+        assign_slots(items, slot_of);
+        int item_at[kWideWidth];
+        for (int s = 0; s < kWideWidth; ++s) item_at[s] = -1;
+        for (int i = 0; i < (int)items.size(); ++i) item_at[slot_of[i]] = i;
+
+        WideNode wn;
+        memset(&wn, 0, sizeof(wn));  // an empty slot: a zero box, neither leaf nor inner child
+        float* pl = reinterpret_cast<float*>(wn.plane);
+        uint32_t tmask[kWideWidth];
+        uint32_t imask = 0;
+        const int32_t child_base = (int32_t)out->size();
+        const int32_t tri_base = (int32_t)src->size();
+        int32_t n_inner = 0;
+        for (int s = 0; s < kWideWidth; ++s) {
+            tmask[s] = 0;
+            const int i = item_at[s];
+            if (i < 0) continue;
+            const Item& it = items[(size_t)i];
+            for (int a = 0; a < 3; ++a) {
+                pl[a * 16 + s] = it.lo[a];
+                pl[a * 16 + 8 + s] = it.hi[a];
+            }
+            if (it.ref >= 0) {
+                imask |= 1u << s;
+                queue.push_back({child_base + n_inner, it.ref});
+                ++n_inner;
+            } else {
+                const int32_t off = (int32_t)src->size() - tri_base;
+                if (it.cnt > kWideMaxLeaf || off > kWideMaxOffset || off + it.cnt > 32) return false;
+                tmask[s] = (uint32_t)(((1ull << it.cnt) - 1ull) << off);
+                for (int32_t r = 0; r < it.cnt; ++r) src->push_back(~it.ref + r);
+            }
+        }
+        out->resize(out->size() + (size_t)n_inner);
+        if (out->size() >= (size_t)1 << 24) return false;  // child_base shares its word with imask
+        wn.refs.x = (int32_t)((uint32_t)child_base | imask << 24);
+        wn.refs.y = tri_base;
+        wn.tris[0] = make_uint4(tmask[0], tmask[1], tmask[2], tmask[3]);
+        wn.tris[1] = make_uint4(tmask[4], tmask[5], tmask[6], tmask[7]);
+        (*out)[(size_t)pd.wide] = wn;
+    }
+    return (int64_t)src->size() == ntri;
+}
+
+__global__ void gather_records_kernel(const TriRec* __restrict__ in, const int32_t* __restrict__ src, int64_t n,
+                                      TriRec* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[src[i]];
+}
+
+int ensure_wide(pbg_scene* s, bool* available, cudaStream_t st) {
+    *available = false;
+    if (s->wide_state < 0) return PBG_OK;
+    if (s->wide_state > 0) {
+        *available = true;
+        return PBG_OK;
+    }
+    s->wide_state = -1;
+    if (s->bvh_nodes <= 0) return PBG_OK;
+    if (s->host_nodes.empty()) {  // a tree built on the device: collapsed on the host
+        s->host_nodes.resize((size_t)s->bvh_nodes);
+        PBG_CUDA(cudaStreamSynchronize(st));
+        PBG_CUDA(cudaMemcpy(s->host_nodes.data(), s->bvh.ptr, s->host_nodes.size() * sizeof(BvhNode),
+                            cudaMemcpyDeviceToHost));
+    }
+    std::vector<WideNode> wn;
+    std::vector<int32_t> src;
+    if (!collapse_wide(s->host_nodes, s->unculled, s->ntri, kWideAbsorb, kWideTriCost, &wn, &src)) return PBG_OK;
+    int rc;
+    DeviceBuffer dsrc;
+    if ((rc = ensure(s->wide, wn.size() * sizeof(WideNode))) ||
+        (rc = ensure(s->tris_wide, (size_t)std::max<int64_t>(s->ntri, 1) * sizeof(TriRec))) ||
+        (rc = ensure(dsrc, (size_t)std::max<int64_t>(s->ntri, 1) * sizeof(int32_t))))
+        return rc;
+    cudaError_t e = cudaMemcpy(s->wide.ptr, wn.data(), wn.size() * sizeof(WideNode), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && s->ntri > 0)
+        e = cudaMemcpy(dsrc.ptr, src.data(), src.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && s->ntri > 0) {
+        gather_records_kernel<<<(unsigned)((s->ntri + 255) / 256), 256, 0, st>>>(
+            (const TriRec*)s->tris.ptr, (const int32_t*)dsrc.ptr, s->ntri, (TriRec*)s->tris_wide.ptr);
+        e = cudaGetLastError();
+        // later batches may run on other streams: the copy is complete before any of them
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        s->counters.kernel_launches += 1;
+    }
+    release(dsrc);
+    if (e != cudaSuccess) return cuda_status(e, "wide BVH upload");
+    s->wide_nodes = (int64_t)wn.size();
+    s->wide_state = 1;
+    *available = true;
+    return PBG_OK;
+}
+
+constexpr int kWideThreads = 128;
+constexpr int kWideMinBlocks = 8;
+constexpr int kWideStack = 64;
+
+// Three-input max / min (one instruction on sm_100 and later); NaN inputs
+// are ignored as by fmaxf / fminf.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// A group's entry distance kept in the upper 16 bits of a stack word,
+// rounded toward -infinity (a popped group is skipped only when it lies
+// beyond the hit found).
+__device__ __forceinline__ uint32_t dist_bits_down(float t) {
+    uint32_t b = __float_as_uint(t);
+    if (b & 0x80000000u) b += 0xffffu;  // negative: a larger magnitude is smaller
+    return b & 0xffff0000u;
+}
+
+template <bool ANY, bool STATS>
+__global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
+    wide_persistent_kernel(const WideNode* __restrict__ nodes, const TriRec* __restrict__ tris,
+                           int32_t unculled, const float4* __restrict__ ro, const float4* __restrict__ rd,
+                           const uint8_t* __restrict__ valid, const int32_t* __restrict__ perm, int64_t n,
+                           int32_t* __restrict__ prim_out, float* __restrict__ t_out,
+                           float* __restrict__ b1_out, float* __restrict__ b2_out, uint8_t* __restrict__ occ,
+                           int* status, unsigned long long* next, unsigned long long* wcount) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    int2 stack[kWideStack];  // (child base, hits | imask << 8 | distance bits)
+    int sp = 0;
+    int64_t ray = 0;
+    bool has = false, exhausted = false, ok = true;
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+    RayInv ri{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float nd = 0.f;
+    WalkHit h{0.f, 0.f, 0.f, -1};
+    uint32_t oct = 0;
+    int32_t gbase = 0;          // the current group: inner children from gbase
+    uint32_t ghits = 0, gimask = 0;  // hit children in visiting order, the node's inner mask
+    float gtn = 0.f;            // the group's nearest entry distance
+    int32_t tbase = 0;          // pending triangles of the last node: records tbase + bit
+    uint32_t tmask = 0;
+    int32_t tbase2 = 0;         // a second node's triangles, found while others searched
+    uint32_t tmask2 = 0;
+    int32_t rcnt = 0;           // pending degenerate records [0, rcnt)
+    WorkCount wc;
+
+    auto finish = [&]() {
+        if (ANY) {
+            occ[ray] = h.prim >= 0 ? 1 : 0;
+            if (prim_out) prim_out[ray] = h.prim;
+        } else {
+            const bool hit = h.prim >= 0;
+            prim_out[ray] = h.prim;
+            t_out[ray] = hit ? h.t : 0.f;
+            b1_out[ray] = hit ? h.b1 : 0.f;
+            b2_out[ray] = hit ? h.b2 : 0.f;
+        }
+        if (!ok) atomicAdd(&status[kStatusOverflow], 1);
+        has = false;
+    };
+
+    for (;;) {
+        // refill the lanes whose ray is done
+        const unsigned need = __ballot_sync(full, !has && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(need));
+            base = __shfl_sync(full, base, leader);
+            if (!has && !exhausted) {
+                const int64_t slot = (int64_t)base + __popc(need & lt);
+                if (slot >= n) {
+                    exhausted = true;
+                } else {
+                    ray = perm ? (int64_t)perm[slot] : slot;
+                    if (valid != nullptr && valid[ray] == 0) {
+                        h = WalkHit{0.f, 0.f, 0.f, -1};
+                        ok = true;
+                        finish();  // invalid: a miss, no walk
+                    } else {
+                        o = ro[ray];
+                        d = rd[ray];
+                        nd = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+                        ri = RayInv{o.x, o.y, o.z, safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+                        oct = (__float_as_uint(ri.ix) >> 31) | (__float_as_uint(ri.iy) >> 31) << 1 |
+                              (__float_as_uint(ri.iz) >> 31) << 2;
+                        h = WalkHit{d.w, 0.f, 0.f, -1};
+                        sp = 0;
+                        ok = true;
+                        gbase = 0;  // the root: slot 0 of a group whose only inner child is node 0
+                        gimask = 1u;
+                        ghits = 1u << oct;
+                        gtn = -INFINITY;
+                        tmask = 0;
+                        tmask2 = 0;
+                        rcnt = unculled;  // degenerate records first
+                        has = true;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(full, has)) {
+            if (__all_sync(full, exhausted)) break;
+            continue;
+        }
+        // nodes until every lane holds triangles or has ended its ray
+        for (;;) {
+            const bool searching = has && tmask == 0 && rcnt == 0;
+            if (!__any_sync(full, searching)) break;
+            // a lane that holds triangles walks on for one more node's
+            // triangles while others search, so the tests below run with
+            // fuller warps
+            if (!has || tmask2 != 0 || rcnt != 0) continue;
+            if (ghits != 0 && gtn > h.t) ghits = 0;  // the whole group lies beyond the hit found
+            if (ghits == 0) {
+                bool got = false;
+                while (sp > 0) {
+                    --sp;
+                    const int2 e = stack[sp];
+                    const float te = __uint_as_float((uint32_t)e.y & 0xffff0000u);
+                    if (te <= h.t) {
+                        gbase = e.x;
+                        ghits = (uint32_t)e.y & 0xffu;
+                        gimask = ((uint32_t)e.y >> 8) & 0xffu;
+                        gtn = te;
+                        got = true;
+                        break;
+                    }
+                }
+                if (!got && tmask == 0) finish();  // nothing left to walk or test
+                continue;
+            }
+            const int pos = __ffs(ghits) - 1;
+            const uint32_t rest = ghits & (ghits - 1u);
+            const int cslot = pos ^ (int)oct;
+            const int32_t child = gbase + __popc(gimask & ((1u << cslot) - 1u));
+
+            const float4* np = reinterpret_cast<const float4*>(nodes + child);
+            const int4 r = __ldg(reinterpret_cast<const int4*>(np + 12));
+            // the near and far planes of the ray's octant, eight slots each
+            const int xo = (int)(oct & 1u) * 2, yo = 4 + (int)(oct & 2u), zo = 8 + (int)(oct & 4u) / 2;
+            const float4 nx0 = __ldg(np + xo), nx1 = __ldg(np + xo + 1);
+            const float4 fx0 = __ldg(np + (2 - xo)), fx1 = __ldg(np + (3 - xo));
+            const float4 ny0 = __ldg(np + yo), ny1 = __ldg(np + yo + 1);
+            const float4 fy0 = __ldg(np + (10 - yo)), fy1 = __ldg(np + (11 - yo));
+            const float4 nz0 = __ldg(np + zo), nz1 = __ldg(np + zo + 1);
+            const float4 fz0 = __ldg(np + (18 - zo)), fz1 = __ldg(np + (19 - zo));
+            const float nxs[8] = {nx0.x, nx0.y, nx0.z, nx0.w, nx1.x, nx1.y, nx1.z, nx1.w};
+            const float fxs[8] = {fx0.x, fx0.y, fx0.z, fx0.w, fx1.x, fx1.y, fx1.z, fx1.w};
+            const float nys[8] = {ny0.x, ny0.y, ny0.z, ny0.w, ny1.x, ny1.y, ny1.z, ny1.w};
+            const float fys[8] = {fy0.x, fy0.y, fy0.z, fy0.w, fy1.x, fy1.y, fy1.z, fy1.w};
+            const float nzs[8] = {nz0.x, nz0.y, nz0.z, nz0.w, nz1.x, nz1.y, nz1.z, nz1.w};
+            const float fzs[8] = {fz0.x, fz0.y, fz0.z, fz0.w, fz1.x, fz1.y, fz1.z, fz1.w};
+            const uint4 lt0 = __ldg(reinterpret_cast<const uint4*>(np + 13));
+            const uint4 lt1 = __ldg(reinterpret_cast<const uint4*>(np + 14));
+            const uint32_t lts[8] = {lt0.x, lt0.y, lt0.z, lt0.w, lt1.x, lt1.y, lt1.z, lt1.w};
+            const uint32_t imask = (uint32_t)r.x >> 24;
+            uint32_t hits = 0, tm = 0;
+            float ntn = INFINITY;  // nearest entry over the hit children: a bound for the group
+#pragma unroll
+            for (int k = 0; k < kWideWidth; ++k) {
+                const float tnx = __fmul_rn(__fsub_rn(nxs[k], ri.ox), ri.ix);
+                const float tfx = __fmul_rn(__fsub_rn(fxs[k], ri.ox), ri.ix);
+                const float tny = __fmul_rn(__fsub_rn(nys[k], ri.oy), ri.iy);
+                const float tfy = __fmul_rn(__fsub_rn(fys[k], ri.oy), ri.iy);
+                const float tnz = __fmul_rn(__fsub_rn(nzs[k], ri.oz), ri.iz);
+                const float tfz = __fmul_rn(__fsub_rn(fzs[k], ri.oz), ri.iz);
+                const float tn = fmax3(tnx, tny, fmaxf(tnz, o.w));
+                const float tf = fmin3(tfx, tfy, fminf(tfz, h.t));
+                const bool hit = tn <= fmaf(fabsf(tf), 2.f * 3.f * 0x1p-24f / (1.f - 3.f * 0x1p-24f), tf);
+                if (hit) {
+                    hits |= 1u << k;
+                    tm |= lts[k];
+                    if (!ANY) ntn = fminf(ntn, tn);
+                }
+            }
+            if (STATS) {
+                uint32_t occupied = imask;
+#pragma unroll
+                for (int k = 0; k < kWideWidth; ++k) occupied |= lts[k] != 0u ? 1u << k : 0u;
+                wc.node += __popc(occupied);
+            }
+            // hit inner children in visiting order: bit (slot ^ octant)
+            uint32_t ih = hits & imask;
+            if (oct & 1u) ih = ((ih & 0x55u) << 1) | ((ih >> 1) & 0x55u);
+            if (oct & 2u) ih = ((ih & 0x33u) << 2) | ((ih >> 2) & 0x33u);
+            if (oct & 4u) ih = ((ih & 0x0fu) << 4) | ((ih >> 4) & 0x0fu);
+            if (ih) {
+                if (rest) {
+                    if (sp < kWideStack) {
+                        stack[sp] = make_int2(gbase, (int)(rest | gimask << 8 | dist_bits_down(gtn)));
+                        ++sp;
+                    } else {
+                        ok = false;
+                    }
+                }
+                gbase = r.x & 0xffffff;
+                ghits = ih;
+                gimask = imask;
+                gtn = ANY ? -INFINITY : ntn;
+            } else {
+                ghits = rest;
+            }
+            if (tmask == 0) {
+                tbase = r.y;
+                tmask = tm;
+            } else {
+                tbase2 = r.y;
+                tmask2 = tm;
+            }
+        }
+        // the triangle tests, converged
+        if (has && (tmask != 0 || tmask2 != 0 || rcnt != 0)) {
+            if (STATS) wc.leaf++;
+            bool done = false;
+            if (rcnt) {
+                done = test_run<ANY, STATS>(tris, 0, rcnt, o, d, nd, h, wc);
+                rcnt = 0;
+            }
+            while (!done && tmask) {
+                const int b = __ffs(tmask) - 1;
+                tmask &= tmask - 1u;
+                done = test_run<ANY, STATS>(tris, tbase + b, 1, o, d, nd, h, wc);
+            }
+            while (!done && tmask2) {
+                const int b = __ffs(tmask2) - 1;
+                tmask2 &= tmask2 - 1u;
+                done = test_run<ANY, STATS>(tris, tbase2 + b, 1, o, d, nd, h, wc);
+            }
+            tmask = 0;
+            tmask2 = 0;
+            if (done) finish();
+        }
+    }
+    if (STATS) wc.flush(wcount);
+}
+
+template <bool ANY>
+int wide_launch(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
+                int64_t n, int32_t* prim, float* t, float* b1, float* b2, uint8_t* occ, cudaStream_t st) {
+    Work& w = s->work;
+    int rc = ensure(w.counters, 64);
+    if (rc) return rc;
+    unsigned long long* next = (unsigned long long*)w.counters.ptr;
+    PBG_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wide_persistent_kernel<ANY, false>, kWideThreads, 0);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    int64_t blocks = (int64_t)std::max(per_sm, 1) * sms;
+    blocks = std::min<int64_t>(blocks, (n + kWideThreads - 1) / kWideThreads);
+    const bool stats = s->prof.level >= 2;
+    auto kern = stats ? wide_persistent_kernel<ANY, true> : wide_persistent_kernel<ANY, false>;
+    kern<<<(unsigned)blocks, kWideThreads, 0, st>>>((const WideNode*)s->wide.ptr, (const TriRec*)s->tris_wide.ptr,
+                                                     s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ,
+                                                     (int*)s->err.ptr, next,
+                                                     stats ? (unsigned long long*)s->workc.ptr : nullptr);
+    return PBG_OK;
+}
+
+int wide_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
+                 int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
+    return wide_launch<false>(s, o, d, valid, perm, n, prim, t, b1, b2, nullptr, st);
+}
+
+int wide_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
+                  int64_t n, int32_t* occluders, uint8_t* occ, cudaStream_t st) {
+    return wide_launch<true>(s, o, d, valid, perm, n, occluders, nullptr, nullptr, nullptr, occ, st);
+}
+
+}  // namespace pbg
