@@ -67,13 +67,17 @@ FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 148_000_000, "ray-bvh": 116_000_00
 # the frame's camera and first shadow batch)
 # dram__bytes_read.sum + dram__bytes_write.sum per traversal launch of the
 # path frame: the average over the 12 traversal launches of one full-size
-# frame (ncu, the automatic walk, first frame of the run)
-PATH_LAUNCH_DRAM_BYTES = 294_658_368
-# smsp__issue_active of the persistent walk on the path frame's bounces
-# (ncu --set full, bounce 2 of the warm-up frame: nearest, any-hit)
-PATH_ISSUE_ACTIVE = {"bvh_persistent_kernel (nearest)": 0.67, "bvh_persistent_kernel (any-hit)": 0.66}
+# frame (ncu, the walks the autotuner picked, the timed frame of the run)
+PATH_LAUNCH_DRAM_BYTES = 202_533_738
+# smsp__issue_active of the bounce walks (ncu --set full, bounce 1 of the
+# first frame of a 256x256 frame of the same scene: nearest, any-hit)
+PATH_ISSUE_ACTIVE = {"wide_persistent_kernel (nearest)": 0.71, "wide_persistent_kernel (any-hit)": 0.59,
+                     "bvh_persistent_kernel (nearest)": 0.72, "bvh_persistent_kernel (any-hit)": 0.50}
 FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, nearest)": 0.72,
                                        "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.73}}
+# the kernel of each ray-bvh walk (pbg_params.walk)
+WALK_KERNEL = {1: "bvh_kernel", 2: "bvh_persistent_kernel", 3: "bvh_packet_kernel (sorted)",
+               4: "bvh_packet_kernel", 5: "wide_persistent_kernel"}
 L2_BYTES = 129 * 1024 * 1024
 CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)
 
@@ -706,7 +710,10 @@ def run_gpu_path(args, rank, world, dev):
                 "api": "pbg_render (camera, light and parameters in, RGB image out; wall time of the host call)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 5), "traffic": PATH_LAUNCH_DRAM_BYTES,
-                     "kernel": "traversal launch (bvh_kernel on bounce 0, bvh_persistent_kernel on bounces 1-5)",
+                     "kernel": "traversal launch (" + ", ".join(
+                         f"{k}: {WALK_KERNEL.get(v['best'].get('walk'), 'walk %s' % v['best'].get('walk'))}"
+                         for k, v in tuned.items()) + ")" if tuned else
+                     "traversal launch (the automatic walks: bvh_kernel on bounce 0, bvh_persistent_kernel after)",
                      "launches_per_step": round(launches_per_frame, 2),
                      "algorithmic_bytes_per_launch": int(per_launch_bytes),
                      "avg_launch_ms": round(avg_launch_ms, 4), "peak_source": peak_kind + " (of measured copy)",

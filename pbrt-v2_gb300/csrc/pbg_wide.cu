@@ -138,23 +138,25 @@ struct Plan {
     std::vector<float> cost;    // [n * 9 + j], j = 1..8
     std::vector<int8_t> how;    // -1 wide node, -2 one leaf, -3 as with j - 1 slots, k >= 0: child 0 takes k
     std::vector<int8_t> split;  // [n]: child 0's slots when n is a wide node
-    std::vector<float> area;    // [n]: surface area of n's box
 };
 
-float item_cost(const Plan& P, const std::vector<Span>& span, const Item& it, int k) {
-    if (empty_item(it)) return 0.f;
-    if (k < 1) return INFINITY;
-    if (it.ref < 0) return P.c_tri * (float)it.cnt * area(it);
-    (void)span;
-    return P.cost[(size_t)it.ref * 9 + (size_t)k];
+// item costs in 0..8 slots (0: only an empty slot fits in none)
+void item_costs(const Plan& P, const Item& it, float* c) {
+    if (empty_item(it)) {
+        for (int k = 0; k <= kWideWidth; ++k) c[k] = 0.f;
+        return;
+    }
+    c[0] = INFINITY;
+    const float leaf = it.ref < 0 ? P.c_tri * (float)it.cnt * area(it) : 0.f;
+    for (int k = 1; k <= kWideWidth; ++k) c[k] = it.ref < 0 ? leaf : P.cost[(size_t)it.ref * 9 + (size_t)k];
 }
 
-// least cost of children a, b in j slots, and child 0's share
-float best_split(const Plan& P, const std::vector<Span>& span, const Item& a, const Item& b, int j, int* k_out) {
+// least cost of two children in j slots (child 0 takes *k_out of them)
+float best_split(const float* ca, const float* cb, int j, int* k_out) {
     float best = INFINITY;
     int bk = -1;
     for (int k = 0; k <= j; ++k) {
-        const float c = item_cost(P, span, a, k) + item_cost(P, span, b, j - k);
+        const float c = ca[k] + cb[j - k];
         if (c < best) {
             best = c;
             bk = k;
@@ -169,27 +171,26 @@ void plan_collapse(const std::vector<BvhNode>& bin, const std::vector<Span>& spa
     P->cost.assign(nn * 9, INFINITY);
     P->how.assign(nn * 9, -1);
     P->split.assign(nn, 4);
-    P->area.assign(nn, 0.f);
     for (size_t i = nn; i-- > 0;) {  // children after parents: bottom up
         const Item a = child_item(bin[i], 0), b = child_item(bin[i], 1);
-        Item u = a;
-        if (empty_item(a)) u = b;
-        for (int ax = 0; ax < 3; ++ax) {
-            if (!empty_item(a) && !empty_item(b)) {
+        Item u = empty_item(a) ? b : a;
+        if (!empty_item(a) && !empty_item(b))
+            for (int ax = 0; ax < 3; ++ax) {
                 u.lo[ax] = std::min(a.lo[ax], b.lo[ax]);
                 u.hi[ax] = std::max(a.hi[ax], b.hi[ax]);
             }
-        }
         const float ar = empty_item(a) && empty_item(b) ? 0.f : area(u);
-        P->area[i] = ar;
+        float ca[kWideWidth + 1], cb[kWideWidth + 1];
+        item_costs(*P, a, ca);
+        item_costs(*P, b, cb);
         int k8 = 0;
-        const float as_node = P->c_node * ar + best_split(*P, span, a, b, kWideWidth, &k8);
+        const float as_node = P->c_node * ar + best_split(ca, cb, kWideWidth, &k8);
         P->split[i] = (int8_t)k8;
         const float as_leaf = span[i].count <= P->absorb ? P->c_tri * (float)span[i].count * ar : INFINITY;
         float* c = &P->cost[i * 9];
         int8_t* h = &P->how[i * 9];
         int k1 = 0;
-        const float s1 = best_split(*P, span, a, b, 1, &k1);
+        const float s1 = best_split(ca, cb, 1, &k1);
         c[1] = as_node;
         h[1] = -1;
         if (as_leaf < c[1]) {
@@ -202,7 +203,7 @@ void plan_collapse(const std::vector<BvhNode>& bin, const std::vector<Span>& spa
         }
         for (int j = 2; j <= kWideWidth; ++j) {
             int kj = 0;
-            const float sj = best_split(*P, span, a, b, j, &kj);
+            const float sj = best_split(ca, cb, j, &kj);
             if (sj < c[j - 1]) {
                 c[j] = sj;
                 h[j] = (int8_t)kj;
@@ -260,27 +261,37 @@ void assign_slots(const std::vector<Item>& items, int slot_of[kWideWidth]) {
             cmax[a] = std::max(cmax[a], it.hi[a]);
         }
     }
-    struct Cost {
-        float c;
-        int item, slot;
-    };
-    std::vector<Cost> cost;
+    float rel[kWideWidth][3];
     for (int i = 0; i < k; ++i)
-        for (int s = 0; s < kWideWidth; ++s) {
-            float c = 0.f;
-            for (int a = 0; a < 3; ++a) {
-                const float rel = 0.5f * (items[i].lo[a] + items[i].hi[a]) - 0.5f * (cmin[a] + cmax[a]);
-                c += (s >> a & 1) ? -rel : rel;
+        for (int a = 0; a < 3; ++a)
+            rel[i][a] = 0.5f * (items[(size_t)i].lo[a] + items[(size_t)i].hi[a]) - 0.5f * (cmin[a] + cmax[a]);
+    float cost[kWideWidth * kWideWidth];  // [child * 8 + slot]
+    for (int i = 0; i < kWideWidth; ++i)
+        for (int sl = 0; sl < kWideWidth; ++sl) {
+            float c = INFINITY;
+            if (i < k) {
+                c = 0.f;
+                for (int a = 0; a < 3; ++a) c += (sl >> a & 1) ? -rel[i][a] : rel[i][a];
             }
-            cost.push_back({c, i, s});
+            cost[i * kWideWidth + sl] = c;
         }
-    std::stable_sort(cost.begin(), cost.end(), [](const Cost& x, const Cost& y) { return x.c < y.c; });
-    bool used_item[kWideWidth] = {}, used_slot[kWideWidth] = {};
+    // greedy: the cheapest (child, slot) pair left, ties to the first in
+    // child-major order
     for (int i = 0; i < kWideWidth; ++i) slot_of[i] = -1;
-    for (const Cost& c : cost) {
-        if (used_item[c.item] || used_slot[c.slot]) continue;
-        used_item[c.item] = used_slot[c.slot] = true;
-        slot_of[c.item] = c.slot;
+    for (int round = 0; round < k; ++round) {
+        int best = 0;
+        float bv = cost[0];
+        for (int t = 1; t < kWideWidth * kWideWidth; ++t) {
+            const bool lt = cost[t] < bv;
+            bv = lt ? cost[t] : bv;
+            best = lt ? t : best;
+        }
+        const int i = best / kWideWidth, sl = best % kWideWidth;
+        slot_of[i] = sl;
+        for (int q = 0; q < kWideWidth; ++q) {
+            cost[i * kWideWidth + q] = INFINITY;
+            cost[q * kWideWidth + sl] = INFINITY;
+        }
     }
 }
 
@@ -425,7 +436,7 @@ int ensure_wide(pbg_scene* s, bool* available, cudaStream_t st) {
 }
 
 constexpr int kWideThreads = 128;
-constexpr int kWideMinBlocks = 8;
+constexpr int kWideMinBlocks = 7;  // CTAs per SM: 7 measured best of 5, 6, 7, 8
 constexpr int kWideStack = 64;
 
 // Three-input max / min (one instruction on sm_100 and later); NaN inputs
