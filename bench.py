@@ -77,7 +77,7 @@ FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, neare
                                        "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.73}}
 # the kernel of each ray-bvh walk (pbg_params.walk)
 WALK_KERNEL = {1: "bvh_kernel", 2: "bvh_persistent_kernel", 3: "bvh_packet_kernel (sorted)",
-               4: "bvh_packet_kernel", 5: "wide_persistent_kernel"}
+               4: "bvh_packet_kernel", 5: "wide_persistent_kernel", 6: "wide_persistent_kernel (warp-spread triangle tests)"}
 L2_BYTES = 129 * 1024 * 1024
 CAMERA = dict(eye=(0.0, 9.0, -14.0), target=(0.0, 0.0, 0.0), fov=50.0)
 
@@ -1340,7 +1340,8 @@ def main():
                     help="rayhierarchy: levels walked by 32-triangle clusters (0 = down to the leaves' parents, <0 = off)")
     ap.add_argument("--walk", type=int, default=0,
                     help="ray-bvh: 0 automatic (or tuned), 1 one thread per ray, 2 persistent warps, "
-                         "3 warp packets over the ray hierarchy's leaves")
+                         "3 warp packets over the ray hierarchy's leaves, 4 warp packets in the caller's order, "
+                         "5 persistent warps over the eight-wide tree, 6 the same with warp-spread triangle tests")
     ap.add_argument("--learn-steps", type=int, default=0, help="SGD steps per frame (0 = 8)")
     ap.add_argument("--learn-lr", type=float, default=0.0, help="learning rate (0 = 0.05)")
     ap.add_argument("--learn-margin", type=float, default=0.0,

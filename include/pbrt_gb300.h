@@ -81,9 +81,10 @@ typedef struct pbg_params {
                            * packet per leaf (rayBVH.cpp:615-836), 4 = the same
                            * packets over the batch in the caller's order,
                            * 5 = persistent warps over the tree collapsed to
-                           * eight children per node with 8-bit quantised
-                           * boxes (built on the first such batch; a tree
-                           * outside that format keeps walk 2).  Every walk
+                           * eight children per node (built on the first
+                           * such batch; a tree outside that format keeps
+                           * walk 2), 6 = the same with each warp's triangle
+                           * tests spread over all its lanes.  Every walk
                            * returns the same results bit for bit. */
     int32_t bvh_build;    /* ray-bvh: 0 = build the SAH tree on the device,
                            * 1 = on the host (the same splits; numbered depth
@@ -473,7 +474,7 @@ int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t M, 
  * of the scene's accelerator -- naive: CTAs per SM of the triangle splits
  * (2, 4, 8, 16); rayhierarchy: nodes of the seed level (64, 256, 1024) x
  * CTAs per SM of the grid-stride kernels (16, 32), per query kind; ray-bvh:
- * walk 1-5 (pbg_params.walk) for this batch class -- times each on `stream`
+ * walk 1-6 (pbg_params.walk) for this batch class -- times each on `stream`
  * (best of `reps` after a warm-up run), checks that every candidate's
  * results equal the first one's bit for bit (else PBG_ERR_INTERNAL and the
  * scene keeps its shapes), and keeps the fastest for later calls.
@@ -483,7 +484,7 @@ int pbg_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t M, 
 typedef struct pbg_tune_result {
     int32_t ncandidates;
     int32_t best;            /* index of the candidate kept */
-    int32_t setting[16][3];  /* naive {ctas}, rayhierarchy {seed nodes, grid}, ray-bvh {walk 1-5} */
+    int32_t setting[16][3];  /* naive {ctas}, rayhierarchy {seed nodes, grid}, ray-bvh {walk 1-6} */
     float ms[16];            /* device time of the batch with each candidate */
     uint64_t mismatches;     /* results that differed from the first candidate's (0) */
 } pbg_tune_result;

@@ -454,15 +454,16 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // (camera rays in image order and the shadow rays that follow them are
     // already coherent)
     const bool packet = (walk == 3 || walk == 4) && !pred;
-    // walk 5: the eight-wide tree (built on first use; a tree that does not
-    // fit its format keeps the persistent two-wide walk, as do ordered walks)
-    bool wide = walk == 5 && !pred;
+    // walks 5 and 6: the eight-wide tree (built on first use; a tree that
+    // does not fit its format keeps the persistent two-wide walk, as do
+    // ordered walks); walk 6 spreads a warp's triangle tests over its lanes
+    bool wide = (walk == 5 || walk == 6) && !pred;
     if (wide) {
         bool avail = false;
         if ((rc = ensure_wide(s, &avail, st))) return rc;
         wide = avail;
     }
-    const bool persistent = walk == 2 || ((walk == 3 || walk == 4 || walk == 5) && pred) || (walk == 5 && !wide);
+    const bool persistent = walk == 2 || (walk >= 3 && walk <= 6 && (pred || !(walk == 3 || walk == 4 || wide)));
     const int32_t* order = perm;  // packet walk 3: the ray hierarchy's leaf order (timed as the sort stage)
     if (packet && walk == 3 && !order) {
         int rc3 = ray_order(s, o, d, n, &order, st);
@@ -486,8 +487,8 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
         kern<<<(unsigned)blocks, kPacketThreads, 0, st>>>(nodes, tris, s->unculled, o, d, valid, order, n, prim, t,
                                                           b1, b2, occ, status, next, stats ? wc : nullptr);
     } else if (wide) {
-        rc = ANY ? wide_occluded(s, o, d, valid, perm, n, prim, occ, st)
-                 : wide_nearest(s, o, d, valid, perm, n, prim, t, b1, b2, st);
+        rc = ANY ? wide_occluded(s, walk == 6, o, d, valid, perm, n, prim, occ, st)
+                 : wide_nearest(s, walk == 6, o, d, valid, perm, n, prim, t, b1, b2, st);
         if (rc) return rc;
     } else if (persistent) {
         // persistent while-while walk: one counter word, zeroed per launch

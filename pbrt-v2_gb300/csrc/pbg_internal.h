@@ -81,7 +81,7 @@ struct Tunables {
     // most), CTAs per SM of the grid-stride kernels
     int rh_seed[2] = {256, 256};
     int rh_grid[2] = {32, 32};
-    int bvh_walk[2][2] = {{0, 0}, {0, 0}};  // ray-bvh [any-hit][incoherent]: 0 automatic, else pbg_params.walk's 1-5
+    int bvh_walk[2][2] = {{0, 0}, {0, 0}};  // ray-bvh [any-hit][incoherent]: 0 automatic, else pbg_params.walk's 1-6
 };
 
 // Per-batch device scratch owned by a scene.
@@ -112,7 +112,7 @@ struct pbg_scene {
     pbg::DeviceBuffer tri9;    // original vertices, float[9*ntri]
     pbg::DeviceBuffer uv6;     // optional per-triangle uvs, float[6*ntri]
     pbg::DeviceBuffer bvh;     // BvhNode[] (ray-bvh)
-    pbg::DeviceBuffer wide;    // WideNode[] (ray-bvh walk 5, built on its first batch)
+    pbg::DeviceBuffer wide;    // WideNode[] (ray-bvh walks 5 and 6, built on their first batch)
     pbg::DeviceBuffer tris_wide; // TriRec[ntri] in the wide tree's leaf order
     int64_t wide_nodes = 0;
     int wide_state = 0;        // 0 not built yet, 1 built, -1 the tree does not fit the wide format
@@ -160,13 +160,14 @@ int bvh_nearest_hinted(pbg_scene* s, const float4* o, const float4* d, const uin
                        const uint16_t* hint, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
 int bvh_occluded_hinted(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                         const uint16_t* hint, uint8_t* occ, int32_t* occluders, cudaStream_t st);
-// Walk 5 over the eight-wide tree; ensure_wide builds it on first use and
-// sets *available = false when the scene keeps the two-wide walks.
+// Walks 5 and 6 (coop) over the eight-wide tree; ensure_wide builds it on
+// first use and sets *available = false when the scene keeps the two-wide
+// walks.
 int ensure_wide(pbg_scene* s, bool* available, cudaStream_t st);
-int wide_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
-                 int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
-int wide_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
-                  int64_t n, int32_t* occluders, uint8_t* occ, cudaStream_t st);
+int wide_nearest(pbg_scene* s, bool coop, const float4* o, const float4* d, const uint8_t* valid,
+                 const int32_t* perm, int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
+int wide_occluded(pbg_scene* s, bool coop, const float4* o, const float4* d, const uint8_t* valid,
+                  const int32_t* perm, int64_t n, int32_t* occluders, uint8_t* occ, cudaStream_t st);
 int rh_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,
                int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
 int rh_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, int64_t n,

@@ -13,7 +13,9 @@
 //                 or not): one thread per ray, persistent warps, warp
 //                 packets over the ray hierarchy's leaves (sorted) or over
 //                 the batch in its own order, or persistent warps over the
-//                 eight-wide tree; skipped when pbg_params.walk fixes the walk
+//                 eight-wide tree (with the warp's triangle tests spread over
+//                 its lanes or not); skipped when pbg_params.walk fixes the
+//                 walk
 // Every candidate traces the same batch; its results must equal the first
 // candidate's bit for bit (prim, t, b1, b2 of hits, or occlusion), else the
 // call fails with PBG_ERR_INTERNAL and the scene keeps its previous shapes.
@@ -97,6 +99,7 @@ std::vector<Candidate> candidates(const pbg_scene* s) {
                 out.push_back({{3, 0, 0}});
                 out.push_back({{4, 0, 0}});
                 out.push_back({{5, 0, 0}});
+                out.push_back({{6, 0, 0}});
             }
             break;
     }

@@ -1,5 +1,6 @@
-// pbg_wide.cu -- ray-bvh walk 5: the binary SAH tree collapsed into an
-// eight-wide tree, walked by persistent warps.
+// pbg_wide.cu -- ray-bvh walks 5 and 6: the binary SAH tree collapsed into
+// an eight-wide tree, walked by persistent warps (walk 6: with the warp's
+// triangle tests spread over all its lanes).
 //
 // The reference walks its two-wide GPU BVH (bvh.cpp:154-206 lays it out,
 // rayBVH.cpp:615-1323 walks it).  Walking one node per step, the two-wide
@@ -461,7 +462,25 @@ __device__ __forceinline__ uint32_t dist_bits_down(float t) {
     return b & 0xffff0000u;
 }
 
-template <bool ANY, bool STATS>
+// COOP (walk 6): the triangle tests of a warp's lanes spread over all 32
+// lanes: lane j of round r tests pending pair r * 32 + j (pairs numbered
+// lane by lane) against its owner's ray, read from shared memory; hits merge
+// per owner by a 64-bit atomic maximum of hit_key (nearer t, then the larger
+// index: the rule of pbrt's in-order loop that the other kernels keep too).
+// It pays on incoherent batches, where a lane's pending triangles range from
+// 1 to 64 (path bounces: nearest hit 1.77 -> 1.65 ms); on coherent ones the
+// lanes' counts are alike and the shared-memory round trip costs more
+// (camera rays 3.29 -> 4.15 ms), so the autotuner picks per batch class.
+
+struct CoopWarp {
+    float4 o[32], d[32];
+    unsigned long long key[32];  // nearest: best hit_key (0: none); any-hit: nonzero once occluded
+    float ht[32], nd[32], t[32], b1[32], b2[32];
+    uint32_t m1[32], m2[32];
+    int32_t base1[32], base2[32], off[32], occluder[32];
+};
+
+template <bool ANY, bool STATS, bool COOP>
 __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
     wide_persistent_kernel(const WideNode* __restrict__ nodes, const TriRec* __restrict__ tris,
                            int32_t unculled, const float4* __restrict__ ro, const float4* __restrict__ rd,
@@ -472,6 +491,7 @@ __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
+    __shared__ CoopWarp coop[COOP ? kWideThreads / 32 : 1];
     int2 stack[kWideStack];  // (child base, hits | imask << 8 | distance bits)
     int sp = 0;
     int64_t ray = 0;
@@ -657,7 +677,110 @@ __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
             }
         }
         // the triangle tests, converged
-        if (has && (tmask != 0 || tmask2 != 0 || rcnt != 0)) {
+        if (COOP) {
+            // degenerate records (a ray's first round only), one lane each
+            if (has && rcnt != 0) {
+                const bool done = test_run<ANY, STATS>(tris, 0, rcnt, o, d, nd, h, wc);
+                rcnt = 0;
+                if (done) {
+                    tmask = tmask2 = 0;
+                    finish();
+                }
+            }
+            const bool mine = has && (tmask | tmask2) != 0;
+            const int c = mine ? __popc(tmask) + __popc(tmask2) : 0;
+            int incl = c;
+#pragma unroll
+            for (int sh = 1; sh < 32; sh <<= 1) {
+                const int v = __shfl_up_sync(full, incl, sh);
+                if (lane >= sh) incl += v;
+            }
+            const int total = __shfl_sync(full, incl, 31);
+            if (total > 0) {
+                CoopWarp& cw = coop[threadIdx.x >> 5];
+                const unsigned long long own = ANY || h.prim < 0 ? 0ull : hit_key(h.t, h.prim);
+                cw.off[lane] = incl - c;
+                if (mine) {
+                    if (STATS) wc.leaf++;
+                    cw.o[lane] = o;
+                    cw.d[lane] = d;
+                    cw.nd[lane] = nd;
+                    cw.ht[lane] = h.t;
+                    cw.m1[lane] = tmask;
+                    cw.m2[lane] = tmask2;
+                    cw.base1[lane] = tbase;
+                    cw.base2[lane] = tbase2;
+                    cw.key[lane] = own;
+                }
+                __syncwarp();
+                for (int g0 = 0; g0 < total; g0 += 32) {
+                    const int g = g0 + lane;
+                    int ci = -1;
+                    unsigned long long ck = 0ull;
+                    float ct = 0.f, cu1 = 0.f, cu2 = 0.f;
+                    if (g < total) {
+                        int i = 0;  // the owner: the last lane whose first pair is <= g
+#pragma unroll
+                        for (int step = 16; step; step >>= 1)
+                            if (cw.off[i + step] <= g) i += step;
+                        const int k = g - cw.off[i];
+                        const uint32_t m1 = cw.m1[i];
+                        const int n1 = __popc(m1);
+                        const int32_t rec = k < n1 ? cw.base1[i] + (int)__fns(m1, 0, k + 1)
+                                                   : cw.base2[i] + (int)__fns(cw.m2[i], 0, k - n1 + 1);
+                        if (!ANY || cw.key[i] == 0ull) {
+                            const float4 oo = cw.o[i], dd = cw.d[i];
+                            const float bound = cw.ht[i];
+                            const TriRec tr = tris[rec];
+                            if (STATS) wc.filt++;
+                            if (pbg_filter(tr, oo, dd, cw.nd[i], bound, STATS ? &wc.filt2 : nullptr)) {
+                                float tt, u1, u2;
+                                if (STATS) wc.exact++;
+                                if (pbg_exact_rec(tr, oo, dd, bound, &tt, &u1, &u2)) {
+                                    if (STATS) wc.hit++;
+                                    const int32_t id = __float_as_int(tr.c.w);
+                                    if (ANY) {
+                                        cw.key[i] = 1ull;
+                                        cw.occluder[i] = id;
+                                    } else {
+                                        ci = i;
+                                        ck = hit_key(tt, id);
+                                        ct = tt;
+                                        cu1 = u1;
+                                        cu2 = u2;
+                                        atomicMax(&cw.key[i], ck);
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    if (!ANY && ci >= 0 && cw.key[ci] == ck) {  // this round's winner for its owner
+                        cw.t[ci] = ct;
+                        cw.b1[ci] = cu1;
+                        cw.b2[ci] = cu2;
+                    }
+                    __syncwarp();
+                }
+                if (mine) {
+                    const unsigned long long kk = cw.key[lane];
+                    if (ANY) {
+                        if (kk != 0ull) {
+                            h.prim = cw.occluder[lane];
+                            finish();
+                        }
+                    } else if (kk != own) {
+                        h.t = cw.t[lane];
+                        h.prim = key_prim(kk);
+                        h.b1 = cw.b1[lane];
+                        h.b2 = cw.b2[lane];
+                    }
+                }
+                __syncwarp();
+            }
+            tmask = 0;
+            tmask2 = 0;
+        } else if (has && (tmask != 0 || tmask2 != 0 || rcnt != 0)) {
             if (STATS) wc.leaf++;
             bool done = false;
             if (rcnt) {
@@ -682,7 +805,7 @@ __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
     if (STATS) wc.flush(wcount);
 }
 
-template <bool ANY>
+template <bool ANY, bool COOP>
 int wide_launch(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
                 int64_t n, int32_t* prim, float* t, float* b1, float* b2, uint8_t* occ, cudaStream_t st) {
     Work& w = s->work;
@@ -691,13 +814,13 @@ int wide_launch(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
     unsigned long long* next = (unsigned long long*)w.counters.ptr;
     PBG_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wide_persistent_kernel<ANY, false>, kWideThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wide_persistent_kernel<ANY, false, COOP>, kWideThreads, 0);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     int64_t blocks = (int64_t)std::max(per_sm, 1) * sms;
     blocks = std::min<int64_t>(blocks, (n + kWideThreads - 1) / kWideThreads);
     const bool stats = s->prof.level >= 2;
-    auto kern = stats ? wide_persistent_kernel<ANY, true> : wide_persistent_kernel<ANY, false>;
+    auto kern = stats ? wide_persistent_kernel<ANY, true, COOP> : wide_persistent_kernel<ANY, false, COOP>;
     kern<<<(unsigned)blocks, kWideThreads, 0, st>>>((const WideNode*)s->wide.ptr, (const TriRec*)s->tris_wide.ptr,
                                                      s->unculled, o, d, valid, perm, n, prim, t, b1, b2, occ,
                                                      (int*)s->err.ptr, next,
@@ -705,14 +828,16 @@ int wide_launch(pbg_scene* s, const float4* o, const float4* d, const uint8_t* v
     return PBG_OK;
 }
 
-int wide_nearest(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
-                 int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
-    return wide_launch<false>(s, o, d, valid, perm, n, prim, t, b1, b2, nullptr, st);
+int wide_nearest(pbg_scene* s, bool coop, const float4* o, const float4* d, const uint8_t* valid,
+                 const int32_t* perm, int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st) {
+    return coop ? wide_launch<false, true>(s, o, d, valid, perm, n, prim, t, b1, b2, nullptr, st)
+                : wide_launch<false, false>(s, o, d, valid, perm, n, prim, t, b1, b2, nullptr, st);
 }
 
-int wide_occluded(pbg_scene* s, const float4* o, const float4* d, const uint8_t* valid, const int32_t* perm,
-                  int64_t n, int32_t* occluders, uint8_t* occ, cudaStream_t st) {
-    return wide_launch<true>(s, o, d, valid, perm, n, occluders, nullptr, nullptr, nullptr, occ, st);
+int wide_occluded(pbg_scene* s, bool coop, const float4* o, const float4* d, const uint8_t* valid,
+                  const int32_t* perm, int64_t n, int32_t* occluders, uint8_t* occ, cudaStream_t st) {
+    return coop ? wide_launch<true, true>(s, o, d, valid, perm, n, occluders, nullptr, nullptr, nullptr, occ, st)
+                : wide_launch<true, false>(s, o, d, valid, perm, n, occluders, nullptr, nullptr, nullptr, occ, st);
 }
 
 }  // namespace pbg

@@ -10,7 +10,7 @@ from pbrt_gb300 import scenes as S
 
 pytestmark = pytest.mark.gpu
 
-EXPECTED = {"naive": 4, "rayhierarchy": 6, "ray-bvh": 5}
+EXPECTED = {"naive": 4, "rayhierarchy": 6, "ray-bvh": 6}
 
 
 def dev(rays):

@@ -1,7 +1,8 @@
 """Every internal path choice gives the same answers: rayhierarchy with and
 without triangle clusters (and splitting at any level), ray-bvh with one
 thread per ray, persistent warps, warp packets over the ray hierarchy's
-leaves or persistent warps over the eight-wide tree, the ray image ordered by the direct
+leaves or persistent warps over the eight-wide tree (triangle tests per
+lane or spread over the warp), the ray image ordered by the direct
 Morton permutation (power-of-two sides) or by sorting (other sides), and
 host buffers read in place (pageable or pinned) or staged through copies.
 All compared bit for bit against the oracle's SAH BVH on the same rays."""
@@ -46,7 +47,7 @@ def test_rayhierarchy_cluster_levels(gpu_lib, terrain, levels):
     np.testing.assert_array_equal(occ == ord("1"), terrain["occ_inc"] == 1)
 
 
-@pytest.mark.parametrize("walk", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("walk", [1, 2, 3, 4, 5, 6])
 def test_raybvh_walks(gpu_lib, terrain, walk):
     acc = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": walk})
     assert_same(acc.Intersect(terrain["cam"].copy()), terrain["want_cam"], f"cam, walk {walk}")
@@ -60,11 +61,12 @@ def test_raybvh_walks(gpu_lib, terrain, walk):
     np.testing.assert_array_equal(got[0][hit], terrain["want_inc"][0][hit])
 
 
-@pytest.mark.parametrize("walk", [3, 4, 5])
+@pytest.mark.parametrize("walk", [3, 4, 5, 6])
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_packet_walk_golden(gpu_lib, case, walk):
     """walks 3 and 4 (warp packets over the ray hierarchy's leaves, or over
-    the batch in its own order) and 5 (the eight-wide tree) on the
+    the batch in its own order), 5 and 6 (the eight-wide tree, the warp's
+    triangle tests on one lane each or spread over its lanes) on the
     reference's own answers: ties, degenerate triangles, limits, empty."""
     g = load_golden(case)
     acc = A.MakeAccelerator("ray-bvh", g["tris"], {"walk": walk})
@@ -99,13 +101,14 @@ def test_packet_walk_sorted_batches(gpu_lib, oracle):
     assert_same(acc.Intersect(cam.copy()), B.nearest(cam), "camera, image order")
 
 
-def test_wide_walk_sorted_masked_and_fallback(gpu_lib, oracle, terrain):
-    """walk 5 over rays in 6-D Morton order, with a validity mask, nearest
-    and any hit; and a tree whose leaves exceed the wide format (leaves of
-    up to 16 triangles) keeps the two-wide persistent walk with the same
-    answers."""
+@pytest.mark.parametrize("walk", [5, 6])
+def test_wide_walk_sorted_masked_and_fallback(gpu_lib, oracle, terrain, walk):
+    """walks 5 and 6 over rays in 6-D Morton order, with a validity mask,
+    nearest and any hit; and a tree whose leaves exceed the wide format
+    (leaves of up to 16 triangles) keeps the two-wide persistent walk with
+    the same answers."""
     inc = terrain["inc"]
-    acc = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": 5, "raySort": 1})
+    acc = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": walk, "raySort": 1})
     assert_same(acc.Intersect(inc.copy()), terrain["want_inc"], "sorted")
     hit = (np.arange(inc.shape[1]) % 4) != 1
     got = acc.Intersect(inc.copy(), hit=hit.copy(), bounce=1)
@@ -114,7 +117,7 @@ def test_wide_walk_sorted_masked_and_fallback(gpu_lib, oracle, terrain):
     occ = acc.IntersectP(inc, hit=hit.copy())
     np.testing.assert_array_equal(occ[hit] == ord("1"), terrain["occ_inc"][hit] == 1)
     assert (occ[~hit] == ord("0")).all()
-    big = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": 5, "maxBVHPrim": 16})
+    big = A.MakeAccelerator("ray-bvh", terrain["tris"], {"walk": walk, "maxBVHPrim": 16})
     assert_same(big.Intersect(inc.copy()), terrain["want_inc"], "leaves of 16")
     np.testing.assert_array_equal(big.IntersectP(inc) == ord("1"), terrain["occ_inc"] == 1)
 
