@@ -348,7 +348,10 @@ typedef struct pbg_batch_params {
     int32_t threads;     /* threads per CTA, multiple of 32 (0 = tuned) */
     int32_t use_graph;   /* 1 = capture and replay a CUDA graph (default 1) */
     int32_t walk;        /* 1 = warps take work items of `tile` rays, 2 = each lane
-                          * refills from one counter over all rays (0 = tuned) */
+                          * refills from one counter over all rays, 3 = the same
+                          * over every scene's eight-wide tree (one launch per
+                          * query kind, 128 threads), 4 = 3 with each warp's
+                          * triangle tests spread over its lanes (0 = tuned) */
     int32_t reserved[7];
 } pbg_batch_params;
 

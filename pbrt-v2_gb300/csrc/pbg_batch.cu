@@ -21,7 +21,8 @@
 //    replayed while the caller passes the same arrays and launch shape.
 //  * Or, per-lane persistent: every lane refills from a counter over all
 //    rays of the set (batch_persistent_kernel) -- better for incoherent
-//    rays, whose walks end at very different times.
+//    rays, whose walks end at very different times; or the same over every
+//    scene's eight-wide tree (pbg_wide.cuh), one launch per query kind.
 //  * The autotuner times the candidate (walk, tile, CTAs per SM, threads)
 //    shapes on the caller's queries and keeps the fastest.
 // No kernel here waits on another CTA: the queue is a plain fetch-and-add.
@@ -34,6 +35,7 @@
 #include "pbg_internal.h"
 #include "pbg_tma.cuh"
 #include "pbg_walk.cuh"
+#include "pbg_wide.cuh"
 
 namespace pbg {
 
@@ -45,6 +47,8 @@ struct SceneDesc {
     const TriRec* tris;
     int32_t unculled;
     int32_t pad;
+    const WideNode* wide;  // the eight-wide tree and its record copy (walks 3 and 4)
+    const TriRec* wtris;
 };
 
 struct BatchArgs {
@@ -80,7 +84,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __global__ void batch_reset_kernel(BatchArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) {
-        *a.head = 0ull;
+        a.head[0] = 0ull;
+        a.head[1] = 0ull;  // the any-hit launch of the wide walks
         *a.start_ns = global_ns();
     }
     if (k < a.nscenes) {
@@ -286,6 +291,70 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_persistent_kernel(Batc
     }
 }
 
+// The rays of one query kind of a whole scene set, for the eight-wide walk
+// (walks 3 and 4: one launch per kind).  A lane's slot is the ray's index in
+// the kind's arrays; its scene is the last one whose first ray is at or
+// before it.
+struct SetRays {
+    static constexpr bool kSet = true;
+    struct Lane {
+        int64_t ray;
+        const WideNode* wn;
+        const TriRec* wt;
+        int32_t unc;
+        int32_t scene;
+    };
+    const SceneDesc* scenes;
+    int32_t nscenes;
+    int32_t kind;            // 0 nearest, 1 any-hit
+    const int64_t* ray_off;  // [2 * nscenes], segment 2k + kind
+    const int64_t* ray_end;
+    const float4* o4;
+    const float4* d4;
+    int32_t* prim;
+    float* t;
+    float* b1;
+    float* b2;
+    uint8_t* occ;
+    unsigned long long* done_ns;
+
+    __device__ __forceinline__ int64_t count() const { return ray_end[2 * (nscenes - 1) + kind]; }
+    __device__ __forceinline__ bool fetch(int64_t slot, Lane& L, float4& o, float4& d) const {
+        int lo = 0, hi = nscenes;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (ray_off[2 * mid + kind] <= slot) lo = mid;
+            else hi = mid;
+        }
+        const SceneDesc sd = scenes[lo];
+        L.ray = slot;
+        L.scene = lo;
+        L.wn = sd.wide;
+        L.wt = sd.wtris;
+        L.unc = sd.unculled;
+        o = o4[slot];
+        d = d4[slot];
+        return true;
+    }
+    __device__ __forceinline__ const WideNode* nodes(const Lane& L) const { return L.wn; }
+    __device__ __forceinline__ const TriRec* tris(const Lane& L) const { return L.wt; }
+    __device__ __forceinline__ int32_t unculled(const Lane& L) const { return L.unc; }
+    template <bool ANY>
+    __device__ __forceinline__ void store(const Lane& L, const WalkHit& h) const {
+        if (ANY) {
+            occ[L.ray] = h.prim >= 0 ? 1 : 0;
+        } else {
+            const bool hit = h.prim >= 0;
+            prim[L.ray] = h.prim;
+            t[L.ray] = hit ? h.t : 0.f;
+            b1[L.ray] = hit ? h.b1 : 0.f;
+            b2[L.ray] = hit ? h.b2 : 0.f;
+        }
+    }
+    __device__ __forceinline__ int scene(const Lane& L) const { return L.scene; }
+    __device__ __forceinline__ void stamp(int sc) const { atomicMax(&done_ns[sc], global_ns()); }
+};
+
 }  // namespace pbg
 
 using namespace pbg;
@@ -295,6 +364,8 @@ struct pbg_sceneset {
     int32_t nscenes = 0;
     cudaStream_t capture_stream = nullptr;
     DeviceBuffer nodes, tris, descs, err;
+    DeviceBuffer wnodes, wtris;  // every scene's eight-wide tree and record copy
+    bool wide_ok = false;        // every scene's tree fits the wide format
     DeviceBuffer head, remaining, done_ns, start_ns;
     std::vector<int64_t> ntri;
     // Segment tables (item_off ++ ray_off ++ ray_end ++ rseg_off) with the
@@ -317,7 +388,9 @@ namespace {
 
 // walk: 1 = work items of `tile` rays (batch_trace_kernel), 2 = per-lane
 // persistent refill (batch_persistent_kernel; tile only sizes the items of
-// the completion bookkeeping).
+// the completion bookkeeping), 3 / 4 = per-lane persistent refill over the
+// eight-wide trees, one launch per query kind (4: the warp's triangle tests
+// spread over its lanes); 128 threads.
 struct Shape {
     int tile, ctas_per_sm, threads, walk;
 };
@@ -325,8 +398,12 @@ struct Shape {
 int max_ctas_per_sm(int threads, int walk) {
     int n = 0;
     const cudaError_t e =
-        walk == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_persistent_kernel<true>, threads, 0)
-                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_trace_kernel, threads, 0);
+        walk == 3   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &n, wide_walk_kernel<false, false, false, SetRays>, kWideThreads, 0)
+        : walk == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &n, wide_walk_kernel<false, false, true, SetRays>, kWideThreads, 0)
+        : walk == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_persistent_kernel<true>, threads, 0)
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_trace_kernel, threads, 0);
     if (e != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
@@ -340,6 +417,7 @@ Shape resolve_shape(const pbg_sceneset* set, const pbg_batch_params* p) {
     if (s.tile <= 0) s.tile = 64;
     if (s.threads <= 0) s.threads = 128;
     if (s.walk <= 0) s.walk = 1;
+    if (s.walk == 3 || s.walk == 4) s.threads = kWideThreads;
     if (s.ctas_per_sm <= 0) s.ctas_per_sm = max_ctas_per_sm(s.threads, s.walk);
     return s;
 }
@@ -347,7 +425,7 @@ Shape resolve_shape(const pbg_sceneset* set, const pbg_batch_params* p) {
 bool shape_ok(const Shape& s) {
     return s.tile >= 32 && s.tile <= 8192 && s.tile % 32 == 0 && s.threads >= 32 &&
            s.threads <= kBatchMaxThreads && s.threads % 32 == 0 && s.ctas_per_sm >= 1 &&
-           s.ctas_per_sm <= 64 && (s.walk == 1 || s.walk == 2);
+           s.ctas_per_sm <= 64 && s.walk >= 1 && s.walk <= 4;
 }
 
 bool offsets_ok(const int64_t* off, int32_t n) {
@@ -426,6 +504,21 @@ int launch_pair(pbg_sceneset* set, const BatchArgs& a, const Shape& s, cudaStrea
     batch_reset_kernel<<<(unsigned)((set->nscenes + 255) / 256), 256, 0, st>>>(a);
     PBG_CUDA(cudaGetLastError());
     const unsigned grid = (unsigned)(s.ctas_per_sm * set->sm_count);
+    if (s.walk == 3 || s.walk == 4) {
+        // the nearest-hit rays of every scene, then the any-hit rays
+        for (int kind = 0; kind < 2; ++kind) {
+            const SetRays src{a.scenes, a.nscenes, kind, a.ray_off, a.ray_end,
+                              kind ? a.o4s : a.o4n, kind ? a.d4s : a.d4n, a.prim, a.t, a.b1, a.b2, a.occ,
+                              a.done_ns};
+            auto kern = kind ? (s.walk == 4 ? wide_walk_kernel<true, false, true, SetRays>
+                                            : wide_walk_kernel<true, false, false, SetRays>)
+                             : (s.walk == 4 ? wide_walk_kernel<false, false, true, SetRays>
+                                            : wide_walk_kernel<false, false, false, SetRays>);
+            kern<<<grid, kWideThreads, 0, st>>>(src, a.status, a.head + kind, nullptr);
+            PBG_CUDA(cudaGetLastError());
+        }
+        return PBG_OK;
+    }
     if (s.walk == 2) {
         // scene-local record starts below 2^24 fit a packed stack entry
         int64_t max_ntri = 0;
@@ -456,6 +549,10 @@ int prepare(pbg_sceneset* set, const Call& c, const Shape& s, cudaStream_t st, u
         (ns > 0 && (!c.o4s || !c.d4s || !c.occ))) {
         set_last_error("pbg_sceneset_trace: NULL ray or result array");
         return PBG_ERR_INVALID_ARGUMENT;
+    }
+    if ((s.walk == 3 || s.walk == 4) && !set->wide_ok) {
+        set_last_error("pbg_sceneset_trace: walks 3 and 4 need every scene's tree in the eight-wide format");
+        return PBG_ERR_UNSUPPORTED;
     }
     if (!shape_ok(s)) {
         set_last_error("pbg_sceneset_trace: tile and threads must be multiples of 32 (tile <= 8192, "
@@ -593,8 +690,12 @@ int pbg_sceneset_create(int32_t nscenes, const float* const* tri9, const int64_t
         e = cudaDeviceGetAttribute(&set->sm_count, cudaDevAttrMultiProcessorCount, device);
         if (e != cudaSuccess) return fail(cuda_status(e, "cudaDeviceGetAttribute"));
     }
-    // BVHs on the host cores, one scene per task
+    // BVHs on the host cores, one scene per task, each also collapsed to the
+    // eight-wide tree (wide records: original triangle of each position)
     std::vector<HostBvh> hb((size_t)nscenes);
+    std::vector<std::vector<WideNode>> wn((size_t)nscenes);
+    std::vector<std::vector<int32_t>> worder((size_t)nscenes);
+    std::atomic<int32_t> wide_fail{0};
     {
         std::atomic<int32_t> next{0};
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
@@ -602,25 +703,44 @@ int pbg_sceneset_create(int32_t nscenes, const float* const* tri9, const int64_t
         std::vector<std::thread> pool;
         for (unsigned i = 0; i < nt; ++i)
             pool.emplace_back([&] {
-                for (int32_t k; (k = next.fetch_add(1)) < nscenes;)
-                    build_bvh(tri9[k], ntri[k], 4, &hb[(size_t)k]);
+                for (int32_t k; (k = next.fetch_add(1)) < nscenes;) {
+                    HostBvh& b = hb[(size_t)k];
+                    build_bvh(tri9[k], ntri[k], 4, &b);
+                    std::vector<int32_t> src;
+                    if (b.nodes.empty() ||
+                        !collapse_wide(b.nodes, b.unculled, ntri[k], kWideAbsorb, kWideTriCost, &wn[(size_t)k], &src)) {
+                        wide_fail.fetch_add(1);
+                        continue;
+                    }
+                    std::vector<int32_t>& wo = worder[(size_t)k];
+                    wo.resize(src.size());
+                    for (size_t r = 0; r < src.size(); ++r) wo[r] = b.order.empty() ? src[r] : b.order[(size_t)src[r]];
+                }
             });
         for (auto& th : pool) th.join();
     }
+    set->wide_ok = wide_fail.load() == 0;
     std::vector<int64_t> node_base((size_t)nscenes + 1, 0), tri_base((size_t)nscenes + 1, 0);
     for (int32_t k = 0; k < nscenes; ++k) {
         node_base[(size_t)k + 1] = node_base[(size_t)k] + (int64_t)hb[(size_t)k].nodes.size();
         tri_base[(size_t)k + 1] = tri_base[(size_t)k] + ntri[k];
     }
     const int64_t total_nodes = node_base[(size_t)nscenes], total_tris = tri_base[(size_t)nscenes];
+    std::vector<int64_t> wnode_base((size_t)nscenes + 1, 0);
+    for (int32_t k = 0; k < nscenes; ++k)
+        wnode_base[(size_t)k + 1] = wnode_base[(size_t)k] + (int64_t)wn[(size_t)k].size();
     int rc;
     if ((rc = ensure(set->nodes, (size_t)total_nodes * sizeof(BvhNode))) ||
         (rc = ensure(set->tris, (size_t)std::max<int64_t>(total_tris, 1) * sizeof(TriRec))) ||
         (rc = ensure(set->descs, (size_t)nscenes * sizeof(SceneDesc))) ||
-        (rc = ensure(set->err, 4 * sizeof(int))) || (rc = ensure(set->head, sizeof(uint64_t))) ||
+        (rc = ensure(set->err, 4 * sizeof(int))) || (rc = ensure(set->head, 2 * sizeof(uint64_t))) ||
         (rc = ensure(set->start_ns, sizeof(uint64_t))) ||
         (rc = ensure(set->remaining, (size_t)nscenes * sizeof(int32_t))) ||
         (rc = ensure(set->done_ns, (size_t)nscenes * sizeof(uint64_t))))
+        return fail(rc);
+    if (set->wide_ok &&
+        ((rc = ensure(set->wnodes, (size_t)std::max<int64_t>(wnode_base[(size_t)nscenes], 1) * sizeof(WideNode))) ||
+         (rc = ensure(set->wtris, (size_t)std::max<int64_t>(total_tris, 1) * sizeof(TriRec)))))
         return fail(rc);
     if (cudaMemset(set->err.ptr, 0, 4 * sizeof(int)) != cudaSuccess)
         return fail(cuda_status(cudaGetLastError(), "cudaMemset"));
@@ -639,9 +759,14 @@ int pbg_sceneset_create(int32_t nscenes, const float* const* tri9, const int64_t
         const HostBvh& b = hb[(size_t)k];
         BvhNode* nodes = (BvhNode*)set->nodes.ptr + node_base[(size_t)k];
         TriRec* tris = (TriRec*)set->tris.ptr + tri_base[(size_t)k];
-        descs[(size_t)k] = SceneDesc{nodes, tris, b.unculled, 0};
+        WideNode* wide = set->wide_ok ? (WideNode*)set->wnodes.ptr + wnode_base[(size_t)k] : nullptr;
+        TriRec* wtris = set->wide_ok ? (TriRec*)set->wtris.ptr + tri_base[(size_t)k] : nullptr;
+        descs[(size_t)k] = SceneDesc{nodes, tris, b.unculled, 0, wide, wtris};
         cudaError_t e = cudaMemcpy(nodes, b.nodes.data(), b.nodes.size() * sizeof(BvhNode),
                                    cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && wide && !wn[(size_t)k].empty())
+            e = cudaMemcpy(wide, wn[(size_t)k].data(), wn[(size_t)k].size() * sizeof(WideNode),
+                           cudaMemcpyHostToDevice);
         if (e == cudaSuccess && ntri[k] > 0) {
             e = cudaMemcpy(v9.ptr, tri9[k], (size_t)ntri[k] * 9 * sizeof(float), cudaMemcpyHostToDevice);
             if (e == cudaSuccess)
@@ -650,6 +775,14 @@ int pbg_sceneset_create(int32_t nscenes, const float* const* tri9, const int64_t
             if (e == cudaSuccess) {
                 rc = launch_build_tris((const float*)v9.ptr, (const int32_t*)ord.ptr, ntri[k], tris, st);
                 if (rc == PBG_OK) e = cudaStreamSynchronize(st);
+            }
+            if (e == cudaSuccess && rc == PBG_OK && wtris) {  // the wide tree's record order
+                e = cudaMemcpy(ord.ptr, worder[(size_t)k].data(), (size_t)ntri[k] * sizeof(int32_t),
+                               cudaMemcpyHostToDevice);
+                if (e == cudaSuccess) {
+                    rc = launch_build_tris((const float*)v9.ptr, (const int32_t*)ord.ptr, ntri[k], wtris, st);
+                    if (rc == PBG_OK) e = cudaStreamSynchronize(st);
+                }
             }
         }
         if (e != cudaSuccess && rc == PBG_OK) rc = cuda_status(e, "pbg_sceneset_create upload");
@@ -670,8 +803,9 @@ void pbg_sceneset_destroy(pbg_sceneset* set) {
     cudaSetDevice(set->device);
     cudaDeviceSynchronize();
     destroy_graph(set);
-    DeviceBuffer* all[] = {&set->nodes, &set->tris,      &set->descs,   &set->err,      &set->slot[0].dev,
-                           &set->slot[1].dev, &set->head, &set->remaining, &set->done_ns, &set->start_ns};
+    DeviceBuffer* all[] = {&set->nodes,       &set->tris, &set->descs,     &set->err,     &set->slot[0].dev,
+                           &set->slot[1].dev, &set->head, &set->remaining, &set->done_ns, &set->start_ns,
+                           &set->wnodes,      &set->wtris};
     for (DeviceBuffer* b : all) release(*b);
     if (set->capture_stream) cudaStreamDestroy(set->capture_stream);
     delete set;
@@ -768,14 +902,15 @@ int pbg_sceneset_autotune(pbg_sceneset* set, const float* o4n, const float* d4n,
     float best_ms = INFINITY;
     Shape win{64, 0, 128, 1};
     int rc = PBG_OK;
-    for (int walk = 1; walk <= 2; ++walk)
+    for (int walk = 1; walk <= 4; ++walk)
     for (int th : threads) {
+        if (walk >= 3 && (th != kWideThreads || !set->wide_ok)) continue;  // the wide walks run 128 threads
         const int full = max_ctas_per_sm(th, walk);
         const int ctas[] = {full, std::max(1, full / 2)};
         for (int ci = 0; ci < 2 && rc == PBG_OK; ++ci) {
             if (ci == 1 && ctas[1] == ctas[0]) continue;
             for (int tile : tiles) {
-                if (walk == 2 && tile != 64) continue;  // the persistent walk does not use tiles
+                if (walk >= 2 && tile != 64) continue;  // the persistent walks do not use tiles
                 const Shape s{tile, ctas[ci], th, walk};
                 uint64_t rays = 0;
                 if ((rc = prepare(set, c, s, st, &rays))) break;

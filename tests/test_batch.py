@@ -95,7 +95,7 @@ def test_golden_scenes_in_one_set(gpu_lib):
     gs = [load_golden(c) for c in GOLDEN_CASES]
     sset = SceneSet([g["tris"] for g in gs])
     pk = Packed([g["rays"] for g in gs], [g["rays"] for g in gs])
-    for tile, walk in ((32, 1), (64, 1), (256, 1), (64, 2)):
+    for tile, walk in ((32, 1), (64, 1), (256, 1), (64, 2), (64, 3), (64, 4)):
         for graph in (False, True):
             sset.trace(**pk.args(), tile=tile, use_graph=graph, walk=walk)
             prim, t, b1, b2, occ = pk.results()
@@ -195,6 +195,12 @@ def test_empty_and_ragged(gpu_lib):
     got_p = pk.results()
     for a, b in zip(got, got_p):
         np.testing.assert_array_equal(a, b)
+    for walk in (3, 4):  # the eight-wide trees, one launch per query kind
+        pk.prim.fill_(-7)
+        pk.occ.fill_(7)
+        sset.trace(**pk.args(), ctas_per_sm=1, use_graph=False, walk=walk)
+        for a, b in zip(got, pk.results()):
+            np.testing.assert_array_equal(a, b)
     for k in range(4):
         want = per_scene(tris[k], near[k], shad[k])
         a, b = pk.near_off[k], pk.near_off[k + 1]
@@ -220,7 +226,7 @@ def test_autotune_and_bad_arguments(gpu_lib):
     pk = Packed([s["near"] for s in scs], [s["shadow"] for s in scs])
     best = sset.autotune(**pk.args())
     assert best["tile"] in (32, 64, 128, 256) and best["threads"] in (64, 128, 256)
-    assert best["ctas_per_sm"] >= 1 and best["walk"] in (1, 2)
+    assert best["ctas_per_sm"] >= 1 and best["walk"] in (1, 2, 3, 4)
     st, _ = sset.trace(**pk.args(), stats=True)
     assert (st["tile"], st["threads"], st["ctas_per_sm"], st["walk"]) == (
         best["tile"], best["threads"], best["ctas_per_sm"], best["walk"])
