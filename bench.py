@@ -698,6 +698,8 @@ def run_gpu_path(args, rank, world, dev):
                    "rays_per_step": int(rays), "nearest_rays": int(near_rays), "shadow_rays": int(sh_rays),
                    "triangles": int(len(tris)), "bvh_build_s": round(build_s, 2),
                    "bvh_nodes": int(acc.stats()["bvh_nodes"]),
+                   "wide_nodes": int(acc.stats()["wide_nodes"]),
+                   "wide_build_s": round(acc.stats()["wide_build_ms"] * 1e-3, 3),
                    "ray_sort": bool(args.ray_sort), "walk": args.walk,
                    "bvh_build": "host" if args.bvh_build == 1 else "device", "parallelism": f"replicas x{world}",
                    "l2": "inputs > L2 (8.4M paths x 32 B rays per bounce)",

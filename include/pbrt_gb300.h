@@ -136,6 +136,11 @@ typedef struct pbg_counters {
      * each launch on its stream): [0] ray sort, [1] hierarchy build,
      * [2] traversal (the intersection kernels), [3] finalize / other. */
     double stage_ms[4];
+    /* ray-bvh walks 5 and 6: nodes of the eight-wide tree (0 until the first
+     * such batch builds it) and the host wall time of that build, ms
+     * (collapse of the two-wide tree on the host cores, uploads) */
+    uint64_t wide_nodes;
+    double wide_build_ms;
 } pbg_counters;
 
 /* Library version, e.g. "pbrt-gb300 1.0 (sm_103a)". */

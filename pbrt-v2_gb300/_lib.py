@@ -62,7 +62,7 @@ class Counters(C.Structure):
                 ("calls", C.c_uint64), ("bvh_nodes", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("timed_launches", C.c_uint64 * 4), ("work", C.c_uint64 * 6),
                 ("origin_reuses", C.c_uint64), ("origin_reruns", C.c_uint64), ("queue_reruns", C.c_uint64),
-                ("stage_ms", C.c_double * 4)]
+                ("stage_ms", C.c_double * 4), ("wide_nodes", C.c_uint64), ("wide_build_ms", C.c_double)]
 
 
 STAGES = ("sort", "build", "traverse", "other")

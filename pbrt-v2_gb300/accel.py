@@ -216,7 +216,8 @@ class Aggregate:
                                   "exact_hits", "filter_stage2"), list(c.work))),
                 "origin_reuses": c.origin_reuses, "origin_reruns": c.origin_reruns,
                 "queue_reruns": c.queue_reruns,
-                "stage_ms": dict(zip(L.STAGES, list(c.stage_ms)))}
+                "stage_ms": dict(zip(L.STAGES, list(c.stage_ms))),
+                "wide_nodes": c.wide_nodes, "wide_build_ms": c.wide_build_ms}
 
     # -- learned traversal ordering (ray-bvh) ------------------------------
 

@@ -42,6 +42,7 @@
 // inner children in visiting order, the group's nearest entry distance), the
 // pending triangle mask of the last node, and a private stack of groups.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -391,6 +392,7 @@ int ensure_wide(pbg_scene* s, bool* available, cudaStream_t st) {
     }
     s->wide_state = -1;
     if (s->bvh_nodes <= 0) return PBG_OK;
+    const auto t0 = std::chrono::steady_clock::now();
     if (s->host_nodes.empty()) {  // a tree built on the device: collapsed on the host
         s->host_nodes.resize((size_t)s->bvh_nodes);
         PBG_CUDA(cudaStreamSynchronize(st));
@@ -421,6 +423,8 @@ int ensure_wide(pbg_scene* s, bool* available, cudaStream_t st) {
     if (e != cudaSuccess) return cuda_status(e, "wide BVH upload");
     s->wide_nodes = (int64_t)wn.size();
     s->wide_state = 1;
+    s->counters.wide_nodes = (uint64_t)wn.size();
+    s->counters.wide_build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     *available = true;
     return PBG_OK;
 }
