@@ -975,6 +975,7 @@ int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf
     const int64_t nitems = ntri - ndeg;
     BvhNode* nodes = (BvhNode*)s->bvh.ptr;
     int32_t node_base = 0;
+    s->bvh_levels.clear();
     if (nitems == 0) {
         empty_root_kernel<<<1, 1, 0, st>>>(nodes);
         PBG_CUDA(cudaGetLastError());
@@ -1024,6 +1025,10 @@ int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf
             PBG_CUDA(cudaStreamSynchronize(st));
             s->counters.kernel_launches += 3;
             const int64_t inner = (int64_t)off + last;
+            if (inner > 0) {
+                s->bvh_levels.push_back(node_base);
+                s->bvh_levels.push_back((int32_t)inner);
+            }
             node_base += (int32_t)inner;
             if (node_base == 0) node_base = 1;  // the root was a leaf
             nseg = 2 * inner;
@@ -1044,6 +1049,7 @@ int build_bvh_device(pbg_scene* s, const float* tri9, int64_t ntri, int max_leaf
         s->scene_lo[a] = ntri > 0 ? dec(h[a]) : 0.f;
         s->scene_hi[a] = ntri > 0 ? dec(h[3 + a]) : 0.f;
     }
+    if (s->bvh_levels.empty()) s->bvh_levels = {0, 1};  // one root node: a leaf, or no triangles
     s->bvh_nodes = node_base;
     s->bvh_depth = (int)h[7];
     s->unculled = ndeg;

@@ -115,6 +115,7 @@ struct pbg_scene {
     pbg::DeviceBuffer wide;    // WideNode[] (ray-bvh walks 5 and 6, built on their first batch)
     pbg::DeviceBuffer tris_wide; // TriRec[ntri] in the wide tree's leaf order
     int64_t wide_nodes = 0;
+    std::vector<int32_t> bvh_levels;  // device-built tree: (first node, nodes) per level, root first
     int wide_state = 0;        // 0 not built yet, 1 built, -1 the tree does not fit the wide format
     pbg::DeviceBuffer spheres; // float4 bounding sphere per record (rayhierarchy)
     pbg::DeviceBuffer clusters; // float4 sphere per kClusterTris consecutive records (rayhierarchy)
@@ -164,6 +165,11 @@ int bvh_occluded_hinted(pbg_scene* s, const float4* o, const float4* d, const ui
 // first use and sets *available = false when the scene keeps the two-wide
 // walks.
 int ensure_wide(pbg_scene* s, bool* available, cudaStream_t st);
+// The collapse on the device from a device-built tree (its levels in
+// s->bvh_levels): fills s->wide and src (per record position of the wide
+// copy, the record's position in the two-wide order); *fits = false when the
+// tree does not fit the wide format.
+int collapse_wide_device(pbg_scene* s, bool* fits, DeviceBuffer& src, int64_t* nwide, cudaStream_t st);
 int wide_nearest(pbg_scene* s, bool coop, const float4* o, const float4* d, const uint8_t* valid,
                  const int32_t* perm, int64_t n, int32_t* prim, float* t, float* b1, float* b2, cudaStream_t st);
 int wide_occluded(pbg_scene* s, bool coop, const float4* o, const float4* d, const uint8_t* valid,

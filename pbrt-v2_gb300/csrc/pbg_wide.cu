@@ -24,7 +24,9 @@
 // the same exact tests, so every walk returns the same prim, t, b1, b2 or
 // occlusion bit for bit.
 //
-// Layout (built lazily on the first walk-5 batch of a scene, 240 bytes per
+// Built lazily on the first walk-5/6 batch of a scene: on the device from a
+// device-built tree (pbg_wide_build.cu), else on the host (collapse_wide).
+// Layout (240 bytes per
 // node: per axis the eight low planes, then the eight high planes; the
 // references; the slots' triangle masks):
 //   * inner children of a node are contiguous from child_base, in slot
@@ -54,8 +56,6 @@ namespace pbg {
 
 namespace {
 
-constexpr int kWideMaxLeaf = 7;    // triangles per leaf child (3 bits)
-constexpr int kWideMaxOffset = 31; // leaf offset within a node (5 bits)
 
 struct Item {
     int32_t ref, cnt;  // binary child reference (>= 0 inner, else ~start) and leaf count
@@ -393,37 +393,49 @@ int ensure_wide(pbg_scene* s, bool* available, cudaStream_t st) {
     s->wide_state = -1;
     if (s->bvh_nodes <= 0) return PBG_OK;
     const auto t0 = std::chrono::steady_clock::now();
-    if (s->host_nodes.empty()) {  // a tree built on the device: collapsed on the host
-        s->host_nodes.resize((size_t)s->bvh_nodes);
-        PBG_CUDA(cudaStreamSynchronize(st));
-        PBG_CUDA(cudaMemcpy(s->host_nodes.data(), s->bvh.ptr, s->host_nodes.size() * sizeof(BvhNode),
-                            cudaMemcpyDeviceToHost));
-    }
-    std::vector<WideNode> wn;
-    std::vector<int32_t> src;
-    if (!collapse_wide(s->host_nodes, s->unculled, s->ntri, kWideAbsorb, kWideTriCost, &wn, &src)) return PBG_OK;
     int rc;
     DeviceBuffer dsrc;
-    if ((rc = ensure(s->wide, wn.size() * sizeof(WideNode))) ||
-        (rc = ensure(s->tris_wide, (size_t)std::max<int64_t>(s->ntri, 1) * sizeof(TriRec))) ||
-        (rc = ensure(dsrc, (size_t)std::max<int64_t>(s->ntri, 1) * sizeof(int32_t))))
+    int64_t nwide = 0;
+    cudaError_t e = cudaSuccess;
+    if (!s->bvh_levels.empty()) {  // a tree built on the device: collapsed there
+        bool fits = false;
+        if ((rc = collapse_wide_device(s, &fits, dsrc, &nwide, st))) {
+            release(dsrc);
+            return rc;
+        }
+        if (!fits) {
+            release(dsrc);
+            return PBG_OK;
+        }
+    } else {  // a tree built on the host: collapsed there
+        std::vector<WideNode> wn;
+        std::vector<int32_t> src;
+        if (!collapse_wide(s->host_nodes, s->unculled, s->ntri, kWideAbsorb, kWideTriCost, &wn, &src)) return PBG_OK;
+        nwide = (int64_t)wn.size();
+        if ((rc = ensure(s->wide, wn.size() * sizeof(WideNode))) ||
+            (rc = ensure(dsrc, (size_t)std::max<int64_t>(s->ntri, 1) * sizeof(int32_t))))
+            return rc;
+        e = cudaMemcpy(s->wide.ptr, wn.data(), wn.size() * sizeof(WideNode), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && s->ntri > 0)
+            e = cudaMemcpy(dsrc.ptr, src.data(), src.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess && (rc = ensure(s->tris_wide, (size_t)std::max<int64_t>(s->ntri, 1) * sizeof(TriRec)))) {
+        release(dsrc);
         return rc;
-    cudaError_t e = cudaMemcpy(s->wide.ptr, wn.data(), wn.size() * sizeof(WideNode), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && s->ntri > 0)
-        e = cudaMemcpy(dsrc.ptr, src.data(), src.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess && s->ntri > 0) {
         gather_records_kernel<<<(unsigned)((s->ntri + 255) / 256), 256, 0, st>>>(
             (const TriRec*)s->tris.ptr, (const int32_t*)dsrc.ptr, s->ntri, (TriRec*)s->tris_wide.ptr);
         e = cudaGetLastError();
-        // later batches may run on other streams: the copy is complete before any of them
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         s->counters.kernel_launches += 1;
     }
+    // later batches may run on other streams: the tree is complete before any of them
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     release(dsrc);
-    if (e != cudaSuccess) return cuda_status(e, "wide BVH upload");
-    s->wide_nodes = (int64_t)wn.size();
+    if (e != cudaSuccess) return cuda_status(e, "wide BVH build");
+    s->wide_nodes = nwide;
     s->wide_state = 1;
-    s->counters.wide_nodes = (uint64_t)wn.size();
+    s->counters.wide_nodes = (uint64_t)nwide;
     s->counters.wide_build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     *available = true;
     return PBG_OK;

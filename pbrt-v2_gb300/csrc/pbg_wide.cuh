@@ -25,6 +25,8 @@ static_assert(sizeof(WideNode) == 240, "wide node is fifteen 16-byte words");
 bool collapse_wide(const std::vector<BvhNode>& bin, int32_t unculled, int64_t ntri, int absorb, float c_tri,
                    std::vector<WideNode>* out, std::vector<int32_t>* src);
 constexpr int kWideWidth = 8;         // children per node
+constexpr int kWideMaxLeaf = 7;       // triangles per leaf child
+constexpr int kWideMaxOffset = 31;    // a leaf's first triangle within its node's 32
 constexpr int kWideAbsorb = 4;        // subtrees of at most this many triangles may become one leaf
 constexpr float kWideTriCost = 0.3f;  // a triangle test against a wide node visit
 

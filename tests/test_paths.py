@@ -122,6 +122,23 @@ def test_wide_walk_sorted_masked_and_fallback(gpu_lib, oracle, terrain, walk):
     np.testing.assert_array_equal(big.IntersectP(inc) == ord("1"), terrain["occ_inc"] == 1)
 
 
+def test_wide_tree_device_and_host_collapse(gpu_lib, terrain):
+    """The eight-wide tree collapsed on the device (from the device-built
+    tree) and on the host (from the host-built tree, the same splits) has
+    the same nodes, and walks 5 and 6 over either give the oracle's hits."""
+    inc = terrain["inc"]
+    stats = []
+    for build in (0, 1):
+        for walk in (5, 6):
+            acc = A.MakeAccelerator("ray-bvh", terrain["tris"], {"bvhBuild": build, "walk": walk})
+            assert_same(acc.Intersect(inc.copy()), terrain["want_inc"], f"build {build} walk {walk}")
+            np.testing.assert_array_equal(acc.IntersectP(inc) == ord("1"), terrain["occ_inc"] == 1)
+            st = acc.stats()
+            assert st["wide_nodes"] > 0
+            stats.append(st["wide_nodes"])
+    assert len(set(stats)) == 1, stats
+
+
 @pytest.mark.parametrize("width,height", [(128, 64), (96, 80)])
 def test_image_order_direct_and_sorted(gpu_lib, oracle, terrain, width, height):
     """A 128 x 64 ray image (power-of-two sides) takes the direct Morton
