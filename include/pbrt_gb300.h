@@ -72,9 +72,11 @@ typedef struct pbg_params {
     int32_t rh_cluster_levels; /* rayhierarchy: hierarchy levels walked by clusters of
                                 * 32 triangles before they split (0 = down to the
                                 * leaves' parents, < 0 = no clusters) */
-    int32_t walk;         /* ray-bvh traversal: 0 = automatic (persistent for bounce
-                           * batches: nearest hit with a validity mask, and the
-                           * renderer's bounces >= 1; or what pbg_autotune chose),
+    int32_t walk;         /* ray-bvh traversal: 0 = automatic (what pbg_autotune
+                           * chose for the batch class, else 6 for bounce
+                           * batches -- nearest hit with a validity mask, and
+                           * the renderer's bounces >= 1 --, 4 for other
+                           * nearest-hit batches, 5 for other any-hit ones),
                            * 1 = one thread per ray, 2 = persistent warps refilled
                            * from a ray counter, 3 = co-traversal of the ray
                            * hierarchy's 32-ray leaves with the BVH, one warp

@@ -441,7 +441,11 @@ static int bvh_launch(pbg_scene* s, const float4* o, const float4* d, const uint
     // is the one with a validity mask (rayhierarchy.cpp:602-813)
     const int hint = s->walk_hint >= 0 ? s->walk_hint : (!ANY && valid != nullptr ? 1 : 0);
     const int tuned = s->tune.bvh_walk[ANY ? 1 : 0][hint == 1 ? 1 : 0];
-    int walk = s->params.walk != 0 ? s->params.walk : (tuned != 0 ? tuned : (hint == 1 ? 2 : 1));
+    // untuned: the walks the autotuner picked on both benchmark scenes' batch
+    // classes (camera rays 4; their shadow rays 5; bounce rays and their
+    // shadows 6), none of them more than 25 % off the class's best there
+    const int fallback = hint == 1 ? 6 : (ANY ? 5 : 4);
+    int walk = s->params.walk != 0 ? s->params.walk : (tuned != 0 ? tuned : fallback);
     // Host-buffer calls run the packets in the caller's order: there the
     // batch arrives in parts whose copies overlap the traversal, and sorting
     // each part cost more than its packets gained (terrain frame end to end:

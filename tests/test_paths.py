@@ -54,7 +54,7 @@ def test_raybvh_walks(gpu_lib, terrain, walk):
     assert_same(acc.Intersect(terrain["inc"].copy()), terrain["want_inc"], f"inc, walk {walk}")
     occ = acc.IntersectP(terrain["inc"])
     np.testing.assert_array_equal(occ == ord("1"), terrain["occ_inc"] == 1)
-    # the bounce form (a validity mask) selects the persistent walk when automatic
+    # the bounce form (a validity mask): the incoherent class when automatic
     hit = (np.arange(terrain["inc"].shape[1]) % 3) != 0
     got = acc.Intersect(terrain["inc"].copy(), hit=hit.copy(), bounce=1)
     assert (got[0][~hit] == -1).all()
