@@ -26,13 +26,26 @@ __device__ __forceinline__ float safe_inv(float d) {
     return isfinite(r) ? r : copysignf(1e30f, d);
 }
 
+// Three-input max / min (one instruction on sm_100 and later); NaN inputs
+// are ignored as by fmaxf / fminf.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 __device__ __forceinline__ bool slab(const RayInv& r, float lx, float hx, float ly, float hy,
                                      float lz, float hz, float tmin, float tmax, float* tnear) {
     float tx0 = (lx - r.ox) * r.ix, tx1 = (hx - r.ox) * r.ix;
     float ty0 = (ly - r.oy) * r.iy, ty1 = (hy - r.oy) * r.iy;
     float tz0 = (lz - r.oz) * r.iz, tz1 = (hz - r.oz) * r.iz;
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    float tn = fmax3(fminf(tx0, tx1), fminf(ty0, ty1), fmaxf(fminf(tz0, tz1), tmin));
+    float tf = fmin3(fmaxf(tx0, tx1), fmaxf(ty0, ty1), fminf(fmaxf(tz0, tz1), tmax));
     *tnear = tn;
     // tf + |tf| * 2*gamma(3): each t carries at most two roundings
     return tn <= fmaf(fabsf(tf), 2.f * 3.f * 0x1p-24f / (1.f - 3.f * 0x1p-24f), tf);

@@ -35,19 +35,6 @@ constexpr int kWideThreads = 128;
 constexpr int kWideMinBlocks = 7;  // CTAs per SM: 7 measured best of 5, 6, 7, 8
 constexpr int kWideStack = 64;
 
-// Three-input max / min (one instruction on sm_100 and later); NaN inputs
-// are ignored as by fmaxf / fminf.
-__device__ __forceinline__ float fmax3(float a, float b, float c) {
-    float d;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-__device__ __forceinline__ float fmin3(float a, float b, float c) {
-    float d;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-
 // A group's entry distance kept in the upper 16 bits of a stack word,
 // rounded toward -infinity (a popped group is skipped only when it lies
 // beyond the hit found).
