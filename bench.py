@@ -1125,8 +1125,10 @@ def run_gpu_batch(args, rank, world, dev):
                 "api": "SceneSet.trace_host: two pbg_sceneset_trace calls over halves of the scenes, pinned host rays in and results out, copies overlapping the other half's trace"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 5), "traffic": BATCH_LAUNCH_DRAM_BYTES,
-                     "kernel": "batch_persistent_kernel (tuned walk)" if tuned.get("walk") == 2
-                               else "batch_trace_kernel (tuned walk)",
+                     "kernel": {1: "batch_trace_kernel", 2: "batch_persistent_kernel",
+                                3: "wide_walk_kernel (set walk 3, one launch per query kind)",
+                                4: "wide_walk_kernel (set walk 4, one launch per query kind)"}.get(
+                         tuned.get("walk"), "walk %s" % tuned.get("walk")) + " (tuned walk; traffic measured with walk 2)",
                      "algorithmic_bytes_per_launch": int(launch_bytes),
                      "avg_launch_ms": round(step_ms, 4), "peak_source": peak_kind},
         "gpu_launches": 2 * args.steps,
