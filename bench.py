@@ -55,9 +55,11 @@ import pbg_import  # noqa: E402
 pbg_import.load()
 
 METRIC = "Mrays/s nearest+any-hit at exact hit-ID match: plain vs learned-ordered, 1 GB300"
-# dram__bytes_read.sum + dram__bytes_write.sum of one tuned trace launch of
-# the 64-scene batch (ncu --set full, the warm-up launch after autotuning)
-BATCH_LAUNCH_DRAM_BYTES = 1_604_272_000
+# dram__bytes_read.sum + dram__bytes_write.sum of one trace step of the
+# 64-scene batch per set walk (walk 2: ncu --set full, the warm-up launch
+# after autotuning; walk 4: its nearest-hit and any-hit launches at 7 CTAs
+# per SM, ncu DRAM counters on the autotuner's trial runs)
+BATCH_STEP_DRAM_BYTES = {2: 1_604_272_000, 4: 1_658_600_000}
 # dram__bytes_read.sum + dram__bytes_write.sum of the traversal stage of one
 # batch call of the terrain frame (every traversal kernel of the warm-up
 # frame's nearest batch and four shadow batches, averaged over the five)
@@ -1124,11 +1126,11 @@ def run_gpu_batch(args, rank, world, dev):
                 "d2h_bytes_per_step": int(d2h),
                 "api": "SceneSet.trace_host: two pbg_sceneset_trace calls over halves of the scenes, pinned host rays in and results out, copies overlapping the other half's trace"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 5), "traffic": BATCH_LAUNCH_DRAM_BYTES,
+                     "frac": round(achieved / hbm, 5), "traffic": BATCH_STEP_DRAM_BYTES.get(tuned.get("walk")),
                      "kernel": {1: "batch_trace_kernel", 2: "batch_persistent_kernel",
                                 3: "wide_walk_kernel (set walk 3, one launch per query kind)",
                                 4: "wide_walk_kernel (set walk 4, one launch per query kind)"}.get(
-                         tuned.get("walk"), "walk %s" % tuned.get("walk")) + " (tuned walk; traffic measured with walk 2)",
+                         tuned.get("walk"), "walk %s" % tuned.get("walk")) + " (tuned walk)",
                      "algorithmic_bytes_per_launch": int(launch_bytes),
                      "avg_launch_ms": round(step_ms, 4), "peak_source": peak_kind},
         "gpu_launches": 2 * args.steps,
