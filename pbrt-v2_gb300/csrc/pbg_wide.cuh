@@ -7,9 +7,13 @@
 // set's completion stamps.  The node layout and the walk are described in
 // pbg_wide.cu.
 #pragma once
+#include <vector>
+
 #include "pbg_internal.h"
+#ifdef __CUDACC__
 #include "pbg_tma.cuh"
 #include "pbg_walk.cuh"
+#endif
 
 namespace pbg {
 
