@@ -261,7 +261,10 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_persistent_kernel(Batc
             const bool h1 = slab(ri, nn.n1.x, nn.n1.y, nn.n1.z, nn.n1.w, nn.n2.z, nn.n2.w, o.w, h.t, &tn1);
             node = -1;
             if (h0 || h1) {
-                const bool near0 = h0 && (!h1 || tn0 <= tn1);
+                // any-hit rays take the farther child first (back to front: a
+                // shadow ray leaves the surface around its origin; 64-scene
+                // step 13.09 -> 12.73 ms)
+                const bool near0 = h0 && (!h1 || (any ? tn1 < tn0 : tn0 <= tn1));
                 const int32_t cn = near0 ? nn.n3.x : nn.n3.y, kn = near0 ? nn.n3.z : nn.n3.w;
                 if (h0 && h1) {
                     const int32_t cf = near0 ? nn.n3.y : nn.n3.x, kf = near0 ? nn.n3.w : nn.n3.z;

@@ -67,6 +67,14 @@ struct CoopWarp {
     int32_t base1[32], base2[32], base3[32], off[32], occluder[32];
 };
 
+// Children in visiting order: slot ^ visit_order(octant).  Nearest hits go
+// front to back; any-hit rays back to front: a shadow ray's first boxes front
+// to back are the surface around its origin, which it leaves, and its
+// occluders lie farther on (path frame: shadow batches 0.70 -> 0.59 ms,
+// camera shadows 3.89 -> 3.50 ms).
+template <bool ANY>
+__device__ __forceinline__ uint32_t visit_order_of(uint32_t oct) { return ANY ? oct ^ 7u : oct; }
+
 template <bool ANY, bool STATS, bool COOP, class Src>
 __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
     wide_walk_kernel(const Src src, int* status, unsigned long long* next, unsigned long long* wcount) {
@@ -131,7 +139,7 @@ __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
                         ok = true;
                         gbase = 0;  // the root: slot 0 of a group whose only inner child is node 0
                         gimask = 1u;
-                        ghits = 1u << oct;
+                        ghits = 1u << visit_order_of<ANY>(oct);
                         gtn = -INFINITY;
                         tmask = 0;
                         tmask2 = 0;
@@ -182,7 +190,7 @@ __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
             }
             const int pos = __ffs(ghits) - 1;
             const uint32_t rest = ghits & (ghits - 1u);
-            const int cslot = pos ^ (int)oct;
+            const int cslot = pos ^ (int)visit_order_of<ANY>(oct);
             const int32_t child = gbase + __popc(gimask & ((1u << cslot) - 1u));
 
             const float4* np = reinterpret_cast<const float4*>(src.nodes(L) + child);
@@ -232,9 +240,10 @@ __global__ void __launch_bounds__(kWideThreads, kWideMinBlocks)
             }
             // hit inner children in visiting order: bit (slot ^ octant)
             uint32_t ih = hits & imask;
-            if (oct & 1u) ih = ((ih & 0x55u) << 1) | ((ih >> 1) & 0x55u);
-            if (oct & 2u) ih = ((ih & 0x33u) << 2) | ((ih >> 2) & 0x33u);
-            if (oct & 4u) ih = ((ih & 0x0fu) << 4) | ((ih >> 4) & 0x0fu);
+            const uint32_t vo = visit_order_of<ANY>(oct);
+            if (vo & 1u) ih = ((ih & 0x55u) << 1) | ((ih >> 1) & 0x55u);
+            if (vo & 2u) ih = ((ih & 0x33u) << 2) | ((ih >> 2) & 0x33u);
+            if (vo & 4u) ih = ((ih & 0x0fu) << 4) | ((ih >> 4) & 0x0fu);
             if (ih) {
                 if (rest) {
                     if (sp < kWideStack) {
