@@ -70,10 +70,10 @@ FRAME_TRAVERSAL_DRAM_BYTES = {"rayhierarchy": 148_000_000, "ray-bvh": 116_000_00
 # dram__bytes_read.sum + dram__bytes_write.sum per traversal launch of the
 # path frame: the average over the 12 traversal launches of one full-size
 # frame (ncu, the walks the autotuner picked, the timed frame of the run)
-PATH_LAUNCH_DRAM_BYTES = 187_171_136
+PATH_LAUNCH_DRAM_BYTES = 175_686_955
 # smsp__issue_active of the bounce walks (ncu --set full, bounce 1 of the
 # first frame of a 256x256 frame of the same scene: nearest, any-hit)
-PATH_ISSUE_ACTIVE = {"walk 6 (nearest)": 0.67, "walk 6 (any-hit)": 0.57, "walk 5 (nearest)": 0.71,
+PATH_ISSUE_ACTIVE = {"walk 6 (nearest)": 0.67, "walk 6 (any-hit)": 0.58, "walk 5 (nearest)": 0.71,
                      "walk 5 (any-hit)": 0.59, "walk 2 (nearest)": 0.72, "walk 2 (any-hit)": 0.50}
 FRAME_ISSUE_ACTIVE = {"rayhierarchy": {"rh_split_test_kernel<0,0> (camera, nearest)": 0.72,
                                        "rh_split_test_kernel<1,0> (shadow, any-hit)": 0.73}}
