@@ -38,7 +38,8 @@
 //   * children sit in slots by the direction octant that meets them first
 //     (a greedy assignment of child centroids to the eight octant
 //     directions), so visiting slots in the order slot ^ octant walks the
-//     children roughly front to back without sorting distances.
+//     children roughly front to back without sorting distances (any-hit
+//     rays take slot ^ octant ^ 7: back to front).
 // A lane reads only the near and far planes its octant needs, by address.
 // Traversal state per lane: the current node group (child base, the hit
 // inner children in visiting order, the group's nearest entry distance), the
